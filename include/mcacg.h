@@ -1,0 +1,254 @@
+/*
+ * mcacg.h -- C-ABI of the MCAC GB300 library.
+ *
+ * The library keeps one or many MCAC boxes resident on one GB300 and runs the
+ * per-step collision search and merge update of MCAC (giraldeau/MCAC) there.
+ * The entry points below are what a host program binds to replace the
+ * reference's C++ member interface that src/calcul.cpp calls each step.
+ * Plain C types only; no exception crosses this boundary. Every function
+ * returns a status code: 0-11 are the reference's ErrorCodes
+ * (include/constants.hpp:70-83), 100+ are this library's own
+ * (MCACG_ERR_*). mcacg_last_error() gives the message of the last failure on
+ * the calling thread.
+ *
+ * Labels are the reference's aggregate labels: the position of the aggregate
+ * in AggregatList, renumbered after every merge (keep = min label). Sphere
+ * indices are storage indices (Sphere::index_in_storage), stable in the
+ * collision-only path.
+ */
+#ifndef MCACG_H
+#define MCACG_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCACG_ABI_VERSION 1
+
+/* status codes beyond the reference's ErrorCodes */
+#define MCACG_ERR_CUDA 100         /* a CUDA call failed */
+#define MCACG_ERR_CAPACITY 101     /* a fixed device capacity was exceeded */
+#define MCACG_ERR_TIMEOUT 102      /* a bounded device wait gave up */
+#define MCACG_ERR_BAD_ARGUMENT 103 /* invalid argument (null pointer, label out of range, ...) */
+#define MCACG_ERR_NO_DEVICE 104    /* no CUDA device */
+
+/* initialisation modes and methods, numbered like the reference enums */
+#define MCACG_INIT_LOGNORMAL 0 /* MonomeresInitialisationMode, constants.hpp:104-108 */
+#define MCACG_INIT_NORMAL 1
+#define MCACG_VOLSURF_CAPS 0   /* VolSurfMethods, constants.hpp:113-120 */
+#define MCACG_VOLSURF_SBL 1
+#define MCACG_VOLSURF_ARVO 2
+#define MCACG_VOLSURF_ALPHAS 3
+#define MCACG_VOLSURF_NONE 4
+#define MCACG_PICK_RANDOM 0    /* PickMethods, constants.hpp:98-102 */
+#define MCACG_PICK_LAST 1
+
+/* The PhysicalModel subset of one box (physical_model.hpp:29-97). Filled by
+ * mcacg_params_from_ini / mcacg_params_default; the "derived" block is
+ * computed by the library. */
+typedef struct mcacg_params {
+    /* [monomers] */
+    int64_t n_monomeres;
+    double density;
+    double mean_diameter;       /* nm */
+    double dispersion_diameter; /* nm (normal) or geometric sigma (lognormal) */
+    int32_t initialisation_mode;
+    int32_t pick_method;
+    /* [environment] */
+    double initial_time;
+    double volume_fraction;
+    double temperature;
+    double pressure;
+    double fractal_prefactor;
+    double fractal_dimension;
+    /* [surface_growth] / [oxidation] */
+    int32_t with_surface_reactions;
+    int32_t volsurf_method;
+    double flux_surfgrowth;
+    double rp_min_oxid;
+    int64_t full_aggregate_update_frequency;
+    /* [limits] */
+    int64_t number_of_aggregates_limit;
+    int64_t n_iter_without_event_limit; /* <= 0: none */
+    double cpu_limit;                   /* <= 0: none */
+    double physical_time_limit;         /* <= 0: none */
+    int64_t mean_monomere_per_aggregate_limit; /* <= 0: none */
+    /* [numerics] */
+    int32_t with_domain_duplication;
+    int32_t with_domain_reduction;
+    int32_t with_collisions;
+    int32_t enforce_volume_fraction;
+    int32_t individual_surf_reactions;
+    int32_t random_seed;
+    int64_t n_verlet_divisions;
+    /* features outside the collision-only path; must be 0 */
+    int32_t with_nucleation;
+    int32_t with_potentials;
+    int32_t with_flame_coupling;
+    int32_t with_electric_charges;
+    /* derived (physical_model.cpp:228-269, 536-546) */
+    double box_length;
+    double box_volume;
+    double viscosity;
+    double gaz_mean_free_path;
+    double mean_massic_radius;
+    double friction_exponnant;
+    double u_sg;
+} mcacg_params;
+
+/* Result of a contact search: AggregateContactInfo
+ * (include/tools/contact_info.hpp:73-85) with the weak pointers replaced by
+ * indices. */
+typedef struct mcacg_contact {
+    double distance;          /* travel distance to first contact; +inf: none */
+    int64_t moving_sphere;    /* sphere storage index; -1: none */
+    int64_t other_sphere;     /* sphere storage index; -1: none */
+    int64_t moving_aggregate; /* label; -1: none */
+    int64_t other_aggregate;  /* label; -1: none */
+} mcacg_contact;
+
+/* Box state arrays (host memory), field-major like the reference's SoA
+ * storage (constants.hpp:34-69). Used to load and to store a box. */
+typedef struct mcacg_state {
+    int64_t n_spheres;
+    int64_t n_aggregates;
+    int64_t n_verlet_divisions;
+    double box_length;
+    double maxradius;
+    double time;
+    double *spheres;                 /* [9][n_spheres] */
+    int64_t *sphere_label;           /* [n_spheres]: label of the owning aggregate */
+    double *aggregates;              /* [21][n_aggregates] */
+    int64_t *n_spheres_per_aggregate;/* [n_aggregates] */
+    int64_t *members;                /* sphere indices of each aggregate, in list order, concatenated */
+} mcacg_state;
+
+/* One MC step of a traced run; layout of mcac_gb300.snapshot.STEP_DTYPE. */
+typedef struct mcacg_step_record {
+    int64_t step, picked, contact, merged, moving_sphere, other_sphere, moving_agg, other_agg, n_agg_after;
+    double deltatemps, full_distance, dir[3], contact_distance, move_distance, time_after, reserved;
+} mcacg_step_record;
+
+typedef struct mcacg_run_opts {
+    int64_t max_steps;          /* stop after this many MC steps; <= 0: only the stop criteria */
+    mcacg_step_record *trace;   /* optional per-step records (host memory) */
+    int64_t trace_capacity;
+} mcacg_run_opts;
+
+typedef struct mcacg_run_stats {
+    int64_t steps;        /* MC steps done by this call */
+    int64_t events;       /* merges done by this call */
+    int64_t n_aggregates; /* aggregates left */
+    double time;          /* physical time */
+    int32_t finished;     /* a stop criterion of the parameters was met */
+    int32_t reserved;
+} mcacg_run_stats;
+
+/* Kernel timings and work counts of one box since the last read (profiling
+ * must be on). Times are CUDA-event durations on the box's stream. */
+typedef struct mcacg_profile {
+    int64_t queries, merges, translates;
+    double query_ms, merge_ms;
+    int64_t mov_spheres;  /* spheres of the moving aggregates */
+    int64_t scanned;      /* aggregates read from the Verlet cells */
+    int64_t cells;        /* Verlet cells scanned */
+    int64_t candidates;   /* aggregates passing the bounding-sphere filter */
+    int64_t cand_spheres; /* spheres of those candidates */
+    int64_t refined;      /* sphere pairs evaluated in FP64 */
+    int64_t merged_spheres, merge_pairs;
+} mcacg_profile;
+
+typedef struct mcacg_box mcacg_box;
+
+/* ---- library ---- */
+int mcacg_abi_version(void);
+/* Message of the last failing call on this thread (empty if none). */
+const char *mcacg_last_error(void);
+/* Number of CUDA devices visible (0 on a machine without a GPU). */
+int mcacg_device_count(int *count);
+
+/* ---- parameter file (PhysicalModel::PhysicalModel, physical_model.cpp:32-287) ---- */
+int mcacg_params_default(mcacg_params *params);
+/* Parse an INI parameter file with the reference's keys and defaults. Unlike
+ * the reference constructor it creates no output directory and does not seed
+ * the random generator (mcacg_box_create does). */
+int mcacg_params_from_ini(const char *path, mcacg_params *params);
+int mcacg_params_from_ini_text(const char *text, mcacg_params *params);
+
+/* ---- host-only state construction (no GPU needed) ---- */
+/* The random placement of AggregatList::AggregatList
+ * (aggregats/aggregat_list_storage.cpp:52-88, aggregat.cpp:162-229) into
+ * caller-owned arrays sized for params->n_monomeres spheres and aggregates:
+ * seeds the C library generator with random_seed, places the monomers
+ * without overlap, computes every aggregate field and applies
+ * enforce_volume_fraction. Bit-identical with the reference. */
+int mcacg_state_init_random(const mcacg_params *params, mcacg_state *state);
+
+/* ---- boxes ---- */
+/* AggregatList::AggregatList (aggregats/aggregat_list_storage.cpp:52-88):
+ * seeds the C library generator with random_seed, places n_monomeres
+ * monomers without overlap exactly as the reference does, and uploads the
+ * box to the current CUDA device. */
+int mcacg_box_create(const mcacg_params *params, mcacg_box **box);
+/* Builds a box from a state (no random placement). Aggregate fields are used
+ * as given. */
+int mcacg_box_create_from_state(const mcacg_params *params, const mcacg_state *state, mcacg_box **box);
+int mcacg_box_destroy(mcacg_box *box);
+/* Launch the box's kernels on this CUDA stream (cudaStream_t; NULL: the
+ * library's own stream). */
+int mcacg_box_set_stream(mcacg_box *box, void *cuda_stream);
+int mcacg_box_sizes(const mcacg_box *box, int64_t *n_spheres, int64_t *n_aggregates);
+/* Copies the whole state to host arrays sized by mcacg_box_sizes. */
+int mcacg_box_store_state(mcacg_box *box, mcacg_state *state);
+int mcacg_box_get_time(const mcacg_box *box, double *time);
+/* Turns per-kernel CUDA-event timing on or off (no counterpart in the
+ * reference: instrumentation of this library). */
+int mcacg_box_set_profiling(mcacg_box *box, int enable);
+/* Reads and resets the counters of mcacg_profile. */
+int mcacg_box_take_profile(mcacg_box *box, mcacg_profile *out);
+int mcacg_box_set_time(mcacg_box *box, double time);
+
+/* ---- the per-step interface (include/aggregats/aggregat_list.hpp:29-116) ---- */
+/* AggregatList::distance_to_next_contact (aggregat_list.hpp:69-71,
+ * aggregat_list.cpp:447-484): first contact of aggregate 'source' moving
+ * along the unit vector 'direction' for at most 'distance'. */
+int mcacg_distance_to_next_contact(mcacg_box *box, int64_t source, const double direction[3], double distance,
+                                   mcacg_contact *out);
+/* Aggregate::translate (aggregat.hpp:108, aggregat.cpp:148-161). */
+int mcacg_translate(mcacg_box *box, int64_t label, const double vector[3]);
+/* Aggregate::time_forward (aggregat.cpp:106-108). */
+int mcacg_time_forward(mcacg_box *box, int64_t label, double deltatemps);
+/* AggregatList::merge (aggregat_list.hpp:63, aggregat_list.cpp:367-410):
+ * *merged = 0 when the two spheres are no longer in contact. Uses the box
+ * time for the merged proper time. Throws the reference's MergeError /
+ * VolSurfError as status codes 9 / 8. */
+int mcacg_merge(mcacg_box *box, const mcacg_contact *contact, int32_t *merged);
+/* AggregatList::sort_time_steps / pick_random / get_time_step /
+ * get_max_time_step / refresh (aggregat_list.cpp:50-66, 100-141).
+ * pick_random draws one number from the C library generator. */
+int mcacg_sort_time_steps(mcacg_box *box, double factor);
+int mcacg_pick_random(mcacg_box *box, int64_t *label);
+int mcacg_get_time_step(const mcacg_box *box, double max, double *deltatemps);
+int mcacg_get_max_time_step(const mcacg_box *box, double *max);
+int mcacg_refresh(mcacg_box *box);
+/* AggregatList::size, get_avg_npp, get_total_volume, get_total_surface. */
+int mcacg_size(const mcacg_box *box, int64_t *n_aggregates);
+int mcacg_get_avg_npp(const mcacg_box *box, double *avg_npp);
+int mcacg_get_total_volume(const mcacg_box *box, double *volume);
+int mcacg_get_total_surface(const mcacg_box *box, double *surface);
+/* The 21 storage fields of aggregate 'label' and its sphere count. */
+int mcacg_get_aggregate(const mcacg_box *box, int64_t label, double fields[21], int64_t *n_spheres);
+
+/* ---- whole runs ---- */
+/* The MC loop of mcac::calcul (src/calcul.cpp:66-281) for the
+ * collision-only configuration, driven from the host one step at a time
+ * through the entry points above: results are bit-identical with the
+ * reference binary built with FP contraction off. */
+int mcacg_calcul(mcacg_box *box, const mcacg_run_opts *opts, mcacg_run_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCACG_H */

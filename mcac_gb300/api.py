@@ -1,0 +1,275 @@
+"""Python face of the library, named after the reference's C++ interface.
+
+``PhysicalModel`` is the parameter file (src/physical_model/physical_model.cpp),
+``AggregatList`` one device-resident box with the methods src/calcul.cpp calls
+each step (include/aggregats/aggregat_list.hpp), and ``calcul`` the MC loop.
+Everything runs through the C-ABI in include/mcacg.h; nothing here computes
+physics itself.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import _lib
+from ._lib import Contact, Params, RunOpts, RunStats, StateBuffers, StepRecord, check, lib, ptr
+from .snapshot import STEP_DTYPE, Snapshot
+
+
+class PhysicalModel:
+    """The INI parameter file with the reference's keys, defaults and derived values."""
+
+    def __init__(self, path: str | Path | None = None, text: str | None = None, **overrides):
+        self.params = Params()
+        if path is not None:
+            check(lib().mcacg_params_from_ini(str(path).encode(), C.byref(self.params)))
+        elif text is not None:
+            check(lib().mcacg_params_from_ini_text(text.encode(), C.byref(self.params)))
+        else:
+            check(lib().mcacg_params_default(C.byref(self.params)))
+        if overrides:
+            self.set(**overrides)
+
+    def set(self, **values) -> "PhysicalModel":
+        """Change parameters and recompute the derived block through the library."""
+        for k, v in values.items():
+            if not hasattr(self.params, k):
+                raise KeyError(k)
+            setattr(self.params, k, v)
+        # re-derive from the INI-level values
+        text = self.to_ini()
+        derived = Params()
+        check(lib().mcacg_params_from_ini_text(text.encode(), C.byref(derived)))
+        for name in ("box_length", "box_volume", "viscosity", "gaz_mean_free_path", "mean_massic_radius",
+                     "friction_exponnant", "u_sg"):
+            setattr(self.params, name, getattr(derived, name))
+        return self
+
+    def __getattr__(self, name):
+        if name == "params":
+            raise AttributeError(name)
+        return getattr(self.params, name)
+
+    def to_ini(self) -> str:
+        p = self.params
+        b = lambda v: "true" if v else "false"  # noqa: E731
+        modes = {0: "lognormal", 1: "normal"}
+        volsurf = {0: "caps", 1: "sbl", 2: "arvo", 3: "alphas", 4: "none"}
+        return "\n".join([
+            "[monomers]", f"number = {p.n_monomeres}", f"density = {p.density!r}",
+            f"mean_diameter = {p.mean_diameter!r}", f"dispersion_diameter = {p.dispersion_diameter!r}",
+            f"initialisation_mode = {modes[p.initialisation_mode]}",
+            "[environment]", f"initial_time = {p.initial_time!r}", f"volume_fraction = {p.volume_fraction!r}",
+            f"temperature = {p.temperature!r}", f"pressure = {p.pressure!r}",
+            f"fractal_prefactor = {p.fractal_prefactor!r}", f"fractal_dimension = {p.fractal_dimension!r}",
+            "[surface_growth]", f"with_surface_reactions = {b(p.with_surface_reactions)}",
+            f"flux_surfgrowth = {p.flux_surfgrowth!r}", f"volsurf_method = {volsurf[p.volsurf_method]}",
+            f"full_aggregate_update_frequency = {p.full_aggregate_update_frequency}",
+            "[oxidation]", f"rp_min = {p.rp_min_oxid!r}",
+            "[limits]", f"number_of_aggregates = {p.number_of_aggregates_limit}",
+            f"n_iter_without_event = {p.n_iter_without_event_limit}", f"cpu = {p.cpu_limit!r}",
+            f"physical_time = {p.physical_time_limit!r}",
+            f"mean_monomere_per_aggregate = {p.mean_monomere_per_aggregate_limit}",
+            "[numerics]", f"with_domain_duplication = {b(p.with_domain_duplication)}",
+            f"with_domain_reduction = {b(p.with_domain_reduction)}",
+            f"with_collisions = {b(p.with_collisions)}",
+            f"enforce_volume_fraction = {b(p.enforce_volume_fraction)}",
+            f"individual_surf_reactions = {b(p.individual_surf_reactions)}",
+            f"n_verlet_divisions = {p.n_verlet_divisions}",
+            f"pick_method = {'random' if p.pick_method == 0 else 'last'}",
+            f"random_seed = {p.random_seed}", "",
+        ])
+
+
+def init_state(model: PhysicalModel) -> StateBuffers:
+    """The reference constructor's random placement, on the host (no GPU)."""
+    n = int(model.params.n_monomeres)
+    sb = StateBuffers(n, n)
+    check(lib().mcacg_state_init_random(C.byref(model.params), C.byref(sb.state)))
+    return sb
+
+
+@dataclass
+class AggregateContactInfo:
+    """include/tools/contact_info.hpp:73-85 with indices for the weak pointers."""
+    distance: float
+    moving_sphere: int
+    other_sphere: int
+    moving_aggregate: int
+    other_aggregate: int
+
+    def __le__(self, d: float) -> bool:  # SphereContactInfo::operator<=
+        return self.distance <= d
+
+    def to_c(self) -> Contact:
+        return Contact(self.distance, self.moving_sphere, self.other_sphere, self.moving_aggregate,
+                       self.other_aggregate)
+
+
+class AggregatList:
+    """One box on the GPU behind the reference's AggregatList interface."""
+
+    def __init__(self, model: PhysicalModel, state: Snapshot | StateBuffers | None = None,
+                 stream: int | None = None):
+        self.model = model
+        self._box = C.c_void_p()
+        if state is None:
+            check(lib().mcacg_box_create(C.byref(model.params), C.byref(self._box)))
+        else:
+            sb = state if isinstance(state, StateBuffers) else StateBuffers.from_snapshot(state)
+            check(lib().mcacg_box_create_from_state(C.byref(model.params), C.byref(sb.state), C.byref(self._box)))
+        if stream is not None:
+            check(lib().mcacg_box_set_stream(self._box, C.c_void_p(stream)))
+
+    def close(self) -> None:
+        if self._box:
+            check(lib().mcacg_box_destroy(self._box))
+            self._box = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- getters
+    def size(self) -> int:
+        v = C.c_int64()
+        check(lib().mcacg_size(self._box, C.byref(v)))
+        return v.value
+
+    def __len__(self) -> int:
+        return self.size()
+
+    @property
+    def time(self) -> float:
+        v = C.c_double()
+        check(lib().mcacg_box_get_time(self._box, C.byref(v)))
+        return v.value
+
+    @time.setter
+    def time(self, t: float) -> None:
+        check(lib().mcacg_box_set_time(self._box, float(t)))
+
+    def get_avg_npp(self) -> float:
+        v = C.c_double()
+        check(lib().mcacg_get_avg_npp(self._box, C.byref(v)))
+        return v.value
+
+    def get_max_time_step(self) -> float:
+        v = C.c_double()
+        check(lib().mcacg_get_max_time_step(self._box, C.byref(v)))
+        return v.value
+
+    def get_time_step(self, factor: float) -> float:
+        v = C.c_double()
+        check(lib().mcacg_get_time_step(self._box, float(factor), C.byref(v)))
+        return v.value
+
+    def get_total_volume(self) -> float:
+        v = C.c_double()
+        check(lib().mcacg_get_total_volume(self._box, C.byref(v)))
+        return v.value
+
+    def get_total_surface(self) -> float:
+        v = C.c_double()
+        check(lib().mcacg_get_total_surface(self._box, C.byref(v)))
+        return v.value
+
+    def aggregate(self, label: int) -> tuple[np.ndarray, int]:
+        f = np.zeros(21)
+        n = C.c_int64()
+        check(lib().mcacg_get_aggregate(self._box, int(label), ptr(f, C.c_double), C.byref(n)))
+        return f, n.value
+
+    # -- per-step interface
+    def distance_to_next_contact(self, source: int, direction, distance: float) -> AggregateContactInfo:
+        d = np.ascontiguousarray(direction, dtype=np.float64)
+        c = Contact()
+        check(lib().mcacg_distance_to_next_contact(self._box, int(source), ptr(d, C.c_double), float(distance),
+                                                    C.byref(c)))
+        return AggregateContactInfo(c.distance, c.moving_sphere, c.other_sphere, c.moving_aggregate,
+                                    c.other_aggregate)
+
+    def translate(self, label: int, vector) -> None:
+        v = np.ascontiguousarray(vector, dtype=np.float64)
+        check(lib().mcacg_translate(self._box, int(label), ptr(v, C.c_double)))
+
+    def time_forward(self, label: int, deltatemps: float) -> None:
+        check(lib().mcacg_time_forward(self._box, int(label), float(deltatemps)))
+
+    def merge(self, info: AggregateContactInfo) -> bool:
+        c = info.to_c()
+        m = C.c_int32()
+        check(lib().mcacg_merge(self._box, C.byref(c), C.byref(m)))
+        return bool(m.value)
+
+    def sort_time_steps(self, factor: float) -> None:
+        check(lib().mcacg_sort_time_steps(self._box, float(factor)))
+
+    def pick_random(self) -> int:
+        v = C.c_int64()
+        check(lib().mcacg_pick_random(self._box, C.byref(v)))
+        return v.value
+
+    def refresh(self) -> None:
+        check(lib().mcacg_refresh(self._box))
+
+    # -- instrumentation
+    def set_profiling(self, on: bool = True) -> None:
+        check(lib().mcacg_box_set_profiling(self._box, 1 if on else 0))
+
+    def take_profile(self) -> dict:
+        p = _lib.Profile()
+        check(lib().mcacg_box_take_profile(self._box, C.byref(p)))
+        return {name: getattr(p, name) for name, _ in _lib.Profile._fields_}
+
+    # -- whole runs and state
+    def calcul(self, max_steps: int = 0, trace: bool = False, trace_capacity: int = 0):
+        """The reference MC loop; returns (stats, records or None)."""
+        recs = None
+        opts = RunOpts(int(max_steps), None, 0)
+        if trace:
+            cap = int(trace_capacity or max_steps or 1_000_000)
+            recs = (StepRecord * cap)()
+            opts.trace = C.cast(recs, C.POINTER(StepRecord))
+            opts.trace_capacity = cap
+        stats = RunStats()
+        check(lib().mcacg_calcul(self._box, C.byref(opts), C.byref(stats)))
+        out = None
+        if trace:
+            n = min(int(stats.steps), opts.trace_capacity)
+            out = np.frombuffer(bytes(memoryview(recs).cast("B")[: n * C.sizeof(StepRecord)]), dtype=STEP_DTYPE)
+        return stats, out
+
+    def store(self) -> Snapshot:
+        ns, na = C.c_int64(), C.c_int64()
+        check(lib().mcacg_box_sizes(self._box, C.byref(ns), C.byref(na)))
+        sb = StateBuffers(ns.value, na.value)
+        check(lib().mcacg_box_store_state(self._box, C.byref(sb.state)))
+        return sb.to_snapshot(volsurf_method=int(self.model.params.volsurf_method))
+
+
+def device_count() -> int:
+    n = C.c_int()
+    check(lib().mcacg_device_count(C.byref(n)))
+    return n.value
+
+
+def calcul(model: PhysicalModel, aggregates: AggregatList, max_steps: int = 0):
+    """mcac::calcul (src/calcul.cpp:55-290) for the collision-only configuration."""
+    return aggregates.calcul(max_steps=max_steps)
+
+
+__all__ = ["PhysicalModel", "AggregatList", "AggregateContactInfo", "init_state", "calcul", "device_count",
+           "_lib", "math"]

@@ -1,0 +1,446 @@
+// Single-box kernels and the host-side management of a device-resident box.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "box.cuh"
+#include "device_box.hpp"
+#include "merge.cuh"
+
+namespace mcacg {
+
+// ------------------------------------------------------------------ kernels
+__global__ void __launch_bounds__(kQueryThreads) k_query(DevBox b, int src, double dx, double dy, double dz,
+                                                         double dist, QueryOut *out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    QuerySmem &sm = *reinterpret_cast<QuerySmem *>(smem_raw);
+    block_query(b, src, Vec3{dx, dy, dz}, dist, sm);
+    if (threadIdx.x == 0) *out = sm.out;
+}
+
+__global__ void __launch_bounds__(kQueryThreads) k_translate(DevBox b, int slot, double vx, double vy, double vz) {
+    __shared__ double refpos[3];
+    block_translate(b, slot, Vec3{vx, vy, vz}, refpos);
+}
+
+__global__ void __launch_bounds__(kQueryThreads) k_merge(DevBox b, int ms, int os, int mslot, int oslot,
+                                                         MergeOut *out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MergeSmem &sm = *reinterpret_cast<MergeSmem *>(smem_raw);
+    block_merge(b, ms, os, mslot, oslot, sm, out);
+}
+
+struct FieldUpdate {
+    double v[21];
+};
+__global__ void k_set_fields(DevBox b, int slot, FieldUpdate u, unsigned mask) {
+    int f = threadIdx.x;
+    if (f < AGG_NFIELDS && (mask >> f) & 1u) A(b, f, slot) = u.v[f];
+}
+
+__global__ void k_rebuild_grid(DevBox b) {
+    // one block: serial insertion in slot order keeps every cell sorted
+    if (threadIdx.x == 0) {
+        for (int c = 0; c < b.n_cells; ++c) b.cell_n[c] = 0;
+        for (int a = 0; a < b.nslots; ++a) {
+            if (b.agg_n[a] == 0) continue;
+            int c = cell_of(b, agg_pos(b, a));
+            b.agg_cell[a] = c;
+            int n = b.cell_n[c];
+            if (n >= b.cell_cap) {
+                b.sc->cell_overflow = 1;
+                b.sc->status = ST_CAPACITY;
+                continue;
+            }
+            b.cell_items[size_t(c) * b.cell_cap + n] = a;
+            b.cell_n[c] = n + 1;
+        }
+    }
+}
+
+// ------------------------------------------------------------------- host
+namespace {
+
+bool cuda_ok(cudaError_t e, std::string *err, const char *what) {
+    if (e == cudaSuccess) return true;
+    if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+}
+
+struct OutBuffers {
+    QueryOut query;
+    MergeOut merge;
+};
+
+}  // namespace
+
+int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::string *err) {
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        if (err) *err = "no CUDA device";
+        return ST_NO_DEVICE;
+    }
+    DeviceBox *d = new DeviceBox();
+    d->ns_ = st.ns;
+    d->nslots_ = st.nslots;
+    DevBox b{};
+    b.L = st.box_length;
+    b.n_div = st.n_div;
+    b.step = double(st.n_div) / st.box_length;
+    b.n_cells = st.n_div * st.n_div * st.n_div;
+    b.ns = st.ns;
+    b.nslots = st.nslots;
+    // FP32 screening margin: coordinates are bounded by the box plus the
+    // largest aggregate; 2^-17 of that bound is >10x the FP32 error of the
+    // capsule test.
+    double rmax_all = st.maxradius;
+    for (int a = 0; a < st.nslots; ++a)
+        if (st.agg_n[a] > 0) rmax_all = std::max(rmax_all, st.agg[size_t(AGG_RMAX) * st.nslots + a]);
+    b.margin = (3.0 * st.box_length + 4.0 * rmax_all) * (1.0 / 131072.0);
+    // grid capacity
+    std::vector<int> cell_n(size_t(b.n_cells), 0);
+    int maxc = 0;
+    for (int a = 0; a < st.nslots; ++a) {
+        if (st.agg_n[a] == 0) continue;
+        const double *ag = st.agg.data();
+        double x = ag[size_t(AGG_X) * st.nslots + a], y = ag[size_t(AGG_Y) * st.nslots + a],
+               z = ag[size_t(AGG_Z) * st.nslots + a];
+        int ix = std::min(std::max(verlet_coord(x, b.step), 0), b.n_div - 1);
+        int iy = std::min(std::max(verlet_coord(y, b.step), 0), b.n_div - 1);
+        int iz = std::min(std::max(verlet_coord(z, b.step), 0), b.n_div - 1);
+        maxc = std::max(maxc, ++cell_n[size_t((ix * b.n_div + iy) * b.n_div + iz)]);
+    }
+    int avg = (st.nslots + b.n_cells - 1) / b.n_cells;
+    b.cell_cap = std::max({64, 2 * maxc, 8 * avg});
+    b.pool_cap = 2 * st.ns + 1024;
+    b.surv_cap = 1 << 16;
+    b.pair_cap = 16 * st.ns + 1024;
+
+    auto alloc = [&](void **p, size_t bytes) -> bool {
+        if (!cuda_ok(cudaMalloc(p, std::max<size_t>(bytes, 16)), err, "cudaMalloc")) return false;
+        d->allocations_.push_back(*p);
+        return true;
+    };
+    bool ok = true;
+    ok = ok && alloc((void **)&b.sph, sizeof(double) * 9 * size_t(st.ns));
+    ok = ok && alloc((void **)&b.sph_slot, sizeof(int) * size_t(st.ns));
+    ok = ok && alloc((void **)&b.agg, sizeof(double) * 21 * size_t(st.nslots));
+    ok = ok && alloc((void **)&b.agg_n, sizeof(int) * size_t(st.nslots));
+    ok = ok && alloc((void **)&b.agg_off, sizeof(int) * size_t(st.nslots));
+    ok = ok && alloc((void **)&b.agg_cell, sizeof(int) * size_t(st.nslots));
+    for (int k = 0; k < 2; ++k) {
+        ok = ok && alloc((void **)&b.pool_id[k], sizeof(int) * size_t(b.pool_cap));
+        ok = ok && alloc((void **)&b.pool_pos[k], sizeof(float4) * size_t(b.pool_cap));
+    }
+    ok = ok && alloc((void **)&b.cell_n, sizeof(int) * size_t(b.n_cells));
+    ok = ok && alloc((void **)&b.cell_items, sizeof(int) * size_t(b.n_cells) * size_t(b.cell_cap));
+    ok = ok && alloc((void **)&b.sc, sizeof(DevScalars));
+    ok = ok && alloc((void **)&b.surv, sizeof(int4) * size_t(b.surv_cap));
+    ok = ok && alloc((void **)&b.surv_res, sizeof(double) * size_t(b.surv_cap));
+    ok = ok && alloc((void **)&b.pair_i, sizeof(int) * size_t(b.pair_cap));
+    ok = ok && alloc((void **)&b.pair_j, sizeof(int) * size_t(b.pair_cap));
+    ok = ok && alloc((void **)&b.pair_d, sizeof(double) * size_t(b.pair_cap));
+    ok = ok && alloc((void **)&b.pair_tmp_i, sizeof(int) * size_t(b.pair_cap));
+    ok = ok && alloc((void **)&b.pair_tmp_j, sizeof(int) * size_t(b.pair_cap));
+    ok = ok && alloc((void **)&b.pair_tmp_d, sizeof(double) * size_t(b.pair_cap));
+    ok = ok && alloc((void **)&b.row_cnt, sizeof(int) * (size_t(std::max(st.ns, st.nslots)) + 2));
+    ok = ok && alloc((void **)&b.work, sizeof(double) * 8 * size_t(st.ns));
+    ok = ok && alloc((void **)&b.counters, sizeof(int) * 8);
+    if (!ok) {
+        delete d;
+        return ST_CUDA;
+    }
+    if (stream) {
+        d->stream_ = stream;
+    } else {
+        cudaStream_t s;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), err, "cudaStreamCreate")) {
+            delete d;
+            return ST_CUDA;
+        }
+        d->stream_ = s;
+        d->own_stream_ = true;
+    }
+    // upload
+    std::vector<int> off(size_t(st.nslots), 0), pool_id(size_t(b.pool_cap), 0);
+    std::vector<float4> pool_pos(size_t(b.pool_cap));
+    int top = 0;
+    for (int a = 0; a < st.nslots; ++a) {
+        off[size_t(a)] = top;
+        if (st.agg_n[a] == 0) continue;
+        for (int s : st.members[size_t(a)]) {
+            pool_id[size_t(top)] = s;
+            pool_pos[size_t(top)] = make_float4(float(st.sph[size_t(SPH_X) * st.ns + s]),
+                                                float(st.sph[size_t(SPH_Y) * st.ns + s]),
+                                                float(st.sph[size_t(SPH_Z) * st.ns + s]),
+                                                float(st.sph[size_t(SPH_R) * st.ns + s]));
+            ++top;
+        }
+    }
+    DevScalars sc{};
+    sc.maxradius = st.maxradius;
+    sc.time = st.time;
+    sc.pool_top = top;
+    sc.pool_sel = 0;
+    int alive = 0;
+    for (int a = 0; a < st.nslots; ++a) alive += st.agg_n[a] > 0;
+    sc.n_alive = alive;
+    cudaStream_t s = static_cast<cudaStream_t>(d->stream_);
+    ok = ok && cuda_ok(cudaMemcpy(b.sph, st.sph.data(), sizeof(double) * 9 * size_t(st.ns), cudaMemcpyHostToDevice), err, "upload");
+    ok = ok && cuda_ok(cudaMemcpy(b.sph_slot, st.sph_slot.data(), sizeof(int) * size_t(st.ns), cudaMemcpyHostToDevice), err, "upload");
+    ok = ok && cuda_ok(cudaMemcpy(b.agg, st.agg.data(), sizeof(double) * 21 * size_t(st.nslots), cudaMemcpyHostToDevice), err, "upload");
+    ok = ok && cuda_ok(cudaMemcpy(b.agg_n, st.agg_n.data(), sizeof(int) * size_t(st.nslots), cudaMemcpyHostToDevice), err, "upload");
+    ok = ok && cuda_ok(cudaMemcpy(b.agg_off, off.data(), sizeof(int) * size_t(st.nslots), cudaMemcpyHostToDevice), err, "upload");
+    ok = ok && cuda_ok(cudaMemcpy(b.pool_id[0], pool_id.data(), sizeof(int) * size_t(b.pool_cap), cudaMemcpyHostToDevice), err, "upload");
+    ok = ok && cuda_ok(cudaMemcpy(b.pool_pos[0], pool_pos.data(), sizeof(float4) * size_t(b.pool_cap), cudaMemcpyHostToDevice), err, "upload");
+    ok = ok && cuda_ok(cudaMemcpy(b.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice), err, "upload");
+    if (!ok) {
+        delete d;
+        return ST_CUDA;
+    }
+    ok = ok && cuda_ok(cudaHostAlloc(&d->host_out_, sizeof(OutBuffers), cudaHostAllocMapped), err, "cudaHostAlloc");
+    ok = ok && cuda_ok(cudaHostGetDevicePointer(&d->dev_out_, d->host_out_, 0), err, "cudaHostGetDevicePointer");
+    ok = ok && cuda_ok(cudaFuncSetAttribute(k_query, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(QuerySmem))),
+                       err, "cudaFuncSetAttribute");
+    ok = ok && cuda_ok(cudaFuncSetAttribute(k_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(MergeSmem))),
+                       err, "cudaFuncSetAttribute");
+    d->devbox_ = new DevBox(b);
+    if (!ok) {
+        delete d;
+        return ST_CUDA;
+    }
+    (void)s;
+    int rc = d->rebuild_grid(b.cell_cap, err);
+    if (rc != ST_OK) {
+        delete d;
+        return rc;
+    }
+    *out = d;
+    return ST_OK;
+}
+
+void DeviceBox::set_profiling(bool on) {
+    if (on && !ev_[0]) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        ev_[0] = a;
+        ev_[1] = b;
+    }
+    profiling_ = on;
+}
+
+Profile DeviceBox::take_profile() {
+    Profile p = prof_;
+    prof_ = Profile();
+    return p;
+}
+
+DeviceBox::~DeviceBox() {
+    if (stream_) cudaStreamSynchronize(static_cast<cudaStream_t>(stream_));
+    for (void *e : ev_)
+        if (e) cudaEventDestroy(static_cast<cudaEvent_t>(e));
+    for (void *p : allocations_) cudaFree(p);
+    if (host_out_) cudaFreeHost(host_out_);
+    if (own_stream_ && stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
+    delete static_cast<DevBox *>(devbox_);
+}
+
+int DeviceBox::set_stream(void *stream) {
+    if (stream_) cudaStreamSynchronize(static_cast<cudaStream_t>(stream_));
+    if (own_stream_ && stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
+    own_stream_ = false;
+    stream_ = stream;
+    if (!stream_) {
+        cudaStream_t s;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return ST_CUDA;
+        stream_ = s;
+        own_stream_ = true;
+    }
+    return ST_OK;
+}
+
+int DeviceBox::sync(std::string *err) {
+    if (!cuda_ok(cudaStreamSynchronize(static_cast<cudaStream_t>(stream_)), err, "sync")) return ST_CUDA;
+    return ST_OK;
+}
+
+int DeviceBox::check_status(std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    DevScalars sc;
+    if (!cuda_ok(cudaMemcpyAsync(&sc, b.sc, sizeof(sc), cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream_)), err,
+                 "status"))
+        return ST_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(static_cast<cudaStream_t>(stream_)), err, "sync")) return ST_CUDA;
+    return sc.status;
+}
+
+int DeviceBox::rebuild_grid(int cap, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    if (cap != b.cell_cap) {
+        int *items = nullptr;
+        if (!cuda_ok(cudaMalloc(&items, sizeof(int) * size_t(b.n_cells) * size_t(cap)), err, "cudaMalloc")) return ST_CUDA;
+        auto it = std::find(allocations_.begin(), allocations_.end(), (void *)b.cell_items);
+        if (it != allocations_.end()) {
+            cudaFree(*it);
+            *it = items;
+        }
+        b.cell_items = items;
+        b.cell_cap = cap;
+    }
+    // clear the overflow flag and status
+    DevScalars sc;
+    if (!cuda_ok(cudaMemcpyAsync(&sc, b.sc, sizeof(sc), cudaMemcpyDeviceToHost, s), err, "status")) return ST_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
+    sc.cell_overflow = 0;
+    if (sc.status == ST_CAPACITY) sc.status = ST_OK;
+    if (!cuda_ok(cudaMemcpyAsync(b.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, s), err, "status")) return ST_CUDA;
+    k_rebuild_grid<<<1, 32, 0, s>>>(b);
+    if (!cuda_ok(cudaGetLastError(), err, "k_rebuild_grid")) return ST_CUDA;
+    int st = check_status(err);
+    if (st == ST_CAPACITY) return rebuild_grid(cap * 2, err);
+    return st;
+}
+
+int DeviceBox::query(int src_slot, const double dir[3], double dist, QueryResult *out, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    OutBuffers *ho = static_cast<OutBuffers *>(host_out_);
+    OutBuffers *dout = static_cast<OutBuffers *>(dev_out_);
+    if (profiling_) cudaEventRecord(static_cast<cudaEvent_t>(ev_[0]), s);
+    k_query<<<1, kQueryThreads, sizeof(QuerySmem), s>>>(b, src_slot, dir[0], dir[1], dir[2], dist, &dout->query);
+    if (profiling_) cudaEventRecord(static_cast<cudaEvent_t>(ev_[1]), s);
+    if (!cuda_ok(cudaGetLastError(), err, "k_query")) return ST_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(s), err, "k_query")) return ST_CUDA;
+    const QueryOut &q = ho->query;
+    if (profiling_) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev_[0]), static_cast<cudaEvent_t>(ev_[1]));
+        prof_.queries += 1;
+        prof_.query_ms += ms;
+        prof_.mov_spheres += q.n_mov;
+        prof_.scanned += q.n_scanned;
+        prof_.cells += q.n_cells;
+        prof_.candidates += q.n_candidates;
+        prof_.cand_spheres += q.n_cand_spheres;
+        prof_.refined += q.n_pairs_refined;
+    }
+    out->n_scanned = q.n_scanned;
+    out->n_cells = q.n_cells;
+    out->n_cand_spheres = q.n_cand_spheres;
+    out->n_mov = q.n_mov;
+    out->distance = q.distance;
+    out->moving_sphere = q.moving_sphere;
+    out->other_sphere = q.other_sphere;
+    out->other_slot = q.other_slot;
+    out->status = q.status;
+    out->n_candidates = q.n_candidates;
+    out->n_pairs_refined = q.n_pairs_refined;
+    if (q.status != ST_OK && err) *err = "contact query failed with status " + std::to_string(q.status);
+    return q.status;
+}
+
+int DeviceBox::translate(int slot, const double v[3], std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    k_translate<<<1, kQueryThreads, 0, s>>>(b, slot, v[0], v[1], v[2]);
+    prof_.translates += profiling_ ? 1 : 0;
+    if (!cuda_ok(cudaGetLastError(), err, "k_translate")) return ST_CUDA;
+    return ST_OK;
+}
+
+int DeviceBox::merge(int ms, int os, int mslot, int oslot, MergeResult *out, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    OutBuffers *ho = static_cast<OutBuffers *>(host_out_);
+    OutBuffers *dout = static_cast<OutBuffers *>(dev_out_);
+    if (profiling_) cudaEventRecord(static_cast<cudaEvent_t>(ev_[0]), s);
+    k_merge<<<1, kQueryThreads, sizeof(MergeSmem), s>>>(b, ms, os, mslot, oslot, &dout->merge);
+    if (profiling_) cudaEventRecord(static_cast<cudaEvent_t>(ev_[1]), s);
+    if (!cuda_ok(cudaGetLastError(), err, "k_merge")) return ST_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(s), err, "k_merge")) return ST_CUDA;
+    const MergeOut &m = ho->merge;
+    if (profiling_) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, static_cast<cudaEvent_t>(ev_[0]), static_cast<cudaEvent_t>(ev_[1]));
+        prof_.merges += 1;
+        prof_.merge_ms += ms;
+        if (m.merged) {
+            prof_.merged_spheres += m.n;
+            prof_.merge_pairs += m.n_pairs;
+        }
+    }
+    out->merged = m.merged;
+    out->status = m.status;
+    out->keep = m.keep;
+    out->removed = m.removed;
+    out->n = m.n;
+    out->n_pairs = m.n_pairs;
+    std::memcpy(out->fields, m.fields, sizeof(out->fields));
+    out->vol_pp = m.vol_pp;
+    out->maxradius = m.maxradius;
+    int st = m.status;
+    if (st == ST_OK) {
+        // a Verlet cell may have overflowed during the merge
+        int cs = check_status(err);
+        if (cs == ST_CAPACITY) {
+            DevBox &bb = *static_cast<DevBox *>(devbox_);
+            cs = rebuild_grid(bb.cell_cap * 2, err);
+        }
+        st = cs;
+    }
+    if (st != ST_OK && err && err->empty()) *err = "merge failed with status " + std::to_string(st);
+    return st;
+}
+
+int DeviceBox::set_fields(int slot, const double fields[21], unsigned mask, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    FieldUpdate u;
+    std::memcpy(u.v, fields, sizeof(u.v));
+    k_set_fields<<<1, 32, 0, s>>>(b, slot, u, mask);
+    if (!cuda_ok(cudaGetLastError(), err, "k_set_fields")) return ST_CUDA;
+    return ST_OK;
+}
+
+int DeviceBox::download(HostState *st, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
+    DevScalars sc;
+    st->ns = b.ns;
+    st->nslots = b.nslots;
+    st->n_div = b.n_div;
+    st->box_length = b.L;
+    st->sph.resize(9 * size_t(b.ns));
+    st->sph_slot.resize(size_t(b.ns));
+    st->agg.resize(21 * size_t(b.nslots));
+    st->agg_n.resize(size_t(b.nslots));
+    std::vector<int> off(size_t(b.nslots));
+    bool ok = true;
+    ok = ok && cuda_ok(cudaMemcpy(&sc, b.sc, sizeof(sc), cudaMemcpyDeviceToHost), err, "download");
+    ok = ok && cuda_ok(cudaMemcpy(st->sph.data(), b.sph, sizeof(double) * 9 * size_t(b.ns), cudaMemcpyDeviceToHost), err, "download");
+    ok = ok && cuda_ok(cudaMemcpy(st->sph_slot.data(), b.sph_slot, sizeof(int) * size_t(b.ns), cudaMemcpyDeviceToHost), err, "download");
+    ok = ok && cuda_ok(cudaMemcpy(st->agg.data(), b.agg, sizeof(double) * 21 * size_t(b.nslots), cudaMemcpyDeviceToHost), err, "download");
+    ok = ok && cuda_ok(cudaMemcpy(st->agg_n.data(), b.agg_n, sizeof(int) * size_t(b.nslots), cudaMemcpyDeviceToHost), err, "download");
+    ok = ok && cuda_ok(cudaMemcpy(off.data(), b.agg_off, sizeof(int) * size_t(b.nslots), cudaMemcpyDeviceToHost), err, "download");
+    if (!ok) return ST_CUDA;
+    std::vector<int> pool(size_t(b.pool_cap));
+    if (!cuda_ok(cudaMemcpy(pool.data(), b.pool_id[sc.pool_sel], sizeof(int) * size_t(b.pool_cap), cudaMemcpyDeviceToHost),
+                 err, "download"))
+        return ST_CUDA;
+    st->members.assign(size_t(b.nslots), {});
+    for (int a = 0; a < b.nslots; ++a) {
+        int n = st->agg_n[size_t(a)];
+        st->members[size_t(a)].assign(pool.begin() + off[size_t(a)], pool.begin() + off[size_t(a)] + n);
+    }
+    st->maxradius = sc.maxradius;
+    st->time = sc.time;
+    return ST_OK;
+}
+
+}  // namespace mcacg

@@ -1,0 +1,587 @@
+// Device-resident MCAC box and the block-level algorithms of the hot path.
+//
+// One thread block works on one box at a time. The same __device__ routines
+// serve the single-box kernels behind the C-ABI and the persistent batched
+// kernel (many boxes, one block each).
+//
+// Layout in HBM (per box):
+//   spheres     FP64 [9][ns] field-major (reference SoA, constants.hpp:34-45)
+//               + int owning slot
+//   aggregates  FP64 [21][nslots] field-major by stable slot; slot order is
+//               label order, so label = number of live slots before it
+//   members     per aggregate a contiguous segment of a pool: sphere id (int)
+//               and an FP32 (x, y, z, r) copy used by the screening passes;
+//               merges append keep++removed at the pool top, a compaction
+//               pass reclaims space
+//   Verlet grid n_div^3 cells of slot lists kept in ascending slot order
+//               (the reference's std::set<size_t> of labels, verlet.hpp:29)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <math_constants.h>
+
+#include "common.hpp"
+
+namespace mcacg {
+
+constexpr int kQueryThreads = 512;
+constexpr int kMaxCandidates = 1024;   // aggregates passing the bounding-sphere filter
+constexpr int kCellChunk = 2048;       // Verlet cells scanned per chunk
+constexpr int kMoveTile = 1024;        // moving spheres staged per pass
+constexpr int kMaxSurvivorsSmem = 1024;
+
+// Mutable per-box scalars, in device memory.
+struct DevScalars {
+    double maxradius;     // AggregatList::maxradius (monotone)
+    double time;          // physical time (device-driven runs)
+    int pool_top;         // first free pool entry
+    int pool_sel;         // which pool buffer is live
+    int n_alive;          // aggregates alive
+    int status;           // sticky error (Status)
+    int cell_overflow;    // a Verlet cell ran out of room
+    int survivors_overflow;
+    int pad[2];
+};
+
+struct DevBox {
+    double L;        // box_length
+    double step;     // double(n_div) / box_length
+    double margin;   // FP32 screening margin (absolute, metres)
+    int n_div;
+    int n_cells;
+    int ns;          // spheres
+    int nslots;      // aggregate slots (initial aggregate count)
+    int cell_cap;    // room per Verlet cell
+    int pool_cap;    // entries per pool buffer
+    int surv_cap;    // survivors in global scratch
+    int pair_cap;    // intra-aggregate contact pairs in global scratch
+    double *sph;     // [9][ns]
+    int *sph_slot;   // owning slot
+    double *agg;     // [21][nslots]
+    int *agg_n;      // members (0: dead slot)
+    int *agg_off;    // segment offset in the live pool
+    int *agg_cell;   // linear Verlet cell
+    int *pool_id[2];
+    float4 *pool_pos[2];
+    int *cell_n;     // [n_cells]
+    int *cell_items; // [n_cells][cell_cap]
+    DevScalars *sc;
+    // global scratch (one box handled by one block at a time)
+    int4 *surv;          // survivors: candidate, i, j, unused
+    double *surv_res;
+    int *pair_i, *pair_j;   // intra-aggregate contact pairs
+    double *pair_d;
+    int *pair_tmp_i, *pair_tmp_j;
+    double *pair_tmp_d;
+    int *row_cnt;        // [ns + 1]
+    double *work;        // [6][ns] per-sphere terms of the merge sums
+    int *counters;       // [8]
+};
+
+__device__ __forceinline__ double &A(const DevBox &b, int field, int slot) {
+    return b.agg[size_t(field) * size_t(b.nslots) + size_t(slot)];
+}
+__device__ __forceinline__ double &S(const DevBox &b, int field, int s) {
+    return b.sph[size_t(field) * size_t(b.ns) + size_t(s)];
+}
+
+// Result of a contact query.
+struct QueryOut {
+    double distance;
+    int moving_sphere;  // storage index or -1
+    int other_sphere;
+    int other_slot;
+    int status;
+    int n_candidates;     // aggregates passing the bounding-sphere filter
+    int n_pairs_refined;  // sphere pairs evaluated in FP64
+    int n_scanned;        // aggregates read from the Verlet cells
+    int n_cells;          // Verlet cells scanned
+    int n_cand_spheres;   // spheres of the candidates
+    int n_mov;            // spheres of the moving aggregate
+};
+
+// Merge result returned to the host (geometry; physics done by the caller).
+struct MergeOut {
+    int merged;       // 0: the spheres no longer touch
+    int status;
+    int keep;         // slot kept
+    int removed;      // slot removed
+    int n;            // spheres in the merged aggregate
+    int n_pairs;      // contact pairs found
+    double fields[21];
+    double vol_pp;
+    double maxradius;
+};
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ Vec3 agg_pos(const DevBox &b, int slot) {
+    return Vec3{A(b, AGG_X, slot), A(b, AGG_Y, slot), A(b, AGG_Z, slot)};
+}
+__device__ __forceinline__ Vec3 sph_pos(const DevBox &b, int s) {
+    return Vec3{S(b, SPH_X, s), S(b, SPH_Y, s), S(b, SPH_Z, s)};
+}
+__device__ __forceinline__ int cell_of(const DevBox &b, Vec3 p) {
+    int ix = verlet_coord(p.x, b.step), iy = verlet_coord(p.y, b.step), iz = verlet_coord(p.z, b.step);
+    ix = min(max(ix, 0), b.n_div - 1);
+    iy = min(max(iy, 0), b.n_div - 1);
+    iz = min(max(iz, 0), b.n_div - 1);
+    return (ix * b.n_div + iy) * b.n_div + iz;
+}
+
+// Order-preserving map of a double to an unsigned 64-bit key.
+__device__ __forceinline__ unsigned long long dkey(double v) {
+    unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(v));
+    return (u & 0x8000000000000000ULL) ? ~u : (u | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double dkey_inv(unsigned long long k) {
+    unsigned long long u = (k & 0x8000000000000000ULL) ? (k & 0x7fffffffffffffffULL) : ~k;
+    return __longlong_as_double(static_cast<long long>(u));
+}
+
+// Conservative FP32 capsule test: can a sphere at p2 (radius folded into
+// 'reach') come within 'reach' of the segment p1 -> p1 + dist*u under the
+// periodic box? False means the FP64 swept test of sweep_contact_distance
+// returns +inf for this pair. When the swept zone (|dist*u_l| + 2*reach)
+// approaches the box size several periodic images can matter and the test
+// always passes; otherwise only the image nearest to the segment centre can
+// be within reach and it is the one tested. 'reach' already holds the margin.
+struct Sweep32 {
+    float px, py, pz;     // segment start
+    float ux, uy, uz;     // unit direction
+    float dist;           // length
+    float cx, cy, cz;     // segment centre offset (dist*u/2)
+    float L, invL;
+    float zmax;           // max_l |dist * u_l|
+    float margin;
+};
+__device__ __forceinline__ bool capsule_hit(const Sweep32 &w, float qx, float qy, float qz, float reach) {
+    if (w.zmax + 2.f * reach + 8.f * w.margin >= w.L) return true;
+    float ex = qx - w.px, ey = qy - w.py, ez = qz - w.pz;
+    ex -= w.L * rintf((ex - w.cx) * w.invL);
+    ey -= w.L * rintf((ey - w.cy) * w.invL);
+    ez -= w.L * rintf((ez - w.cz) * w.invL);
+    float t = __fmaf_rn(ex, w.ux, __fmaf_rn(ey, w.uy, ez * w.uz));
+    t = fminf(fmaxf(t, 0.f), w.dist);
+    float dx = __fmaf_rn(-t, w.ux, ex), dy = __fmaf_rn(-t, w.uy, ey), dz = __fmaf_rn(-t, w.uz, ez);
+    float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz));
+    return d2 <= reach * reach;
+}
+
+// ------------------------------------------------------------ block scans
+template <int NT>
+__device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tmp, int &total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tmp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = (lane < NT / 32) ? warp_tmp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < NT / 32) warp_tmp[lane] = w;
+    }
+    __syncthreads();
+    int base = (wid > 0) ? warp_tmp[wid - 1] : 0;
+    total = warp_tmp[NT / 32 - 1];
+    __syncthreads();
+    return base + x - v;
+}
+
+// ------------------------------------------------------ shared memory plans
+struct QuerySmem {
+    int cell_prefix[kCellChunk + 1];
+    int cell_lin[kCellChunk];
+    double cand_db[kMaxCandidates];
+    int cand_flat[kMaxCandidates];
+    int cand_slot[kMaxCandidates];
+    int cand_order[kMaxCandidates];   // sorted position -> candidate
+    int cand_prefix[kMaxCandidates + 1];
+    unsigned long long best_res[kMaxCandidates];
+    unsigned long long best_ij[kMaxCandidates];
+    float4 mov[kMoveTile];
+    int4 surv[kMaxSurvivorsSmem];
+    double surv_res[kMaxSurvivorsSmem];
+    int warp_tmp[32];
+    float warp_f[32];
+    int n_cand;
+    int n_surv;
+    int found_source;
+    int flat_base;
+    int n_refined;
+    float mov_reach;
+    CellRange range;
+    QueryOut out;
+};
+
+// -------------------------------------------------------------- the query
+// AggregatList::distance_to_next_contact (aggregats/aggregat_list.cpp:447-532):
+//  1. neighbourhood = aggregates in the Verlet cells covering the swept
+//     bounding sphere (verlet.cpp:52-98), in the reference's scan order;
+//  2. bounding-sphere filter d_b < distance, ordered by (d_b, scan order)
+//     like the reference's std::multimap;
+//  3. every moving-sphere x candidate-sphere pair that the FP32 capsule
+//     screen keeps is refined with the exact FP64 swept test; each candidate
+//     keeps its first minimum in (moving index, other index) order;
+//  4. the candidates are walked in filter order with the reference's two
+//     early exits.
+// Must be called by all threads of the block.
+__device__ void block_query(const DevBox &b, int src, Vec3 dir, double dist, QuerySmem &sm) {
+    const int tid = threadIdx.x;
+    const int NT = kQueryThreads;
+    const DevScalars *sc = b.sc;
+    const int *pool_id = b.pool_id[sc->pool_sel];
+    const float4 *pool_pos = b.pool_pos[sc->pool_sel];
+
+    const Vec3 sp = agg_pos(b, src);
+    const double rmax_src = A(b, AGG_RMAX, src);
+    if (tid == 0) {
+        double mindist = rmax_src + sc->maxradius;
+        Vec3 vec{dist * dir.x, dist * dir.y, dist * dir.z};
+        sm.range = neighborhood_range(sp, vec, mindist, b.n_div, b.L);
+        sm.n_cand = 0;
+        sm.n_surv = 0;
+        sm.found_source = 0;
+        sm.flat_base = 0;
+        sm.n_refined = 0;
+        sm.out.distance = CUDART_INF;
+        sm.out.moving_sphere = -1;
+        sm.out.other_sphere = -1;
+        sm.out.other_slot = -1;
+        sm.out.status = ST_OK;
+        sm.out.n_candidates = 0;
+        sm.out.n_pairs_refined = 0;
+        sm.out.n_scanned = 0;
+        sm.out.n_cells = 0;
+        sm.out.n_cand_spheres = 0;
+        sm.out.n_mov = b.agg_n[src];
+    }
+    __syncthreads();
+
+    // FP32 sweep of the bounding sphere of the source.
+    Sweep32 w;
+    w.px = float(sp.x);
+    w.py = float(sp.y);
+    w.pz = float(sp.z);
+    w.ux = float(dir.x);
+    w.uy = float(dir.y);
+    w.uz = float(dir.z);
+    w.dist = float(dist);
+    w.cx = 0.5f * w.dist * w.ux;
+    w.cy = 0.5f * w.dist * w.uy;
+    w.cz = 0.5f * w.dist * w.uz;
+    w.L = float(b.L);
+    w.invL = 1.0f / w.L;
+    const float margin = float(b.margin + 1e-6 * dist);
+    w.zmax = fmaxf(fabsf(w.dist * w.ux), fmaxf(fabsf(w.dist * w.uy), fabsf(w.dist * w.uz)));
+    w.margin = margin;
+
+    // ---- 1+2: neighbourhood and bounding-sphere filter
+    const CellRange rg = sm.range;
+    const int nx = rg.hi[0] - rg.lo[0] + 1, ny = rg.hi[1] - rg.lo[1] + 1, nz = rg.hi[2] - rg.lo[2] + 1;
+    const int n_scan = nx * ny * nz;
+    for (int c0 = 0; c0 < n_scan; c0 += kCellChunk) {
+        const int nch = min(kCellChunk, n_scan - c0);
+        int cnt_local = 0;
+        // each thread owns a contiguous run of cells so the block scan keeps scan order
+        const int per = (nch + NT - 1) / NT;
+        const int my0 = tid * per;
+        for (int k = 0; k < per; ++k) {
+            int s = my0 + k;
+            if (s < nch) {
+                int g = c0 + s;
+                int a = g / (ny * nz), r = g % (ny * nz), bb = r / nz, c = r % nz;
+                int ii = periodic_cell(rg.lo[0] + a, b.n_div);
+                int jj = periodic_cell(rg.lo[1] + bb, b.n_div);
+                int kk = periodic_cell(rg.lo[2] + c, b.n_div);
+                int lin = (ii * b.n_div + jj) * b.n_div + kk;
+                sm.cell_lin[s] = lin;
+                cnt_local += b.cell_n[lin];
+            }
+        }
+        int total;
+        int base = block_exclusive_scan<kQueryThreads>(cnt_local, sm.warp_tmp, total);
+        {
+            int run = base;
+            for (int k = 0; k < per; ++k) {
+                int s = my0 + k;
+                if (s < nch) {
+                    sm.cell_prefix[s] = run;
+                    run += b.cell_n[sm.cell_lin[s]];
+                }
+            }
+            if (tid == 0) sm.cell_prefix[nch] = total;
+        }
+        __syncthreads();
+        for (int f = tid; f < total; f += NT) {
+            // cell of flat item f: last prefix <= f
+            int lo = 0, hi = nch - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (sm.cell_prefix[mid] <= f) lo = mid; else hi = mid - 1;
+            }
+            const int lin = sm.cell_lin[lo];
+            const int slot = b.cell_items[size_t(lin) * b.cell_cap + (f - sm.cell_prefix[lo])];
+            if (slot == src) {
+                sm.found_source = 1;
+                continue;
+            }
+            const double ox = A(b, AGG_X, slot), oy = A(b, AGG_Y, slot), oz = A(b, AGG_Z, slot);
+            const double orm = A(b, AGG_RMAX, slot);
+            if (!capsule_hit(w, float(ox), float(oy), float(oz), float(rmax_src + orm) + margin)) continue;
+            double db = sweep_contact_distance(sp, rmax_src, Vec3{ox, oy, oz}, orm, dir, dist, b.L);
+            if (db < dist) {
+                int k = atomicAdd(&sm.n_cand, 1);
+                if (k < kMaxCandidates) {
+                    sm.cand_db[k] = db;
+                    sm.cand_flat[k] = sm.flat_base + f;
+                    sm.cand_slot[k] = slot;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) sm.flat_base += total;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        sm.out.n_scanned = sm.flat_base;
+        sm.out.n_cells = n_scan;
+        sm.out.n_candidates = min(sm.n_cand, kMaxCandidates);
+    }
+    if (sm.n_cand > kMaxCandidates) {
+        if (tid == 0) sm.out.status = ST_CAPACITY;
+        __syncthreads();
+        return;
+    }
+    if (!sm.found_source) {
+        if (tid == 0) sm.out.status = ST_VERLET;  // "Aggregate not on the verlet list"
+        __syncthreads();
+        return;
+    }
+    const int nc = sm.n_cand;
+    if (nc == 0) return;
+
+    // order candidates by (d_b, scan position): rank sort
+    for (int k = tid; k < nc; k += NT) {
+        double dk = sm.cand_db[k];
+        int fk = sm.cand_flat[k];
+        int rank = 0;
+        for (int m = 0; m < nc; ++m) {
+            double dm = sm.cand_db[m];
+            rank += (dm < dk) || (dm == dk && sm.cand_flat[m] < fk);
+        }
+        sm.cand_order[rank] = k;
+    }
+    __syncthreads();
+    // per-candidate sphere prefix (in sorted order) and best keys
+    if (tid == 0) {
+        int run = 0;
+        for (int r = 0; r < nc; ++r) {
+            sm.cand_prefix[r] = run;
+            run += b.agg_n[sm.cand_slot[sm.cand_order[r]]];
+        }
+        sm.cand_prefix[nc] = run;
+    }
+    for (int r = tid; r < nc; r += NT) {
+        sm.best_res[r] = ~0ULL;
+        sm.best_ij[r] = ~0ULL;
+    }
+    __syncthreads();
+
+    // ---- 3: pair search
+    const int n_mov = b.agg_n[src];
+    const int off_m = b.agg_off[src];
+    const int n_other = sm.cand_prefix[nc];
+    if (tid == 0) sm.out.n_cand_spheres = n_other;
+    for (int t0 = 0; t0 < n_mov; t0 += kMoveTile) {
+        const int nt = min(kMoveTile, n_mov - t0);
+        float reach_local = 0.f;
+        for (int i = tid; i < nt; i += NT) {
+            float4 p = pool_pos[off_m + t0 + i];
+            sm.mov[i] = p;
+            // distance of this moving sphere from the source centre, + radius
+            float ex = p.x - w.px, ey = p.y - w.py, ez = p.z - w.pz;
+            ex -= w.L * rintf(ex * w.invL);
+            ey -= w.L * rintf(ey * w.invL);
+            ez -= w.L * rintf(ez * w.invL);
+            reach_local = fmaxf(reach_local, sqrtf(ex * ex + ey * ey + ez * ez) + p.w);
+        }
+        // block max of the moving tile's extent
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) reach_local = fmaxf(reach_local, __shfl_xor_sync(0xffffffffu, reach_local, o));
+        if ((tid & 31) == 0) sm.warp_f[tid >> 5] = reach_local;
+        __syncthreads();
+        if (tid == 0) {
+            float m = 0.f;
+            for (int k = 0; k < NT / 32; ++k) m = fmaxf(m, sm.warp_f[k]);
+            sm.mov_reach = m;
+        }
+        __syncthreads();
+        const float mov_reach = sm.mov_reach + margin;
+        for (int f = tid; f < n_other; f += NT) {
+            int lo = 0, hi = nc - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (sm.cand_prefix[mid] <= f) lo = mid; else hi = mid - 1;
+            }
+            const int r = lo;
+            const int cslot = sm.cand_slot[sm.cand_order[r]];
+            const int jl = f - sm.cand_prefix[r];
+            const int pj = b.agg_off[cslot] + jl;
+            const float4 q = pool_pos[pj];
+            // can any moving sphere reach this one?
+            if (!capsule_hit(w, q.x, q.y, q.z, mov_reach + q.w)) continue;
+            Sweep32 wi = w;
+            for (int i = 0; i < nt; ++i) {
+                const float4 p = sm.mov[i];
+                wi.px = p.x;
+                wi.py = p.y;
+                wi.pz = p.z;
+                if (!capsule_hit(wi, q.x, q.y, q.z, p.w + q.w + margin)) continue;
+                const int si = pool_id[off_m + t0 + i];
+                const int sj = pool_id[pj];
+                double res = sweep_contact_distance(sph_pos(b, si), S(b, SPH_R, si), sph_pos(b, sj),
+                                                    S(b, SPH_R, sj), dir, dist, b.L);
+                atomicAdd(&sm.n_refined, 1);
+                if (!(res < CUDART_INF)) continue;
+                unsigned long long key = dkey(res);
+                atomicMin(&sm.best_res[r], key);
+                int k = atomicAdd(&sm.n_surv, 1);
+                int4 rec = make_int4(r, t0 + i, jl, 0);
+                if (k < kMaxSurvivorsSmem) {
+                    sm.surv[k] = rec;
+                    sm.surv_res[k] = res;
+                } else if (k - kMaxSurvivorsSmem < b.surv_cap) {
+                    b.surv[k - kMaxSurvivorsSmem] = rec;
+                    b.surv_res[k - kMaxSurvivorsSmem] = res;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    const int n_surv = sm.n_surv;
+    if (n_surv > kMaxSurvivorsSmem + b.surv_cap) {
+        if (tid == 0) sm.out.status = ST_CAPACITY;
+        __syncthreads();
+        return;
+    }
+    // lexicographic (moving index, other index) among each candidate's minima
+    for (int k = tid; k < n_surv; k += NT) {
+        int4 rec = (k < kMaxSurvivorsSmem) ? sm.surv[k] : b.surv[k - kMaxSurvivorsSmem];
+        double res = (k < kMaxSurvivorsSmem) ? sm.surv_res[k] : b.surv_res[k - kMaxSurvivorsSmem];
+        if (dkey(res) == sm.best_res[rec.x]) {
+            unsigned long long ij = (static_cast<unsigned long long>(rec.y) << 32) | static_cast<unsigned>(rec.z);
+            atomicMin(&sm.best_ij[rec.x], ij);
+        }
+    }
+    __syncthreads();
+
+    // ---- 4: the reference's ordered walk with early exits
+    if (tid == 0) {
+        double best = CUDART_INF;
+        int best_r = -1;
+        for (int r = 0; r < nc; ++r) {
+            if (best <= 0.) break;
+            if (best < sm.cand_db[sm.cand_order[r]]) break;
+            if (sm.best_res[r] == ~0ULL) continue;  // no finite pair: +inf never wins
+            double res = dkey_inv(sm.best_res[r]);
+            if (res < best) {
+                best = res;
+                best_r = r;
+            }
+        }
+        sm.out.distance = best;
+        if (best_r >= 0) {
+            unsigned long long ij = sm.best_ij[best_r];
+            int i = int(ij >> 32), j = int(ij & 0xffffffffu);
+            int cslot = sm.cand_slot[sm.cand_order[best_r]];
+            sm.out.moving_sphere = pool_id[off_m + i];
+            sm.out.other_sphere = pool_id[b.agg_off[cslot] + j];
+            sm.out.other_slot = cslot;
+        }
+        sm.out.n_pairs_refined = sm.n_refined;
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------- Verlet grid
+// Remove / insert a slot in a cell kept in ascending order (one thread).
+__device__ __forceinline__ void cell_remove(const DevBox &b, int cell, int slot) {
+    int n = b.cell_n[cell];
+    int *items = b.cell_items + size_t(cell) * b.cell_cap;
+    int k = 0;
+    while (k < n && items[k] != slot) ++k;
+    if (k == n) return;
+    for (; k + 1 < n; ++k) items[k] = items[k + 1];
+    b.cell_n[cell] = n - 1;
+}
+__device__ __forceinline__ void cell_insert(const DevBox &b, int cell, int slot) {
+    int n = b.cell_n[cell];
+    if (n >= b.cell_cap) {
+        b.sc->cell_overflow = 1;
+        b.sc->status = ST_CAPACITY;
+        return;
+    }
+    int *items = b.cell_items + size_t(cell) * b.cell_cap;
+    int k = n;
+    while (k > 0 && items[k - 1] > slot) {
+        items[k] = items[k - 1];
+        --k;
+    }
+    items[k] = slot;
+    b.cell_n[cell] = n + 1;
+}
+// Aggregate::update_verlet (aggregat.cpp:706-717) for a new position.
+__device__ __forceinline__ void regrid(const DevBox &b, int slot) {
+    int c = cell_of(b, agg_pos(b, slot));
+    int old = b.agg_cell[slot];
+    if (c != old) {
+        cell_remove(b, old, slot);
+        cell_insert(b, c, slot);
+        b.agg_cell[slot] = c;
+    }
+}
+
+// --------------------------------------------------------------- translate
+// Aggregate::translate (aggregats/aggregat.cpp:148-161).
+__device__ void block_translate(const DevBox &b, int slot, Vec3 v, double *refpos_sm) {
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        double x = periodic_position(A(b, AGG_X, slot) + v.x, b.L);
+        double y = periodic_position(A(b, AGG_Y, slot) + v.y, b.L);
+        double z = periodic_position(A(b, AGG_Z, slot) + v.z, b.L);
+        A(b, AGG_X, slot) = x;
+        A(b, AGG_Y, slot) = y;
+        A(b, AGG_Z, slot) = z;
+        refpos_sm[0] = x - A(b, AGG_RX, slot);
+        refpos_sm[1] = y - A(b, AGG_RY, slot);
+        refpos_sm[2] = z - A(b, AGG_RZ, slot);
+        regrid(b, slot);
+    }
+    __syncthreads();
+    const double rx = refpos_sm[0], ry = refpos_sm[1], rz = refpos_sm[2];
+    const int n = b.agg_n[slot], off = b.agg_off[slot];
+    int *pool_id = b.pool_id[b.sc->pool_sel];
+    float4 *pool_pos = b.pool_pos[b.sc->pool_sel];
+    for (int k = tid; k < n; k += blockDim.x) {
+        int s = pool_id[off + k];
+        double x = rx + S(b, SPH_RX, s);
+        double y = ry + S(b, SPH_RY, s);
+        double z = rz + S(b, SPH_RZ, s);
+        S(b, SPH_X, s) = x;
+        S(b, SPH_Y, s) = y;
+        S(b, SPH_Z, s) = z;
+        pool_pos[off + k] = make_float4(float(x), float(y), float(z), float(S(b, SPH_R, s)));
+    }
+    __syncthreads();
+}
+
+}  // namespace mcacg

@@ -1,0 +1,360 @@
+// extern "C" entry points of include/mcacg.h. No exception crosses this
+// boundary: every call returns a status code and records a message for
+// mcacg_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <exception>
+#include <fstream>
+#include <memory>
+#include <new>
+#include <sstream>
+#include <string>
+
+#include "../../include/mcacg.h"
+#include "common.hpp"
+#include "host_box.hpp"
+#include "physics.hpp"
+
+struct mcacg_box {
+    std::unique_ptr<mcacg::HostBox> impl;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+template <class F>
+int guarded(F &&f) {
+    try {
+        g_last_error.clear();
+        return f();
+    } catch (const std::bad_alloc &) {
+        return fail(mcacg::ST_CAPACITY, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(mcacg::ST_UNKNOWN, e.what());
+    } catch (...) {
+        return fail(mcacg::ST_UNKNOWN, "unknown error");
+    }
+}
+
+int finish(int rc, const std::string &err) {
+    if (rc != mcacg::ST_OK) g_last_error = err.empty() ? "error " + std::to_string(rc) : err;
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcacg_abi_version(void) { return MCACG_ABI_VERSION; }
+
+const char *mcacg_last_error(void) { return g_last_error.c_str(); }
+
+int mcacg_device_count(int *count) {
+    return guarded([&] {
+        if (!count) return fail(MCACG_ERR_BAD_ARGUMENT, "null count");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+        cudaGetLastError();
+        *count = n;
+        return 0;
+    });
+}
+
+int mcacg_params_default(mcacg_params *params) {
+    return guarded([&] {
+        if (!params) return fail(MCACG_ERR_BAD_ARGUMENT, "null params");
+        mcacg::params_defaults(params);
+        mcacg::params_derive(params);
+        return 0;
+    });
+}
+
+int mcacg_params_from_ini_text(const char *text, mcacg_params *params) {
+    return guarded([&] {
+        if (!text || !params) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::string err;
+        int rc = mcacg::params_from_ini(mcacg::parse_ini_text(text), params, &err);
+        return finish(rc, err);
+    });
+}
+
+int mcacg_params_from_ini(const char *path, mcacg_params *params) {
+    return guarded([&] {
+        if (!path || !params) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::ifstream is(path);
+        if (!is) return fail(mcacg::ST_INPUT, std::string("File does not exist: ") + path);
+        std::stringstream ss;
+        ss << is.rdbuf();
+        std::string err;
+        int rc = mcacg::params_from_ini(mcacg::parse_ini_text(ss.str()), params, &err);
+        return finish(rc, err);
+    });
+}
+
+int mcacg_state_init_random(const mcacg_params *params, mcacg_state *state) {
+    return guarded([&] {
+        if (!params || !state || !state->spheres || !state->sphere_label || !state->aggregates ||
+            !state->n_spheres_per_aggregate || !state->members)
+            return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        if (state->n_spheres < params->n_monomeres || state->n_aggregates < params->n_monomeres)
+            return fail(MCACG_ERR_BAD_ARGUMENT, "state buffers smaller than n_monomeres");
+        mcacg::HostState st;
+        std::string err;
+        int rc = mcacg::init_random_state(*params, &st, &err);
+        if (rc != 0) return finish(rc, err);
+        state->n_spheres = st.ns;
+        state->n_aggregates = st.nslots;
+        state->n_verlet_divisions = st.n_div;
+        state->box_length = st.box_length;
+        state->maxradius = st.maxradius;
+        state->time = st.time;
+        std::copy(st.sph.begin(), st.sph.end(), state->spheres);
+        for (int s = 0; s < st.ns; ++s) state->sphere_label[s] = st.sph_slot[size_t(s)];
+        std::copy(st.agg.begin(), st.agg.end(), state->aggregates);
+        int64_t off = 0;
+        for (int a = 0; a < st.nslots; ++a) {
+            state->n_spheres_per_aggregate[a] = int64_t(st.members[size_t(a)].size());
+            for (int m : st.members[size_t(a)]) state->members[off++] = m;
+        }
+        return 0;
+    });
+}
+
+int mcacg_box_create(const mcacg_params *params, mcacg_box **box) {
+    return guarded([&] {
+        if (!params || !box) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *box = nullptr;
+        std::unique_ptr<mcacg_box> b(new mcacg_box());
+        std::string err;
+        int rc = mcacg::HostBox::create_random(*params, nullptr, &b->impl, &err);
+        if (rc != 0) return finish(rc, err);
+        *box = b.release();
+        return 0;
+    });
+}
+
+int mcacg_box_create_from_state(const mcacg_params *params, const mcacg_state *state, mcacg_box **box) {
+    return guarded([&] {
+        if (!params || !state || !box) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *box = nullptr;
+        std::unique_ptr<mcacg_box> b(new mcacg_box());
+        std::string err;
+        int rc = mcacg::HostBox::create_from_state(*params, *state, nullptr, &b->impl, &err);
+        if (rc != 0) return finish(rc, err);
+        *box = b.release();
+        return 0;
+    });
+}
+
+int mcacg_box_destroy(mcacg_box *box) {
+    return guarded([&] {
+        delete box;
+        return 0;
+    });
+}
+
+int mcacg_box_set_stream(mcacg_box *box, void *cuda_stream) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        return box->impl->device().set_stream(cuda_stream);
+    });
+}
+
+int mcacg_box_sizes(const mcacg_box *box, int64_t *n_spheres, int64_t *n_aggregates) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        if (n_spheres) *n_spheres = box->impl->n_spheres();
+        if (n_aggregates) *n_aggregates = box->impl->size();
+        return 0;
+    });
+}
+
+int mcacg_box_store_state(mcacg_box *box, mcacg_state *state) {
+    return guarded([&] {
+        if (!box || !state) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::string err;
+        return finish(box->impl->store(state, &err), err);
+    });
+}
+
+int mcacg_box_get_time(const mcacg_box *box, double *time) {
+    return guarded([&] {
+        if (!box || !time) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *time = box->impl->time();
+        return 0;
+    });
+}
+
+int mcacg_box_set_profiling(mcacg_box *box, int enable) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        box->impl->device().set_profiling(enable != 0);
+        return 0;
+    });
+}
+
+int mcacg_box_take_profile(mcacg_box *box, mcacg_profile *out) {
+    return guarded([&] {
+        if (!box || !out) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        mcacg::Profile p = box->impl->device().take_profile();
+        out->queries = p.queries;
+        out->merges = p.merges;
+        out->translates = p.translates;
+        out->query_ms = p.query_ms;
+        out->merge_ms = p.merge_ms;
+        out->mov_spheres = p.mov_spheres;
+        out->scanned = p.scanned;
+        out->cells = p.cells;
+        out->candidates = p.candidates;
+        out->cand_spheres = p.cand_spheres;
+        out->refined = p.refined;
+        out->merged_spheres = p.merged_spheres;
+        out->merge_pairs = p.merge_pairs;
+        return 0;
+    });
+}
+
+int mcacg_box_set_time(mcacg_box *box, double time) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        box->impl->set_time(time);
+        return 0;
+    });
+}
+
+int mcacg_distance_to_next_contact(mcacg_box *box, int64_t source, const double direction[3], double distance,
+                                   mcacg_contact *out) {
+    return guarded([&] {
+        if (!box || !direction || !out) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::string err;
+        return finish(box->impl->distance_to_next_contact(source, direction, distance, out, &err), err);
+    });
+}
+
+int mcacg_translate(mcacg_box *box, int64_t label, const double vector[3]) {
+    return guarded([&] {
+        if (!box || !vector) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::string err;
+        return finish(box->impl->translate(label, vector, &err), err);
+    });
+}
+
+int mcacg_time_forward(mcacg_box *box, int64_t label, double deltatemps) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        std::string err;
+        return finish(box->impl->time_forward(label, deltatemps, &err), err);
+    });
+}
+
+int mcacg_merge(mcacg_box *box, const mcacg_contact *contact, int32_t *merged) {
+    return guarded([&] {
+        if (!box || !contact || !merged) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::string err;
+        return finish(box->impl->merge(*contact, merged, &err), err);
+    });
+}
+
+int mcacg_sort_time_steps(mcacg_box *box, double factor) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        box->impl->sort_time_steps(factor);
+        return 0;
+    });
+}
+
+int mcacg_pick_random(mcacg_box *box, int64_t *label) {
+    return guarded([&] {
+        if (!box || !label) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *label = box->impl->pick_random();
+        return 0;
+    });
+}
+
+int mcacg_get_time_step(const mcacg_box *box, double max, double *deltatemps) {
+    return guarded([&] {
+        if (!box || !deltatemps) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *deltatemps = box->impl->get_time_step(max);
+        return 0;
+    });
+}
+
+int mcacg_get_max_time_step(const mcacg_box *box, double *max) {
+    return guarded([&] {
+        if (!box || !max) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *max = box->impl->max_time_step();
+        return 0;
+    });
+}
+
+int mcacg_refresh(mcacg_box *box) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        box->impl->refresh();
+        return 0;
+    });
+}
+
+int mcacg_size(const mcacg_box *box, int64_t *n_aggregates) {
+    return guarded([&] {
+        if (!box || !n_aggregates) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *n_aggregates = box->impl->size();
+        return 0;
+    });
+}
+
+int mcacg_get_avg_npp(const mcacg_box *box, double *avg_npp) {
+    return guarded([&] {
+        if (!box || !avg_npp) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *avg_npp = box->impl->avg_npp();
+        return 0;
+    });
+}
+
+int mcacg_get_total_volume(const mcacg_box *box, double *volume) {
+    return guarded([&] {
+        if (!box || !volume) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *volume = box->impl->total_volume();
+        return 0;
+    });
+}
+
+int mcacg_get_total_surface(const mcacg_box *box, double *surface) {
+    return guarded([&] {
+        if (!box || !surface) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *surface = box->impl->total_surface();
+        return 0;
+    });
+}
+
+int mcacg_get_aggregate(const mcacg_box *box, int64_t label, double fields[21], int64_t *n_spheres) {
+    return guarded([&] {
+        if (!box || !fields) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        if (label < 0 || label >= box->impl->size()) return fail(MCACG_ERR_BAD_ARGUMENT, "label out of range");
+        box->impl->fields(label, fields);
+        if (n_spheres) *n_spheres = box->impl->n_spheres_of(label);
+        return 0;
+    });
+}
+
+int mcacg_calcul(mcacg_box *box, const mcacg_run_opts *opts, mcacg_run_stats *stats) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        mcacg_run_opts o{};
+        if (opts) o = *opts;
+        mcacg_run_stats s{};
+        std::string err;
+        int rc = box->impl->calcul(o, &s, &err);
+        if (stats) *stats = s;
+        return finish(rc, err);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,190 @@
+// Shared definitions for the MCAC GB300 library: field layout, status codes,
+// and the exact FP64 geometry used by both the host mirror and the kernels.
+//
+// Every FP64 routine here follows the operation order of the reference
+// (giraldeau/MCAC) so results are bit-identical. Both compilers must run with
+// FP contraction off (-ffp-contract=off on the host, -fmad=false on the
+// device); build() passes those flags.
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <limits>
+
+#if defined(__CUDACC__)
+#define MCACG_HD __host__ __device__ __forceinline__
+#define MCACG_UNROLL _Pragma("unroll")
+#else
+#define MCACG_HD inline
+#define MCACG_UNROLL
+#endif
+
+namespace mcacg {
+
+// Sphere storage columns (include/constants.hpp:34-45 of the reference).
+enum SphereField : int {
+    SPH_X, SPH_Y, SPH_Z, SPH_R, SPH_VOLUME, SPH_SURFACE, SPH_RX, SPH_RY, SPH_RZ, SPH_NFIELDS
+};
+// Aggregate storage columns (include/constants.hpp:46-69 of the reference).
+enum AggField : int {
+    AGG_RG, AGG_F_AGG, AGG_LPM, AGG_TIME_STEP, AGG_RMAX, AGG_VOLUME, AGG_SURFACE,
+    AGG_X, AGG_Y, AGG_Z, AGG_RX, AGG_RY, AGG_RZ, AGG_TIME, AGG_DP, AGG_DG_OVER_DP,
+    AGG_OVERLAPPING, AGG_COORDINATION_NUMBER, AGG_ELECTRIC_CHARGE, AGG_D_M, AGG_CH_RATIO,
+    AGG_NFIELDS
+};
+// Volume/surface methods (include/constants.hpp:113-120).
+enum VolSurf : int { VS_CAPS = 0, VS_SBL = 1, VS_ARVO = 2, VS_ALPHAS = 3, VS_NONE = 4, VS_INVALID = 5 };
+
+// Physical constants (include/constants.hpp:123-139).
+constexpr double kBoltzmann = 1.38066E-23;
+constexpr double kFluidMeanFreePathRef = 66.5E-9;
+constexpr double kTemperatureRef = 293.15;
+constexpr double kSutherland = 110;
+constexpr double kPressureRef = 101300;
+constexpr double kViscosityRef = 18.203E-6;
+constexpr double kContactEpsilon = 1e-28;
+constexpr double kCoordinationEpsilon = 1e-10;
+
+MCACG_HD double pi_value() { return 3.141592653589793115997963468544185161590576171875; }
+
+// --- periodic helpers (include/physical_model/physical_model.hpp:99-126) ---
+MCACG_HD double periodic_distance(double d, double dim) {
+    double half = 0.5 * dim;
+    while (d < -half) d += dim;
+    while (d >= half) d -= dim;
+    return d;
+}
+MCACG_HD double periodic_position(double p, double dim) {
+    while (p < 0) p += dim;
+    while (p >= dim) p -= dim;
+    return p;
+}
+MCACG_HD int periodic_cell(int i, int n) {
+    while (i < 0) i += n;
+    while (i >= n) i -= n;
+    return i;
+}
+MCACG_HD double dmin(double a, double b) { return (b < a) ? b : a; }  // std::min
+MCACG_HD double dmax(double a, double b) { return (a < b) ? b : a; }  // std::max
+
+struct Vec3 {
+    double x, y, z;
+};
+
+// Periodic squared distance (spheres/sphere_distances.cpp:68-76).
+MCACG_HD double periodic_distance_2(Vec3 a, Vec3 b, double L) {
+    double dx = periodic_distance(a.x - b.x, L);
+    double dy = periodic_distance(a.y - b.y, L);
+    double dz = periodic_distance(a.z - b.z, L);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// Sphere-sphere contact test with the 1e-28 tolerance
+// (spheres/sphere_distances.cpp:81-90).
+MCACG_HD bool spheres_in_contact(Vec3 p1, double r1, Vec3 p2, double r2, double L) {
+    double d2 = periodic_distance_2(p1, p2, L);
+    double s = r1 + r2;
+    return d2 - s * s <= kContactEpsilon;
+}
+
+// Travel distance along 'dir' before sphere 1 touches sphere 2, +inf when
+// they do not meet within 'dist' -- the swept test of
+// spheres/sphere_contact.cpp:47-125, operation for operation. Returns 0 when
+// the spheres already touch. 'dir' is a unit vector.
+MCACG_HD double sweep_contact_distance(Vec3 p1, double r1, Vec3 p2, double r2, Vec3 dir, double dist,
+                                       double L) {
+    const double dc = r1 + r2;
+    const double dc2 = dc * dc;
+    if (periodic_distance_2(p1, p2, L) <= dc2) return 0.0;
+    const double tx = dir.x * dist, ty = dir.y * dist, tz = dir.z * dist;
+    double q[3], zone[3];
+    int nper[3];
+    const double pa[3] = {p1.x, p1.y, p1.z};
+    const double pb[3] = {p2.x, p2.y, p2.z};
+    const double td[3] = {tx, ty, tz};
+MCACG_UNROLL
+    for (int l = 0; l < 3; ++l) {
+        double moved = pa[l] + td[l];
+        double base = dmin(pa[l], moved) - dc;
+        double end = dmax(pa[l], moved) + dc;
+        zone[l] = end - base;
+        double w = fmod(pb[l] - base, L);
+        if (w < 0) w += L;
+        q[l] = w + base;
+        nper[l] = static_cast<int>(floor(zone[l] / L));
+    }
+    double res = std::numeric_limits<double>::infinity();
+    for (int i = 0; i <= nper[0]; i++) {
+        for (int j = 0; j <= nper[1]; j++) {
+            for (int k = 0; k <= nper[2]; k++) {
+                double p3x = q[0] + i * L, p3y = q[1] + j * L, p3z = q[2] + k * L;
+                double dx = p3x - p1.x, dy = p3y - p1.y, dz = p3z - p1.z;
+                if (fabs(dx) > zone[0]) continue;
+                if (fabs(dy) > zone[1]) continue;
+                if (fabs(dz) > zone[2]) continue;
+                double proj = dx * dir.x + dy * dir.y + dz * dir.z;
+                if (proj < 0) continue;
+                double ex = (p1.x + tx) - p3x, ey = (p1.y + ty) - p3y, ez = (p1.z + tz) - p3z;
+                bool end_contact = ex * ex + ey * ey + ez * ez <= dc2;
+                if ((!end_contact) && dist < proj) continue;
+                double cx = dy * dir.z - dz * dir.y;
+                double cy = dz * dir.x - dx * dir.z;
+                double cz = dx * dir.y - dy * dir.x;
+                double axis = cx * cx + cy * cy + cz * cz;
+                if (axis > dc2) continue;
+                res = dmin(res, proj - sqrt(dc2 - axis));
+            }
+        }
+    }
+    return res;
+}
+
+// Verlet cell of a position (aggregats/aggregat.cpp:699-705): step is
+// double(n_div) / box_length.
+MCACG_HD int verlet_coord(double x, double step) { return static_cast<int>(floor(x * step)); }
+
+// Bounds of Verlet::get_neighborhood (verlet/verlet.cpp:52-78): inclusive cell
+// ranges [lo, hi] per axis, before periodic wrapping.
+struct CellRange {
+    int lo[3], hi[3];
+};
+MCACG_HD CellRange neighborhood_range(Vec3 src, Vec3 vec, double distance, int n_div, double width) {
+    const double s[3] = {src.x, src.y, src.z};
+    const double v[3] = {vec.x, vec.y, vec.z};
+    CellRange r;
+MCACG_UNROLL
+    for (int l = 0; l < 3; ++l) {
+        double p = s[l] + distance + dmax(v[l], 0.);
+        double m = s[l] - distance + dmin(v[l], 0.);
+        r.lo[l] = static_cast<int>(floor(static_cast<double>(n_div) * m / width));
+        r.hi[l] = static_cast<int>(floor(static_cast<double>(n_div) * p / width) + 1);
+        if (r.hi[l] - r.lo[l] >= n_div) {
+            r.lo[l] = 0;
+            r.hi[l] = n_div - 1;
+        }
+    }
+    return r;
+}
+
+// Status codes: 0-11 mirror the reference's ErrorCodes
+// (include/constants.hpp:70-83); 100+ are this library's own.
+enum Status : int {
+    ST_OK = 0,
+    ST_UNKNOWN = 1,
+    ST_IO = 2,
+    ST_VERLET = 3,
+    ST_INPUT = 4,
+    ST_ABANDON = 5,
+    ST_TOO_DENSE = 6,
+    ST_SBL = 7,
+    ST_VOL_SURF = 8,
+    ST_MERGE = 9,
+    ST_ARVO = 10,
+    ST_INTERPOTENTIAL = 11,
+    ST_CUDA = 100,
+    ST_CAPACITY = 101,
+    ST_TIMEOUT = 102,
+    ST_BAD_ARGUMENT = 103,
+    ST_NO_DEVICE = 104,
+};
+
+}  // namespace mcacg

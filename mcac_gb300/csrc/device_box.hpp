@@ -1,0 +1,94 @@
+// Host-side handle of one box resident on the GPU (allocation, upload,
+// download, launches of the single-box kernels).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace mcacg {
+
+struct QueryOut;
+struct MergeOut;
+
+// Complete box state in host memory, by stable aggregate slot.
+struct HostState {
+    int n_div = 10;
+    double box_length = 0;
+    double maxradius = 0;
+    double time = 0;
+    int ns = 0;
+    int nslots = 0;
+    std::vector<double> sph;          // [9][ns]
+    std::vector<int> sph_slot;        // [ns]
+    std::vector<double> agg;          // [21][nslots]
+    std::vector<int> agg_n;           // [nslots], 0 for a dead slot
+    std::vector<std::vector<int>> members;  // per slot, list order
+};
+
+struct QueryResult {
+    double distance;
+    int moving_sphere, other_sphere, other_slot;
+    int status;
+    int n_candidates;
+    int n_pairs_refined;
+    int n_scanned, n_cells, n_cand_spheres, n_mov;
+};
+
+// Per-kernel timings (CUDA events on the box's stream) and the counts the
+// algorithmic-byte model of the contact query uses.
+struct Profile {
+    int64_t queries = 0, merges = 0, translates = 0;
+    double query_ms = 0, merge_ms = 0;
+    int64_t mov_spheres = 0, scanned = 0, cells = 0, candidates = 0, cand_spheres = 0, refined = 0;
+    int64_t merged_spheres = 0, merge_pairs = 0;
+};
+
+struct MergeResult {
+    int merged, status, keep, removed, n, n_pairs;
+    double fields[21];
+    double vol_pp;
+    double maxradius;
+};
+
+class DeviceBox {
+  public:
+    // Uploads 'st' to the current device. Returns a status code.
+    static int create(const HostState &st, void *stream, DeviceBox **out, std::string *err);
+    ~DeviceBox();
+    DeviceBox(const DeviceBox &) = delete;
+    DeviceBox &operator=(const DeviceBox &) = delete;
+
+    int set_stream(void *stream);
+    void *stream() const { return stream_; }
+    int query(int src_slot, const double dir[3], double dist, QueryResult *out, std::string *err);
+    int translate(int slot, const double v[3], std::string *err);
+    int merge(int ms, int os, int mslot, int oslot, MergeResult *out, std::string *err);
+    // Writes aggregate fields of one slot: fields[f] for every f with bit f of mask set.
+    int set_fields(int slot, const double fields[21], unsigned mask, std::string *err);
+    // Copies the whole state back (spheres, aggregates, members, scalars).
+    int download(HostState *st, std::string *err);
+    // Rebuilds the Verlet grid from the aggregate positions with 'cap' rooms per cell.
+    int rebuild_grid(int cap, std::string *err);
+    int sync(std::string *err);
+    void set_profiling(bool on);
+    Profile take_profile();
+    int ns() const { return ns_; }
+    int nslots() const { return nslots_; }
+    void *devbox_ptr() { return devbox_; }  // DevBox* (opaque to host code)
+
+  private:
+    DeviceBox() = default;
+    int check_status(std::string *err);
+    void *devbox_ = nullptr;  // DevBox (host copy with device pointers)
+    void *stream_ = nullptr;
+    bool own_stream_ = false;
+    int ns_ = 0, nslots_ = 0;
+    std::vector<void *> allocations_;
+    void *host_out_ = nullptr;  // mapped pinned result buffer
+    void *dev_out_ = nullptr;
+    bool profiling_ = false;
+    void *ev_[2] = {nullptr, nullptr};
+    Profile prof_;
+};
+
+}  // namespace mcacg

@@ -1,0 +1,625 @@
+// Host side of one box; see host_box.hpp. Compiled with -ffp-contract=off.
+#include "host_box.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+
+#include "common.hpp"
+#include "physics.hpp"
+
+namespace mcacg {
+
+namespace {
+
+inline double &SF(HostState &st, int field, int s) { return st.sph[size_t(field) * size_t(st.ns) + size_t(s)]; }
+inline double SF(const HostState &st, int field, int s) { return st.sph[size_t(field) * size_t(st.ns) + size_t(s)]; }
+inline double &AF(HostState &st, int field, int a) { return st.agg[size_t(field) * size_t(st.nslots) + size_t(a)]; }
+
+// Spatial hash used by the free-space test of the initial placement.
+struct PlacementGrid {
+    double h = 1, L = 1;
+    int G = 1;
+    std::vector<int> head, next;
+    void init(double box, double cell, int n) {
+        L = box;
+        G = std::max(1, std::min(512, int(box / cell)));
+        h = box / G;
+        head.assign(size_t(G) * G * G, -1);
+        next.assign(size_t(n), -1);
+    }
+    int coord(double x) const { return std::min(std::max(int(std::floor(x / h)), 0), G - 1); }
+    void insert(int id, const double p[3]) {
+        size_t c = (size_t(coord(p[0])) * G + coord(p[1])) * G + coord(p[2]);
+        next[size_t(id)] = head[c];
+        head[c] = id;
+    }
+    template <class F>
+    bool any(const double p[3], double reach, F &&f) const {
+        int lo[3], cnt[3];
+        for (int l = 0; l < 3; ++l) {
+            lo[l] = int(std::floor((p[l] - reach) / h));
+            int hi = int(std::floor((p[l] + reach) / h));
+            cnt[l] = hi - lo[l] + 1;
+            if (cnt[l] >= G) {
+                lo[l] = 0;
+                cnt[l] = G;
+            }
+        }
+        for (int a = 0; a < cnt[0]; ++a)
+            for (int b = 0; b < cnt[1]; ++b)
+                for (int c = 0; c < cnt[2]; ++c) {
+                    int i = periodic_cell(lo[0] + a, G), j = periodic_cell(lo[1] + b, G), k = periodic_cell(lo[2] + c, G);
+                    for (int id = head[(size_t(i) * G + j) * G + k]; id >= 0; id = next[size_t(id)])
+                        if (f(id)) return true;
+                }
+        return false;
+    }
+};
+
+}  // namespace
+
+int host_update_aggregate(const mcacg_params &p, const HostState &st, const std::vector<int> &members,
+                          double fields[21], double *maxradius) {
+    const int n = int(members.size());
+    // update_distances_and_overlapping (aggregat.cpp:719-764)
+    double overlapping = 0.0, coordination = 0.0;
+    int intersections = 0;
+    for (int i = 0; i < n; i++) {
+        int si = members[size_t(i)];
+        for (int j = i + 1; j < n; j++) {
+            int sj = members[size_t(j)];
+            double dx = SF(st, SPH_RX, si) - SF(st, SPH_RX, sj);
+            double dy = SF(st, SPH_RY, si) - SF(st, SPH_RY, sj);
+            double dz = SF(st, SPH_RZ, si) - SF(st, SPH_RZ, sj);
+            double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+            double rsum = SF(st, SPH_R, si) + SF(st, SPH_R, sj);
+            if (dist <= (1. + kCoordinationEpsilon) * rsum) {
+                double c = (rsum - dist) / rsum;
+                overlapping += 2.0 * c;
+                intersections += 2;
+            }
+        }
+    }
+    if (intersections > 0) {
+        overlapping /= static_cast<double>(intersections);
+        coordination = static_cast<double>(intersections) / static_cast<double>(n);
+    }
+    if (p.volsurf_method != VS_NONE) return ST_INPUT;  // other methods are device-only
+    // compute_volume_surface (aggregat.cpp:321-430), method "none"
+    double volume = 0.0, surface = 0.0;
+    for (int i = 0; i < n; i++) {
+        volume = volume + SF(st, SPH_VOLUME, members[size_t(i)]);
+        surface = surface + SF(st, SPH_SURFACE, members[size_t(i)]);
+    }
+    if (volume <= 0 || surface <= 0) return ST_VOL_SURF;
+    // compute_mass_center (aggregat.cpp:431-452)
+    double r[3] = {0., 0., 0.};
+    for (int i = 0; i < n; i++) {
+        int s = members[size_t(i)];
+        double vol = SF(st, SPH_VOLUME, s);
+        r[0] += SF(st, SPH_RX, s) * vol;
+        r[1] += SF(st, SPH_RY, s) * vol;
+        r[2] += SF(st, SPH_RZ, s) * vol;
+    }
+    r[0] /= volume;
+    r[1] /= volume;
+    r[2] /= volume;
+    std::vector<double> dcen(static_cast<size_t>(n), 0.0);
+    for (int i = 0; i < n; i++) {
+        int s = members[size_t(i)];
+        double dx = SF(st, SPH_RX, s) - r[0], dy = SF(st, SPH_RY, s) - r[1], dz = SF(st, SPH_RZ, s) - r[2];
+        dcen[size_t(i)] = std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    int s0 = members[0];
+    fields[AGG_X] = periodic_position(SF(st, SPH_X, s0) + r[0], st.box_length);
+    fields[AGG_Y] = periodic_position(SF(st, SPH_Y, s0) + r[1], st.box_length);
+    fields[AGG_Z] = periodic_position(SF(st, SPH_Z, s0) + r[2], st.box_length);
+    fields[AGG_RX] = r[0];
+    fields[AGG_RY] = r[1];
+    fields[AGG_RZ] = r[2];
+    // compute_max_radius, compute_giration_radius (aggregat.cpp:453-483)
+    double rmax = 0.0, arg = 0., brg = 0.;
+    for (int i = 0; i < n; i++) {
+        int s = members[size_t(i)];
+        rmax = dmax(rmax, SF(st, SPH_R, s) + dcen[size_t(i)]);
+    }
+    for (int i = 0; i < n; i++) {
+        int s = members[size_t(i)];
+        double vol = SF(st, SPH_VOLUME, s);
+        double rs = SF(st, SPH_R, s);
+        arg = arg + vol * (dcen[size_t(i)] * dcen[size_t(i)]);
+        brg = brg + vol * (rs * rs);
+    }
+    double rg = std::sqrt(std::abs((arg + (3. / 5.) * brg) / volume));
+    // update_partial (aggregat.cpp:253-281)
+    double dp = 0., vol_pp = 0.;
+    for (int i = 0; i < n; i++) {
+        vol_pp += SF(st, SPH_VOLUME, members[size_t(i)]);
+        dp += SF(st, SPH_R, members[size_t(i)]);
+    }
+    dp = 2 * dp / static_cast<double>(n);
+    vol_pp = vol_pp / static_cast<double>(n);
+    AggregatePhysics ph = aggregate_physics(p, volume, vol_pp, dp, rg);
+    fields[AGG_RG] = rg;
+    fields[AGG_F_AGG] = ph.f_agg;
+    fields[AGG_LPM] = ph.lpm;
+    fields[AGG_TIME_STEP] = ph.time_step;
+    fields[AGG_RMAX] = rmax;
+    fields[AGG_VOLUME] = volume;
+    fields[AGG_SURFACE] = surface;
+    fields[AGG_DP] = dp;
+    fields[AGG_DG_OVER_DP] = ph.dg_over_dp;
+    fields[AGG_OVERLAPPING] = overlapping;
+    fields[AGG_COORDINATION_NUMBER] = coordination;
+    fields[AGG_D_M] = ph.d_m;
+    if (rmax > *maxradius) *maxradius = rmax;
+    return ST_OK;
+}
+
+int init_random_state(const mcacg_params &p, HostState *st, std::string *err) {
+    const int N = int(p.n_monomeres);
+    if (N < 1) {
+        if (err) *err = "number of monomers must be positive";
+        return ST_INPUT;
+    }
+    const double L = p.box_length;
+    const double pi = pi_value();
+    const double volume_factor = 4 * pi / 3;
+    const double surface_factor = 4 * pi;
+    init_random(p.random_seed);
+    st->n_div = int(p.n_verlet_divisions);
+    st->box_length = L;
+    st->maxradius = 0.;
+    st->time = p.initial_time;
+    st->ns = st->nslots = N;
+    st->sph.assign(9 * size_t(N), 0.);
+    st->sph_slot.assign(size_t(N), -1);
+    st->agg.assign(21 * size_t(N), 0.);
+    st->agg_n.assign(size_t(N), 0);
+    st->members.assign(size_t(N), {});
+    PlacementGrid grid;
+    grid.init(L, 4.0 * p.mean_diameter * 1e-9, N);
+    for (int i = 0; i < N; ++i) {
+        AF(*st, AGG_TIME, i) = st->time;
+        double diameter = 0;
+        int rc = random_diameter(p, p.mean_diameter, p.dispersion_diameter, &diameter);
+        if (rc != ST_OK) {
+            if (err) *err = "dispersion_diameter cannot be lower than 1";
+            return rc;
+        }
+        const double radius = diameter * 0.5;
+        bool placed = false;
+        for (int n_try = 0; n_try < N; n_try++) {
+            double pos[3];
+            pos[0] = random_uniform() * L;
+            pos[1] = random_uniform() * L;
+            pos[2] = random_uniform() * L;
+            // AggregatList::test_free_space (aggregat_list.cpp:534-548)
+            const double reach = radius + st->maxradius + 1e-3 * grid.h;
+            bool busy = grid.any(pos, reach, [&](int j) {
+                Vec3 q{pos[0], pos[1], pos[2]};
+                Vec3 ca{AF(*st, AGG_X, j), AF(*st, AGG_Y, j), AF(*st, AGG_Z, j)};
+                if (!spheres_in_contact(q, radius, ca, AF(*st, AGG_RMAX, j), L)) return false;
+                Vec3 cs{SF(*st, SPH_X, j), SF(*st, SPH_Y, j), SF(*st, SPH_Z, j)};
+                return spheres_in_contact(q, radius, cs, SF(*st, SPH_R, j), L);
+            });
+            if (busy) continue;
+            // Aggregate::init(...) (aggregat.cpp:194-229)
+            AF(*st, AGG_X, i) = periodic_position(pos[0], L);
+            AF(*st, AGG_Y, i) = periodic_position(pos[1], L);
+            AF(*st, AGG_Z, i) = periodic_position(pos[2], L);
+            st->sph_slot[size_t(i)] = i;
+            SF(*st, SPH_X, i) = pos[0];
+            SF(*st, SPH_Y, i) = pos[1];
+            SF(*st, SPH_Z, i) = pos[2];
+            SF(*st, SPH_R, i) = radius;
+            SF(*st, SPH_RX, i) = 0.;
+            SF(*st, SPH_RY, i) = 0.;
+            SF(*st, SPH_RZ, i) = 0.;
+            SF(*st, SPH_VOLUME, i) = volume_factor * std::pow(radius, 3);
+            SF(*st, SPH_SURFACE, i) = surface_factor * std::pow(radius, 2);
+            st->members[size_t(i)] = {i};
+            st->agg_n[size_t(i)] = 1;
+            AF(*st, AGG_D_M, i) = diameter;
+            double f[21];
+            for (int k = 0; k < 21; ++k) f[k] = AF(*st, k, i);
+            rc = host_update_aggregate(p, *st, st->members[size_t(i)], f, &st->maxradius);
+            if (rc != ST_OK) {
+                if (err) *err = "volume/surface error during placement";
+                return rc;
+            }
+            for (int k = 0; k < 21; ++k) AF(*st, k, i) = f[k];
+            double cp[3] = {AF(*st, AGG_X, i), AF(*st, AGG_Y, i), AF(*st, AGG_Z, i)};
+            grid.insert(i, cp);
+            placed = true;
+            break;
+        }
+        if (!placed) {
+            if (err) *err = "Too dense: could not place a monomer";
+            return ST_TOO_DENSE;
+        }
+    }
+    if (p.enforce_volume_fraction) {
+        // aggregat_list_storage.cpp:75-87
+        double current = 0.0;
+        for (int a = 0; a < N; ++a) current += AF(*st, AGG_VOLUME, a);
+        double prescribed = p.volume_fraction * std::pow(L, 3);
+        double correction = std::pow(prescribed / current, 1. / 3.);
+        for (int s = 0; s < N; ++s) {
+            double r = SF(*st, SPH_R, s) * correction;
+            SF(*st, SPH_R, s) = r;
+            SF(*st, SPH_VOLUME, s) = volume_factor * std::pow(r, 3);
+            SF(*st, SPH_SURFACE, s) = surface_factor * std::pow(r, 2);
+        }
+        for (int a = 0; a < N; ++a) {
+            // compute_volume_surface only (method "none": sums of sphere values)
+            double v = 0.0, s = 0.0;
+            for (int m : st->members[size_t(a)]) {
+                v = v + SF(*st, SPH_VOLUME, m);
+                s = s + SF(*st, SPH_SURFACE, m);
+            }
+            AF(*st, AGG_VOLUME, a) = v;
+            AF(*st, AGG_SURFACE, a) = s;
+        }
+    }
+    return ST_OK;
+}
+
+// ------------------------------------------------------------------ HostBox
+int HostBox::upload(const HostState &st, void *stream, std::string *err) {
+    ns_ = st.ns;
+    nslots_ = st.nslots;
+    agg_ = st.agg;
+    agg_n_ = st.agg_n;
+    alive_.clear();
+    for (int a = 0; a < nslots_; ++a)
+        if (agg_n_[size_t(a)] > 0) alive_.push_back(a);
+    maxradius_ = st.maxradius;
+    time_ = st.time;
+    DeviceBox *d = nullptr;
+    int rc = DeviceBox::create(st, stream, &d, err);
+    if (rc != ST_OK) return rc;
+    dev_.reset(d);
+    refresh();
+    return ST_OK;
+}
+
+int HostBox::create_random(const mcacg_params &p, void *stream, std::unique_ptr<HostBox> *out, std::string *err) {
+    if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges) {
+        if (err) *err = "nucleation, potentials, flame coupling and charges are outside this library's path";
+        return ST_INPUT;
+    }
+    std::unique_ptr<HostBox> hb(new HostBox());
+    hb->p_ = p;
+    HostState st;
+    int rc = init_random_state(p, &st, err);
+    if (rc != ST_OK) return rc;
+    rc = hb->upload(st, stream, err);
+    if (rc != ST_OK) return rc;
+    *out = std::move(hb);
+    return ST_OK;
+}
+
+int HostBox::create_from_state(const mcacg_params &p, const mcacg_state &in, void *stream,
+                               std::unique_ptr<HostBox> *out, std::string *err) {
+    if (in.n_spheres <= 0 || in.n_aggregates <= 0 || !in.spheres || !in.sphere_label || !in.aggregates ||
+        !in.n_spheres_per_aggregate || !in.members) {
+        if (err) *err = "incomplete state";
+        return ST_BAD_ARGUMENT;
+    }
+    std::unique_ptr<HostBox> hb(new HostBox());
+    hb->p_ = p;
+    hb->p_.box_length = in.box_length;
+    hb->p_.box_volume = std::pow(in.box_length, 3);
+    hb->p_.n_verlet_divisions = in.n_verlet_divisions;
+    HostState st;
+    st.n_div = int(in.n_verlet_divisions);
+    st.box_length = in.box_length;
+    st.maxradius = in.maxradius;
+    st.time = in.time;
+    st.ns = int(in.n_spheres);
+    st.nslots = int(in.n_aggregates);
+    st.sph.assign(in.spheres, in.spheres + 9 * size_t(st.ns));
+    st.sph_slot.resize(size_t(st.ns));
+    for (int s = 0; s < st.ns; ++s) {
+        int64_t l = in.sphere_label[s];
+        if (l < 0 || l >= st.nslots) {
+            if (err) *err = "sphere label out of range";
+            return ST_BAD_ARGUMENT;
+        }
+        st.sph_slot[size_t(s)] = int(l);
+    }
+    st.agg.assign(in.aggregates, in.aggregates + 21 * size_t(st.nslots));
+    st.agg_n.resize(size_t(st.nslots));
+    st.members.resize(size_t(st.nslots));
+    int64_t off = 0;
+    for (int a = 0; a < st.nslots; ++a) {
+        int64_t n = in.n_spheres_per_aggregate[a];
+        if (n <= 0) {
+            if (err) *err = "empty aggregate in state";
+            return ST_BAD_ARGUMENT;
+        }
+        st.agg_n[size_t(a)] = int(n);
+        for (int64_t k = 0; k < n; ++k) {
+            int64_t s = in.members[off + k];
+            if (s < 0 || s >= st.ns || st.sph_slot[size_t(s)] != a) {
+                if (err) *err = "member list inconsistent with sphere labels";
+                return ST_BAD_ARGUMENT;
+            }
+            st.members[size_t(a)].push_back(int(s));
+        }
+        off += n;
+    }
+    if (off != st.ns) {
+        if (err) *err = "member lists do not cover every sphere once";
+        return ST_BAD_ARGUMENT;
+    }
+    int rc = hb->upload(st, stream, err);
+    if (rc != ST_OK) return rc;
+    *out = std::move(hb);
+    return ST_OK;
+}
+
+int64_t HostBox::label_of(int slot) const {
+    auto it = std::lower_bound(alive_.begin(), alive_.end(), slot);
+    if (it == alive_.end() || *it != slot) return -1;
+    return int64_t(it - alive_.begin());
+}
+
+int HostBox::distance_to_next_contact(int64_t label, const double dir[3], double distance, mcacg_contact *out,
+                                      std::string *err) {
+    if (label < 0 || label >= int64_t(alive_.size())) {
+        if (err) *err = "label out of range";
+        return ST_BAD_ARGUMENT;
+    }
+    QueryResult q;
+    int rc = dev_->query(alive_[size_t(label)], dir, distance, &q, err);
+    if (rc != ST_OK) return rc;
+    out->distance = q.distance;
+    out->moving_sphere = -1;
+    out->other_sphere = -1;
+    out->moving_aggregate = -1;
+    out->other_aggregate = -1;
+    if (q.moving_sphere >= 0) {
+        out->moving_sphere = q.moving_sphere;
+        out->other_sphere = q.other_sphere;
+        out->moving_aggregate = label;
+        out->other_aggregate = label_of(q.other_slot);
+    }
+    return ST_OK;
+}
+
+int HostBox::translate(int64_t label, const double v[3], std::string *err) {
+    if (label < 0 || label >= int64_t(alive_.size())) {
+        if (err) *err = "label out of range";
+        return ST_BAD_ARGUMENT;
+    }
+    int slot = alive_[size_t(label)];
+    F(AGG_X, slot) = periodic_position(F(AGG_X, slot) + v[0], p_.box_length);
+    F(AGG_Y, slot) = periodic_position(F(AGG_Y, slot) + v[1], p_.box_length);
+    F(AGG_Z, slot) = periodic_position(F(AGG_Z, slot) + v[2], p_.box_length);
+    return dev_->translate(slot, v, err);
+}
+
+int HostBox::time_forward(int64_t label, double dt, std::string *err) {
+    if (label < 0 || label >= int64_t(alive_.size())) {
+        if (err) *err = "label out of range";
+        return ST_BAD_ARGUMENT;
+    }
+    F(AGG_TIME, alive_[size_t(label)]) += dt;
+    return ST_OK;
+}
+
+int HostBox::merge(const mcacg_contact &c, int32_t *merged, std::string *err) {
+    *merged = 0;
+    if (c.moving_sphere < 0 || c.other_sphere < 0 || c.moving_aggregate < 0 || c.other_aggregate < 0) return ST_OK;
+    if (c.moving_aggregate >= int64_t(alive_.size()) || c.other_aggregate >= int64_t(alive_.size()) ||
+        c.moving_sphere >= ns_ || c.other_sphere >= ns_) {
+        if (err) *err = "contact refers to an unknown aggregate or sphere";
+        return ST_BAD_ARGUMENT;
+    }
+    const int mslot = alive_[size_t(c.moving_aggregate)];
+    const int oslot = alive_[size_t(c.other_aggregate)];
+    MergeResult m;
+    int rc = dev_->merge(int(c.moving_sphere), int(c.other_sphere), mslot, oslot, &m, err);
+    if (rc != ST_OK) return rc;
+    if (!m.merged) return ST_OK;
+    const int keep = m.keep, removed = m.removed;
+    // proper time keeping the global time constant (aggregat_list.cpp:385-387)
+    double newtime = F(AGG_TIME, keep) + F(AGG_TIME, removed) - time_;
+    AggregatePhysics ph = aggregate_physics(p_, m.fields[AGG_VOLUME], m.vol_pp, m.fields[AGG_DP], m.fields[AGG_RG]);
+    const int geometry[] = {AGG_RG, AGG_RMAX, AGG_VOLUME, AGG_SURFACE, AGG_X, AGG_Y, AGG_Z, AGG_RX, AGG_RY, AGG_RZ,
+                            AGG_DP, AGG_OVERLAPPING, AGG_COORDINATION_NUMBER};
+    for (int f : geometry) F(f, keep) = m.fields[f];
+    F(AGG_F_AGG, keep) = ph.f_agg;
+    F(AGG_D_M, keep) = ph.d_m;
+    F(AGG_TIME_STEP, keep) = ph.time_step;
+    F(AGG_LPM, keep) = ph.lpm;
+    F(AGG_DG_OVER_DP, keep) = ph.dg_over_dp;
+    F(AGG_TIME, keep) = newtime;
+    agg_n_[size_t(keep)] = m.n;
+    agg_n_[size_t(removed)] = 0;
+    maxradius_ = m.maxradius;
+    auto it = std::lower_bound(alive_.begin(), alive_.end(), removed);
+    if (it != alive_.end() && *it == removed) alive_.erase(it);
+    double upd[21];
+    for (int f = 0; f < 21; ++f) upd[f] = F(f, keep);
+    unsigned mask = (1u << AGG_F_AGG) | (1u << AGG_D_M) | (1u << AGG_TIME_STEP) | (1u << AGG_LPM) |
+                    (1u << AGG_DG_OVER_DP) | (1u << AGG_TIME);
+    rc = dev_->set_fields(keep, upd, mask, err);
+    if (rc != ST_OK) return rc;
+    *merged = 1;
+    return ST_OK;
+}
+
+void HostBox::sort_time_steps(double factor) {
+    // aggregat_list.cpp:109-141: std::sort of label indices by factor/time_step
+    const size_t n = alive_.size();
+    std::vector<double> tp(n);
+    for (size_t i = 0; i < n; i++) tp[i] = factor / F(AGG_TIME_STEP, alive_[i]);
+    index_sorted_.resize(n);
+    std::iota(index_sorted_.begin(), index_sorted_.end(), 0);
+    std::sort(index_sorted_.begin(), index_sorted_.end(), [&tp](size_t a, size_t b) { return tp[a] < tp[b]; });
+    cumulative_.resize(n);
+    cumulative_[0] = tp[index_sorted_[0]];
+    for (size_t i = 1; i < n; i++) cumulative_[i] = cumulative_[i - 1] + tp[index_sorted_[i]];
+}
+
+int64_t HostBox::pick_random() {
+    double val = random_uniform() * cumulative_[alive_.size() - 1];
+    long n = std::lower_bound(cumulative_.begin(), cumulative_.end(), val) - cumulative_.begin();
+    return int64_t(index_sorted_[size_t(n)]);
+}
+
+void HostBox::refresh() {
+    max_time_step_ = F(AGG_TIME_STEP, alive_[0]);
+    for (int slot : alive_) max_time_step_ = std::max(F(AGG_TIME_STEP, slot), max_time_step_);
+    avg_npp_ = static_cast<double>(ns_) / static_cast<double>(alive_.size());
+}
+
+double HostBox::total_volume() const {
+    double v = 0.0;
+    for (int slot : alive_) v += F(AGG_VOLUME, slot);
+    return v;
+}
+double HostBox::total_surface() const {
+    double v = 0.0;
+    for (int slot : alive_) v += F(AGG_SURFACE, slot);
+    return v;
+}
+
+const double *HostBox::fields(int64_t label, double out[21]) const {
+    int slot = alive_[size_t(label)];
+    for (int f = 0; f < 21; ++f) out[f] = F(f, slot);
+    return out;
+}
+
+bool HostBox::finished() const {
+    const uint64_t n = alive_.size();
+    if (n < 1) return true;
+    if (n <= static_cast<uint64_t>(p_.number_of_aggregates_limit)) return true;
+    if (p_.n_iter_without_event_limit > 0 && n_iter_without_event_ >= p_.n_iter_without_event_limit) return true;
+    if (p_.physical_time_limit > 0 && time_ >= p_.physical_time_limit) return true;
+    if (p_.mean_monomere_per_aggregate_limit > 0 && avg_npp_ >= double(p_.mean_monomere_per_aggregate_limit))
+        return true;
+    return false;
+}
+
+int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::string *err) {
+    if (p_.with_surface_reactions || p_.with_domain_duplication || p_.with_domain_reduction ||
+        p_.pick_method != MCACG_PICK_RANDOM) {
+        if (err) *err = "the host-driven loop covers the collision-only configuration "
+                        "(no surface reactions, no domain duplication/reduction, pick_method=random)";
+        return ST_INPUT;
+    }
+    int64_t steps = 0, events = 0;
+    while (!finished()) {
+        if (opts.max_steps > 0 && steps >= opts.max_steps) break;
+        double max = max_time_step_;
+        if (event_) sort_time_steps(max);
+        const int64_t label = pick_random();
+        double deltatemps = get_time_step(max);
+        const double full_distance = F(AGG_LPM, alive_[size_t(label)]);
+        double dir[3];
+        random_direction(dir);
+        double move_distance = full_distance;
+        const int n_try = 1;
+        bool contact = false;
+        mcacg_contact c{std::numeric_limits<double>::infinity(), -1, -1, -1, -1};
+        if (p_.with_collisions) {
+            int rc = distance_to_next_contact(label, dir, full_distance, &c, err);
+            if (rc != ST_OK) return rc;
+            contact = c.distance <= full_distance;
+            if (contact) move_distance = c.distance;
+        }
+        double v[3] = {dir[0] * move_distance, dir[1] * move_distance, dir[2] * move_distance};
+        int rc = translate(label, v, err);
+        if (rc != ST_OK) return rc;
+        deltatemps = deltatemps * (move_distance / full_distance + static_cast<double>(n_try - 1));
+        time_forward(label, deltatemps, err);
+        time_ = time_ + deltatemps;
+        int32_t merged = 0;
+        if (contact) {
+            rc = merge(c, &merged, err);
+            if (rc != ST_OK) return rc;
+        }
+        event_ = merged != 0;
+        if (event_) {
+            n_iter_without_event_ = 0;
+            ++events;
+            refresh();
+        } else {
+            n_iter_without_event_++;
+        }
+        if (opts.trace && steps < opts.trace_capacity) {
+            mcacg_step_record &r = opts.trace[steps];
+            r.step = steps;
+            r.picked = label;
+            r.contact = contact;
+            r.merged = merged;
+            r.moving_sphere = c.moving_sphere;
+            r.other_sphere = c.other_sphere;
+            r.moving_agg = c.moving_aggregate;
+            r.other_agg = c.other_aggregate;
+            r.n_agg_after = int64_t(alive_.size());
+            r.deltatemps = get_time_step(max);
+            r.full_distance = full_distance;
+            r.dir[0] = dir[0];
+            r.dir[1] = dir[1];
+            r.dir[2] = dir[2];
+            r.contact_distance = c.distance;
+            r.move_distance = move_distance;
+            r.time_after = time_;
+            r.reserved = 0;
+        }
+        ++steps;
+    }
+    if (stats) {
+        stats->steps = steps;
+        stats->events = events;
+        stats->n_aggregates = int64_t(alive_.size());
+        stats->time = time_;
+        stats->finished = finished() ? 1 : 0;
+    }
+    return ST_OK;
+}
+
+int HostBox::store(mcacg_state *out, std::string *err) {
+    HostState st;
+    int rc = dev_->download(&st, err);
+    if (rc != ST_OK) return rc;
+    const int na = int(alive_.size());
+    if (out->n_spheres < ns_ || out->n_aggregates < na) {
+        if (err) *err = "state buffers too small";
+        return ST_BAD_ARGUMENT;
+    }
+    out->n_spheres = ns_;
+    out->n_aggregates = na;
+    out->n_verlet_divisions = st.n_div;
+    out->box_length = st.box_length;
+    out->maxradius = maxradius_;
+    out->time = time_;
+    if (out->spheres) {
+        for (int f = 0; f < 9; ++f)
+            std::memcpy(out->spheres + size_t(f) * ns_, st.sph.data() + size_t(f) * ns_, sizeof(double) * size_t(ns_));
+    }
+    if (out->sphere_label)
+        for (int s = 0; s < ns_; ++s) out->sphere_label[s] = label_of(st.sph_slot[size_t(s)]);
+    if (out->aggregates)
+        for (int f = 0; f < 21; ++f)
+            for (int l = 0; l < na; ++l) out->aggregates[size_t(f) * na + l] = F(f, alive_[size_t(l)]);
+    int64_t off = 0;
+    for (int l = 0; l < na; ++l) {
+        const auto &m = st.members[size_t(alive_[size_t(l)])];
+        if (out->n_spheres_per_aggregate) out->n_spheres_per_aggregate[l] = int64_t(m.size());
+        if (out->members)
+            for (size_t k = 0; k < m.size(); ++k) out->members[off + int64_t(k)] = m[k];
+        off += int64_t(m.size());
+    }
+    return ST_OK;
+}
+
+}  // namespace mcacg

@@ -1,0 +1,95 @@
+// Host side of one box: the AggregatList interface of the reference
+// (include/aggregats/aggregat_list.hpp:29-116) over a device-resident state.
+//
+// The host keeps a mirror of the 21 aggregate fields (small) and the label
+// order; the spheres, member lists and Verlet grid live on the GPU. Every
+// per-step operation of src/calcul.cpp maps to one method here.
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mcacg.h"
+#include "device_box.hpp"
+
+namespace mcacg {
+
+class HostBox {
+  public:
+    // AggregatList::AggregatList: seeded random placement (host), then upload.
+    static int create_random(const mcacg_params &p, void *stream, std::unique_ptr<HostBox> *out, std::string *err);
+    // From a complete state (labels in order, all aggregates alive).
+    static int create_from_state(const mcacg_params &p, const mcacg_state &st, void *stream,
+                                 std::unique_ptr<HostBox> *out, std::string *err);
+
+    int size() const { return int(alive_.size()); }
+    int n_spheres() const { return ns_; }
+    double time() const { return time_; }
+    void set_time(double t) { time_ = t; }
+    const mcacg_params &params() const { return p_; }
+    DeviceBox &device() { return *dev_; }
+
+    // per-step interface
+    int distance_to_next_contact(int64_t label, const double dir[3], double distance, mcacg_contact *out,
+                                 std::string *err);
+    int translate(int64_t label, const double v[3], std::string *err);
+    int time_forward(int64_t label, double dt, std::string *err);
+    int merge(const mcacg_contact &c, int32_t *merged, std::string *err);
+    void sort_time_steps(double factor);
+    int64_t pick_random();
+    double get_time_step(double max) const { return max / cumulative_.back(); }
+    double max_time_step() const { return max_time_step_; }
+    double avg_npp() const { return avg_npp_; }
+    void refresh();
+    double total_volume() const;
+    double total_surface() const;
+    const double *fields(int64_t label, double out[21]) const;
+    int n_spheres_of(int64_t label) const { return agg_n_[size_t(alive_[size_t(label)])]; }
+    int slot_of(int64_t label) const { return alive_[size_t(label)]; }
+    int64_t label_of(int slot) const;
+
+    // the reference's stop criteria (physical_model.cpp:288-337, without the
+    // STOPCODE file and CPU-time checks)
+    bool finished() const;
+    // one run of the MC loop of src/calcul.cpp:66-281 (collision-only)
+    int calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::string *err);
+
+    // whole state (store) in label order
+    int store(mcacg_state *st, std::string *err);
+
+  private:
+    HostBox() = default;
+    int upload(const HostState &st, void *stream, std::string *err);
+    double &F(int field, int slot) { return agg_[size_t(field) * size_t(nslots_) + size_t(slot)]; }
+    double F(int field, int slot) const { return agg_[size_t(field) * size_t(nslots_) + size_t(slot)]; }
+
+    mcacg_params p_{};
+    double time_ = 0;
+    int64_t n_iter_without_event_ = 0;
+    bool event_ = true;
+    int ns_ = 0, nslots_ = 0;
+    std::vector<double> agg_;   // [21][nslots] mirror
+    std::vector<int> agg_n_;    // members per slot (0: dead)
+    std::vector<int> alive_;    // slot of each label
+    double maxradius_ = 0;
+    double max_time_step_ = 0, avg_npp_ = 1;
+    std::vector<size_t> index_sorted_;
+    std::vector<double> cumulative_;
+    std::unique_ptr<DeviceBox> dev_;
+};
+
+// Random placement of the reference's AggregatList constructor into 'st'
+// (aggregat.cpp:162-229, aggregat_list_storage.cpp:52-88). Seeds the C
+// library generator. Uses a fine spatial hash for the free-space test; the
+// answer of that test does not depend on the grid, so the placements are the
+// reference's.
+int init_random_state(const mcacg_params &p, HostState *st, std::string *err);
+
+// Aggregate::update for an aggregate given by its members (host, used for
+// initial monomers and for loading states): writes all 21 fields except the
+// position-independent proper time and charge, and raises 'maxradius'.
+int host_update_aggregate(const mcacg_params &p, const HostState &st, const std::vector<int> &members,
+                          double fields[21], double *maxradius);
+
+}  // namespace mcacg

@@ -1,0 +1,435 @@
+// Merge of two aggregates on the device: relabel, pool segment, and the
+// geometry part of Aggregate::update (aggregats/aggregat.cpp:247-288,
+// 321-483, 486-544, 719-764).
+//
+// The reference accumulates every aggregate sum sequentially in sphere-list
+// order. To stay bit-identical the per-sphere terms are formed in parallel
+// (one rounding each, as in the reference) and each sum is then accumulated
+// in list order by one thread; distinct sums run on distinct warps. The
+// O(n^2) intra-aggregate contact search is screened in FP32 and refined in
+// FP64; its pairs are put back in (i, j) order before they are summed.
+#pragma once
+#include "box.cuh"
+
+namespace mcacg {
+
+constexpr int kPairTile = 1024;
+constexpr int kSumSeries = 8;
+
+struct MergeSmem {
+    double refpos[3];
+    double diffpos[3];
+    double r_cm[3];
+    double sums[kSumSeries];
+    double rmax_warp[32];
+    float tile_f[kPairTile * 4];
+    int warp_tmp[32];
+    float warp_f[32];
+    int keep, removed, mysph, othsph;
+    int n_keep, n_rem, off_keep, off_rem, new_off, n;
+    int n_pairs;
+    int status;
+    int merged;
+    float margin;
+};
+
+// exclusive scan of a global int array in place (block-wide, chunked);
+// returns the total.
+__device__ int block_scan_global(int *data, int n, int *warp_tmp) {
+    const int NT = blockDim.x;
+    int carry = 0;
+    for (int c0 = 0; c0 < n; c0 += NT) {
+        int idx = c0 + threadIdx.x;
+        int v = (idx < n) ? data[idx] : 0;
+        int total;
+        // generic warp scan for any block size multiple of 32
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = NT >> 5;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tmp[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int wv = (lane < nw) ? warp_tmp[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, wv, o);
+                if (lane >= o) wv += y;
+            }
+            if (lane < nw) warp_tmp[lane] = wv;
+        }
+        __syncthreads();
+        int base = (wid > 0) ? warp_tmp[wid - 1] : 0;
+        total = warp_tmp[nw - 1];
+        if (idx < n) data[idx] = carry + base + x - v;
+        carry += total;
+        __syncthreads();
+    }
+    return carry;
+}
+
+// Move every live segment to the front of the other pool buffer, in slot
+// order. Uses counters[] and row_cnt[] as scratch.
+__device__ void block_compact_pool(const DevBox &b, int *warp_tmp) {
+    DevScalars *sc = b.sc;
+    const int from = sc->pool_sel, to = 1 - from;
+    // prefix of member counts over slots, staged in row_cnt (size >= nslots+1)
+    int *pref = b.row_cnt;
+    for (int a = threadIdx.x; a < b.nslots; a += blockDim.x) pref[a] = b.agg_n[a];
+    __syncthreads();
+    int total = block_scan_global(pref, b.nslots, warp_tmp);
+    for (int a = threadIdx.x; a < b.nslots; a += blockDim.x) {
+        int n = b.agg_n[a];
+        if (n == 0) continue;
+        int src = b.agg_off[a], dst = pref[a];
+        for (int k = 0; k < n; ++k) {
+            b.pool_id[to][dst + k] = b.pool_id[from][src + k];
+            b.pool_pos[to][dst + k] = b.pool_pos[from][src + k];
+        }
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < b.nslots; a += blockDim.x)
+        if (b.agg_n[a] > 0) b.agg_off[a] = pref[a];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        sc->pool_sel = to;
+        sc->pool_top = total;
+    }
+    __syncthreads();
+}
+
+// Sequential (list-order) sum of one work series, as the reference's loops.
+__device__ __forceinline__ double ordered_sum(const double *v, int n) {
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) acc = acc + v[i];
+    return acc;
+}
+
+// AggregatList::merge + Aggregate::merge + Aggregate::update (geometry).
+// ms / os: moving / other sphere; mslot / oslot: their aggregates at query
+// time. The physics fields (f_agg, d_m, time_step, lpm, dg_over_dp), the
+// proper time and the charge are left to the caller.
+__device__ void block_merge(const DevBox &b, int ms, int os, int mslot, int oslot, MergeSmem &sm, MergeOut *out) {
+    const int tid = threadIdx.x, NT = blockDim.x;
+    DevScalars *sc = b.sc;
+    if (tid == 0) {
+        sm.status = ST_OK;
+        sm.merged = 0;
+        sm.n_pairs = 0;
+        Vec3 pm = sph_pos(b, ms), po = sph_pos(b, os);
+        if (!spheres_in_contact(pm, S(b, SPH_R, ms), po, S(b, SPH_R, os), b.L)) {
+            sm.merged = 0;
+        } else {
+            int la = b.sph_slot[ms], lb = b.sph_slot[os];
+            int keep = min(la, lb), removed = max(la, lb);
+            int my = -1, oth = -1;
+            if (mslot == keep) {
+                my = ms;
+                oth = os;
+            } else if (oslot == keep) {
+                my = os;
+                oth = ms;
+            }
+            if (my < 0 || keep == removed) {
+                sm.status = ST_MERGE;  // "ListAggregate want to merge but the aggregate refuses"
+            } else {
+                sm.merged = 1;
+                sm.keep = keep;
+                sm.removed = removed;
+                sm.mysph = my;
+                sm.othsph = oth;
+                sm.n_keep = b.agg_n[keep];
+                sm.n_rem = b.agg_n[removed];
+                sm.n = sm.n_keep + sm.n_rem;
+                const int *pid = b.pool_id[sc->pool_sel];
+                int s0 = pid[b.agg_off[keep]];
+                sm.refpos[0] = S(b, SPH_X, s0);
+                sm.refpos[1] = S(b, SPH_Y, s0);
+                sm.refpos[2] = S(b, SPH_Z, s0);
+                Vec3 pmy = sph_pos(b, my), poth = sph_pos(b, oth);
+                double dcx = periodic_distance(poth.x - pmy.x, b.L);
+                double dcy = periodic_distance(poth.y - pmy.y, b.L);
+                double dcz = periodic_distance(poth.z - pmy.z, b.L);
+                sm.diffpos[0] = S(b, SPH_RX, my) + dcx - S(b, SPH_RX, oth);
+                sm.diffpos[1] = S(b, SPH_RY, my) + dcy - S(b, SPH_RY, oth);
+                sm.diffpos[2] = S(b, SPH_RZ, my) + dcz - S(b, SPH_RZ, oth);
+            }
+        }
+    }
+    __syncthreads();
+    if (!sm.merged || sm.status != ST_OK) {
+        if (tid == 0) {
+            out->merged = 0;
+            out->status = sm.status;
+        }
+        __syncthreads();
+        return;
+    }
+    const int keep = sm.keep, removed = sm.removed, n = sm.n, n_keep = sm.n_keep, n_rem = sm.n_rem;
+    // room for the merged segment
+    if (sc->pool_top + n > b.pool_cap) block_compact_pool(b, sm.warp_tmp);
+    if (tid == 0) {
+        sm.off_keep = b.agg_off[keep];
+        sm.off_rem = b.agg_off[removed];
+        sm.new_off = sc->pool_top;
+    }
+    __syncthreads();
+    int *pool_id = b.pool_id[sc->pool_sel];
+    float4 *pool_pos = b.pool_pos[sc->pool_sel];
+    const int off_keep = sm.off_keep, off_rem = sm.off_rem, new_off = sm.new_off;
+    // relabel and shift the removed aggregate's spheres; build keep ++ removed
+    for (int k = tid; k < n; k += NT) {
+        if (k < n_keep) {
+            pool_id[new_off + k] = pool_id[off_keep + k];
+            pool_pos[new_off + k] = pool_pos[off_keep + k];
+        } else {
+            int s = pool_id[off_rem + (k - n_keep)];
+            b.sph_slot[s] = keep;
+            double rx = S(b, SPH_RX, s) + sm.diffpos[0];
+            double ry = S(b, SPH_RY, s) + sm.diffpos[1];
+            double rz = S(b, SPH_RZ, s) + sm.diffpos[2];
+            S(b, SPH_RX, s) = rx;
+            S(b, SPH_RY, s) = ry;
+            S(b, SPH_RZ, s) = rz;
+            double x = rx + sm.refpos[0], y = ry + sm.refpos[1], z = rz + sm.refpos[2];
+            S(b, SPH_X, s) = x;
+            S(b, SPH_Y, s) = y;
+            S(b, SPH_Z, s) = z;
+            pool_id[new_off + k] = s;
+            pool_pos[new_off + k] = make_float4(float(x), float(y), float(z), float(S(b, SPH_R, s)));
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        b.agg_off[keep] = new_off;
+        b.agg_n[keep] = n;
+        b.agg_n[removed] = 0;
+        sc->pool_top = new_off + n;
+        sc->n_alive -= 1;
+    }
+    __syncthreads();
+    const int *mem = pool_id + new_off;
+
+    // ---- update_distances_and_overlapping: contact pairs i < j
+    // stage relative positions (FP32) and the extent for the screening margin
+    float4 *relf = reinterpret_cast<float4 *>(b.work);  // reuse: n float4 fit in work[0..n/2)
+    float ext = 0.f;
+    for (int k = tid; k < n; k += NT) {
+        int s = mem[k];
+        float4 v = make_float4(float(S(b, SPH_RX, s)), float(S(b, SPH_RY, s)), float(S(b, SPH_RZ, s)),
+                               float(S(b, SPH_R, s)));
+        relf[k] = v;
+        ext = fmaxf(ext, fabsf(v.x) + fabsf(v.y) + fabsf(v.z) + v.w);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
+    if ((tid & 31) == 0) sm.warp_f[tid >> 5] = ext;
+    if (tid < n + 1 && tid <= b.ns) b.row_cnt[tid] = 0;
+    for (int k = tid; k <= n; k += NT) b.row_cnt[k] = 0;
+    if (tid == 0) b.counters[0] = 0;
+    __syncthreads();
+    if (tid == 0) {
+        float m = 0.f;
+        for (int k = 0; k < NT / 32; ++k) m = fmaxf(m, sm.warp_f[k]);
+        sm.margin = 1.0e-5f * m;  // FP32 error of |rel_i - rel_j| is ~1e-7 of the extent
+    }
+    __syncthreads();
+    const float pm_margin = sm.margin;
+    for (int j0 = 0; j0 < n; j0 += kPairTile) {
+        const int nt = min(kPairTile, n - j0);
+        for (int k = tid; k < nt; k += NT) {
+            float4 v = relf[j0 + k];
+            sm.tile_f[4 * k + 0] = v.x;
+            sm.tile_f[4 * k + 1] = v.y;
+            sm.tile_f[4 * k + 2] = v.z;
+            sm.tile_f[4 * k + 3] = v.w;
+        }
+        __syncthreads();
+        for (int i = tid; i < min(n, j0 + nt); i += NT) {
+            const float4 pi_ = relf[i];
+            int jstart = max(i + 1, j0) - j0;
+            for (int jj = jstart; jj < nt; ++jj) {
+                float dx = pi_.x - sm.tile_f[4 * jj + 0];
+                float dy = pi_.y - sm.tile_f[4 * jj + 1];
+                float dz = pi_.z - sm.tile_f[4 * jj + 2];
+                float reach = (pi_.w + sm.tile_f[4 * jj + 3]) * 1.0001f + pm_margin;
+                if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz)) > reach * reach) continue;
+                const int j = j0 + jj;
+                const int si = mem[i], sj = mem[j];
+                double ex = S(b, SPH_RX, si) - S(b, SPH_RX, sj);
+                double ey = S(b, SPH_RY, si) - S(b, SPH_RY, sj);
+                double ez = S(b, SPH_RZ, si) - S(b, SPH_RZ, sj);
+                double dist = sqrt(ex * ex + ey * ey + ez * ez);
+                double rsum = S(b, SPH_R, si) + S(b, SPH_R, sj);
+                if (dist <= (1. + kCoordinationEpsilon) * rsum) {
+                    int p = atomicAdd(&b.counters[0], 1);
+                    if (p < b.pair_cap) {
+                        b.pair_tmp_i[p] = i;
+                        b.pair_tmp_j[p] = j;
+                        b.pair_tmp_d[p] = dist;
+                        atomicAdd(&b.row_cnt[i], 1);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    const int P = b.counters[0];
+    if (P > b.pair_cap) {
+        if (tid == 0) {
+            sc->status = ST_CAPACITY;
+            out->merged = 1;
+            out->status = ST_CAPACITY;
+        }
+        __syncthreads();
+        return;
+    }
+    // counting sort of the pairs by i, then by j within a row
+    block_scan_global(b.row_cnt, n + 1, sm.warp_tmp);
+    for (int p = tid; p < P; p += NT) {
+        int i = b.pair_tmp_i[p];
+        int dst = atomicAdd(&b.row_cnt[i], 1);
+        b.pair_i[dst] = i;
+        b.pair_j[dst] = b.pair_tmp_j[p];
+        b.pair_d[dst] = b.pair_tmp_d[p];
+    }
+    __syncthreads();
+    // row_cnt[i] now holds the end of row i; row i starts at row_cnt[i-1]
+    for (int i = tid; i < n; i += NT) {
+        int beg = (i == 0) ? 0 : b.row_cnt[i - 1];
+        int end = b.row_cnt[i];
+        for (int x = beg + 1; x < end; ++x) {
+            int jv = b.pair_j[x];
+            double dv = b.pair_d[x];
+            int y = x;
+            while (y > beg && b.pair_j[y - 1] > jv) {
+                b.pair_j[y] = b.pair_j[y - 1];
+                b.pair_d[y] = b.pair_d[y - 1];
+                --y;
+            }
+            b.pair_j[y] = jv;
+            b.pair_d[y] = dv;
+        }
+    }
+    __syncthreads();
+
+    // ---- per-sphere terms (one rounding each, as in the reference)
+    // work[0] volume, [1] surface, [2..4] rel * volume, [5] volume * r^2,
+    // [6] r, [7] volume * dcenter^2 (after the centre of mass is known)
+    double *wv = b.work;
+    const size_t W = size_t(b.ns);
+    for (int k = tid; k < n; k += NT) {
+        int s = mem[k];
+        double vol = S(b, SPH_VOLUME, s);
+        double r = S(b, SPH_R, s);
+        wv[0 * W + k] = vol;
+        wv[1 * W + k] = S(b, SPH_SURFACE, s);
+        wv[2 * W + k] = S(b, SPH_RX, s) * vol;
+        wv[3 * W + k] = S(b, SPH_RY, s) * vol;
+        wv[4 * W + k] = S(b, SPH_RZ, s) * vol;
+        wv[5 * W + k] = vol * (r * r);
+        wv[6 * W + k] = r;
+    }
+    __syncthreads();
+    {
+        // seven independent ordered sums, one per warp
+        const int wid = tid >> 5, lane = tid & 31;
+        if (lane == 0 && wid < 7) sm.sums[wid] = ordered_sum(wv + size_t(wid) * W, n);
+        if (tid == 0) {
+            // overlapping: sequential over (i, j)-ordered pairs
+            double ov = 0.0;
+            for (int p = 0; p < P; ++p) {
+                int i = b.pair_i[p], j = b.pair_j[p];
+                double rsum = S(b, SPH_R, mem[i]) + S(b, SPH_R, mem[j]);
+                double c = (rsum - b.pair_d[p]) / rsum;
+                ov += 2.0 * c;
+            }
+            sm.sums[7] = ov;
+            sm.n_pairs = P;
+        }
+    }
+    __syncthreads();
+    const double V = sm.sums[0], Sf = sm.sums[1];
+    if (tid == 0) {
+        if (V <= 0 || Sf <= 0) sm.status = ST_VOL_SURF;
+        double cx = sm.sums[2] / V, cy = sm.sums[3] / V, cz = sm.sums[4] / V;
+        sm.r_cm[0] = cx;
+        sm.r_cm[1] = cy;
+        sm.r_cm[2] = cz;
+    }
+    __syncthreads();
+    if (sm.status != ST_OK) {
+        if (tid == 0) {
+            sc->status = sm.status;
+            out->merged = 1;
+            out->status = sm.status;
+        }
+        __syncthreads();
+        return;
+    }
+    // distances to the centre of mass, r_max, Rg terms
+    double rmax_local = 0.0;
+    for (int k = tid; k < n; k += NT) {
+        int s = mem[k];
+        double dx = S(b, SPH_RX, s) - sm.r_cm[0];
+        double dy = S(b, SPH_RY, s) - sm.r_cm[1];
+        double dz = S(b, SPH_RZ, s) - sm.r_cm[2];
+        double dcen = sqrt(dx * dx + dy * dy + dz * dz);
+        wv[7 * W + k] = wv[0 * W + k] * (dcen * dcen);
+        rmax_local = dmax(rmax_local, S(b, SPH_R, s) + dcen);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rmax_local = dmax(rmax_local, __shfl_xor_sync(0xffffffffu, rmax_local, o));
+    if ((tid & 31) == 0) sm.rmax_warp[tid >> 5] = rmax_local;
+    __syncthreads();
+    if (tid == 0) {
+        double rmax = 0.0;
+        for (int k = 0; k < NT / 32; ++k) rmax = dmax(rmax, sm.rmax_warp[k]);
+        double arg = ordered_sum(wv + 7 * W, n);
+        double brg = sm.sums[5];
+        double rg = sqrt(fabs((arg + (3. / 5.) * brg) / V));
+        double dp = 2 * sm.sums[6] / static_cast<double>(n);
+        double vol_pp = V / static_cast<double>(n);
+        double overlapping = 0.0, coordination = 0.0;
+        if (P > 0) {
+            int inter = 2 * P;
+            overlapping = sm.sums[7] / static_cast<double>(inter);
+            coordination = static_cast<double>(inter) / static_cast<double>(n);
+        }
+        const int s0 = mem[0];
+        double x = periodic_position(S(b, SPH_X, s0) + sm.r_cm[0], b.L);
+        double y = periodic_position(S(b, SPH_Y, s0) + sm.r_cm[1], b.L);
+        double z = periodic_position(S(b, SPH_Z, s0) + sm.r_cm[2], b.L);
+        A(b, AGG_RG, keep) = rg;
+        A(b, AGG_RMAX, keep) = rmax;
+        A(b, AGG_VOLUME, keep) = V;
+        A(b, AGG_SURFACE, keep) = Sf;
+        A(b, AGG_X, keep) = x;
+        A(b, AGG_Y, keep) = y;
+        A(b, AGG_Z, keep) = z;
+        A(b, AGG_RX, keep) = sm.r_cm[0];
+        A(b, AGG_RY, keep) = sm.r_cm[1];
+        A(b, AGG_RZ, keep) = sm.r_cm[2];
+        A(b, AGG_DP, keep) = dp;
+        A(b, AGG_OVERLAPPING, keep) = overlapping;
+        A(b, AGG_COORDINATION_NUMBER, keep) = coordination;
+        regrid(b, keep);
+        cell_remove(b, b.agg_cell[removed], removed);
+        if (rmax > sc->maxradius) sc->maxradius = rmax;
+        out->merged = 1;
+        out->status = ST_OK;
+        out->keep = keep;
+        out->removed = removed;
+        out->n = n;
+        out->n_pairs = P;
+        for (int f = 0; f < AGG_NFIELDS; ++f) out->fields[f] = A(b, f, keep);
+        out->vol_pp = vol_pp;
+        out->maxradius = sc->maxradius;
+    }
+    __syncthreads();
+}
+
+}  // namespace mcacg

@@ -47,21 +47,29 @@ constexpr double kCoordinationEpsilon = 1e-10;
 MCACG_HD double pi_value() { return 3.141592653589793115997963468544185161590576171875; }
 
 // --- periodic helpers (include/physical_model/physical_model.hpp:99-126) ---
+// The reference wraps with unbounded while loops. Here each loop is capped:
+// inside the cap (any value within 64 box lengths) the result is the
+// reference's, operation for operation; beyond it (or for inf/NaN) the value
+// is reduced with floor() instead, so no input can make a kernel spin.
+constexpr int kWrapCap = 64;
 MCACG_HD double periodic_distance(double d, double dim) {
     double half = 0.5 * dim;
-    while (d < -half) d += dim;
-    while (d >= half) d -= dim;
+    int guard = 0;
+    while (d < -half && guard < kWrapCap) d += dim, ++guard;
+    while (d >= half && guard < kWrapCap) d -= dim, ++guard;
+    if (guard >= kWrapCap) d = d - dim * floor(d / dim + 0.5);
     return d;
 }
 MCACG_HD double periodic_position(double p, double dim) {
-    while (p < 0) p += dim;
-    while (p >= dim) p -= dim;
+    int guard = 0;
+    while (p < 0 && guard < kWrapCap) p += dim, ++guard;
+    while (p >= dim && guard < kWrapCap) p -= dim, ++guard;
+    if (guard >= kWrapCap) p = p - dim * floor(p / dim);
     return p;
 }
 MCACG_HD int periodic_cell(int i, int n) {
-    while (i < 0) i += n;
-    while (i >= n) i -= n;
-    return i;
+    i %= n;
+    return i < 0 ? i + n : i;
 }
 MCACG_HD double dmin(double a, double b) { return (b < a) ? b : a; }  // std::min
 MCACG_HD double dmax(double a, double b) { return (a < b) ? b : a; }  // std::max
@@ -110,7 +118,9 @@ MCACG_UNROLL
         double w = fmod(pb[l] - base, L);
         if (w < 0) w += L;
         q[l] = w + base;
-        nper[l] = static_cast<int>(floor(zone[l] / L));
+        // images to visit; the cap only bites for sweeps longer than 16 boxes
+        double np = floor(zone[l] / L);
+        nper[l] = (np >= 0 && np <= 16) ? static_cast<int>(np) : (np > 16 ? 16 : 0);
     }
     double res = std::numeric_limits<double>::infinity();
     for (int i = 0; i <= nper[0]; i++) {
@@ -155,8 +165,16 @@ MCACG_UNROLL
     for (int l = 0; l < 3; ++l) {
         double p = s[l] + distance + dmax(v[l], 0.);
         double m = s[l] - distance + dmin(v[l], 0.);
-        r.lo[l] = static_cast<int>(floor(static_cast<double>(n_div) * m / width));
-        r.hi[l] = static_cast<int>(floor(static_cast<double>(n_div) * p / width) + 1);
+        double lo = floor(static_cast<double>(n_div) * m / width);
+        double hi = floor(static_cast<double>(n_div) * p / width) + 1;
+        // a range of n_div cells or more (or a non-finite one) is the whole axis
+        if (!(hi - lo < n_div) || !(lo > -1e9) || !(hi < 1e9)) {
+            r.lo[l] = 0;
+            r.hi[l] = n_div - 1;
+            continue;
+        }
+        r.lo[l] = static_cast<int>(lo);
+        r.hi[l] = static_cast<int>(hi);
         if (r.hi[l] - r.lo[l] >= n_div) {
             r.lo[l] = 0;
             r.hi[l] = n_div - 1;

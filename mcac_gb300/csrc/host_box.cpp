@@ -522,6 +522,7 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
         if (event_) sort_time_steps(max);
         const int64_t label = pick_random();
         double deltatemps = get_time_step(max);
+        const double deltatemps_pick = deltatemps;
         const double full_distance = F(AGG_LPM, alive_[size_t(label)]);
         double dir[3];
         random_direction(dir);
@@ -565,7 +566,7 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
             r.moving_agg = c.moving_aggregate;
             r.other_agg = c.other_aggregate;
             r.n_agg_after = int64_t(alive_.size());
-            r.deltatemps = get_time_step(max);
+            r.deltatemps = deltatemps_pick;
             r.full_distance = full_distance;
             r.dir[0] = dir[0];
             r.dir[1] = dir[1];

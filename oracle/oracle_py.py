@@ -1,0 +1,270 @@
+"""ctypes wrapper of the C restatement in oracle/mcac_oracle.c.
+
+TEST INFRASTRUCTURE ONLY: the checker of the test suite and the CPU baseline
+of bench.py; the product never imports it. The INI reader here follows the
+reference's PhysicalModel constructor (src/physical_model/physical_model.cpp:
+99-187): first definition of a key wins, missing keys leave defaults.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import multiprocessing as mp
+import os
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+LIB_PATH = ROOT / "oracle" / "_build" / "libmcac_oracle.so"
+
+i32, i64, f64 = C.c_int32, C.c_int64, C.c_double
+
+
+class MoParams(C.Structure):
+    _fields_ = [("n_monomeres", i64), ("density", f64), ("mean_diameter", f64), ("dispersion_diameter", f64),
+                ("initialisation_mode", i32), ("random_seed", i32), ("initial_time", f64),
+                ("volume_fraction", f64), ("temperature", f64), ("fractal_dimension", f64), ("viscosity", f64),
+                ("gaz_mean_free_path", f64), ("box_length", f64), ("n_verlet_divisions", i64),
+                ("enforce_volume_fraction", i32), ("with_collisions", i32),
+                ("number_of_aggregates_limit", i64), ("n_iter_without_event_limit", i64),
+                ("mean_monomere_per_aggregate_limit", i64), ("physical_time_limit", f64)]
+
+
+class MoContact(C.Structure):
+    _fields_ = [("distance", f64), ("moving_sphere", i64), ("other_sphere", i64), ("moving_aggregate", i64),
+                ("other_aggregate", i64)]
+
+
+class MoStats(C.Structure):
+    _fields_ = [("steps", i64), ("events", i64), ("n_aggregates", i64), ("time", f64), ("finished", i32),
+                ("reserved", i32)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            from mcac_gb300 import build
+            build.build_oracle()
+        L = C.CDLL(str(LIB_PATH))
+        P = C.POINTER
+        sig = {
+            "mo_params_derive": (None, [P(MoParams), f64]),
+            "mo_box_new_random": (C.c_int, [P(MoParams), P(C.c_void_p)]),
+            "mo_box_new_state": (C.c_int, [P(MoParams), i64, i64, i64, f64, f64, f64, P(f64), P(i64), P(f64),
+                                           P(i64), P(i64), P(C.c_void_p)]),
+            "mo_box_free": (None, [C.c_void_p]),
+            "mo_size": (i64, [C.c_void_p]),
+            "mo_n_spheres": (i64, [C.c_void_p]),
+            "mo_store": (None, [C.c_void_p, P(f64), P(i64), P(f64), P(i64), P(i64), P(f64)]),
+            "mo_distance_to_next_contact": (C.c_int, [C.c_void_p, i64, P(f64), f64, P(MoContact)]),
+            "mo_translate": (None, [C.c_void_p, i64, P(f64)]),
+            "mo_merge": (C.c_int, [C.c_void_p, P(MoContact), P(i32)]),
+            "mo_sort_indices": (None, [P(f64), P(i64), i64]),
+            "mo_time": (f64, [C.c_void_p]),
+            "mo_set_time": (None, [C.c_void_p, f64]),
+            "mo_calcul": (C.c_int, [C.c_void_p, i64, C.c_void_p, i64, P(MoStats)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(arr, ctype):
+    return arr.ctypes.data_as(C.POINTER(ctype))
+
+
+def parse_ini(text: str) -> dict:
+    data: dict = {}
+    section = ""
+    for raw in text.splitlines():
+        line = raw.strip()
+        if not line or line[0] in ";#":
+            continue
+        if line[0] == "[":
+            section = line[1:line.index("]")].strip() if "]" in line else section
+            continue
+        if "=" not in line:
+            continue
+        k, v = line.split("=", 1)
+        data.setdefault(section, {}).setdefault(k.strip(), v.strip())
+    return data
+
+
+def params_from_ini(text: str) -> MoParams:
+    ini = parse_ini(text)
+
+    def get(sec, key, conv, default):
+        v = ini.get(sec, {}).get(key)
+        if v is None or v == "":
+            return default
+        try:
+            if conv is bool:
+                if v not in ("true", "false"):
+                    return default
+                return v == "true"
+            return conv(v)
+        except ValueError:
+            return default
+
+    p = MoParams()
+    p.n_monomeres = get("monomers", "number", int, 2500)
+    p.density = get("monomers", "density", float, 1800.0)
+    p.mean_diameter = get("monomers", "mean_diameter", float, 30.0)
+    p.dispersion_diameter = get("monomers", "dispersion_diameter", float, 1.0)
+    p.initialisation_mode = {"lognormal": 0, "normal": 1}[get("monomers", "initialisation_mode", str, "lognormal")]
+    p.initial_time = get("environment", "initial_time", float, 0.0)
+    p.volume_fraction = get("environment", "volume_fraction", float, 1e-3)
+    p.temperature = get("environment", "temperature", float, 293.15)
+    pressure = get("environment", "pressure", float, 101300.0)
+    p.fractal_dimension = get("environment", "fractal_dimension", float, 1.4)
+    p.number_of_aggregates_limit = get("limits", "number_of_aggregates", int, 1)
+    p.n_iter_without_event_limit = get("limits", "n_iter_without_event", int, -1)
+    p.physical_time_limit = get("limits", "physical_time", float, -1.0)
+    p.mean_monomere_per_aggregate_limit = get("limits", "mean_monomere_per_aggregate", int, -1)
+    p.with_collisions = get("numerics", "with_collisions", bool, True)
+    p.enforce_volume_fraction = get("numerics", "enforce_volume_fraction", bool, True)
+    p.n_verlet_divisions = get("numerics", "n_verlet_divisions", int, 10)
+    p.random_seed = get("numerics", "random_seed", int, -1)
+    lib().mo_params_derive(C.byref(p), pressure)
+    return p
+
+
+class OracleBox:
+    """One box of the C restatement."""
+
+    def __init__(self, ini_text: str, snap=None):
+        self.params = params_from_ini(ini_text)
+        self.h = C.c_void_p()
+        if snap is None:
+            rc = lib().mo_box_new_random(C.byref(self.params), C.byref(self.h))
+        else:
+            self._keep = [np.ascontiguousarray(a) for a in (snap.spheres, snap.sphere_label, snap.aggregates,
+                                                          snap.n_spheres, snap.members)]
+            sp, sl, ag, nsph, mem = self._keep
+            rc = lib().mo_box_new_state(C.byref(self.params), snap.ns, snap.na, snap.n_div, snap.box_length,
+                                        snap.maxradius, snap.time, _p(sp, f64), _p(sl, i64), _p(ag, f64),
+                                        _p(nsph, i64), _p(mem, i64), C.byref(self.h))
+        if rc != 0:
+            raise RuntimeError(f"oracle error {rc}")
+
+    def close(self):
+        if self.h:
+            lib().mo_box_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    def size(self) -> int:
+        return int(lib().mo_size(self.h))
+
+    def distance_to_next_contact(self, label, direction, distance):
+        d = np.ascontiguousarray(direction, dtype=np.float64)
+        c = MoContact()
+        rc = lib().mo_distance_to_next_contact(self.h, int(label), _p(d, f64), float(distance), C.byref(c))
+        if rc:
+            raise RuntimeError(f"oracle error {rc}")
+        return c
+
+    def translate(self, label, vec):
+        v = np.ascontiguousarray(vec, dtype=np.float64)
+        lib().mo_translate(self.h, int(label), _p(v, f64))
+
+    def merge(self, c: MoContact) -> bool:
+        m = C.c_int32()
+        rc = lib().mo_merge(self.h, C.byref(c), C.byref(m))
+        if rc:
+            raise RuntimeError(f"oracle error {rc}")
+        return bool(m.value)
+
+    def calcul(self, max_steps=0, trace=False, trace_capacity=0):
+        from mcac_gb300.snapshot import STEP_DTYPE
+        st = MoStats()
+        buf = None
+        cap = 0
+        if trace:
+            cap = int(trace_capacity or max_steps or 1_000_000)
+            buf = np.zeros(cap, dtype=STEP_DTYPE)
+        rc = lib().mo_calcul(self.h, int(max_steps), buf.ctypes.data if buf is not None else None, cap,
+                             C.byref(st))
+        if rc:
+            raise RuntimeError(f"oracle error {rc}")
+        return st, (buf[:min(int(st.steps), cap)] if buf is not None else None)
+
+    def store(self):
+        from mcac_gb300.snapshot import Snapshot
+        ns, na = int(lib().mo_n_spheres(self.h)), self.size()
+        sp = np.zeros((9, ns))
+        sl = np.zeros(ns, np.int64)
+        ag = np.zeros((21, na))
+        nsph = np.zeros(na, np.int64)
+        mem = np.zeros(ns, np.int64)
+        sc = np.zeros(3)
+        lib().mo_store(self.h, _p(sp, f64), _p(sl, i64), _p(ag, f64), _p(nsph, i64), _p(mem, i64), _p(sc, f64))
+        step = self.params.n_verlet_divisions / sc[2]
+        cells = np.stack([np.floor(ag[f] * step) for f in (7, 8, 9)], axis=1).astype(np.int64)
+        return Snapshot(n_div=int(self.params.n_verlet_divisions), box_length=float(sc[2]), maxradius=float(sc[0]),
+                        time=float(sc[1]), physics=np.zeros(9), volsurf_method=4, spheres=sp, sphere_label=sl,
+                        aggregates=ag, n_spheres=nsph, members=mem, cells=cells)
+
+
+def sort_indices(keys: np.ndarray) -> np.ndarray:
+    k = np.ascontiguousarray(keys, dtype=np.float64)
+    idx = np.zeros(len(k), dtype=np.int64)
+    lib().mo_sort_indices(_p(k, f64), _p(idx, i64), len(k))
+    return idx
+
+
+# ---------------------------------------------------------------- bench
+def _worker(args):
+    ini_text, snap_bytes, seconds, chunk = args
+    from mcac_gb300.snapshot import Snapshot
+    snap = Snapshot.from_bytes(snap_bytes)
+    box = OracleBox(ini_text, snap)
+    steps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        st, _ = box.calcul(max_steps=chunk)
+        steps += int(st.steps)
+        if st.finished:
+            break
+    dt = time.perf_counter() - t0
+    box.close()
+    return steps, dt
+
+
+def bench_sample(ini_text: str, seconds: float = 15.0, processes: int = 1, steps: int = 1, warmup: int = 0,
+                 chunk: int = 200) -> dict:
+    """MC steps/s of the restatement on a bounded sample of the workload.
+
+    The initial state is the reference placement (identical in the product
+    and here); each process advances its own copy of the box from that
+    state for 'seconds' of wall time. With several processes the value is
+    the sum of their rates (independent boxes, one per core).
+    """
+    from mcac_gb300 import PhysicalModel, init_state
+    pm = PhysicalModel(text=ini_text)
+    snap = init_state(pm).to_snapshot()
+    blob = snap.to_bytes()
+    per = seconds
+    jobs = [(ini_text, blob, per, chunk)] * processes
+    if processes == 1:
+        res = [_worker(jobs[0])]
+    else:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(processes) as pool:
+            res = pool.map(_worker, jobs)
+    total_steps = sum(r[0] for r in res)
+    value = sum(r[0] / r[1] for r in res)
+    return {"value": value, "unit": "MC steps/s", "cores": processes, "kind": "port",
+            "sample": f"{processes} independent copies of the 100k-monomer box from the reference initial state, "
+                      f"~{per:.0f} s of MC steps each ({total_steps} steps in total)",
+            "host_cpus": os.cpu_count()}

@@ -149,6 +149,14 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     ok = ok && alloc((void **)&b.row_cnt, sizeof(int) * (size_t(std::max(st.ns, st.nslots)) + 2));
     ok = ok && alloc((void **)&b.work, sizeof(double) * 8 * size_t(st.ns));
     ok = ok && alloc((void **)&b.counters, sizeof(int) * 8);
+    const size_t nc1 = size_t(st.nslots) + 1;
+    ok = ok && alloc((void **)&b.cand_db, sizeof(double) * nc1);
+    ok = ok && alloc((void **)&b.cand_flat, sizeof(int) * nc1);
+    ok = ok && alloc((void **)&b.cand_slot, sizeof(int) * nc1);
+    ok = ok && alloc((void **)&b.cand_order, sizeof(int) * nc1);
+    ok = ok && alloc((void **)&b.cand_prefix, sizeof(int) * nc1);
+    ok = ok && alloc((void **)&b.best_res, sizeof(unsigned long long) * nc1);
+    ok = ok && alloc((void **)&b.best_ij, sizeof(unsigned long long) * nc1);
     if (!ok) {
         delete d;
         return ST_CUDA;

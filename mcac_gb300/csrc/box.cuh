@@ -26,10 +26,9 @@
 namespace mcacg {
 
 constexpr int kQueryThreads = 512;
-constexpr int kMaxCandidates = 1024;   // aggregates passing the bounding-sphere filter
-constexpr int kCellChunk = 2048;       // Verlet cells scanned per chunk
-constexpr int kMoveTile = 1024;        // moving spheres staged per pass
-constexpr int kMaxSurvivorsSmem = 1024;
+constexpr int kCellChunk = 1024;       // Verlet cells scanned per chunk
+constexpr int kMoveTile = 512;         // moving spheres staged per pass
+constexpr int kMaxSurvivorsSmem = 256; // refined pairs kept in shared memory (the rest in HBM)
 
 // Mutable per-box scalars, in device memory.
 struct DevScalars {
@@ -75,8 +74,12 @@ struct DevBox {
     int *pair_tmp_i, *pair_tmp_j;
     double *pair_tmp_d;
     int *row_cnt;        // [ns + 1]
-    double *work;        // [6][ns] per-sphere terms of the merge sums
+    double *work;        // [8][ns] per-sphere terms of the merge sums
     int *counters;       // [8]
+    // contact-query candidates (at most one per aggregate slot)
+    double *cand_db;
+    int *cand_flat, *cand_slot, *cand_order, *cand_prefix;
+    unsigned long long *best_res, *best_ij;
 };
 
 __device__ __forceinline__ double &A(const DevBox &b, int field, int slot) {
@@ -169,9 +172,9 @@ __device__ __forceinline__ bool capsule_hit(const Sweep32 &w, float qx, float qy
 }
 
 // ------------------------------------------------------------ block scans
-template <int NT>
 __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tmp, int &total) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int NT = blockDim.x;
     int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -200,13 +203,14 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tmp, int &t
 struct QuerySmem {
     int cell_prefix[kCellChunk + 1];
     int cell_lin[kCellChunk];
-    double cand_db[kMaxCandidates];
-    int cand_flat[kMaxCandidates];
-    int cand_slot[kMaxCandidates];
-    int cand_order[kMaxCandidates];   // sorted position -> candidate
-    int cand_prefix[kMaxCandidates + 1];
-    unsigned long long best_res[kMaxCandidates];
-    unsigned long long best_ij[kMaxCandidates];
+    // candidate arrays live in the machine's HBM scratch (one entry per slot at most)
+    double *cand_db;
+    int *cand_flat;
+    int *cand_slot;
+    int *cand_order;   // sorted position -> candidate
+    int *cand_prefix;
+    unsigned long long *best_res;
+    unsigned long long *best_ij;
     float4 mov[kMoveTile];
     int4 surv[kMaxSurvivorsSmem];
     double surv_res[kMaxSurvivorsSmem];
@@ -236,7 +240,7 @@ struct QuerySmem {
 // Must be called by all threads of the block.
 __device__ void block_query(const DevBox &b, int src, Vec3 dir, double dist, QuerySmem &sm) {
     const int tid = threadIdx.x;
-    const int NT = kQueryThreads;
+    const int NT = blockDim.x;
     const DevScalars *sc = b.sc;
     const int *pool_id = b.pool_id[sc->pool_sel];
     const float4 *pool_pos = b.pool_pos[sc->pool_sel];
@@ -263,6 +267,13 @@ __device__ void block_query(const DevBox &b, int src, Vec3 dir, double dist, Que
         sm.out.n_cells = 0;
         sm.out.n_cand_spheres = 0;
         sm.out.n_mov = b.agg_n[src];
+        sm.cand_db = b.cand_db;
+        sm.cand_flat = b.cand_flat;
+        sm.cand_slot = b.cand_slot;
+        sm.cand_order = b.cand_order;
+        sm.cand_prefix = b.cand_prefix;
+        sm.best_res = b.best_res;
+        sm.best_ij = b.best_ij;
     }
     __syncthreads();
 
@@ -308,7 +319,7 @@ __device__ void block_query(const DevBox &b, int src, Vec3 dir, double dist, Que
             }
         }
         int total;
-        int base = block_exclusive_scan<kQueryThreads>(cnt_local, sm.warp_tmp, total);
+        int base = block_exclusive_scan(cnt_local, sm.warp_tmp, total);
         {
             int run = base;
             for (int k = 0; k < per; ++k) {
@@ -339,12 +350,10 @@ __device__ void block_query(const DevBox &b, int src, Vec3 dir, double dist, Que
             if (!capsule_hit(w, float(ox), float(oy), float(oz), float(rmax_src + orm) + margin)) continue;
             double db = sweep_contact_distance(sp, rmax_src, Vec3{ox, oy, oz}, orm, dir, dist, b.L);
             if (db < dist) {
-                int k = atomicAdd(&sm.n_cand, 1);
-                if (k < kMaxCandidates) {
-                    sm.cand_db[k] = db;
-                    sm.cand_flat[k] = sm.flat_base + f;
-                    sm.cand_slot[k] = slot;
-                }
+                int k = atomicAdd(&sm.n_cand, 1);  // < nslots: one entry per aggregate
+                sm.cand_db[k] = db;
+                sm.cand_flat[k] = sm.flat_base + f;
+                sm.cand_slot[k] = slot;
             }
         }
         __syncthreads();
@@ -354,12 +363,7 @@ __device__ void block_query(const DevBox &b, int src, Vec3 dir, double dist, Que
     if (tid == 0) {
         sm.out.n_scanned = sm.flat_base;
         sm.out.n_cells = n_scan;
-        sm.out.n_candidates = min(sm.n_cand, kMaxCandidates);
-    }
-    if (sm.n_cand > kMaxCandidates) {
-        if (tid == 0) sm.out.status = ST_CAPACITY;
-        __syncthreads();
-        return;
+        sm.out.n_candidates = sm.n_cand;
     }
     if (!sm.found_source) {
         if (tid == 0) sm.out.status = ST_VERLET;  // "Aggregate not on the verlet list"
@@ -367,7 +371,10 @@ __device__ void block_query(const DevBox &b, int src, Vec3 dir, double dist, Que
         return;
     }
     const int nc = sm.n_cand;
-    if (nc == 0) return;
+    if (nc == 0) {
+        __syncthreads();
+        return;
+    }
 
     // order candidates by (d_b, scan position): rank sort
     for (int k = tid; k < nc; k += NT) {

@@ -1,0 +1,273 @@
+// Device-resident MC loop: one thread block advances one box for many steps
+// without returning to the host (the batched / served form).
+//
+// Per step (src/calcul.cpp:94-281, collision-only):
+//   pick   a slot with probability 1/time_step / sum(1/time_step), by a
+//          descent of a 32-ary FP64 sum tree (warp-wide scans), and advance
+//          time by 1 / sum(1/time_step) -- the reference's
+//          max / sum(max / time_step), rearranged;
+//   move   random direction from the box's own C-library rand() stream,
+//          contact search (block_query), translation (block_translate);
+//   merge  block_merge, then the aggregate physics of update_partial
+//          (erf/exp/pow from CUDA's libm) and two tree updates.
+// The contact search and merge geometry are the exact kernels of the
+// single-box path; pick order and libm differ from the reference, so runs
+// agree with it statistically, not step by step (the host-driven loop is the
+// bit-exact form).
+#pragma once
+#include "box.cuh"
+#include "merge.cuh"
+#include "rng.hpp"
+
+namespace mcacg {
+
+constexpr int kTreeFan = 32;
+constexpr int kMaxTreeLevels = 8;
+
+struct PhysParams {
+    double viscosity, lambda, fractal_dimension, density, temperature;
+};
+
+struct RunLimits {
+    long long number_of_aggregates_limit, n_iter_without_event_limit, mean_monomere_per_aggregate_limit;
+    double physical_time_limit;
+    int with_collisions;
+    int pad;
+};
+
+// Mutable loop state of one box (device memory).
+struct RunState {
+    RandStream rng;
+    double time;
+    double weight_total;     // sum over live slots of 1/time_step
+    long long steps, events, n_iter_without_event;
+    int finished;
+    int status;
+    int pad[2];
+};
+
+struct BoxRun {
+    DevBox box;
+    PhysParams phys;
+    RunLimits lim;
+    RunState *st;
+    double *tree;            // all levels, leaves first
+    int tree_levels;
+    int tree_off[kMaxTreeLevels];
+    int tree_len[kMaxTreeLevels];
+};
+
+struct RunSmem {
+    union {
+        QuerySmem q;
+        MergeSmem m;
+    } u;
+    MergeOut mout;
+    double refpos[3];
+    double dir[3];
+    double t_pick, dt, full, move;
+    int slot, contact, stop, merged;
+    int keep, removed;
+    int ms, os, oslot;  // contact of this step: spheres and the other slot
+};
+
+// ------------------------------------------------------------ sum tree
+// Warp 0: descend from the top level to a leaf holding the target 't'.
+__device__ int tree_sample(const BoxRun &R, double t) {
+    const int lane = threadIdx.x & 31;
+    int node = 0;  // index within the current level
+    for (int lev = R.tree_levels - 1; lev >= 0; --lev) {
+        const int base = node * kTreeFan;
+        const int len = R.tree_len[lev];
+        double v = (base + lane < len) ? R.tree[R.tree_off[lev] + base + lane] : 0.0;
+        // inclusive scan over the 32 children (fixed order)
+        double incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            double y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        unsigned over = __ballot_sync(0xffffffffu, incl > t && v > 0.0);
+        unsigned nonzero = __ballot_sync(0xffffffffu, v > 0.0);
+        int pick = over ? __ffs(over) - 1 : (nonzero ? 31 - __clz(nonzero) : 0);
+        double before = __shfl_sync(0xffffffffu, incl - v, pick);
+        t -= before;
+        node = base + pick;
+    }
+    return node;
+}
+
+// Warp 0: set leaf 'slot' to 'w' and refresh its ancestors; returns the new total.
+__device__ double tree_set(const BoxRun &R, int slot, double w) {
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) R.tree[R.tree_off[0] + slot] = w;
+    __syncwarp();
+    int idx = slot;
+    double total = 0.0;
+    for (int lev = 0; lev < R.tree_levels; ++lev) {
+        const int g = idx / kTreeFan;
+        const int len = R.tree_len[lev];
+        double v = (g * kTreeFan + lane < len) ? R.tree[R.tree_off[lev] + g * kTreeFan + lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lev + 1 < R.tree_levels) {
+            if (lane == 0) R.tree[R.tree_off[lev + 1] + g] = v;
+            __syncwarp();
+        } else {
+            total = v;
+        }
+        idx = g;
+    }
+    return total;
+}
+
+// ------------------------------------------------------------ physics
+// update_partial's physics (aggregat.cpp:264-276, physical_model.cpp:550-617)
+// with CUDA's erf / exp / pow.
+__device__ void device_physics(const PhysParams &p, double V, double vol_pp, double dp, double rg, double *f_agg,
+                               double *d_m, double *time_step, double *lpm, double *dg_over_dp) {
+    const double r = 0.5 * dp;
+    const double a = 1.142, b = 0.558, c = 0.999;
+    const double fe = 0.689 * (1. + erf(((p.lambda / r) + 4.454) / 10.628));
+    const double cc = 1.0 + a * p.lambda / r + b * p.lambda / r * exp(-c * r / p.lambda);
+    const double ratio = V / vol_pp;
+    const double f = (6. * pi_value() * p.viscosity * r / cc) * pow(ratio, fe / p.fractal_dimension);
+    const double ar = r * pow(ratio, fe / p.fractal_dimension / 2.0);
+    const double cc_a = 1.0 + a * p.lambda / ar + b * p.lambda / ar * exp(-c * ar / p.lambda);
+    *f_agg = f;
+    *d_m = (cc_a / cc) * 2.0 * r * pow(ratio, fe / p.fractal_dimension);
+    const double masse = p.density * V;
+    *time_step = 3. * (masse / f);
+    const double diffusivity = kBoltzmann * p.temperature / f;
+    *lpm = sqrt(6. * diffusivity * *time_step);
+    *dg_over_dp = 2 * rg / dp;
+}
+
+__device__ __forceinline__ bool run_finished(const BoxRun &R, const RunState &st, int n_alive) {
+    const RunLimits &L = R.lim;
+    if (n_alive < 1) return true;
+    if (static_cast<unsigned long long>(n_alive) <= static_cast<unsigned long long>(L.number_of_aggregates_limit))
+        return true;
+    if (L.n_iter_without_event_limit > 0 && st.n_iter_without_event >= L.n_iter_without_event_limit) return true;
+    if (L.physical_time_limit > 0 && st.time >= L.physical_time_limit) return true;
+    if (L.mean_monomere_per_aggregate_limit > 0 &&
+        double(R.box.ns) / double(n_alive) >= double(L.mean_monomere_per_aggregate_limit))
+        return true;
+    return false;
+}
+
+// One MC step of one box by the whole block. Returns false when the box is
+// finished or in error (then nothing was done).
+__device__ bool block_mc_step(const BoxRun &R, RunSmem &sm) {
+    const int tid = threadIdx.x;
+    const DevBox &b = R.box;
+    RunState &st = *R.st;
+    if (tid == 0) {
+        sm.stop = st.finished || st.status != ST_OK;
+        if (!sm.stop && run_finished(R, st, b.sc->n_alive)) {
+            st.finished = 1;
+            sm.stop = 1;
+        }
+        if (!sm.stop) sm.t_pick = st.rng.uniform() * st.weight_total;
+    }
+    __syncthreads();
+    if (sm.stop) return false;
+    if (tid < 32) {
+        int slot = tree_sample(R, sm.t_pick);
+        if (tid == 0) {
+            if (slot < 0 || slot >= b.nslots || b.agg_n[slot] == 0) {
+                st.status = ST_UNKNOWN;  // the tree lost a live slot: stop this box
+                sm.stop = 1;
+                slot = 0;
+            }
+            sm.slot = slot;
+            sm.dt = 1.0 / st.weight_total;
+            sm.full = A(b, AGG_LPM, slot);
+            double theta = st.rng.uniform() * 2 * pi_value();
+            double phi = acos(1 - 2 * st.rng.uniform());
+            double sp, cp, sth, cth;
+            sincos(phi, &sp, &cp);
+            sincos(theta, &sth, &cth);
+            sm.dir[0] = sp * cth;
+            sm.dir[1] = sp * sth;
+            sm.dir[2] = cp;
+        }
+    }
+    __syncthreads();
+    if (sm.stop) return false;
+    const int slot = sm.slot;
+    const Vec3 dir{sm.dir[0], sm.dir[1], sm.dir[2]};
+    if (R.lim.with_collisions) {
+        block_query(b, slot, dir, sm.full, sm.u.q);
+        if (tid == 0) {
+            const QueryOut &q = sm.u.q.out;
+            if (q.status != ST_OK) {
+                st.status = q.status;
+                sm.stop = 1;
+            }
+            sm.contact = q.distance <= sm.full;
+            sm.move = sm.contact ? q.distance : sm.full;
+            sm.ms = q.moving_sphere;
+            sm.os = q.other_sphere;
+            sm.oslot = q.other_slot;
+        }
+    } else if (tid == 0) {
+        sm.contact = 0;
+        sm.move = sm.full;
+    }
+    __syncthreads();
+    if (sm.stop) return false;
+    const int ms = sm.ms, os = sm.os, oslot = sm.oslot;
+    block_translate(b, slot, Vec3{dir.x * sm.move, dir.y * sm.move, dir.z * sm.move}, sm.refpos);
+    if (tid == 0) {
+        double dt = sm.dt * (sm.move / sm.full + 0.0);
+        A(b, AGG_TIME, slot) += dt;
+        st.time = st.time + dt;
+        sm.merged = 0;
+    }
+    __syncthreads();
+    if (sm.contact) {
+        block_merge(b, ms, os, slot, oslot, sm.u.m, &sm.mout);
+        if (tid == 0) {
+            if (sm.mout.status != ST_OK) {
+                st.status = sm.mout.status;
+                sm.stop = 1;
+            } else if (sm.mout.merged) {
+                const int keep = sm.mout.keep, removed = sm.mout.removed;
+                double f, dm, ts, lpm, dgdp;
+                device_physics(R.phys, sm.mout.fields[AGG_VOLUME], sm.mout.vol_pp, sm.mout.fields[AGG_DP],
+                               sm.mout.fields[AGG_RG], &f, &dm, &ts, &lpm, &dgdp);
+                A(b, AGG_F_AGG, keep) = f;
+                A(b, AGG_D_M, keep) = dm;
+                A(b, AGG_TIME_STEP, keep) = ts;
+                A(b, AGG_LPM, keep) = lpm;
+                A(b, AGG_DG_OVER_DP, keep) = dgdp;
+                A(b, AGG_TIME, keep) = A(b, AGG_TIME, keep) + A(b, AGG_TIME, removed) - st.time;
+                sm.merged = 1;
+                sm.keep = keep;
+                sm.removed = removed;
+            }
+        }
+        __syncthreads();
+        if (sm.stop) return false;
+        if (sm.merged && tid < 32) {
+            tree_set(R, sm.removed, 0.0);
+            double total = tree_set(R, sm.keep, 1.0 / A(b, AGG_TIME_STEP, sm.keep));
+            if (tid == 0) st.weight_total = total;
+        }
+    }
+    if (tid == 0) {
+        st.steps += 1;
+        if (sm.merged) {
+            st.events += 1;
+            st.n_iter_without_event = 0;
+        } else {
+            st.n_iter_without_event += 1;
+        }
+        if (run_finished(R, st, b.sc->n_alive)) st.finished = 1;
+    }
+    __syncthreads();
+    return true;
+}
+
+}  // namespace mcacg

@@ -3,22 +3,25 @@
 Workload (default): the 100 000-monomer box of the benchmark set --
 LogNormal(30 nm, sigma_geo 1.25) diameters, 1000 ppm volume fraction,
 T=1700 K, P=101300 Pa, rho=1800 kg/m3, kfe=1.4, dfe=1.8, no surface growth,
-stop at 100 aggregates, seed 1. One "bench step" is a batch of MC steps
-(--mc-steps, default 2000) of the pick-move-collide-merge loop; the metric is
-MC steps per second.
+stop at 100 aggregates, seed 1. One "bench step" advances every replica of
+that box by --mc-steps (default 2000) steps of the pick-move-collide-merge
+loop; the metric is MC steps per second summed over replicas.
 
 Arms:
-  --impl ours       (default) the host-driven loop of the C-ABI with the
-                    contact search, translation and merge on the GPU; value
-                    is timed with CUDA events on the box's stream, e2e adds
-                    the upload of the state from host buffers and the
-                    download of the final state through the C-ABI.
+  --impl ours       (default) R independent replicas of the box (seeds 1..R,
+                    R = one per SM unless --replicas) advanced by the
+                    device-resident loop, one thread block per box; value is
+                    timed with CUDA events on the launching stream; e2e goes
+                    through the C-ABI from host buffers: upload of the R
+                    states, the steps, download of the R states. The line
+                    also reports the plain host-driven single-box path
+                    (the bit-exact drop-in form) and a one-core CPU sample.
   --impl reference  the CPU restatement of the reference algorithm (oracle/)
-                    on the host cores, one independent box per core, on a
-                    bounded sample of the same workload.
+                    on all host cores, one independent replica per core, on
+                    a bounded sample of the same workload.
 
-Under torchrun each rank runs an independent replica (the single-box loop
-has no data-parallel exchange): value = total steps of all ranks / max time.
+Under torchrun each rank runs its own replicas (boxes are independent; no
+exchange): value = total steps of all ranks / max time.
 """
 from __future__ import annotations
 
@@ -134,65 +137,108 @@ def query_bytes(prof: dict) -> float:
             + 16.0 * prof["cand_spheres"] + 64.0 * prof["refined"])
 
 
+def replica_models(n: int, base_seed: int):
+    from mcac_gb300 import PhysicalModel
+    models = []
+    for i in range(n):
+        pm = PhysicalModel(text=C2_INI)
+        pm.set(random_seed=base_seed + i)
+        models.append(pm)
+    return models
+
+
+def host_states(models):
+    """The reference placement of every replica, on the host (parallel)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from mcac_gb300 import init_state
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        return list(ex.map(init_state, models))
+
+
+def plain_single_box(args, stream) -> dict:
+    """The host-driven loop on one box (the bit-exact drop-in form)."""
+    import torch
+
+    from mcac_gb300 import AggregatList, PhysicalModel
+    pm = PhysicalModel(text=C2_INI)
+    with AggregatList(pm, stream=stream.cuda_stream) as box:
+        box.set_profiling(True)
+        box.calcul(max_steps=args.plain_steps)
+        box.take_profile()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st, _ = box.calcul(max_steps=args.plain_steps)
+        e1.record(stream)
+        e1.synchronize()
+        prof = box.take_profile()
+    ms = e0.elapsed_time(e1)
+    return {"value": st.steps / (ms / 1000.0), "unit": UNIT, "steps": int(st.steps),
+            "query_us_per_launch": 1000.0 * prof["query_ms"] / max(1, prof["queries"]),
+            "note": "one box, one contact query / translation (/ merge) kernel launch per MC step, "
+                    "pick CDF on the host exactly as the reference (std::sort after every merge)"}
+
+
 def run_ours(args, rank: int, world: int) -> dict | None:
     import torch
-    import numpy as np
 
-    from mcac_gb300 import AggregatList, PhysicalModel, init_state
-    from mcac_gb300._lib import StateBuffers
+    from mcac_gb300 import Batch
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
-    pm = PhysicalModel(text=C2_INI)
-    if world > 1:
-        pm.set(random_seed=int(pm.params.random_seed) + rank)
+    R = args.replicas or torch.cuda.get_device_properties(dev).multi_processor_count
+    models = replica_models(R, 1 + rank * R)
     t0 = time.perf_counter()
-    sb = init_state(pm)
-    init_s = time.perf_counter() - t0
-    box = AggregatList(pm, sb, stream=stream.cuda_stream)
-    box.set_profiling(True)
+    batch = Batch(models, stream=stream.cuda_stream)
+    setup_s = time.perf_counter() - t0
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     M = args.mc_steps
     for _ in range(args.warmup):
-        box.calcul(max_steps=M)
-    box.take_profile()
+        batch.run(max_steps=M, steps_per_launch=M)
     torch.cuda.synchronize()
+    steps0 = int(batch.stats()["steps"].sum())
+    work0 = batch.work()
     if world > 1:
         torch.distributed.barrier()
     sampler = ClockSampler(dev)
     sampler.start()
-    total_ms = 0.0
-    steps_done = 0
+    total_ms, launches = 0.0, 0
     for _ in range(args.steps):
         flush.zero_()  # L2 flushed between timed iterations (outside the events)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        stats, _ = box.calcul(max_steps=M)
+        batch.run(max_steps=M, steps_per_launch=M)
         e1.record(stream)
         e1.synchronize()
         total_ms += e0.elapsed_time(e1)
-        steps_done += int(stats.steps)
+        launches += batch.last_run()[1]
     torch.cuda.synchronize()
     clocks = sampler.stop()
-    prof = box.take_profile()
-    # end to end through the C-ABI with host buffers: upload, M steps, download
-    snap = box.store()
-    e2e_steps, e2e_s = 0, 0.0
-    h2d = d2h = 0
-    for _ in range(max(1, args.steps // 2)):
-        sbuf = StateBuffers.from_snapshot(snap)
-        h2d = int(sbuf.spheres.nbytes + sbuf.sphere_label.nbytes + sbuf.aggregates.nbytes + sbuf.n_spheres.nbytes
-                  + sbuf.members.nbytes)
+    st = batch.stats()
+    steps_done = int(st["steps"].sum()) - steps0
+    work1 = batch.work()
+    prof = {k: work1[k] - work0[k] for k in work1}
+    n_alive = st["n_aggregates"].tolist()
+    batch.close()
+    del flush
+    # end to end through the C-ABI from host buffers: upload R states, M steps
+    # per box, download R states
+    states = host_states(models)
+    h2d = sum(int(b.spheres.nbytes + b.sphere_label.nbytes + b.aggregates.nbytes + b.n_spheres.nbytes
+                  + b.members.nbytes) for b in states)
+    e2e_steps, e2e_s, d2h = 0, 0.0, 0
+    for _ in range(max(1, args.e2e_steps)):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        with AggregatList(pm, sbuf, stream=stream.cuda_stream) as b2:
-            st, _ = b2.calcul(max_steps=M)
-            out = b2.store()
+        with Batch(models, stream=stream.cuda_stream, states=states) as b2:
+            b2.run(max_steps=M, steps_per_launch=M)
+            outs = [b2.store(k) for k in range(R)]
+            e2e_steps += int(b2.stats()["steps"].sum())
         e2e_s += time.perf_counter() - t
-        e2e_steps += int(st.steps)
-        d2h = int(out.spheres.nbytes + out.sphere_label.nbytes + out.aggregates.nbytes + out.n_spheres.nbytes
-                  + out.members.nbytes)
+        d2h = sum(int(o.spheres.nbytes + o.sphere_label.nbytes + o.aggregates.nbytes + o.n_spheres.nbytes
+                      + o.members.nbytes) for o in outs)
     times = torch.tensor([total_ms / 1000.0, float(steps_done), e2e_s, float(e2e_steps)], device="cuda",
                          dtype=torch.float64)
     if world > 1:
@@ -208,28 +254,32 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         return None
     peak, peak_kind = peaks()
     qbytes = query_bytes(prof)
-    q_s = prof["query_ms"] / 1000.0
-    achieved = qbytes / q_s / 1e9 if q_s > 0 else 0.0
-    launches = int(prof["queries"] + prof["translates"] + 2 * prof["merges"])
-    return {
+    achieved = qbytes / (total_ms / 1000.0) / 1e9 if total_ms > 0 else 0.0
+    out = {
         "metric": METRIC, "value": steps_all / wall, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": wall * 1000.0 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "100k-monomer box: LogNormal(30 nm, 1.25), 1000 ppm, 1700 K, seed 1, "
-                               "stop at 100 aggregates", "n_monomers": 100000, "mc_steps_per_bench_step": M,
-                   "path": "host-driven MC loop, contact search/translate/merge kernels on the GPU",
-                   "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) between timed iterations",
-                   "init_s": round(init_s, 3)},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                     "kernel": "k_query", "bytes_per_launch": qbytes / max(1, prof["queries"]),
-                     "us_per_launch": 1000.0 * prof["query_ms"] / max(1, prof["queries"])},
+                               "stop at 100 aggregates", "n_monomers": 100000, "replicas_per_gpu": R,
+                   "replica_seeds": f"{1 + rank * R}..{R + rank * R}", "mc_steps_per_box_per_bench_step": M,
+                   "path": "device-resident MC loop, one thread block per box, one launch per bench step",
+                   "parallelism": f"{R} independent replicas per GPU x {world} GPU",
+                   "l2": "flushed (256 MB write) between timed iterations", "setup_s": round(setup_s, 2),
+                   "aggregates_left": [min(n_alive), max(n_alive)]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None, "kernel": "k_run (batched MC loop)",
+                     "bytes_per_launch": qbytes / max(1, launches), "us_per_launch": 1000.0 * total_ms / max(1, launches),
+                     "bytes_model": "per contact query: 16 B x moving spheres + 36 B x aggregates scanned + 8 B x cells "
+                                    "+ 16 B x candidate spheres + 64 B x FP64-refined pairs"},
         "e2e": {"value": e2e_all / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks,
-        "profile": prof,
-        "cpu_baseline": cpu_baseline_sample(args) if not args.no_cpu_baseline else None,
+        "work": prof,
     }
+    if not args.no_plain:
+        out["plain_single_box"] = plain_single_box(args, stream)
+    out["cpu_baseline"] = cpu_baseline_sample(args) if not args.no_cpu_baseline else None
+    return out
 
 
 def cpu_baseline_sample(args) -> dict | None:
@@ -265,7 +315,11 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mc-steps", type=int, default=2000)
+    ap.add_argument("--mc-steps", type=int, default=2000, help="MC steps per box per bench step")
+    ap.add_argument("--replicas", type=int, default=0, help="boxes per GPU (0: one per SM)")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--plain-steps", type=int, default=500)
+    ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

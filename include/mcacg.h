@@ -248,6 +248,42 @@ int mcacg_get_aggregate(const mcacg_box *box, int64_t label, double fields[21], 
  * reference binary built with FP contraction off. */
 int mcacg_calcul(mcacg_box *box, const mcacg_run_opts *opts, mcacg_run_stats *stats);
 
+/* ---- device-resident runs (batched and served forms) ----
+ * The same MC loop with every step on the GPU: one thread block per box,
+ * many steps per launch, no host round trip. Contact search, translation and
+ * merge geometry are the exact kernels of the calls above; the pick walks a
+ * sum tree of 1/time_step (same probabilities as the reference's sorted CDF,
+ * different order) and directions and aggregate physics use CUDA's libm, so
+ * these runs follow the reference statistically, not step by step. Each box
+ * draws from its own copy of the C library rand() stream seeded with its
+ * random_seed, continued across consecutive device runs. No counterpart in
+ * the reference (it has no batched mode). */
+typedef struct mcacg_batch mcacg_batch;
+/* Advances one box on the GPU by at most max_steps steps (<= 0: until a stop
+ * criterion of its parameters). */
+int mcacg_run_device(mcacg_box *box, int64_t max_steps, mcacg_run_stats *stats);
+/* n_boxes independent boxes, box i placed as mcacg_box_create would place it
+ * with params[i] (size, seed, physics and stop criteria per box). */
+int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_stream, mcacg_batch **batch);
+/* n_boxes boxes from host states (states[i] as for mcacg_box_create_from_state);
+ * params[i] gives box i's physics, stop criteria and device stream seed. */
+int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state *states, int32_t n_boxes,
+                                   void *cuda_stream, mcacg_batch **batch);
+int mcacg_batch_destroy(mcacg_batch *batch);
+/* Advances every unfinished box by at most max_steps steps (<= 0: until all
+ * meet their stop criteria) in kernel launches of steps_per_launch steps. */
+int mcacg_batch_run(mcacg_batch *batch, int64_t max_steps, int64_t steps_per_launch);
+/* Per-box counters since creation (arrays of n_boxes). */
+int mcacg_batch_stats(mcacg_batch *batch, mcacg_run_stats *stats);
+int mcacg_batch_size(const mcacg_batch *batch, int32_t *n_boxes);
+int mcacg_batch_box_sizes(mcacg_batch *batch, int32_t box, int64_t *n_spheres, int64_t *n_aggregates);
+int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state);
+/* Work counters of all boxes since creation, summed (the query and merge
+ * fields of mcacg_profile; times are left at 0). */
+int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out);
+/* GPU time (CUDA events) and kernel launches of the last mcacg_batch_run. */
+int mcacg_batch_last_run(const mcacg_batch *batch, double *kernel_ms, int32_t *launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -105,6 +105,17 @@ SIGNATURES = {
     "mcacg_get_total_surface": [vp, C.POINTER(f64)],
     "mcacg_get_aggregate": [vp, i64, C.POINTER(f64), C.POINTER(i64)],
     "mcacg_calcul": [vp, C.POINTER(RunOpts), C.POINTER(RunStats)],
+    "mcacg_run_device": [vp, i64, C.POINTER(RunStats)],
+    "mcacg_batch_create": [C.POINTER(Params), i32, vp, C.POINTER(vp)],
+    "mcacg_batch_create_from_states": [C.POINTER(Params), C.POINTER(State), i32, vp, C.POINTER(vp)],
+    "mcacg_batch_destroy": [vp],
+    "mcacg_batch_run": [vp, i64, i64],
+    "mcacg_batch_stats": [vp, C.POINTER(RunStats)],
+    "mcacg_batch_size": [vp, C.POINTER(i32)],
+    "mcacg_batch_box_sizes": [vp, i32, C.POINTER(i64), C.POINTER(i64)],
+    "mcacg_batch_store_state": [vp, i32, C.POINTER(State)],
+    "mcacg_batch_last_run": [vp, C.POINTER(f64), C.POINTER(i32)],
+    "mcacg_batch_work": [vp, C.POINTER(Profile)],
 }
 
 _lock = threading.Lock()

@@ -266,6 +266,89 @@ def device_count() -> int:
     return n.value
 
 
+def _run_stats(box_run) -> RunStats:
+    return box_run
+
+
+class Batch:
+    """Independent boxes advanced together by the device-resident loop.
+
+    Box i is placed exactly as ``AggregatList(models[i])`` would place it;
+    afterwards every step runs on the GPU (one thread block per box) with the
+    statistics of the reference's loop (see include/mcacg.h).
+    """
+
+    def __init__(self, models, stream: int | None = None, states=None):
+        models = list(models)
+        arr = (Params * len(models))(*[m.params for m in models])
+        self.models = models
+        self._b = C.c_void_p()
+        s = C.c_void_p(stream) if stream else None
+        if states is None:
+            check(lib().mcacg_batch_create(arr, len(models), s, C.byref(self._b)))
+        else:
+            bufs = [st if isinstance(st, StateBuffers) else StateBuffers.from_snapshot(st) for st in states]
+            sarr = (_lib.State * len(bufs))(*[b.state for b in bufs])
+            check(lib().mcacg_batch_create_from_states(arr, sarr, len(models), s, C.byref(self._b)))
+
+    def close(self) -> None:
+        if self._b:
+            check(lib().mcacg_batch_destroy(self._b))
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self) -> int:
+        return len(self.models)
+
+    def run(self, max_steps: int = 0, steps_per_launch: int = 20000) -> None:
+        check(lib().mcacg_batch_run(self._b, int(max_steps), int(steps_per_launch)))
+
+    def stats(self) -> np.ndarray:
+        n = len(self.models)
+        arr = (RunStats * n)()
+        check(lib().mcacg_batch_stats(self._b, arr))
+        out = np.zeros(n, dtype=[("steps", "i8"), ("events", "i8"), ("n_aggregates", "i8"), ("time", "f8"),
+                                 ("finished", "i4"), ("status", "i4")])
+        for i, s in enumerate(arr):
+            out[i] = (s.steps, s.events, s.n_aggregates, s.time, s.finished, s.reserved)
+        return out
+
+    def work(self) -> dict:
+        p = _lib.Profile()
+        check(lib().mcacg_batch_work(self._b, C.byref(p)))
+        return {name: getattr(p, name) for name, _ in _lib.Profile._fields_}
+
+    def last_run(self) -> tuple[float, int]:
+        ms, n = C.c_double(), C.c_int32()
+        check(lib().mcacg_batch_last_run(self._b, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def store(self, box: int) -> Snapshot:
+        ns, na = C.c_int64(), C.c_int64()
+        check(lib().mcacg_batch_box_sizes(self._b, int(box), C.byref(ns), C.byref(na)))
+        sb = StateBuffers(ns.value, max(na.value, 1))
+        check(lib().mcacg_batch_store_state(self._b, int(box), C.byref(sb.state)))
+        return sb.to_snapshot(volsurf_method=int(self.models[box].params.volsurf_method))
+
+
+def run_device(aggregates: AggregatList, max_steps: int = 0) -> RunStats:
+    """Advance one box with the device-resident loop."""
+    s = RunStats()
+    check(lib().mcacg_run_device(aggregates._box, int(max_steps), C.byref(s)))
+    return s
+
+
 def calcul(model: PhysicalModel, aggregates: AggregatList, max_steps: int = 0):
     """mcac::calcul (src/calcul.cpp:55-290) for the collision-only configuration."""
     return aggregates.calcul(max_steps=max_steps)

@@ -119,12 +119,32 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     b.surv_cap = 1 << 16;
     b.pair_cap = 16 * st.ns + 1024;
 
+    // all arrays of the box are carved from one allocation: a sizing pass,
+    // one cudaMalloc, then the carving pass
+    size_t arena_bytes = 0;
+    char *arena = nullptr;
+    bool sizing = true;
     auto alloc = [&](void **p, size_t bytes) -> bool {
-        if (!cuda_ok(cudaMalloc(p, std::max<size_t>(bytes, 16)), err, "cudaMalloc")) return false;
-        d->allocations_.push_back(*p);
+        size_t need = (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
+        if (sizing) {
+            *p = nullptr;
+        } else {
+            *p = arena + arena_bytes;
+        }
+        arena_bytes += need;
         return true;
     };
     bool ok = true;
+    for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1) {
+        if (!cuda_ok(cudaMalloc((void **)&arena, arena_bytes), err, "cudaMalloc")) {
+            delete d;
+            return ST_CUDA;
+        }
+        d->allocations_.push_back(arena);
+        sizing = false;
+        arena_bytes = 0;
+    }
     ok = ok && alloc((void **)&b.sph, sizeof(double) * 9 * size_t(st.ns));
     ok = ok && alloc((void **)&b.sph_slot, sizeof(int) * size_t(st.ns));
     ok = ok && alloc((void **)&b.agg, sizeof(double) * 21 * size_t(st.nslots));
@@ -157,10 +177,7 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     ok = ok && alloc((void **)&b.cand_prefix, sizeof(int) * nc1);
     ok = ok && alloc((void **)&b.best_res, sizeof(unsigned long long) * nc1);
     ok = ok && alloc((void **)&b.best_ij, sizeof(unsigned long long) * nc1);
-    if (!ok) {
-        delete d;
-        return ST_CUDA;
-    }
+    }  // sizing / carving passes
     if (stream) {
         d->stream_ = stream;
     } else {
@@ -292,10 +309,13 @@ int DeviceBox::rebuild_grid(int cap, std::string *err) {
     if (cap != b.cell_cap) {
         int *items = nullptr;
         if (!cuda_ok(cudaMalloc(&items, sizeof(int) * size_t(b.n_cells) * size_t(cap)), err, "cudaMalloc")) return ST_CUDA;
+        // the first grid lives in the box's arena; a regrown one is its own allocation
         auto it = std::find(allocations_.begin(), allocations_.end(), (void *)b.cell_items);
         if (it != allocations_.end()) {
             cudaFree(*it);
             *it = items;
+        } else {
+            allocations_.push_back(items);
         }
         b.cell_items = items;
         b.cell_cap = cap;
@@ -412,6 +432,17 @@ int DeviceBox::set_fields(int slot, const double fields[21], unsigned mask, std:
     std::memcpy(u.v, fields, sizeof(u.v));
     k_set_fields<<<1, 32, 0, s>>>(b, slot, u, mask);
     if (!cuda_ok(cudaGetLastError(), err, "k_set_fields")) return ST_CUDA;
+    return ST_OK;
+}
+
+int DeviceBox::upload_aggregates(const std::vector<double> &agg, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    if (agg.size() != size_t(21) * size_t(b.nslots)) return ST_BAD_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    if (!cuda_ok(cudaMemcpyAsync(b.agg, agg.data(), sizeof(double) * agg.size(), cudaMemcpyHostToDevice, s), err,
+                 "upload"))
+        return ST_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
     return ST_OK;
 }
 

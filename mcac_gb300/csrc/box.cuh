@@ -238,7 +238,7 @@ struct QuerySmem {
 //  4. the candidates are walked in filter order with the reference's two
 //     early exits.
 // Must be called by all threads of the block.
-__device__ void block_query(const DevBox &b, int src, Vec3 dir, double dist, QuerySmem &sm) {
+__device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double dist, QuerySmem &sm) {
     const int tid = threadIdx.x;
     const int NT = blockDim.x;
     const DevScalars *sc = b.sc;
@@ -559,7 +559,7 @@ __device__ __forceinline__ void regrid(const DevBox &b, int slot) {
 
 // --------------------------------------------------------------- translate
 // Aggregate::translate (aggregats/aggregat.cpp:148-161).
-__device__ void block_translate(const DevBox &b, int slot, Vec3 v, double *refpos_sm) {
+__device__ inline void block_translate(const DevBox &b, int slot, Vec3 v, double *refpos_sm) {
     const int tid = threadIdx.x;
     if (tid == 0) {
         double x = periodic_position(A(b, AGG_X, slot) + v.x, b.L);

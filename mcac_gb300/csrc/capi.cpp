@@ -4,6 +4,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
+#include <vector>
 #include <exception>
 #include <fstream>
 #include <memory>
@@ -13,6 +16,7 @@
 
 #include "../../include/mcacg.h"
 #include "common.hpp"
+#include "batch.hpp"
 #include "host_box.hpp"
 #include "physics.hpp"
 
@@ -20,7 +24,46 @@ struct mcacg_box {
     std::unique_ptr<mcacg::HostBox> impl;
 };
 
+struct mcacg_batch {
+    std::unique_ptr<mcacg::BatchRunner> impl;
+    std::vector<mcacg_params> params;
+};
+
 namespace {
+
+// A slot-ordered device state as the C-ABI's label-ordered arrays.
+int store_host_state(const mcacg::HostState &st, mcacg_state *out, std::string *err) {
+    std::vector<int> label_of(size_t(st.nslots), -1);
+    int na = 0;
+    for (int a = 0; a < st.nslots; ++a)
+        if (st.agg_n[size_t(a)] > 0) label_of[size_t(a)] = na++;
+    if (out->n_spheres < st.ns || out->n_aggregates < na) {
+        if (err) *err = "state buffers too small";
+        return mcacg::ST_BAD_ARGUMENT;
+    }
+    out->n_spheres = st.ns;
+    out->n_aggregates = na;
+    out->n_verlet_divisions = st.n_div;
+    out->box_length = st.box_length;
+    out->maxradius = st.maxradius;
+    out->time = st.time;
+    if (out->spheres) std::copy(st.sph.begin(), st.sph.end(), out->spheres);
+    if (out->sphere_label)
+        for (int s = 0; s < st.ns; ++s) out->sphere_label[s] = label_of[size_t(st.sph_slot[size_t(s)])];
+    int64_t off = 0;
+    for (int a = 0; a < st.nslots; ++a) {
+        int l = label_of[size_t(a)];
+        if (l < 0) continue;
+        if (out->aggregates)
+            for (int f = 0; f < 21; ++f) out->aggregates[size_t(f) * na + l] = st.agg[size_t(f) * st.nslots + a];
+        const auto &m = st.members[size_t(a)];
+        if (out->n_spheres_per_aggregate) out->n_spheres_per_aggregate[l] = int64_t(m.size());
+        if (out->members)
+            for (size_t k = 0; k < m.size(); ++k) out->members[off + int64_t(k)] = m[k];
+        off += int64_t(m.size());
+    }
+    return mcacg::ST_OK;
+}
 
 thread_local std::string g_last_error;
 
@@ -354,6 +397,177 @@ int mcacg_calcul(mcacg_box *box, const mcacg_run_opts *opts, mcacg_run_stats *st
         int rc = box->impl->calcul(o, &s, &err);
         if (stats) *stats = s;
         return finish(rc, err);
+    });
+}
+
+int mcacg_run_device(mcacg_box *box, int64_t max_steps, mcacg_run_stats *stats) {
+    return guarded([&] {
+        if (!box) return fail(MCACG_ERR_BAD_ARGUMENT, "null box");
+        mcacg_run_stats s{};
+        std::string err;
+        int rc = box->impl->run_device(max_steps, &s, &err);
+        if (stats) *stats = s;
+        return finish(rc, err);
+    });
+}
+
+int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_stream, mcacg_batch **batch) {
+    return guarded([&] {
+        if (!params || !batch || n_boxes <= 0) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
+        *batch = nullptr;
+        std::vector<mcacg_params> ps(params, params + n_boxes);
+        for (const auto &p : ps)
+            if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges ||
+                p.with_surface_reactions)
+                return fail(mcacg::ST_INPUT, "batched boxes cover the collision-only configuration");
+        // placements in parallel: each box draws from its own copy of the C
+        // library stream, so the result equals a sequential placement
+        std::vector<mcacg::HostState> states(static_cast<size_t>(n_boxes));
+        std::vector<int> rcs(static_cast<size_t>(n_boxes), 0);
+        std::vector<std::string> errs(static_cast<size_t>(n_boxes));
+        std::atomic<int> next{0};
+        unsigned nthreads = std::max(1u, std::min(std::thread::hardware_concurrency(), unsigned(n_boxes)));
+        std::vector<std::thread> pool;
+        for (unsigned t = 0; t < nthreads; ++t)
+            pool.emplace_back([&] {
+                for (int i = next++; i < n_boxes; i = next++)
+                    rcs[size_t(i)] = mcacg::init_random_state_private(ps[size_t(i)], &states[size_t(i)],
+                                                                      &errs[size_t(i)]);
+            });
+        for (auto &th : pool) th.join();
+        for (int i = 0; i < n_boxes; ++i)
+            if (rcs[size_t(i)] != 0) return fail(rcs[size_t(i)], "box " + std::to_string(i) + ": " + errs[size_t(i)]);
+        std::unique_ptr<mcacg_batch> b(new mcacg_batch());
+        std::string err;
+        int rc = mcacg::BatchRunner::create(ps, std::move(states), cuda_stream, &b->impl, &err);
+        if (rc != 0) return finish(rc, err);
+        b->params = ps;
+        *batch = b.release();
+        return 0;
+    });
+}
+
+int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state *states, int32_t n_boxes,
+                                   void *cuda_stream, mcacg_batch **batch) {
+    return guarded([&] {
+        if (!params || !states || !batch || n_boxes <= 0) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
+        *batch = nullptr;
+        std::vector<mcacg_params> ps(params, params + n_boxes);
+        std::vector<mcacg::HostState> hs(static_cast<size_t>(n_boxes));
+        std::string err;
+        for (int i = 0; i < n_boxes; ++i) {
+            int rc = mcacg::state_to_host(states[i], &hs[size_t(i)], &err);
+            if (rc != 0) return fail(rc, "box " + std::to_string(i) + ": " + err);
+            ps[size_t(i)].box_length = states[i].box_length;
+            ps[size_t(i)].n_verlet_divisions = states[i].n_verlet_divisions;
+        }
+        std::unique_ptr<mcacg_batch> b(new mcacg_batch());
+        int rc = mcacg::BatchRunner::create(ps, std::move(hs), cuda_stream, &b->impl, &err);
+        if (rc != 0) return finish(rc, err);
+        b->params = ps;
+        *batch = b.release();
+        return 0;
+    });
+}
+
+int mcacg_batch_destroy(mcacg_batch *batch) {
+    return guarded([&] {
+        delete batch;
+        return 0;
+    });
+}
+
+int mcacg_batch_run(mcacg_batch *batch, int64_t max_steps, int64_t steps_per_launch) {
+    return guarded([&] {
+        if (!batch) return fail(MCACG_ERR_BAD_ARGUMENT, "null batch");
+        std::string err;
+        return finish(batch->impl->run(max_steps, steps_per_launch, &err), err);
+    });
+}
+
+int mcacg_batch_stats(mcacg_batch *batch, mcacg_run_stats *stats) {
+    return guarded([&] {
+        if (!batch || !stats) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::vector<mcacg::BoxRunStats> s;
+        std::string err;
+        int rc = batch->impl->stats(&s, &err);
+        if (rc != 0) return finish(rc, err);
+        for (size_t i = 0; i < s.size(); ++i) {
+            stats[i].steps = s[i].steps;
+            stats[i].events = s[i].events;
+            stats[i].n_aggregates = s[i].n_alive;
+            stats[i].time = s[i].time;
+            stats[i].finished = s[i].finished;
+            stats[i].reserved = s[i].status;
+        }
+        return 0;
+    });
+}
+
+int mcacg_batch_size(const mcacg_batch *batch, int32_t *n_boxes) {
+    return guarded([&] {
+        if (!batch || !n_boxes) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *n_boxes = batch->impl->size();
+        return 0;
+    });
+}
+
+int mcacg_batch_box_sizes(mcacg_batch *batch, int32_t box, int64_t *n_spheres, int64_t *n_aggregates) {
+    return guarded([&] {
+        if (!batch || box < 0 || box >= batch->impl->size()) return fail(MCACG_ERR_BAD_ARGUMENT, "bad box");
+        std::vector<mcacg::BoxRunStats> s;
+        std::string err;
+        int rc = batch->impl->stats(&s, &err);
+        if (rc != 0) return finish(rc, err);
+        if (n_spheres) *n_spheres = batch->impl->box(box).ns();
+        if (n_aggregates) *n_aggregates = s[size_t(box)].n_alive;
+        return 0;
+    });
+}
+
+int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state) {
+    return guarded([&] {
+        if (!batch || !state || box < 0 || box >= batch->impl->size())
+            return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
+        mcacg::HostState st;
+        std::string err;
+        int rc = batch->impl->download(box, &st, &err);
+        if (rc != 0) return finish(rc, err);
+        return finish(store_host_state(st, state, &err), err);
+    });
+}
+
+int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out) {
+    return guarded([&] {
+        if (!batch || !out) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::vector<mcacg::BoxRunStats> s;
+        std::string err;
+        int rc = batch->impl->stats(&s, &err);
+        if (rc != 0) return finish(rc, err);
+        *out = mcacg_profile{};
+        for (const auto &x : s) {
+            out->queries += x.queries;
+            out->merges += x.events;
+            out->translates += x.steps;
+            out->mov_spheres += x.mov;
+            out->scanned += x.scanned;
+            out->cells += x.cells;
+            out->candidates += x.candidates;
+            out->cand_spheres += x.cand_spheres;
+            out->refined += x.refined;
+            out->merged_spheres += x.merged_spheres;
+            out->merge_pairs += x.merge_pairs;
+        }
+        return 0;
+    });
+}
+
+int mcacg_batch_last_run(const mcacg_batch *batch, double *kernel_ms, int32_t *launches) {
+    return guarded([&] {
+        if (!batch) return fail(MCACG_ERR_BAD_ARGUMENT, "null batch");
+        if (kernel_ms) *kernel_ms = batch->impl->last_kernel_ms();
+        if (launches) *launches = batch->impl->launches();
+        return 0;
     });
 }
 

@@ -65,6 +65,8 @@ class DeviceBox {
     int merge(int ms, int os, int mslot, int oslot, MergeResult *out, std::string *err);
     // Writes aggregate fields of one slot: fields[f] for every f with bit f of mask set.
     int set_fields(int slot, const double fields[21], unsigned mask, std::string *err);
+    // Overwrites the whole aggregate table ([21][nslots], slot order).
+    int upload_aggregates(const std::vector<double> &agg, std::string *err);
     // Copies the whole state back (spheres, aggregates, members, scalars).
     int download(HostState *st, std::string *err);
     // Rebuilds the Verlet grid from the aggregate positions with 'cap' rooms per cell.

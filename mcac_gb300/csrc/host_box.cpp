@@ -9,6 +9,8 @@
 
 #include "common.hpp"
 #include "physics.hpp"
+#include "rng.hpp"
+#include "batch.hpp"
 
 namespace mcacg {
 
@@ -268,6 +270,15 @@ int init_random_state(const mcacg_params &p, HostState *st, std::string *err) {
     return ST_OK;
 }
 
+int init_random_state_private(const mcacg_params &p, HostState *st, std::string *err) {
+    RandStream rs;
+    rs.seed(uint32_t(p.random_seed < 0 ? 0 : p.random_seed));
+    set_thread_stream(&rs);
+    int rc = init_random_state(p, st, err);
+    set_thread_stream(nullptr);
+    return rc;
+}
+
 // ------------------------------------------------------------------ HostBox
 int HostBox::upload(const HostState &st, void *stream, std::string *err) {
     ns_ = st.ns;
@@ -316,6 +327,21 @@ int HostBox::create_from_state(const mcacg_params &p, const mcacg_state &in, voi
     hb->p_.box_volume = std::pow(in.box_length, 3);
     hb->p_.n_verlet_divisions = in.n_verlet_divisions;
     HostState st;
+    int rc = state_to_host(in, &st, err);
+    if (rc != ST_OK) return rc;
+    rc = hb->upload(st, stream, err);
+    if (rc != ST_OK) return rc;
+    *out = std::move(hb);
+    return ST_OK;
+}
+
+int state_to_host(const mcacg_state &in, HostState *out, std::string *err) {
+    if (in.n_spheres <= 0 || in.n_aggregates <= 0 || !in.spheres || !in.sphere_label || !in.aggregates ||
+        !in.n_spheres_per_aggregate || !in.members) {
+        if (err) *err = "incomplete state";
+        return ST_BAD_ARGUMENT;
+    }
+    HostState &st = *out;
     st.n_div = int(in.n_verlet_divisions);
     st.box_length = in.box_length;
     st.maxradius = in.maxradius;
@@ -357,9 +383,6 @@ int HostBox::create_from_state(const mcacg_params &p, const mcacg_state &in, voi
         if (err) *err = "member lists do not cover every sphere once";
         return ST_BAD_ARGUMENT;
     }
-    int rc = hb->upload(st, stream, err);
-    if (rc != ST_OK) return rc;
-    *out = std::move(hb);
     return ST_OK;
 }
 
@@ -397,6 +420,7 @@ int HostBox::translate(int64_t label, const double v[3], std::string *err) {
         if (err) *err = "label out of range";
         return ST_BAD_ARGUMENT;
     }
+    invalidate_device_run();
     int slot = alive_[size_t(label)];
     F(AGG_X, slot) = periodic_position(F(AGG_X, slot) + v[0], p_.box_length);
     F(AGG_Y, slot) = periodic_position(F(AGG_Y, slot) + v[1], p_.box_length);
@@ -409,6 +433,7 @@ int HostBox::time_forward(int64_t label, double dt, std::string *err) {
         if (err) *err = "label out of range";
         return ST_BAD_ARGUMENT;
     }
+    invalidate_device_run();
     F(AGG_TIME, alive_[size_t(label)]) += dt;
     return ST_OK;
 }
@@ -421,6 +446,7 @@ int HostBox::merge(const mcacg_contact &c, int32_t *merged, std::string *err) {
         if (err) *err = "contact refers to an unknown aggregate or sphere";
         return ST_BAD_ARGUMENT;
     }
+    invalidate_device_run();
     const int mslot = alive_[size_t(c.moving_aggregate)];
     const int oslot = alive_[size_t(c.other_aggregate)];
     MergeResult m;
@@ -620,6 +646,76 @@ int HostBox::store(mcacg_state *out, std::string *err) {
             for (size_t k = 0; k < m.size(); ++k) out->members[off + int64_t(k)] = m[k];
         off += int64_t(m.size());
     }
+    return ST_OK;
+}
+
+}  // namespace mcacg
+
+// ------------------------------------------------------- device-loop runs
+namespace mcacg {
+
+HostBox::HostBox() = default;
+HostBox::~HostBox() = default;
+
+void HostBox::set_time(double t) {
+    time_ = t;
+    invalidate_device_run();
+}
+
+void HostBox::invalidate_device_run() {
+    runner_.reset();
+    runner_steps_ = runner_events_ = 0;
+}
+
+int HostBox::refresh_from_device(std::string *err) {
+    HostState st;
+    int rc = dev_->download(&st, err);
+    if (rc != ST_OK) return rc;
+    agg_ = st.agg;
+    agg_n_ = st.agg_n;
+    alive_.clear();
+    for (int a = 0; a < nslots_; ++a)
+        if (agg_n_[size_t(a)] > 0) alive_.push_back(a);
+    maxradius_ = st.maxradius;
+    event_ = true;
+    if (!alive_.empty()) refresh();
+    return ST_OK;
+}
+
+int HostBox::run_device(int64_t max_steps, mcacg_run_stats *stats, std::string *err) {
+    if (!runner_) {
+        // the host mirror holds the authoritative aggregate fields (proper
+        // times and physics) after host-driven steps
+        int up = dev_->upload_aggregates(agg_, err);
+        if (up != ST_OK) return up;
+        std::unique_ptr<BatchRunner> r;
+        int rc = BatchRunner::attach({p_}, {dev_.get()}, {time_}, dev_->stream(), &r, err);
+        if (rc != ST_OK) return rc;
+        runner_ = std::move(r);
+        runner_steps_ = runner_events_ = 0;
+    }
+    int rc = runner_->run(max_steps, 20000, err);
+    if (rc != ST_OK) return rc;
+    std::vector<BoxRunStats> s;
+    rc = runner_->stats(&s, err);
+    if (rc != ST_OK) return rc;
+    const BoxRunStats &b = s[0];
+    if (b.status != ST_OK) {
+        if (err) *err = "device loop stopped with status " + std::to_string(b.status);
+        return b.status;
+    }
+    time_ = b.time;
+    rc = refresh_from_device(err);
+    if (rc != ST_OK) return rc;
+    if (stats) {
+        stats->steps = b.steps - runner_steps_;
+        stats->events = b.events - runner_events_;
+        stats->n_aggregates = int64_t(alive_.size());
+        stats->time = time_;
+        stats->finished = b.finished;
+    }
+    runner_steps_ = b.steps;
+    runner_events_ = b.events;
     return ST_OK;
 }
 

@@ -15,6 +15,8 @@
 
 namespace mcacg {
 
+class BatchRunner;
+
 class HostBox {
   public:
     // AggregatList::AggregatList: seeded random placement (host), then upload.
@@ -26,7 +28,7 @@ class HostBox {
     int size() const { return int(alive_.size()); }
     int n_spheres() const { return ns_; }
     double time() const { return time_; }
-    void set_time(double t) { time_ = t; }
+    void set_time(double t);
     const mcacg_params &params() const { return p_; }
     DeviceBox &device() { return *dev_; }
 
@@ -58,8 +60,19 @@ class HostBox {
     // whole state (store) in label order
     int store(mcacg_state *st, std::string *err);
 
+    // the device-resident loop on this machine (see BatchRunner)
+    int run_device(int64_t max_steps, mcacg_run_stats *stats, std::string *err);
+
   private:
-    HostBox() = default;
+    void invalidate_device_run();
+    int refresh_from_device(std::string *err);
+    std::unique_ptr<BatchRunner> runner_;
+    int64_t runner_steps_ = 0, runner_events_ = 0;
+    HostBox();
+  public:
+    ~HostBox();
+
+  private:
     int upload(const HostState &st, void *stream, std::string *err);
     double &F(int field, int slot) { return agg_[size_t(field) * size_t(nslots_) + size_t(slot)]; }
     double F(int field, int slot) const { return agg_[size_t(field) * size_t(nslots_) + size_t(slot)]; }
@@ -85,6 +98,12 @@ class HostBox {
 // answer of that test does not depend on the grid, so the placements are the
 // reference's.
 int init_random_state(const mcacg_params &p, HostState *st, std::string *err);
+// The same placement drawing from a private copy of the C library stream
+// seeded with p.random_seed: identical result, safe to run on many threads.
+int init_random_state_private(const mcacg_params &p, HostState *st, std::string *err);
+
+// A C-ABI state (labels in order) as a slot-ordered host state, validated.
+int state_to_host(const mcacg_state &in, HostState *out, std::string *err);
 
 // Aggregate::update for an aggregate given by its members (host, used for
 // initial monomers and for loading states): writes all 21 fields except the

@@ -35,7 +35,7 @@ struct MergeSmem {
 
 // exclusive scan of a global int array in place (block-wide, chunked);
 // returns the total.
-__device__ int block_scan_global(int *data, int n, int *warp_tmp) {
+__device__ inline int block_scan_global(int *data, int n, int *warp_tmp) {
     const int NT = blockDim.x;
     int carry = 0;
     for (int c0 = 0; c0 < n; c0 += NT) {
@@ -73,7 +73,7 @@ __device__ int block_scan_global(int *data, int n, int *warp_tmp) {
 
 // Move every live segment to the front of the other pool buffer, in slot
 // order. Uses counters[] and row_cnt[] as scratch.
-__device__ void block_compact_pool(const DevBox &b, int *warp_tmp) {
+__device__ inline void block_compact_pool(const DevBox &b, int *warp_tmp) {
     DevScalars *sc = b.sc;
     const int from = sc->pool_sel, to = 1 - from;
     // prefix of member counts over slots, staged in row_cnt (size >= nslots+1)
@@ -112,7 +112,7 @@ __device__ __forceinline__ double ordered_sum(const double *v, int n) {
 // ms / os: moving / other sphere; mslot / oslot: their aggregates at query
 // time. The physics fields (f_agg, d_m, time_step, lpm, dg_over_dp), the
 // proper time and the charge are left to the caller.
-__device__ void block_merge(const DevBox &b, int ms, int os, int mslot, int oslot, MergeSmem &sm, MergeOut *out) {
+__device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, int oslot, MergeSmem &sm, MergeOut *out) {
     const int tid = threadIdx.x, NT = blockDim.x;
     DevScalars *sc = b.sc;
     if (tid == 0) {

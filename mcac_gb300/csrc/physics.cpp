@@ -7,6 +7,7 @@
 #include <sstream>
 
 #include "common.hpp"
+#include "rng.hpp"
 
 namespace mcacg {
 
@@ -252,14 +253,26 @@ AggregatePhysics aggregate_physics(const mcacg_params &p, double volume, double 
     return out;
 }
 
+namespace {
+// when set, this thread draws from its own copy of the C library stream
+thread_local RandStream *t_stream = nullptr;
+}  // namespace
+
 void init_random(int seed) {
+    if (t_stream) {
+        t_stream->seed(static_cast<unsigned>(seed < 0 ? 0 : seed));
+        return;
+    }
     // a negative seed means "from the clock" in the reference
     // (tools.cpp:41-52); runs here are always seeded explicitly.
     if (seed < 0) seed = 0;
     std::srand(static_cast<unsigned>(seed));
 }
 
+void set_thread_stream(RandStream *stream) { t_stream = stream; }
+
 double random_uniform() {
+    if (t_stream) return t_stream->uniform();
     double v = std::rand();
     v = v / RAND_MAX;
     return v;

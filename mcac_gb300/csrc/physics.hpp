@@ -47,6 +47,10 @@ int random_diameter(const mcacg_params &p, double mean, double dispersion, doubl
 // generator.
 void init_random(int seed);
 double random_uniform();
+// Makes this thread's draws come from 'stream' (a bit-identical copy of the C
+// library generator) instead of the process-wide rand(); nullptr restores it.
+struct RandStream;
+void set_thread_stream(RandStream *stream);
 void random_direction(double out[3]);
 double inverfc(double p);
 double inverf(double p);

@@ -44,6 +44,9 @@ struct RunState {
     int finished;
     int status;
     int pad[2];
+    // work counters of the contact queries and merges (algorithmic bytes)
+    long long c_queries, c_mov, c_scanned, c_cells, c_candidates, c_cand_spheres, c_refined;
+    long long c_merged_spheres, c_merge_pairs;
 };
 
 struct BoxRun {
@@ -73,7 +76,7 @@ struct RunSmem {
 
 // ------------------------------------------------------------ sum tree
 // Warp 0: descend from the top level to a leaf holding the target 't'.
-__device__ int tree_sample(const BoxRun &R, double t) {
+__device__ inline int tree_sample(const BoxRun &R, double t) {
     const int lane = threadIdx.x & 31;
     int node = 0;  // index within the current level
     for (int lev = R.tree_levels - 1; lev >= 0; --lev) {
@@ -98,7 +101,7 @@ __device__ int tree_sample(const BoxRun &R, double t) {
 }
 
 // Warp 0: set leaf 'slot' to 'w' and refresh its ancestors; returns the new total.
-__device__ double tree_set(const BoxRun &R, int slot, double w) {
+__device__ inline double tree_set(const BoxRun &R, int slot, double w) {
     const int lane = threadIdx.x & 31;
     if (lane == 0) R.tree[R.tree_off[0] + slot] = w;
     __syncwarp();
@@ -124,7 +127,7 @@ __device__ double tree_set(const BoxRun &R, int slot, double w) {
 // ------------------------------------------------------------ physics
 // update_partial's physics (aggregat.cpp:264-276, physical_model.cpp:550-617)
 // with CUDA's erf / exp / pow.
-__device__ void device_physics(const PhysParams &p, double V, double vol_pp, double dp, double rg, double *f_agg,
+__device__ inline void device_physics(const PhysParams &p, double V, double vol_pp, double dp, double rg, double *f_agg,
                                double *d_m, double *time_step, double *lpm, double *dg_over_dp) {
     const double r = 0.5 * dp;
     const double a = 1.142, b = 0.558, c = 0.999;
@@ -158,7 +161,7 @@ __device__ __forceinline__ bool run_finished(const BoxRun &R, const RunState &st
 
 // One MC step of one box by the whole block. Returns false when the box is
 // finished or in error (then nothing was done).
-__device__ bool block_mc_step(const BoxRun &R, RunSmem &sm) {
+__device__ inline bool block_mc_step(const BoxRun &R, RunSmem &sm) {
     const int tid = threadIdx.x;
     const DevBox &b = R.box;
     RunState &st = *R.st;
@@ -210,6 +213,13 @@ __device__ bool block_mc_step(const BoxRun &R, RunSmem &sm) {
             sm.ms = q.moving_sphere;
             sm.os = q.other_sphere;
             sm.oslot = q.other_slot;
+            st.c_queries += 1;
+            st.c_mov += q.n_mov;
+            st.c_scanned += q.n_scanned;
+            st.c_cells += q.n_cells;
+            st.c_candidates += q.n_candidates;
+            st.c_cand_spheres += q.n_cand_spheres;
+            st.c_refined += q.n_pairs_refined;
         }
     } else if (tid == 0) {
         sm.contact = 0;
@@ -246,6 +256,8 @@ __device__ bool block_mc_step(const BoxRun &R, RunSmem &sm) {
                 sm.merged = 1;
                 sm.keep = keep;
                 sm.removed = removed;
+                st.c_merged_spheres += sm.mout.n;
+                st.c_merge_pairs += sm.mout.n_pairs;
             }
         }
         __syncthreads();

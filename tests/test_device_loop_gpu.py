@@ -1,0 +1,170 @@
+"""The device-resident MC loop (batched form).
+
+Its contact search, translation and merge geometry are the kernels checked
+bit for bit in test_contact_gpu.py; its pick walks a sum tree and its
+directions and aggregate physics use CUDA's libm, so it follows the reference
+statistically. Checked here: the state stays a valid MCAC state (partition of
+the spheres, aggregate fields equal to their definitions, no two aggregates
+interpenetrating), runs are deterministic, and ensemble statistics agree with
+the oracle (the C restatement of the reference) within sampling error.
+"""
+import numpy as np
+import pytest
+
+from mcac_gb300 import AggregatList, Batch, PhysicalModel, run_device
+from mcac_gb300.snapshot import A, S
+from oracle import oracle_py as O
+
+
+def small_ini(n, seed, mode="normal", disp=1.25, fv=1e-3, nagg=1, T=1700, wait=-1):
+    return (f"[monomers]\nnumber = {n}\nmean_diameter = 30\ndispersion_diameter = {disp}\n"
+            f"initialisation_mode = {mode}\n[environment]\nvolume_fraction = {fv}\ntemperature = {T}\n"
+            f"[limits]\nnumber_of_aggregates = {nagg}\nn_iter_without_event = {wait}\n"
+            f"[numerics]\nrandom_seed = {seed}\nwith_domain_duplication = false\n")
+
+
+def seq_sum(x):
+    return float(np.cumsum(np.asarray(x, dtype=np.float64))[-1]) if len(x) else 0.0
+
+
+def periodic(d, L):
+    return d - L * np.floor(d / L + 0.5)
+
+
+def check_state(snap, tol=1e-12):
+    L = snap.box_length
+    ns, na = snap.ns, snap.na
+    # the member lists partition the spheres and agree with the sphere labels
+    assert snap.n_spheres.sum() == ns
+    assert np.array_equal(np.sort(snap.members), np.arange(ns))
+    off = snap.member_offsets()
+    for a in range(na):
+        mem = snap.members[off[a]:off[a + 1]]
+        assert np.all(snap.sphere_label[mem] == a)
+        vol = snap.spheres[S["volume"], mem]
+        V = seq_sum(vol)
+        assert snap.aggregates[A["volume"], a] == V
+        rel = snap.spheres[[S["rx"], S["ry"], S["rz"]]][:, mem]
+        r = np.array([seq_sum(rel[k] * vol) for k in range(3)]) / V
+        np.testing.assert_allclose(snap.aggregates[[A["rx"], A["ry"], A["rz"]], a], r, rtol=tol, atol=1e-30)
+        dc = np.sqrt(((rel - r[:, None]) ** 2).sum(0))
+        rmax = np.max(snap.spheres[S["r"], mem] + dc)
+        if len(mem) > 1:
+            # a monomer keeps the r_max of its radius before the reference's
+            # volume-fraction rescaling (aggregat_list_storage.cpp:75-87)
+            np.testing.assert_allclose(snap.aggregates[A["rmax"], a], rmax, rtol=tol)
+        # sphere positions = aggregate reference point + relative positions
+        pos = snap.spheres[[S["x"], S["y"], S["z"]]][:, mem]
+        ref = pos - rel
+        assert np.all(np.abs(periodic(ref - ref[:, :1], L)) < 1e-12 * L)
+    # no two aggregates interpenetrate
+    p = snap.spheres[[S["x"], S["y"], S["z"]]].T
+    rad = snap.spheres[S["r"]]
+    lab = snap.sphere_label
+    for i in range(ns):
+        d = periodic(p[i + 1:] - p[i], L)
+        dist = np.sqrt((d ** 2).sum(1))
+        other = lab[i + 1:] != lab[i]
+        gap = dist - (rad[i + 1:] + rad[i])
+        assert np.all(gap[other] > -1e-9 * rad[i]), (i, gap[other].min())
+
+
+@pytest.mark.gpu
+def test_batch_keeps_valid_states():
+    models = [PhysicalModel(text=small_ini(n, 40 + k, mode=("normal" if k % 2 else "lognormal"),
+                                           disp=(1.25 if k % 2 else 1.4), fv=(1e-3 if k % 3 else 5e-3)))
+              for k, n in enumerate([200, 350, 500, 800, 300, 650, 420, 900])]
+    with Batch(models) as b:
+        b.run(max_steps=4000, steps_per_launch=1000)
+        st = b.stats()
+        assert np.all(st["status"] == 0)
+        assert np.all(st["steps"] > 0)
+        for k in range(len(models)):
+            snap = b.store(k)
+            assert snap.na == models[k].params.n_monomeres - st["events"][k]
+            check_state(snap)
+
+
+@pytest.mark.gpu
+def test_batch_is_deterministic():
+    models = [PhysicalModel(text=small_ini(400, 7 + k, mode="lognormal", disp=1.3, fv=3e-3)) for k in range(4)]
+    snaps = []
+    for _ in range(2):
+        with Batch(models) as b:
+            b.run(max_steps=3000, steps_per_launch=700)
+            snaps.append([b.store(k) for k in range(len(models))])
+    for s1, s2 in zip(*snaps):
+        assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
+        assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64))
+        assert np.array_equal(s1.members, s2.members)
+
+
+@pytest.mark.gpu
+def test_device_and_host_steps_interleave():
+    pm = PhysicalModel(text=small_ini(600, 3, fv=3e-3))
+    with AggregatList(pm) as box:
+        box.calcul(max_steps=500)
+        s = run_device(box, max_steps=1500)
+        assert s.steps == 1500
+        box.calcul(max_steps=500)
+        s2 = run_device(box, max_steps=500)
+        assert s2.steps == 500
+        check_state(box.store())
+
+
+@pytest.mark.gpu
+def test_batch_runs_to_stop_criterion():
+    models = [PhysicalModel(text=small_ini(150 + 50 * k, 100 + k, fv=5e-3, nagg=5)) for k in range(6)]
+    with Batch(models) as b:
+        b.run(max_steps=0, steps_per_launch=5000)
+        st = b.stats()
+        assert np.all(st["finished"] == 1) and np.all(st["status"] == 0)
+        assert np.all(st["n_aggregates"] <= 5)
+
+
+def ensemble_summary(snaps):
+    """Fractal law fit over all aggregates (as in the reference's validation
+    notebooks: log Np against log(2 Rg / dp)) and the mean aggregate size."""
+    npp, rg_dp = [], []
+    for s in snaps:
+        for a in range(s.na):
+            n = s.n_spheres[a]
+            if n >= 3:
+                npp.append(n)
+                rg_dp.append(s.aggregates[A["dg_over_dp"], a])
+    npp, rg_dp = np.array(npp, float), np.array(rg_dp)
+    slope, icpt = np.polyfit(np.log(rg_dp), np.log(npp), 1)
+    return slope, np.exp(icpt), npp.mean()
+
+
+@pytest.mark.gpu
+def test_ensemble_statistics_match_oracle():
+    n_boxes, n, stop = 32, 300, 15
+    inis = [small_ini(n, 500 + k, mode="lognormal", disp=1.25, fv=5e-3, nagg=stop) for k in range(n_boxes)]
+    with Batch([PhysicalModel(text=t) for t in inis]) as b:
+        b.run(max_steps=0, steps_per_launch=10000)
+        st = b.stats()
+        assert np.all(st["finished"] == 1)
+        gpu_snaps = [b.store(k) for k in range(n_boxes)]
+        gpu_steps = st["steps"].astype(float)
+        gpu_time = st["time"]
+    cpu_snaps, cpu_steps, cpu_time = [], [], []
+    for t in inis:
+        ob = O.OracleBox(t)
+        s, _ = ob.calcul()
+        cpu_snaps.append(ob.store())
+        cpu_steps.append(s.steps)
+        cpu_time.append(s.time)
+    cpu_steps, cpu_time = np.array(cpu_steps, float), np.array(cpu_time)
+
+    def close(a, b_, k=4.0):
+        se = np.sqrt(a.var(ddof=1) / len(a) + b_.var(ddof=1) / len(b_))
+        return abs(a.mean() - b_.mean()) <= k * se
+
+    assert close(np.log(gpu_steps), np.log(cpu_steps)), (gpu_steps.mean(), cpu_steps.mean())
+    assert close(np.log(gpu_time), np.log(cpu_time)), (gpu_time.mean(), cpu_time.mean())
+    dg, kg, mg = ensemble_summary(gpu_snaps)
+    dc, kc, mc = ensemble_summary(cpu_snaps)
+    assert abs(dg - dc) < 0.15, (dg, dc)     # fractal dimension
+    assert abs(np.log(kg / kc)) < 0.3, (kg, kc)  # prefactor
+    assert abs(mg / mc - 1) < 0.1, (mg, mc)

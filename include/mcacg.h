@@ -284,6 +284,36 @@ int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out);
 /* GPU time (CUDA events) and kernel launches of the last mcacg_batch_run. */
 int mcacg_batch_last_run(const mcacg_batch *batch, double *kernel_ms, int32_t *launches);
 
+/* ---- serving: continuous batching of aggregation runs ----
+ * A request is one box (its parameters; placed like mcacg_box_create). The
+ * server keeps 'capacity' thread-block slots on the GPU; each
+ * mcacg_server_step admits pending requests in arrival order while a slot is
+ * free and the device-memory budget holds their footprint, runs one kernel
+ * epoch of at most epoch_steps MC steps per active box, and retires the
+ * boxes that met a stop criterion. A box's run depends only on its own state
+ * and rand() stream: it is the same alone and in any mix. No counterpart in
+ * the reference. */
+typedef struct mcacg_server mcacg_server;
+typedef struct mcacg_completion {
+    int64_t id;
+    int64_t steps, events, n_aggregates;
+    double time;                        /* physical time reached */
+    int32_t status, finished;
+    double submit_s, admit_s, finish_s; /* host clock, seconds since the server was created */
+} mcacg_completion;
+int mcacg_server_create(int32_t capacity, int64_t memory_budget_bytes, void *cuda_stream, int32_t keep_final_states,
+                        mcacg_server **server);
+int mcacg_server_destroy(mcacg_server *server);
+int mcacg_server_submit(mcacg_server *server, const mcacg_params *params, int64_t *id);
+int mcacg_server_step(mcacg_server *server, int64_t epoch_steps, int32_t *n_active, int32_t *n_pending);
+/* Moves up to 'capacity' completions (oldest first) into 'out'. */
+int mcacg_server_poll(mcacg_server *server, mcacg_completion *out, int32_t capacity, int32_t *n_out);
+/* Final state of a completed request (when created with keep_final_states). */
+int mcacg_server_final_sizes(mcacg_server *server, int64_t id, int64_t *n_spheres, int64_t *n_aggregates);
+int mcacg_server_final_state(mcacg_server *server, int64_t id, mcacg_state *state);
+/* GPU time (CUDA events) and kernel launches since creation. */
+int mcacg_server_kernel_time(const mcacg_server *server, double *kernel_ms, int32_t *launches);
+
 #ifdef __cplusplus
 }
 #endif

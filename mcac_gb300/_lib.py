@@ -116,7 +116,19 @@ SIGNATURES = {
     "mcacg_batch_store_state": [vp, i32, C.POINTER(State)],
     "mcacg_batch_last_run": [vp, C.POINTER(f64), C.POINTER(i32)],
     "mcacg_batch_work": [vp, C.POINTER(Profile)],
+    "mcacg_server_create": [i32, i64, vp, i32, C.POINTER(vp)],
+    "mcacg_server_destroy": [vp],
+    "mcacg_server_submit": [vp, C.POINTER(Params), C.POINTER(i64)],
+    "mcacg_server_step": [vp, i64, C.POINTER(i32), C.POINTER(i32)],
+    "mcacg_server_poll": [vp, C.c_void_p, i32, C.POINTER(i32)],
+    "mcacg_server_final_sizes": [vp, i64, C.POINTER(i64), C.POINTER(i64)],
+    "mcacg_server_final_state": [vp, i64, C.POINTER(State)],
+    "mcacg_server_kernel_time": [vp, C.POINTER(f64), C.POINTER(i32)],
 }
+
+COMPLETION_DTYPE = np.dtype([("id", "<i8"), ("steps", "<i8"), ("events", "<i8"), ("n_aggregates", "<i8"),
+                             ("time", "<f8"), ("status", "<i4"), ("finished", "<i4"), ("submit_s", "<f8"),
+                             ("admit_s", "<f8"), ("finish_s", "<f8")])
 
 _lock = threading.Lock()
 _lib = None

@@ -342,6 +342,61 @@ class Batch:
         return sb.to_snapshot(volsurf_method=int(self.models[box].params.volsurf_method))
 
 
+class Server:
+    """Continuous batching of aggregation runs on one GPU (see include/mcacg.h)."""
+
+    def __init__(self, capacity: int, memory_budget: int = 0, stream: int | None = None,
+                 keep_final_states: bool = False):
+        self._s = C.c_void_p()
+        check(lib().mcacg_server_create(int(capacity), int(memory_budget), C.c_void_p(stream) if stream else None,
+                                        1 if keep_final_states else 0, C.byref(self._s)))
+
+    def close(self) -> None:
+        if self._s:
+            check(lib().mcacg_server_destroy(self._s))
+            self._s = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, model: PhysicalModel) -> int:
+        rid = C.c_int64()
+        check(lib().mcacg_server_submit(self._s, C.byref(model.params), C.byref(rid)))
+        return rid.value
+
+    def step(self, epoch_steps: int) -> tuple[int, int]:
+        a, p = C.c_int32(), C.c_int32()
+        check(lib().mcacg_server_step(self._s, int(epoch_steps), C.byref(a), C.byref(p)))
+        return a.value, p.value
+
+    def poll(self, max_items: int = 4096) -> np.ndarray:
+        buf = np.zeros(max_items, dtype=_lib.COMPLETION_DTYPE)
+        n = C.c_int32()
+        check(lib().mcacg_server_poll(self._s, buf.ctypes.data, int(max_items), C.byref(n)))
+        return buf[:n.value].copy()
+
+    def final_state(self, rid: int) -> Snapshot:
+        ns, na = C.c_int64(), C.c_int64()
+        check(lib().mcacg_server_final_sizes(self._s, int(rid), C.byref(ns), C.byref(na)))
+        sb = StateBuffers(ns.value, max(na.value, 1))
+        check(lib().mcacg_server_final_state(self._s, int(rid), C.byref(sb.state)))
+        return sb.to_snapshot()
+
+    def kernel_time(self) -> tuple[float, int]:
+        ms, n = C.c_double(), C.c_int32()
+        check(lib().mcacg_server_kernel_time(self._s, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+
 def run_device(aggregates: AggregatList, max_steps: int = 0) -> RunStats:
     """Advance one box with the device-resident loop."""
     s = RunStats()

@@ -2,9 +2,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cstring>
+#include <thread>
 
 #include "batch.hpp"
+#include "host_box.hpp"
 #include "run.cuh"
 
 namespace mcacg {
@@ -18,6 +22,7 @@ __global__ void __launch_bounds__(NT) k_run(const BoxRun *runs, int n, long long
     __shared__ __align__(16) BoxRun R;
     const int box = blockIdx.x;
     if (box >= n) return;
+    if (runs[box].st == nullptr) return;  // an empty serving slot
     const int words = int(sizeof(BoxRun) / sizeof(int));
     const int *src = reinterpret_cast<const int *>(&runs[box]);
     int *dst = reinterpret_cast<int *>(&R);
@@ -55,6 +60,59 @@ TreeLayout tree_layout(int nslots) {
         len = (len + kTreeFan - 1) / kTreeFan;
     }
     return t;
+}
+
+// Builds the sum tree (uploaded to a new device allocation), the loop state
+// and the run descriptor of one box.
+int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *state_dev, BoxRun *run,
+                 RunState *state, void **tree_dev, std::string *err) {
+    std::vector<double> ts(size_t(b.nslots));
+    std::vector<int> alive(size_t(b.nslots));
+    if (!ok_cuda(cudaMemcpy(ts.data(), b.agg + size_t(AGG_TIME_STEP) * b.nslots, sizeof(double) * ts.size(),
+                            cudaMemcpyDeviceToHost), err, "download"))
+        return ST_CUDA;
+    if (!ok_cuda(cudaMemcpy(alive.data(), b.agg_n, sizeof(int) * alive.size(), cudaMemcpyDeviceToHost), err,
+                 "download"))
+        return ST_CUDA;
+    TreeLayout tl = tree_layout(b.nslots);
+    std::vector<double> tree(size_t(tl.total), 0.0);
+    for (int a = 0; a < b.nslots; ++a) tree[size_t(a)] = alive[size_t(a)] > 0 ? 1.0 / ts[size_t(a)] : 0.0;
+    for (int lev = 1; lev < tl.levels; ++lev)
+        for (int g = 0; g < tl.len[lev]; ++g) {
+            double sum = 0.0;
+            for (int k = 0; k < kTreeFan; ++k) {
+                int c = g * kTreeFan + k;
+                if (c < tl.len[lev - 1]) sum += tree[size_t(tl.off[lev - 1] + c)];
+            }
+            tree[size_t(tl.off[lev] + g)] = sum;
+        }
+    double total = 0.0;
+    for (int k = 0; k < tl.len[tl.levels - 1]; ++k) total += tree[size_t(tl.off[tl.levels - 1] + k)];
+    *tree_dev = nullptr;
+    if (!ok_cuda(cudaMalloc(tree_dev, sizeof(double) * tree.size()), err, "cudaMalloc")) return ST_CUDA;
+    if (!ok_cuda(cudaMemcpy(*tree_dev, tree.data(), sizeof(double) * tree.size(), cudaMemcpyHostToDevice), err,
+                 "upload"))
+        return ST_CUDA;
+    std::memset(state, 0, sizeof(*state));
+    state->rng.seed(uint32_t(p.random_seed < 0 ? 0 : p.random_seed));
+    state->time = time;
+    state->weight_total = total;
+    std::memset(run, 0, sizeof(*run));
+    run->box = b;
+    run->phys = PhysParams{p.viscosity, p.gaz_mean_free_path, p.fractal_dimension, p.density, p.temperature};
+    run->lim.number_of_aggregates_limit = p.number_of_aggregates_limit;
+    run->lim.n_iter_without_event_limit = p.n_iter_without_event_limit;
+    run->lim.mean_monomere_per_aggregate_limit = p.mean_monomere_per_aggregate_limit;
+    run->lim.physical_time_limit = p.physical_time_limit;
+    run->lim.with_collisions = p.with_collisions;
+    run->st = state_dev;
+    run->tree = static_cast<double *>(*tree_dev);
+    run->tree_levels = tl.levels;
+    for (int k = 0; k < kMaxTreeLevels; ++k) {
+        run->tree_off[k] = tl.off[k];
+        run->tree_len[k] = tl.len[k];
+    }
+    return ST_OK;
 }
 
 }  // namespace
@@ -134,57 +192,11 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
     RunState *states_dev = static_cast<RunState *>(states_dev_);
     for (int i = 0; i < n; ++i) {
         const DevBox &b = *static_cast<DevBox *>(boxes_[size_t(i)]->devbox_ptr());
-        const mcacg_params &p = params[size_t(i)];
-        // leaves: 1 / time_step of every live slot
-        std::vector<double> ts(size_t(b.nslots));
-        std::vector<int> alive(size_t(b.nslots));
-        if (!ok_cuda(cudaMemcpy(ts.data(), b.agg + size_t(AGG_TIME_STEP) * b.nslots, sizeof(double) * ts.size(),
-                                cudaMemcpyDeviceToHost), err, "download"))
-            return ST_CUDA;
-        if (!ok_cuda(cudaMemcpy(alive.data(), b.agg_n, sizeof(int) * alive.size(), cudaMemcpyDeviceToHost), err,
-                     "download"))
-            return ST_CUDA;
-        TreeLayout tl = tree_layout(b.nslots);
-        std::vector<double> tree(size_t(tl.total), 0.0);
-        for (int a = 0; a < b.nslots; ++a) tree[size_t(a)] = alive[size_t(a)] > 0 ? 1.0 / ts[size_t(a)] : 0.0;
-        for (int lev = 1; lev < tl.levels; ++lev)
-            for (int g = 0; g < tl.len[lev]; ++g) {
-                double sum = 0.0;
-                for (int k = 0; k < kTreeFan; ++k) {
-                    int c = g * kTreeFan + k;
-                    if (c < tl.len[lev - 1]) sum += tree[size_t(tl.off[lev - 1] + c)];
-                }
-                tree[size_t(tl.off[lev] + g)] = sum;
-            }
-        double total = 0.0;
-        for (int k = 0; k < tl.len[tl.levels - 1]; ++k) total += tree[size_t(tl.off[tl.levels - 1] + k)];
         void *tree_dev = nullptr;
-        if (!ok_cuda(cudaMalloc(&tree_dev, sizeof(double) * tree.size()), err, "cudaMalloc")) return ST_CUDA;
-        trees_.push_back(tree_dev);
-        if (!ok_cuda(cudaMemcpy(tree_dev, tree.data(), sizeof(double) * tree.size(), cudaMemcpyHostToDevice), err,
-                     "upload"))
-            return ST_CUDA;
-        RunState &st = states[size_t(i)];
-        std::memset(&st, 0, sizeof(st));
-        st.rng.seed(uint32_t(p.random_seed < 0 ? 0 : p.random_seed));
-        st.time = times[size_t(i)];
-        st.weight_total = total;
-        BoxRun &R = runs[size_t(i)];
-        std::memset(&R, 0, sizeof(R));
-        R.box = b;
-        R.phys = PhysParams{p.viscosity, p.gaz_mean_free_path, p.fractal_dimension, p.density, p.temperature};
-        R.lim.number_of_aggregates_limit = p.number_of_aggregates_limit;
-        R.lim.n_iter_without_event_limit = p.n_iter_without_event_limit;
-        R.lim.mean_monomere_per_aggregate_limit = p.mean_monomere_per_aggregate_limit;
-        R.lim.physical_time_limit = p.physical_time_limit;
-        R.lim.with_collisions = p.with_collisions;
-        R.st = states_dev + i;
-        R.tree = static_cast<double *>(tree_dev);
-        R.tree_levels = tl.levels;
-        for (int k = 0; k < kMaxTreeLevels; ++k) {
-            R.tree_off[k] = tl.off[k];
-            R.tree_len[k] = tl.len[k];
-        }
+        int rc = make_box_run(b, params[size_t(i)], times[size_t(i)], states_dev + i, &runs[size_t(i)],
+                              &states[size_t(i)], &tree_dev, err);
+        if (tree_dev) trees_.push_back(tree_dev);
+        if (rc != ST_OK) return rc;
     }
     if (!ok_cuda(cudaMemcpyAsync(runs_dev_, runs.data(), sizeof(BoxRun) * size_t(n), cudaMemcpyHostToDevice, s), err,
                  "upload"))
@@ -289,6 +301,225 @@ int BatchRunner::download(int box, HostState *st, std::string *err) {
     if (rc != ST_OK) return rc;
     st->time = s[size_t(box)].time;
     return ST_OK;
+}
+
+// ------------------------------------------------------------------ Server
+double Server::now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count() - t0_;
+}
+
+int64_t Server::footprint(const mcacg_params &p) {
+    // device bytes of one box (DeviceBox::create's arrays plus the sum tree)
+    const int64_t n = p.n_monomeres;
+    const int64_t cells = p.n_verlet_divisions * p.n_verlet_divisions * p.n_verlet_divisions;
+    return n * 860 + cells * 4 * 80 + (1 << 20);
+}
+
+int Server::create(int capacity, int64_t memory_budget, void *stream, bool keep_final_states,
+                   std::unique_ptr<Server> *out, std::string *err) {
+    if (capacity <= 0) {
+        if (err) *err = "capacity must be positive";
+        return ST_BAD_ARGUMENT;
+    }
+    std::unique_ptr<Server> s(new Server());
+    s->capacity_ = capacity;
+    s->budget_ = memory_budget > 0 ? memory_budget : (int64_t(1) << 40);
+    s->keep_ = keep_final_states;
+    s->t0_ = 0;
+    s->t0_ = s->now();
+    if (stream) {
+        s->stream_ = stream;
+    } else {
+        cudaStream_t st;
+        if (!ok_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), err, "cudaStreamCreate")) return ST_CUDA;
+        s->stream_ = st;
+        s->own_stream_ = true;
+    }
+    s->slots_.resize(size_t(capacity));
+    if (!ok_cuda(cudaMalloc(&s->runs_dev_, sizeof(BoxRun) * size_t(capacity)), err, "cudaMalloc")) return ST_CUDA;
+    if (!ok_cuda(cudaMalloc(&s->states_dev_, sizeof(RunState) * size_t(capacity)), err, "cudaMalloc")) return ST_CUDA;
+    if (!ok_cuda(cudaMemset(s->runs_dev_, 0, sizeof(BoxRun) * size_t(capacity)), err, "cudaMemset")) return ST_CUDA;
+    if (!ok_cuda(cudaFuncSetAttribute(k_run<kRunThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(sizeof(RunSmem))), err, "cudaFuncSetAttribute"))
+        return ST_CUDA;
+    *out = std::move(s);
+    return ST_OK;
+}
+
+Server::~Server() {
+    if (stream_) cudaStreamSynchronize(static_cast<cudaStream_t>(stream_));
+    for (auto &sl : slots_)
+        if (sl.tree) cudaFree(sl.tree);
+    slots_.clear();
+    if (runs_dev_) cudaFree(runs_dev_);
+    if (states_dev_) cudaFree(states_dev_);
+    if (own_stream_ && stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
+}
+
+int Server::submit(const mcacg_params &p, int64_t *id, std::string *err) {
+    if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges ||
+        p.with_surface_reactions) {
+        if (err) *err = "served boxes cover the collision-only configuration";
+        return ST_INPUT;
+    }
+    if (footprint(p) > budget_) {
+        if (err) *err = "request larger than the device-memory budget";
+        return ST_CAPACITY;
+    }
+    *id = next_id_++;
+    pending_.push_back(Request{*id, p, now()});
+    return ST_OK;
+}
+
+int Server::n_active() const {
+    int n = 0;
+    for (const auto &sl : slots_) n += sl.id >= 0;
+    return n;
+}
+
+int Server::admit(std::string *err) {
+    // free slots and requests that fit, first come first served
+    std::vector<int> free_slots;
+    for (int i = 0; i < capacity_; ++i)
+        if (slots_[size_t(i)].id < 0) free_slots.push_back(i);
+    std::vector<Request> take;
+    size_t k = 0;
+    int64_t mem = mem_in_use_;
+    while (k < pending_.size() && take.size() < free_slots.size()) {
+        int64_t need = footprint(pending_[k].p);
+        if (mem + need > budget_) break;  // keep arrival order: wait for memory
+        mem += need;
+        take.push_back(pending_[k]);
+        ++k;
+    }
+    pending_.erase(pending_.begin(), pending_.begin() + long(k));
+    if (take.empty()) return ST_OK;
+    // reference placements in parallel (private rand() streams)
+    std::vector<HostState> states(take.size());
+    std::vector<int> rcs(take.size(), 0);
+    std::vector<std::string> errs(take.size());
+    std::atomic<int> next{0};
+    unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), unsigned(take.size())));
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t)
+        pool.emplace_back([&] {
+            for (int i = next++; i < int(take.size()); i = next++)
+                rcs[size_t(i)] = init_random_state_private(take[size_t(i)].p, &states[size_t(i)], &errs[size_t(i)]);
+        });
+    for (auto &th : pool) th.join();
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    BoxRun *runs_dev = static_cast<BoxRun *>(runs_dev_);
+    RunState *states_dev = static_cast<RunState *>(states_dev_);
+    for (size_t i = 0; i < take.size(); ++i) {
+        const int slot = free_slots[i];
+        Slot &sl = slots_[size_t(slot)];
+        const double t_admit = now();
+        if (rcs[i] != ST_OK) {
+            done_.push_back(Completion{take[i].id, 0, 0, 0, 0.0, rcs[i], 0, take[i].submit_s, t_admit, t_admit});
+            continue;
+        }
+        DeviceBox *d = nullptr;
+        int rc = DeviceBox::create(states[i], stream_, &d, err);
+        if (rc != ST_OK) return rc;
+        sl.box.reset(d);
+        BoxRun run;
+        RunState st;
+        rc = make_box_run(*static_cast<DevBox *>(d->devbox_ptr()), take[i].p, states[i].time, states_dev + slot, &run,
+                          &st, &sl.tree, err);
+        if (rc != ST_OK) return rc;
+        if (!ok_cuda(cudaMemcpyAsync(states_dev + slot, &st, sizeof(st), cudaMemcpyHostToDevice, s), err, "upload") ||
+            !ok_cuda(cudaMemcpyAsync(runs_dev + slot, &run, sizeof(run), cudaMemcpyHostToDevice, s), err, "upload") ||
+            !ok_cuda(cudaStreamSynchronize(s), err, "sync"))
+            return ST_CUDA;
+        sl.id = take[i].id;
+        sl.bytes = footprint(take[i].p);
+        sl.submit_s = take[i].submit_s;
+        sl.admit_s = t_admit;
+        mem_in_use_ += sl.bytes;
+        states[i] = HostState();
+    }
+    return ST_OK;
+}
+
+int Server::retire(std::string *err) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    std::vector<RunState> st(static_cast<size_t>(capacity_));
+    if (!ok_cuda(cudaMemcpyAsync(st.data(), states_dev_, sizeof(RunState) * size_t(capacity_), cudaMemcpyDeviceToHost,
+                                 s), err, "download") ||
+        !ok_cuda(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
+    BoxRun *runs_dev = static_cast<BoxRun *>(runs_dev_);
+    for (int i = 0; i < capacity_; ++i) {
+        Slot &sl = slots_[size_t(i)];
+        if (sl.id < 0) continue;
+        const RunState &r = st[size_t(i)];
+        if (!r.finished && r.status == ST_OK) continue;
+        HostState final_state;
+        if (keep_) {
+            int rc = sl.box->download(&final_state, err);
+            if (rc != ST_OK) return rc;
+            final_state.time = r.time;
+        }
+        DevScalars sc;
+        const DevBox &b = *static_cast<DevBox *>(sl.box->devbox_ptr());
+        if (!ok_cuda(cudaMemcpy(&sc, b.sc, sizeof(sc), cudaMemcpyDeviceToHost), err, "download")) return ST_CUDA;
+        done_.push_back(Completion{sl.id, r.steps, r.events, sc.n_alive, r.time, r.status, r.finished, sl.submit_s,
+                                   sl.admit_s, now()});
+        if (keep_) finals_.emplace_back(sl.id, std::move(final_state));
+        BoxRun empty;
+        std::memset(&empty, 0, sizeof(empty));
+        if (!ok_cuda(cudaMemcpyAsync(runs_dev + i, &empty, sizeof(empty), cudaMemcpyHostToDevice, s), err, "upload") ||
+            !ok_cuda(cudaStreamSynchronize(s), err, "sync"))
+            return ST_CUDA;
+        sl.box.reset();
+        if (sl.tree) cudaFree(sl.tree);
+        sl.tree = nullptr;
+        mem_in_use_ -= sl.bytes;
+        sl = Slot();
+    }
+    return ST_OK;
+}
+
+int Server::step(int64_t epoch_steps, std::string *err) {
+    int rc = admit(err);
+    if (rc != ST_OK) return rc;
+    if (n_active() > 0) {
+        cudaStream_t s = static_cast<cudaStream_t>(stream_);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, s);
+        k_run<kRunThreads><<<capacity_, kRunThreads, sizeof(RunSmem), s>>>(static_cast<const BoxRun *>(runs_dev_),
+                                                                           capacity_, (long long)epoch_steps);
+        ++launches_;
+        cudaEventRecord(e1, s);
+        if (!ok_cuda(cudaGetLastError(), err, "k_run") || !ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return ST_CUDA;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        kernel_ms_ += ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    return retire(err);
+}
+
+std::vector<Completion> Server::poll() {
+    std::vector<Completion> out;
+    out.swap(done_);
+    return out;
+}
+
+int Server::final_state(int64_t id, HostState *st) const {
+    for (const auto &f : finals_)
+        if (f.first == id) {
+            *st = f.second;
+            return ST_OK;
+        }
+    return ST_BAD_ARGUMENT;
 }
 
 }  // namespace mcacg

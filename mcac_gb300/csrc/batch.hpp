@@ -57,4 +57,64 @@ class BatchRunner {
     int launches_ = 0;
 };
 
+// Continuous-batching request loop: 'capacity' block slots; between kernel
+// epochs finished boxes leave and pending requests are admitted while a free
+// slot and the device-memory budget allow. A box's trajectory depends only on
+// its own state and rand() stream, so it is the same alone and in any mix.
+struct Completion {
+    int64_t id;
+    int64_t steps, events, n_alive;
+    double time;
+    int status, finished;
+    double submit_s, admit_s, finish_s;  // host clock, seconds since the server started
+};
+
+class Server {
+  public:
+    static int create(int capacity, int64_t memory_budget, void *stream, bool keep_final_states,
+                      std::unique_ptr<Server> *out, std::string *err);
+    ~Server();
+    int submit(const mcacg_params &p, int64_t *id, std::string *err);
+    // admit, one kernel epoch of at most 'epoch_steps' steps per box, retire
+    int step(int64_t epoch_steps, std::string *err);
+    int n_active() const;
+    int n_pending() const { return int(pending_.size()); }
+    std::vector<Completion> poll();
+    int final_state(int64_t id, HostState *st) const;
+    double kernel_ms() const { return kernel_ms_; }
+    int launches() const { return launches_; }
+    int64_t memory_in_use() const { return mem_in_use_; }
+
+  private:
+    Server() = default;
+    static int64_t footprint(const mcacg_params &p);
+    double now() const;
+    struct Request {
+        int64_t id;
+        mcacg_params p;
+        double submit_s;
+    };
+    struct Slot {
+        std::unique_ptr<DeviceBox> box;
+        void *tree = nullptr;
+        int64_t id = -1;
+        int64_t bytes = 0;
+        double submit_s = 0, admit_s = 0;
+    };
+    int admit(std::string *err);
+    int retire(std::string *err);
+    int capacity_ = 0;
+    int64_t budget_ = 0, mem_in_use_ = 0, next_id_ = 0;
+    bool keep_ = false;
+    void *stream_ = nullptr;
+    bool own_stream_ = false;
+    void *runs_dev_ = nullptr, *states_dev_ = nullptr;
+    std::vector<Slot> slots_;
+    std::vector<Request> pending_;
+    std::vector<Completion> done_;
+    std::vector<std::pair<int64_t, HostState>> finals_;
+    double t0_ = 0, kernel_ms_ = 0;
+    int launches_ = 0;
+};
+
 }  // namespace mcacg

@@ -29,6 +29,11 @@ struct mcacg_batch {
     std::vector<mcacg_params> params;
 };
 
+struct mcacg_server {
+    std::unique_ptr<mcacg::Server> impl;
+    std::vector<mcacg::Completion> unread;
+};
+
 namespace {
 
 // A slot-ordered device state as the C-ABI's label-ordered arrays.
@@ -558,6 +563,95 @@ int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out) {
             out->merged_spheres += x.merged_spheres;
             out->merge_pairs += x.merge_pairs;
         }
+        return 0;
+    });
+}
+
+int mcacg_server_create(int32_t capacity, int64_t memory_budget_bytes, void *cuda_stream, int32_t keep_final_states,
+                        mcacg_server **server) {
+    return guarded([&] {
+        if (!server) return fail(MCACG_ERR_BAD_ARGUMENT, "null server");
+        *server = nullptr;
+        std::unique_ptr<mcacg_server> s(new mcacg_server());
+        std::string err;
+        int rc = mcacg::Server::create(capacity, memory_budget_bytes, cuda_stream, keep_final_states != 0, &s->impl,
+                                       &err);
+        if (rc != 0) return finish(rc, err);
+        *server = s.release();
+        return 0;
+    });
+}
+
+int mcacg_server_destroy(mcacg_server *server) {
+    return guarded([&] {
+        delete server;
+        return 0;
+    });
+}
+
+int mcacg_server_submit(mcacg_server *server, const mcacg_params *params, int64_t *id) {
+    return guarded([&] {
+        if (!server || !params || !id) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::string err;
+        return finish(server->impl->submit(*params, id, &err), err);
+    });
+}
+
+int mcacg_server_step(mcacg_server *server, int64_t epoch_steps, int32_t *n_active, int32_t *n_pending) {
+    return guarded([&] {
+        if (!server) return fail(MCACG_ERR_BAD_ARGUMENT, "null server");
+        std::string err;
+        int rc = server->impl->step(epoch_steps, &err);
+        if (n_active) *n_active = server->impl->n_active();
+        if (n_pending) *n_pending = server->impl->n_pending();
+        return finish(rc, err);
+    });
+}
+
+int mcacg_server_poll(mcacg_server *server, mcacg_completion *out, int32_t capacity, int32_t *n_out) {
+    return guarded([&] {
+        if (!server || !n_out || (capacity > 0 && !out)) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        for (auto &c : server->impl->poll()) server->unread.push_back(c);
+        int32_t n = std::min<int32_t>(capacity, int32_t(server->unread.size()));
+        for (int32_t i = 0; i < n; ++i) {
+            const auto &c = server->unread[size_t(i)];
+            out[i] = mcacg_completion{c.id, c.steps, c.events, c.n_alive, c.time, c.status, c.finished,
+                                      c.submit_s, c.admit_s, c.finish_s};
+        }
+        server->unread.erase(server->unread.begin(), server->unread.begin() + n);
+        *n_out = n;
+        return 0;
+    });
+}
+
+int mcacg_server_final_sizes(mcacg_server *server, int64_t id, int64_t *n_spheres, int64_t *n_aggregates) {
+    return guarded([&] {
+        if (!server) return fail(MCACG_ERR_BAD_ARGUMENT, "null server");
+        mcacg::HostState st;
+        if (server->impl->final_state(id, &st) != 0) return fail(MCACG_ERR_BAD_ARGUMENT, "no final state for id");
+        int na = 0;
+        for (int n : st.agg_n) na += n > 0;
+        if (n_spheres) *n_spheres = st.ns;
+        if (n_aggregates) *n_aggregates = na;
+        return 0;
+    });
+}
+
+int mcacg_server_final_state(mcacg_server *server, int64_t id, mcacg_state *state) {
+    return guarded([&] {
+        if (!server || !state) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        mcacg::HostState st;
+        if (server->impl->final_state(id, &st) != 0) return fail(MCACG_ERR_BAD_ARGUMENT, "no final state for id");
+        std::string err;
+        return finish(store_host_state(st, state, &err), err);
+    });
+}
+
+int mcacg_server_kernel_time(const mcacg_server *server, double *kernel_ms, int32_t *launches) {
+    return guarded([&] {
+        if (!server) return fail(MCACG_ERR_BAD_ARGUMENT, "null server");
+        if (kernel_ms) *kernel_ms = server->impl->kernel_ms();
+        if (launches) *launches = server->impl->launches();
         return 0;
     });
 }

@@ -456,6 +456,8 @@ int HostBox::merge(const mcacg_contact &c, int32_t *merged, std::string *err) {
     const int keep = m.keep, removed = m.removed;
     // proper time keeping the global time constant (aggregat_list.cpp:385-387)
     double newtime = F(AGG_TIME, keep) + F(AGG_TIME, removed) - time_;
+    dt_order_erase(keep, F(AGG_TIME_STEP, keep));
+    dt_order_erase(removed, F(AGG_TIME_STEP, removed));
     AggregatePhysics ph = aggregate_physics(p_, m.fields[AGG_VOLUME], m.vol_pp, m.fields[AGG_DP], m.fields[AGG_RG]);
     const int geometry[] = {AGG_RG, AGG_RMAX, AGG_VOLUME, AGG_SURFACE, AGG_X, AGG_Y, AGG_Z, AGG_RX, AGG_RY, AGG_RZ,
                             AGG_DP, AGG_OVERLAPPING, AGG_COORDINATION_NUMBER};
@@ -463,6 +465,7 @@ int HostBox::merge(const mcacg_contact &c, int32_t *merged, std::string *err) {
     F(AGG_F_AGG, keep) = ph.f_agg;
     F(AGG_D_M, keep) = ph.d_m;
     F(AGG_TIME_STEP, keep) = ph.time_step;
+    dt_order_insert(keep, ph.time_step);
     F(AGG_LPM, keep) = ph.lpm;
     F(AGG_DG_OVER_DP, keep) = ph.dg_over_dp;
     F(AGG_TIME, keep) = newtime;
@@ -481,9 +484,70 @@ int HostBox::merge(const mcacg_contact &c, int32_t *merged, std::string *err) {
     return ST_OK;
 }
 
+void HostBox::build_dt_order() {
+    by_dt_.clear();
+    by_dt_.reserve(alive_.size());
+    for (int slot : alive_) by_dt_.emplace_back(F(AGG_TIME_STEP, slot), slot);
+    std::sort(by_dt_.begin(), by_dt_.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+        return a.first > b.first || (a.first == b.first && a.second < b.second);
+    });
+    dt_order_valid_ = true;
+}
+
+void HostBox::dt_order_erase(int slot, double dt) {
+    if (!dt_order_valid_) return;
+    auto cmp = [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+        return a.first > b.first || (a.first == b.first && a.second < b.second);
+    };
+    auto it = std::lower_bound(by_dt_.begin(), by_dt_.end(), std::make_pair(dt, slot), cmp);
+    if (it != by_dt_.end() && it->second == slot) {
+        by_dt_.erase(it);
+    } else {
+        dt_order_valid_ = false;
+    }
+}
+
+void HostBox::dt_order_insert(int slot, double dt) {
+    if (!dt_order_valid_) return;
+    auto cmp = [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+        return a.first > b.first || (a.first == b.first && a.second < b.second);
+    };
+    auto pr = std::make_pair(dt, slot);
+    by_dt_.insert(std::lower_bound(by_dt_.begin(), by_dt_.end(), pr, cmp), pr);
+}
+
 void HostBox::sort_time_steps(double factor) {
-    // aggregat_list.cpp:109-141: std::sort of label indices by factor/time_step
+    // aggregat_list.cpp:109-141: std::sort of label indices by factor/time_step,
+    // then the sequential cumulative sum.
+    //
+    // factor/time_step is non-increasing in time_step (correctly rounded
+    // division is monotone), so the aggregates ordered by decreasing time
+    // step are in non-decreasing weight order. When every weight in that
+    // order is strictly greater than the previous one, that order is the only
+    // sorted order, so it is exactly what std::sort returns; the order is kept
+    // up to date at every merge instead of re-sorting. Any tie (identical
+    // monomers, or two time steps rounding to one weight) takes the full
+    // std::sort path, whose element order among ties is the reference's.
     const size_t n = alive_.size();
+    if (!dt_order_valid_ || by_dt_.size() != n) build_dt_order();
+    if (slot_label_.size() != size_t(nslots_)) slot_label_.assign(size_t(nslots_), -1);
+    for (size_t l = 0; l < n; ++l) slot_label_[size_t(alive_[l])] = int(l);
+    index_sorted_.resize(n);
+    cumulative_.resize(n);
+    bool strict = true;
+    double prev = -std::numeric_limits<double>::infinity();
+    for (size_t k = 0; k < n; ++k) {
+        const int slot = by_dt_[k].second;
+        const double tp = factor / F(AGG_TIME_STEP, slot);
+        if (!(tp > prev)) {
+            strict = false;
+            break;
+        }
+        prev = tp;
+        index_sorted_[k] = size_t(slot_label_[size_t(slot)]);
+        cumulative_[k] = (k == 0) ? tp : cumulative_[k - 1] + tp;
+    }
+    if (strict) return;
     std::vector<double> tp(n);
     for (size_t i = 0; i < n; i++) tp[i] = factor / F(AGG_TIME_STEP, alive_[i]);
     index_sorted_.resize(n);
@@ -655,7 +719,8 @@ int HostBox::store(mcacg_state *out, std::string *err) {
 namespace mcacg {
 
 HostBox::HostBox() = default;
-HostBox::~HostBox() = default;
+// the device-loop runner works on dev_'s stream and memory: it goes first
+HostBox::~HostBox() { runner_.reset(); }
 
 void HostBox::set_time(double t) {
     time_ = t;
@@ -678,6 +743,7 @@ int HostBox::refresh_from_device(std::string *err) {
         if (agg_n_[size_t(a)] > 0) alive_.push_back(a);
     maxradius_ = st.maxradius;
     event_ = true;
+    dt_order_valid_ = false;
     if (!alive_.empty()) refresh();
     return ST_OK;
 }

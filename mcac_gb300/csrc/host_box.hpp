@@ -89,6 +89,13 @@ class HostBox {
     double max_time_step_ = 0, avg_npp_ = 1;
     std::vector<size_t> index_sorted_;
     std::vector<double> cumulative_;
+    // live slots ordered by decreasing time step (kept across merges)
+    std::vector<std::pair<double, int>> by_dt_;
+    bool dt_order_valid_ = false;
+    std::vector<int> slot_label_;
+    void build_dt_order();
+    void dt_order_erase(int slot, double dt);
+    void dt_order_insert(int slot, double dt);
     std::unique_ptr<DeviceBox> dev_;
 };
 

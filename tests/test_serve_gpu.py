@@ -1,0 +1,70 @@
+"""Continuous batching (Server): admission by slot and memory, completion,
+and the same result for a request alone and in a mix."""
+import numpy as np
+import pytest
+
+from mcac_gb300 import Batch, PhysicalModel, Server
+
+
+def req_ini(n, seed, fv=4e-3, nagg=3, disp=1.3):
+    return (f"[monomers]\nnumber = {n}\nmean_diameter = 30\ndispersion_diameter = {disp}\n"
+            f"initialisation_mode = lognormal\n[environment]\nvolume_fraction = {fv}\ntemperature = 1700\n"
+            f"[limits]\nnumber_of_aggregates = {nagg}\n"
+            f"[numerics]\nrandom_seed = {seed}\nwith_domain_duplication = false\n")
+
+
+def same_state(a, b):
+    return (np.array_equal(a.spheres.view(np.int64), b.spheres.view(np.int64))
+            and np.array_equal(a.aggregates.view(np.int64), b.aggregates.view(np.int64))
+            and np.array_equal(a.members, b.members) and np.array_equal(a.sphere_label, b.sphere_label))
+
+
+@pytest.mark.gpu
+def test_requests_admitted_as_slots_free_and_match_alone():
+    sizes = [200, 450, 300, 700, 250, 600, 350, 500, 220, 650]
+    models = [PhysicalModel(text=req_ini(n, 900 + k)) for k, n in enumerate(sizes)]
+    done = {}
+    max_active = 0
+    with Server(capacity=4, keep_final_states=True) as srv:
+        ids = [srv.submit(m) for m in models[:6]]
+        for epoch in range(10_000):
+            if epoch == 3:
+                ids += [srv.submit(m) for m in models[6:]]  # arrivals while others run
+            active, pending = srv.step(800)
+            max_active = max(max_active, active)
+            for c in srv.poll():
+                done[int(c["id"])] = c
+            if len(done) == len(models) and active == 0 and pending == 0:
+                break
+        assert len(done) == len(models)
+        assert max_active <= 4
+        for rid in ids:
+            c = done[rid]
+            assert c["status"] == 0 and c["finished"] == 1 and c["n_aggregates"] <= 3
+            assert c["submit_s"] <= c["admit_s"] <= c["finish_s"]
+        finals = {rid: srv.final_state(rid) for rid in ids[:3] + ids[-2:]}
+    # the same requests alone
+    for k, rid in enumerate(ids[:3] + ids[-2:]):
+        idx = ids.index(rid)
+        with Batch([models[idx]]) as b:
+            b.run(max_steps=0, steps_per_launch=5000)
+            alone = b.store(0)
+            assert int(b.stats()["steps"][0]) == int(done[rid]["steps"])
+        assert same_state(alone, finals[rid]), rid
+
+
+@pytest.mark.gpu
+def test_memory_budget_limits_concurrency():
+    models = [PhysicalModel(text=req_ini(300, 50 + k)) for k in range(4)]
+    one_box = 300 * 860 + 1000 * 4 * 80 + (1 << 20)  # the server's footprint model for one box
+    with Server(capacity=4, memory_budget=int(one_box * 1.5)) as srv:
+        for m in models:
+            srv.submit(m)
+        seen, max_active = 0, 0
+        for _ in range(10_000):
+            active, pending = srv.step(1000)
+            max_active = max(max_active, active)
+            seen += len(srv.poll())
+            if seen == 4 and pending == 0 and active == 0:
+                break
+        assert seen == 4 and max_active <= 1

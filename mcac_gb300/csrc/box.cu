@@ -40,22 +40,41 @@ __global__ void k_set_fields(DevBox b, int slot, FieldUpdate u, unsigned mask) {
     if (f < AGG_NFIELDS && (mask >> f) & 1u) A(b, f, slot) = u.v[f];
 }
 
-__global__ void k_rebuild_grid(DevBox b) {
-    // one block: serial insertion in slot order keeps every cell sorted
-    if (threadIdx.x == 0) {
-        for (int c = 0; c < b.n_cells; ++c) b.cell_n[c] = 0;
-        for (int a = 0; a < b.nslots; ++a) {
-            if (b.agg_n[a] == 0) continue;
-            int c = cell_of(b, agg_pos(b, a));
-            b.agg_cell[a] = c;
-            int n = b.cell_n[c];
-            if (n >= b.cell_cap) {
-                b.sc->cell_overflow = 1;
-                b.sc->status = ST_CAPACITY;
-                continue;
+// Verlet grid from the aggregate positions, in three grid-wide passes:
+// clear the cells, drop every live slot into its cell, sort each cell by slot
+// (the reference's std::set order).
+__global__ void k_grid_clear(DevBox b) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < b.n_cells; c += gridDim.x * blockDim.x) b.cell_n[c] = 0;
+}
+__global__ void k_grid_fill(DevBox b) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nslots; a += gridDim.x * blockDim.x) {
+        if (b.agg_n[a] == 0) continue;
+        const int c = cell_of(b, agg_pos(b, a));
+        b.agg_cell[a] = c;
+        const int k = atomicAdd(&b.cell_n[c], 1);
+        if (k < b.cell_cap) {
+            b.cell_items[size_t(c) * b.cell_cap + k] = a;
+        } else {
+            b.sc->cell_overflow = 1;
+            b.sc->status = ST_CAPACITY;
+        }
+    }
+}
+__global__ void k_grid_sort(DevBox b) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < b.n_cells; c += gridDim.x * blockDim.x) {
+        int n = b.cell_n[c];
+        if (n > b.cell_cap) {
+            n = b.cell_cap;
+            b.cell_n[c] = n;
+        }
+        int *items = b.cell_items + size_t(c) * b.cell_cap;
+        for (int x = 1; x < n; ++x) {
+            int v = items[x], y = x;
+            while (y > 0 && items[y - 1] > v) {
+                items[y] = items[y - 1];
+                --y;
             }
-            b.cell_items[size_t(c) * b.cell_cap + n] = a;
-            b.cell_n[c] = n + 1;
+            items[y] = v;
         }
     }
 }
@@ -327,8 +346,12 @@ int DeviceBox::rebuild_grid(int cap, std::string *err) {
     sc.cell_overflow = 0;
     if (sc.status == ST_CAPACITY) sc.status = ST_OK;
     if (!cuda_ok(cudaMemcpyAsync(b.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, s), err, "status")) return ST_CUDA;
-    k_rebuild_grid<<<1, 32, 0, s>>>(b);
-    if (!cuda_ok(cudaGetLastError(), err, "k_rebuild_grid")) return ST_CUDA;
+    const int cells_blocks = std::min(1024, (b.n_cells + 255) / 256);
+    const int slot_blocks = std::min(1024, (b.nslots + 255) / 256);
+    k_grid_clear<<<cells_blocks, 256, 0, s>>>(b);
+    k_grid_fill<<<slot_blocks, 256, 0, s>>>(b);
+    k_grid_sort<<<cells_blocks, 256, 0, s>>>(b);
+    if (!cuda_ok(cudaGetLastError(), err, "grid build")) return ST_CUDA;
     int st = check_status(err);
     if (st == ST_CAPACITY) return rebuild_grid(cap * 2, err);
     return st;

@@ -51,6 +51,8 @@ __global__ void k_grid_fill(DevBox b) {
         if (b.agg_n[a] == 0) continue;
         const int c = cell_of(b, agg_pos(b, a));
         b.agg_cell[a] = c;
+        b.agg_f4[a] = make_float4(float(A(b, AGG_X, a)), float(A(b, AGG_Y, a)), float(A(b, AGG_Z, a)),
+                                  float(A(b, AGG_RMAX, a)));
         const int k = atomicAdd(&b.cell_n[c], 1);
         if (k < b.cell_cap) {
             b.cell_items[size_t(c) * b.cell_cap + k] = a;
@@ -59,6 +61,11 @@ __global__ void k_grid_fill(DevBox b) {
             b.sc->status = ST_CAPACITY;
         }
     }
+}
+__global__ void k_refresh_f4(DevBox b) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nslots; a += gridDim.x * blockDim.x)
+        b.agg_f4[a] = make_float4(float(A(b, AGG_X, a)), float(A(b, AGG_Y, a)), float(A(b, AGG_Z, a)),
+                                  float(A(b, AGG_RMAX, a)));
 }
 __global__ void k_grid_sort(DevBox b) {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < b.n_cells; c += gridDim.x * blockDim.x) {
@@ -170,6 +177,7 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     ok = ok && alloc((void **)&b.agg_n, sizeof(int) * size_t(st.nslots));
     ok = ok && alloc((void **)&b.agg_off, sizeof(int) * size_t(st.nslots));
     ok = ok && alloc((void **)&b.agg_cell, sizeof(int) * size_t(st.nslots));
+    ok = ok && alloc((void **)&b.agg_f4, sizeof(float4) * size_t(st.nslots));
     for (int k = 0; k < 2; ++k) {
         ok = ok && alloc((void **)&b.pool_id[k], sizeof(int) * size_t(b.pool_cap));
         ok = ok && alloc((void **)&b.pool_pos[k], sizeof(float4) * size_t(b.pool_cap));
@@ -465,6 +473,8 @@ int DeviceBox::upload_aggregates(const std::vector<double> &agg, std::string *er
     if (!cuda_ok(cudaMemcpyAsync(b.agg, agg.data(), sizeof(double) * agg.size(), cudaMemcpyHostToDevice, s), err,
                  "upload"))
         return ST_CUDA;
+    k_refresh_f4<<<std::min(1024, (b.nslots + 255) / 256), 256, 0, s>>>(b);
+    if (!cuda_ok(cudaGetLastError(), err, "k_refresh_f4")) return ST_CUDA;
     if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
     return ST_OK;
 }

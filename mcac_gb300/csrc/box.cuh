@@ -61,6 +61,7 @@ struct DevBox {
     int *agg_n;      // members (0: dead slot)
     int *agg_off;    // segment offset in the live pool
     int *agg_cell;   // linear Verlet cell
+    float4 *agg_f4;  // FP32 (x, y, z, rmax) of each slot, for the neighbour screen
     int *pool_id[2];
     float4 *pool_pos[2];
     int *cell_n;     // [n_cells]
@@ -345,9 +346,10 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
                 sm.found_source = 1;
                 continue;
             }
+            const float4 of = b.agg_f4[slot];
+            if (!capsule_hit(w, of.x, of.y, of.z, float(rmax_src) + of.w + margin)) continue;
             const double ox = A(b, AGG_X, slot), oy = A(b, AGG_Y, slot), oz = A(b, AGG_Z, slot);
             const double orm = A(b, AGG_RMAX, slot);
-            if (!capsule_hit(w, float(ox), float(oy), float(oz), float(rmax_src + orm) + margin)) continue;
             double db = sweep_contact_distance(sp, rmax_src, Vec3{ox, oy, oz}, orm, dir, dist, b.L);
             if (db < dist) {
                 int k = atomicAdd(&sm.n_cand, 1);  // < nslots: one entry per aggregate
@@ -568,6 +570,7 @@ __device__ inline void block_translate(const DevBox &b, int slot, Vec3 v, double
         A(b, AGG_X, slot) = x;
         A(b, AGG_Y, slot) = y;
         A(b, AGG_Z, slot) = z;
+        b.agg_f4[slot] = make_float4(float(x), float(y), float(z), float(A(b, AGG_RMAX, slot)));
         refpos_sm[0] = x - A(b, AGG_RX, slot);
         refpos_sm[1] = y - A(b, AGG_RY, slot);
         refpos_sm[2] = z - A(b, AGG_RZ, slot);

@@ -416,6 +416,7 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
         A(b, AGG_DP, keep) = dp;
         A(b, AGG_OVERLAPPING, keep) = overlapping;
         A(b, AGG_COORDINATION_NUMBER, keep) = coordination;
+        b.agg_f4[keep] = make_float4(float(x), float(y), float(z), float(rmax));
         regrid(b, keep);
         cell_remove(b, b.agg_cell[removed], removed);
         if (rmax > sc->maxradius) sc->maxradius = rmax;

@@ -57,16 +57,24 @@ def check_state(snap, tol=1e-12):
         pos = snap.spheres[[S["x"], S["y"], S["z"]]][:, mem]
         ref = pos - rel
         assert np.all(np.abs(periodic(ref - ref[:, :1], L)) < 1e-12 * L)
-    # no two aggregates interpenetrate
+    # no two aggregates interpenetrate, except by what the reference's own
+    # bounding-sphere filter can miss: a monomer that was never merged keeps
+    # the r_max of its radius before the volume-fraction rescaling, so its
+    # sphere may reach r - r_max beyond its bounding sphere
     p = snap.spheres[[S["x"], S["y"], S["z"]]].T
     rad = snap.spheres[S["r"]]
     lab = snap.sphere_label
+    agg_slack = np.where(snap.n_spheres == 1,
+                         np.maximum(0.0, rad[snap.members[snap.member_offsets()[:-1]]]
+                                    - snap.aggregates[A["rmax"]]), 0.0)
+    slack = agg_slack[lab]
     for i in range(ns):
         d = periodic(p[i + 1:] - p[i], L)
         dist = np.sqrt((d ** 2).sum(1))
         other = lab[i + 1:] != lab[i]
         gap = dist - (rad[i + 1:] + rad[i])
-        assert np.all(gap[other] > -1e-9 * rad[i]), (i, gap[other].min())
+        allowed = -(slack[i + 1:] + slack[i]) - 1e-9 * rad[i]
+        assert np.all(gap[other] > allowed[other]), (i, (gap - allowed)[other].min())
 
 
 @pytest.mark.gpu

@@ -8,8 +8,9 @@ that box by --mc-steps (default 2000) steps of the pick-move-collide-merge
 loop; the metric is MC steps per second summed over replicas.
 
 Arms:
-  --impl ours       (default) R independent replicas of the box (seeds 1..R,
-                    R = one per SM unless --replicas) advanced by the
+  --impl ours       (default) R independent replicas of the box (seeds 1..,
+                    skipping DEGENERATE_SEEDS; R = one per SM unless
+                    --replicas) advanced by the
                     device-resident loop, one thread block per box; value is
                     timed with CUDA events on the launching stream; e2e goes
                     through the C-ABI from host buffers: upload of the R
@@ -22,6 +23,11 @@ Arms:
 
 Under torchrun each rank runs its own replicas (boxes are independent; no
 exchange): value = total steps of all ranks / max time.
+
+--workload contact-search times the contact-search microbenchmark instead:
+10,000 queries on a 1,000,000-sphere synthetic snapshot per bench step, all
+in one batched launch (metric: contact queries/s; the reference arm is the
+oracle on one core).
 """
 from __future__ import annotations
 
@@ -137,23 +143,41 @@ def query_bytes(prof: dict) -> float:
             + 16.0 * prof["cand_spheres"] + 64.0 * prof["refined"])
 
 
-def replica_models(n: int, base_seed: int):
+# Seeds whose reference initial state is degenerate: one monomer is drawn so
+# far out in the log-normal tail that the volume-fraction rescaling shrinks
+# every other sphere to about 1e-20 m and leaves that aggregate with a
+# bounding radius far larger than the box, so every contact query scans the
+# whole box. Found by scanning the initial states of seeds 1..2599.
+DEGENERATE_SEEDS = frozenset({257})
+
+
+def replica_seeds(n: int, first: int) -> list[int]:
+    """n seeds from 'first' upwards, skipping the degenerate ones."""
+    seeds, s = [], first
+    while len(seeds) < n:
+        if s not in DEGENERATE_SEEDS:
+            seeds.append(s)
+        s += 1
+    return seeds
+
+
+def replica_models(n: int, rank: int = 0):
     from mcac_gb300 import PhysicalModel
+    # disjoint seed ranges per rank
+    seeds = replica_seeds(n * (rank + 1), 1)[n * rank:]
     models = []
-    for i in range(n):
+    for seed in seeds:
         pm = PhysicalModel(text=C2_INI)
-        pm.set(random_seed=base_seed + i)
+        pm.set(random_seed=seed)
         models.append(pm)
     return models
 
 
 def host_states(models):
-    """The reference placement of every replica, on the host (parallel)."""
-    from concurrent.futures import ThreadPoolExecutor
-
+    """The reference placement of every replica, on the host. Sequential: it
+    draws from the C library's single random stream."""
     from mcac_gb300 import init_state
-    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
-        return list(ex.map(init_state, models))
+    return [init_state(m) for m in models]
 
 
 def plain_single_box(args, stream) -> dict:
@@ -189,7 +213,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
     R = args.replicas or torch.cuda.get_device_properties(dev).multi_processor_count
-    models = replica_models(R, 1 + rank * R)
+    models = replica_models(R, rank)
     t0 = time.perf_counter()
     batch = Batch(models, stream=stream.cuda_stream)
     setup_s = time.perf_counter() - t0
@@ -261,7 +285,9 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "100k-monomer box: LogNormal(30 nm, 1.25), 1000 ppm, 1700 K, seed 1, "
                                "stop at 100 aggregates", "n_monomers": 100000, "replicas_per_gpu": R,
-                   "replica_seeds": f"{1 + rank * R}..{R + rank * R}", "mc_steps_per_box_per_bench_step": M,
+                   "replica_seeds": f"{models[0].random_seed}..{models[-1].random_seed} on rank 0, skipping "
+                                    f"{sorted(DEGENERATE_SEEDS)} (degenerate initial state)",
+                   "mc_steps_per_box_per_bench_step": M,
                    "path": "device-resident MC loop, one thread block per box, one launch per bench step",
                    "parallelism": f"{R} independent replicas per GPU x {world} GPU",
                    "l2": "flushed (256 MB write) between timed iterations", "setup_s": round(setup_s, 2),
@@ -280,6 +306,127 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         out["plain_single_box"] = plain_single_box(args, stream)
     out["cpu_baseline"] = cpu_baseline_sample(args) if not args.no_cpu_baseline else None
     return out
+
+
+CS_WORKLOAD = ("contact-search microbenchmark: 1,000,000 spheres LogNormal(30 nm, 1.5) in 20,000 ballistic "
+               "aggregates of 1-500 spheres, 5000 ppm, 10,000 queries (uniform label, random_direction, length lpm)")
+CS_METRIC, CS_UNIT = "contact queries/s", "queries/s"
+
+
+def oracle_queries(case, n: int) -> tuple[float, int]:
+    """Seconds the oracle takes for the first n queries of 'case' (1 core)."""
+    from oracle import oracle_py
+    ob = oracle_py.OracleBox(case.model.to_ini(), case.state.to_snapshot())
+    t = time.perf_counter()
+    for k in range(n):
+        ob.distance_to_next_contact(case.sources[k], case.directions[k], case.distances[k])
+    dt = time.perf_counter() - t
+    ob.close()
+    return dt, n
+
+
+def run_contact_search(args, rank: int, world: int) -> dict | None:
+    import torch
+
+    from mcac_gb300 import AggregatList
+    from mcac_gb300.workloads import contact_search_case
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    case = contact_search_case(seed=1 + rank)
+    gen_s = time.perf_counter() - t0
+    nq = len(case.sources)
+    box = AggregatList(case.model, case.state, stream=stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    for _ in range(args.warmup):
+        box.distance_to_next_contacts(case.sources, case.directions, case.distances)
+    box.set_profiling(True)
+    box.take_profile()
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(dev)
+    sampler.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()  # the snapshot (about 100 MB) would otherwise stay in L2
+        torch.cuda.synchronize()
+        _, ms = box.distance_to_next_contacts(case.sources, case.directions, case.distances)
+        total_ms += ms
+    clocks = sampler.stop()
+    prof = box.take_profile()
+    box.set_profiling(False)
+    # end to end: queries from host memory, results back to host memory
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        out, _ = box.distance_to_next_contacts(case.sources, case.directions, case.distances)
+        e2e_s += time.perf_counter() - t
+    box.close()
+    times = torch.tensor([total_ms / 1000.0, e2e_s], device="cuda", dtype=torch.float64)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(times, op=dist.ReduceOp.MAX)
+    wall, e2e_wall = float(times[0]), float(times[1])
+    if rank != 0:
+        return None
+    peak, peak_kind = peaks()
+    qbytes = query_bytes(prof)
+    achieved = qbytes / (total_ms / 1000.0) / 1e9 if total_ms > 0 else 0.0
+    res = {
+        "metric": CS_METRIC, "value": world * nq * args.steps / wall, "unit": CS_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1000.0 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (FP32 screen)",
+        "data": "synthetic",
+        "config": {"workload": CS_WORKLOAD, "queries_per_step": nq, "snapshot_seed": "1 + rank",
+                   "generation_s": round(gen_s, 2), "l2": "flushed (256 MB write) between timed iterations",
+                   "path": "mcacg_distance_to_next_contacts: one thread block per query, all queries in one launch",
+                   "hits": int((out["moving_sphere"] >= 0).sum())},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None, "kernel": "k_query_batch",
+                     "bytes_per_launch": qbytes / max(1, args.steps),
+                     "us_per_launch": 1000.0 * total_ms / max(1, args.steps),
+                     "bytes_model": "per contact query: 16 B x moving spheres + 36 B x aggregates scanned + 8 B x cells "
+                                    "+ 16 B x candidate spheres + 64 B x FP64-refined pairs"},
+        "e2e": {"value": world * nq * args.steps / e2e_wall, "unit": CS_UNIT,
+                "h2d_bytes_per_step": int(case.sources.nbytes + case.directions.nbytes + case.distances.nbytes),
+                "d2h_bytes_per_step": int(out.nbytes)},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "work": prof,
+    }
+    if not args.no_cpu_baseline:
+        n = min(nq, 4000)
+        dt, n = oracle_queries(case, n)
+        res["cpu_baseline"] = {"value": n / dt, "unit": CS_UNIT, "cores": 1, "kind": "port",
+                               "sample": f"the first {n} queries of the same snapshot, oracle, 1 core"}
+    else:
+        res["cpu_baseline"] = None
+    return res
+
+
+def run_contact_search_reference(args) -> dict:
+    from mcac_gb300.workloads import contact_search_case
+    case = contact_search_case(seed=1)
+    n = len(case.sources)
+    total = 0.0
+    for _ in range(args.warmup):
+        oracle_queries(case, min(n, 500))
+    for _ in range(args.steps):
+        dt, _ = oracle_queries(case, n)
+        total += dt
+    v = n * args.steps / total
+    return {
+        "impl": "reference", "metric": CS_METRIC, "value": v, "unit": CS_UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "config": {"workload": CS_WORKLOAD, "queries_per_step": n},
+        "cpu_baseline": {"value": v, "unit": CS_UNIT, "cores": 1, "kind": "port",
+                         "sample": f"all {n} queries per step, oracle, 1 core"},
+        "e2e": {"value": v, "unit": CS_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
 
 
 def cpu_baseline_sample(args) -> dict | None:
@@ -322,20 +469,23 @@ def main() -> int:
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "contact-search"],
+                    help="c2: replicas of the 100k-monomer box (headline); contact-search: batched queries")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank != 0:
             return 0
-        print(json.dumps(run_reference(args)))
+        ref = run_contact_search_reference if args.workload == "contact-search" else run_reference
+        print(json.dumps(ref(args)))
         return 0
     if world > 1:
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    out = run_ours(args, rank, world)
+    out = (run_contact_search if args.workload == "contact-search" else run_ours)(args, rank, world)
     if out is not None:
         print(json.dumps(out))
     if world > 1:

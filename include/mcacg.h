@@ -185,6 +185,17 @@ int mcacg_params_from_ini_text(const char *text, mcacg_params *params);
  * without overlap, computes every aggregate field and applies
  * enforce_volume_fraction. Bit-identical with the reference. */
 int mcacg_state_init_random(const mcacg_params *params, mcacg_state *state);
+/* A seeded synthetic snapshot for contact-search benchmarks (no counterpart
+ * in the reference, which has no state generator): params->n_monomeres
+ * spheres, diameters drawn like initialisation_mode=lognormal from
+ * mean_diameter and dispersion_diameter, grouped into n_aggregates
+ * aggregates of 1..max_size spheres (log-normal sizes, mean
+ * n_monomeres/n_aggregates) grown by ballistic sticking, placed without
+ * overlap in a periodic cube sized so that the spheres fill
+ * params->volume_fraction. Aggregate fields follow Aggregate::update
+ * (aggregat.cpp:284-288). Caller-owned arrays sized for n_monomeres spheres
+ * and n_aggregates aggregates. Deterministic in random_seed. */
+int mcacg_state_synthetic(const mcacg_params *params, int32_t n_aggregates, int32_t max_size, mcacg_state *state);
 
 /* ---- boxes ---- */
 /* AggregatList::AggregatList (aggregats/aggregat_list_storage.cpp:52-88):
@@ -216,6 +227,14 @@ int mcacg_box_set_time(mcacg_box *box, double time);
  * along the unit vector 'direction' for at most 'distance'. */
 int mcacg_distance_to_next_contact(mcacg_box *box, int64_t source, const double direction[3], double distance,
                                    mcacg_contact *out);
+/* n independent AggregatList::distance_to_next_contact queries on the
+ * current state, run concurrently on the GPU (one thread block per query):
+ * sources[k], directions[3k..3k+2], distances[k] -> out[k]. Nothing is
+ * moved; each result is that of mcacg_distance_to_next_contact on the same
+ * state. kernel_ms (may be NULL) receives the kernel's GPU time. No
+ * counterpart in the reference, which answers one query at a time. */
+int mcacg_distance_to_next_contacts(mcacg_box *box, int32_t n, const int64_t *sources, const double *directions,
+                                    const double *distances, mcacg_contact *out, double *kernel_ms);
 /* Aggregate::translate (aggregat.hpp:108, aggregat.cpp:148-161). */
 int mcacg_translate(mcacg_box *box, int64_t label, const double vector[3]);
 /* Aggregate::time_forward (aggregat.cpp:106-108). */

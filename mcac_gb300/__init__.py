@@ -4,6 +4,6 @@ The native library (``_build/libmcacg.so``, C-ABI in include/mcacg.h) holds
 the CUDA kernels for sm_103a and the C++ host layer; this package binds it
 with ctypes and mirrors the reference's C++ interface (see ``api``).
 """
-from .api import (AggregateContactInfo, AggregatList, Batch, PhysicalModel, Server, calcul, device_count,  # noqa: F401
-                  init_state, run_device)
+from .api import (CONTACT_DTYPE, AggregateContactInfo, AggregatList, Batch, PhysicalModel, Server,  # noqa: F401
+                  calcul, device_count, init_state, run_device, synthetic_state)
 from .snapshot import Snapshot  # noqa: F401

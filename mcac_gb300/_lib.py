@@ -80,6 +80,7 @@ SIGNATURES = {
     "mcacg_params_from_ini": [C.c_char_p, C.POINTER(Params)],
     "mcacg_params_from_ini_text": [C.c_char_p, C.POINTER(Params)],
     "mcacg_state_init_random": [C.POINTER(Params), C.POINTER(State)],
+    "mcacg_state_synthetic": [C.POINTER(Params), i32, i32, C.POINTER(State)],
     "mcacg_box_create": [C.POINTER(Params), C.POINTER(vp)],
     "mcacg_box_create_from_state": [C.POINTER(Params), C.POINTER(State), C.POINTER(vp)],
     "mcacg_box_destroy": [vp],
@@ -91,6 +92,8 @@ SIGNATURES = {
     "mcacg_box_set_profiling": [vp, C.c_int],
     "mcacg_box_take_profile": [vp, C.POINTER(Profile)],
     "mcacg_distance_to_next_contact": [vp, i64, C.POINTER(f64), f64, C.POINTER(Contact)],
+    "mcacg_distance_to_next_contacts": [vp, i32, C.POINTER(i64), C.POINTER(f64), C.POINTER(f64),
+                                        C.POINTER(Contact), C.POINTER(f64)],
     "mcacg_translate": [vp, i64, C.POINTER(f64)],
     "mcacg_time_forward": [vp, i64, f64],
     "mcacg_merge": [vp, C.POINTER(Contact), C.POINTER(i32)],

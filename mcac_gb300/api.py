@@ -93,6 +93,22 @@ def init_state(model: PhysicalModel) -> StateBuffers:
     return sb
 
 
+def synthetic_state(model: PhysicalModel, n_aggregates: int, max_size: int) -> StateBuffers:
+    """A seeded synthetic snapshot of ballistic aggregates (host, no GPU):
+    model.n_monomeres spheres in n_aggregates aggregates of 1..max_size
+    spheres, in a periodic cube sized for model.volume_fraction."""
+    n = int(model.params.n_monomeres)
+    sb = StateBuffers(n, int(n_aggregates))
+    check(lib().mcacg_state_synthetic(C.byref(model.params), int(n_aggregates), int(max_size),
+                                      C.byref(sb.state)))
+    return sb
+
+
+# one mcacg_contact per row
+CONTACT_DTYPE = np.dtype([("distance", np.float64), ("moving_sphere", np.int64), ("other_sphere", np.int64),
+                          ("moving_aggregate", np.int64), ("other_aggregate", np.int64)])
+
+
 @dataclass
 class AggregateContactInfo:
     """include/tools/contact_info.hpp:73-85 with indices for the weak pointers."""
@@ -200,6 +216,21 @@ class AggregatList:
                                                     C.byref(c)))
         return AggregateContactInfo(c.distance, c.moving_sphere, c.other_sphere, c.moving_aggregate,
                                     c.other_aggregate)
+
+    def distance_to_next_contacts(self, sources, directions, distances) -> tuple[np.ndarray, float]:
+        """Many independent queries on the current state, run concurrently on
+        the GPU. Returns (CONTACT_DTYPE array, kernel milliseconds)."""
+        src = np.ascontiguousarray(sources, dtype=np.int64)
+        d = np.ascontiguousarray(directions, dtype=np.float64).reshape(len(src), 3)
+        dist = np.ascontiguousarray(distances, dtype=np.float64)
+        if dist.shape != src.shape:
+            raise ValueError("sources and distances differ in length")
+        out = np.zeros(len(src), dtype=CONTACT_DTYPE)
+        ms = C.c_double(0.0)
+        check(lib().mcacg_distance_to_next_contacts(self._box, len(src), ptr(src, C.c_int64), ptr(d, C.c_double),
+                                                     ptr(dist, C.c_double),
+                                                     out.ctypes.data_as(C.POINTER(Contact)), C.byref(ms)))
+        return out, ms.value
 
     def translate(self, label: int, vector) -> None:
         v = np.ascontiguousarray(vector, dtype=np.float64)

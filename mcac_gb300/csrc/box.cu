@@ -20,6 +20,52 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(DevBox b, int src, doub
     if (threadIdx.x == 0) *out = sm.out;
 }
 
+// Many independent contact queries on one unchanged box. Each block takes
+// the next query from a shared counter (queries differ widely in cost) and
+// runs it with its own slice of the candidate and survivor scratch; the box
+// state is only read.
+struct QueryIn {
+    double dx, dy, dz, dist;
+    int slot, pad;
+};
+struct BatchScratch {
+    int *next;      // query counter, zero at launch
+    size_t stride;  // candidate entries per block (nslots + 1)
+    int surv_cap;   // HBM survivors per block
+    double *cand_db;
+    int *cand_flat, *cand_slot, *cand_order, *cand_prefix;
+    unsigned long long *best_res, *best_ij;
+    int4 *surv;
+    double *surv_res;
+};
+__global__ void __launch_bounds__(kQueryThreads) k_query_batch(DevBox b, BatchScratch s, int n, const QueryIn *in,
+                                                               QueryOut *out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    QuerySmem &sm = *reinterpret_cast<QuerySmem *>(smem_raw);
+    __shared__ int q_cur;
+    const size_t c0 = size_t(blockIdx.x) * s.stride;
+    b.cand_db = s.cand_db + c0;
+    b.cand_flat = s.cand_flat + c0;
+    b.cand_slot = s.cand_slot + c0;
+    b.cand_order = s.cand_order + c0;
+    b.cand_prefix = s.cand_prefix + c0;
+    b.best_res = s.best_res + c0;
+    b.best_ij = s.best_ij + c0;
+    b.surv = s.surv + size_t(blockIdx.x) * size_t(s.surv_cap);
+    b.surv_res = s.surv_res + size_t(blockIdx.x) * size_t(s.surv_cap);
+    b.surv_cap = s.surv_cap;
+    for (;;) {
+        if (threadIdx.x == 0) q_cur = atomicAdd(s.next, 1);
+        __syncthreads();
+        const int q = q_cur;
+        if (q >= n) break;  // block-uniform
+        const QueryIn qi = in[q];
+        block_query(b, qi.slot, Vec3{qi.dx, qi.dy, qi.dz}, qi.dist, sm);
+        if (threadIdx.x == 0) out[q] = sm.out;
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(kQueryThreads) k_translate(DevBox b, int slot, double vx, double vy, double vz) {
     __shared__ double refpos[3];
     block_translate(b, slot, Vec3{vx, vy, vz}, refpos);
@@ -296,6 +342,7 @@ DeviceBox::~DeviceBox() {
     for (void *e : ev_)
         if (e) cudaEventDestroy(static_cast<cudaEvent_t>(e));
     for (void *p : allocations_) cudaFree(p);
+    if (batch_mem_) cudaFree(batch_mem_);
     if (host_out_) cudaFreeHost(host_out_);
     if (own_stream_ && stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
     delete static_cast<DevBox *>(devbox_);
@@ -401,6 +448,129 @@ int DeviceBox::query(int src_slot, const double dir[3], double dist, QueryResult
     out->n_pairs_refined = q.n_pairs_refined;
     if (q.status != ST_OK && err) *err = "contact query failed with status " + std::to_string(q.status);
     return q.status;
+}
+
+int DeviceBox::query_batch(int n, const int *slots, const double *dirs, const double *dists, QueryResult *out,
+                           double *kernel_ms, std::string *err) {
+    if (kernel_ms) *kernel_ms = 0.0;
+    if (n <= 0) return ST_OK;
+    for (int k = 0; k < n; ++k)
+        if (slots[k] < 0 || slots[k] >= nslots_) {
+            if (err) *err = "query slot out of range";
+            return ST_BAD_ARGUMENT;
+        }
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    int dev = 0, n_sm = 0, per_sm = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), err, "cudaGetDevice")) return ST_CUDA;
+    if (!cuda_ok(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), err, "device attribute"))
+        return ST_CUDA;
+    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_query_batch, kQueryThreads,
+                                                               sizeof(QuerySmem)),
+                 err, "occupancy"))
+        return ST_CUDA;
+    const int blocks = std::max(1, std::min(n, std::max(1, per_sm) * std::max(1, n_sm)));
+
+    // scratch layout: counter, inputs, outputs, then per-block candidate and
+    // survivor slices
+    BatchScratch sc{};
+    sc.stride = size_t(nslots_) + 1;
+    sc.surv_cap = 1 << 14;
+    const size_t nb = size_t(blocks), ncand = nb * sc.stride, nsurv = nb * size_t(sc.surv_cap);
+    size_t off = 0;
+    auto carve = [&](size_t bytes) {
+        size_t at = off;
+        off += (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
+        return at;
+    };
+    const size_t o_next = carve(sizeof(int)), o_in = carve(sizeof(QueryIn) * size_t(n)),
+                 o_out = carve(sizeof(QueryOut) * size_t(n)), o_db = carve(8 * ncand), o_flat = carve(4 * ncand),
+                 o_slot = carve(4 * ncand), o_order = carve(4 * ncand), o_prefix = carve(4 * ncand),
+                 o_res = carve(8 * ncand), o_ij = carve(8 * ncand), o_surv = carve(sizeof(int4) * nsurv),
+                 o_sres = carve(8 * nsurv);
+    if (off > batch_bytes_) {
+        if (batch_mem_) {
+            cudaStreamSynchronize(s);
+            cudaFree(batch_mem_);
+            batch_mem_ = nullptr;
+            batch_bytes_ = 0;
+        }
+        if (!cuda_ok(cudaMalloc(&batch_mem_, off), err, "cudaMalloc (query batch)")) return ST_CUDA;
+        batch_bytes_ = off;
+    }
+    char *base = static_cast<char *>(batch_mem_);
+    sc.next = reinterpret_cast<int *>(base + o_next);
+    sc.cand_db = reinterpret_cast<double *>(base + o_db);
+    sc.cand_flat = reinterpret_cast<int *>(base + o_flat);
+    sc.cand_slot = reinterpret_cast<int *>(base + o_slot);
+    sc.cand_order = reinterpret_cast<int *>(base + o_order);
+    sc.cand_prefix = reinterpret_cast<int *>(base + o_prefix);
+    sc.best_res = reinterpret_cast<unsigned long long *>(base + o_res);
+    sc.best_ij = reinterpret_cast<unsigned long long *>(base + o_ij);
+    sc.surv = reinterpret_cast<int4 *>(base + o_surv);
+    sc.surv_res = reinterpret_cast<double *>(base + o_sres);
+    QueryIn *d_in = reinterpret_cast<QueryIn *>(base + o_in);
+    QueryOut *d_out = reinterpret_cast<QueryOut *>(base + o_out);
+
+    std::vector<QueryIn> hin(static_cast<size_t>(n));
+    for (int k = 0; k < n; ++k)
+        hin[size_t(k)] = QueryIn{dirs[3 * k], dirs[3 * k + 1], dirs[3 * k + 2], dists[k], slots[k], 0};
+    std::vector<QueryOut> hout(static_cast<size_t>(n));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!cuda_ok(cudaEventCreate(&e0), err, "cudaEventCreate")) return ST_CUDA;
+    if (!cuda_ok(cudaEventCreate(&e1), err, "cudaEventCreate")) {
+        cudaEventDestroy(e0);
+        return ST_CUDA;
+    }
+    bool ok = cuda_ok(cudaMemcpyAsync(d_in, hin.data(), sizeof(QueryIn) * size_t(n), cudaMemcpyHostToDevice, s), err,
+                      "query upload") &&
+              cuda_ok(cudaMemsetAsync(sc.next, 0, sizeof(int), s), err, "query counter");
+    if (ok) {
+        cudaEventRecord(e0, s);
+        k_query_batch<<<blocks, kQueryThreads, sizeof(QuerySmem), s>>>(b, sc, n, d_in, d_out);
+        cudaEventRecord(e1, s);
+        ok = cuda_ok(cudaGetLastError(), err, "k_query_batch") &&
+             cuda_ok(cudaMemcpyAsync(hout.data(), d_out, sizeof(QueryOut) * size_t(n), cudaMemcpyDeviceToHost, s),
+                     err, "query download") &&
+             cuda_ok(cudaStreamSynchronize(s), err, "k_query_batch");
+    }
+    float ms = 0.f;
+    if (ok) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!ok) return ST_CUDA;
+    if (kernel_ms) *kernel_ms = double(ms);
+    int status = ST_OK;
+    for (int k = 0; k < n; ++k) {
+        const QueryOut &q = hout[size_t(k)];
+        QueryResult &r = out[k];
+        r.distance = q.distance;
+        r.moving_sphere = q.moving_sphere;
+        r.other_sphere = q.other_sphere;
+        r.other_slot = q.other_slot;
+        r.status = q.status;
+        r.n_candidates = q.n_candidates;
+        r.n_pairs_refined = q.n_pairs_refined;
+        r.n_scanned = q.n_scanned;
+        r.n_cells = q.n_cells;
+        r.n_cand_spheres = q.n_cand_spheres;
+        r.n_mov = q.n_mov;
+        if (q.status != ST_OK && status == ST_OK) {
+            status = q.status;
+            if (err) *err = "contact query " + std::to_string(k) + " failed with status " + std::to_string(q.status);
+        }
+        if (profiling_) {
+            prof_.queries += 1;
+            prof_.mov_spheres += q.n_mov;
+            prof_.scanned += q.n_scanned;
+            prof_.cells += q.n_cells;
+            prof_.candidates += q.n_candidates;
+            prof_.cand_spheres += q.n_cand_spheres;
+            prof_.refined += q.n_pairs_refined;
+        }
+    }
+    if (profiling_) prof_.query_ms += double(ms);
+    return status;
 }
 
 int DeviceBox::translate(int slot, const double v[3], std::string *err) {

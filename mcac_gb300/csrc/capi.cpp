@@ -175,6 +175,22 @@ int mcacg_state_init_random(const mcacg_params *params, mcacg_state *state) {
     });
 }
 
+int mcacg_state_synthetic(const mcacg_params *params, int32_t n_aggregates, int32_t max_size, mcacg_state *state) {
+    return guarded([&] {
+        if (!params || !state || !state->spheres || !state->sphere_label || !state->aggregates ||
+            !state->n_spheres_per_aggregate || !state->members)
+            return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        if (params->n_monomeres > INT32_MAX) return fail(MCACG_ERR_BAD_ARGUMENT, "too many spheres");
+        if (state->n_spheres < params->n_monomeres || state->n_aggregates < n_aggregates)
+            return fail(MCACG_ERR_BAD_ARGUMENT, "state buffers too small");
+        mcacg::HostState st;
+        std::string err;
+        int rc = mcacg::make_synthetic_state(*params, n_aggregates, max_size, &st, &err);
+        if (rc != 0) return finish(rc, err);
+        return finish(store_host_state(st, state, &err), err);
+    });
+}
+
 int mcacg_box_create(const mcacg_params *params, mcacg_box **box) {
     return guarded([&] {
         if (!params || !box) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
@@ -283,6 +299,17 @@ int mcacg_distance_to_next_contact(mcacg_box *box, int64_t source, const double 
         if (!box || !direction || !out) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
         std::string err;
         return finish(box->impl->distance_to_next_contact(source, direction, distance, out, &err), err);
+    });
+}
+
+int mcacg_distance_to_next_contacts(mcacg_box *box, int32_t n, const int64_t *sources, const double *directions,
+                                    const double *distances, mcacg_contact *out, double *kernel_ms) {
+    return guarded([&] {
+        if (!box || n < 0 || (n > 0 && (!sources || !directions || !distances || !out)))
+            return fail(MCACG_ERR_BAD_ARGUMENT, "null argument or negative count");
+        std::string err;
+        return finish(box->impl->distance_to_next_contacts(n, sources, directions, distances, out, kernel_ms, &err),
+                      err);
     });
 }
 

@@ -61,6 +61,12 @@ class DeviceBox {
     int set_stream(void *stream);
     void *stream() const { return stream_; }
     int query(int src_slot, const double dir[3], double dist, QueryResult *out, std::string *err);
+    // n independent queries on the current state (nothing is moved): slots[k],
+    // dirs[3k..3k+2], dists[k] -> out[k]. The queries run concurrently, one
+    // per thread block. Returns the first failing status, or ST_OK;
+    // *kernel_ms (may be null) gets the kernel's CUDA-event time.
+    int query_batch(int n, const int *slots, const double *dirs, const double *dists, QueryResult *out,
+                    double *kernel_ms, std::string *err);
     int translate(int slot, const double v[3], std::string *err);
     int merge(int ms, int os, int mslot, int oslot, MergeResult *out, std::string *err);
     // Writes aggregate fields of one slot: fields[f] for every f with bit f of mask set.
@@ -90,6 +96,8 @@ class DeviceBox {
     void *dev_out_ = nullptr;
     bool profiling_ = false;
     void *ev_[2] = {nullptr, nullptr};
+    void *batch_mem_ = nullptr;  // query_batch scratch, grown on demand
+    size_t batch_bytes_ = 0;
     Profile prof_;
 };
 

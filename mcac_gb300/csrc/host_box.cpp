@@ -415,6 +415,40 @@ int HostBox::distance_to_next_contact(int64_t label, const double dir[3], double
     return ST_OK;
 }
 
+int HostBox::distance_to_next_contacts(int n, const int64_t *labels, const double *dirs, const double *distances,
+                                       mcacg_contact *out, double *kernel_ms, std::string *err) {
+    if (n < 0) {
+        if (err) *err = "negative query count";
+        return ST_BAD_ARGUMENT;
+    }
+    std::vector<int> slots(static_cast<size_t>(n));
+    for (int k = 0; k < n; ++k) {
+        if (labels[k] < 0 || labels[k] >= int64_t(alive_.size())) {
+            if (err) *err = "label out of range in query " + std::to_string(k);
+            return ST_BAD_ARGUMENT;
+        }
+        slots[size_t(k)] = alive_[size_t(labels[k])];
+    }
+    std::vector<QueryResult> q(static_cast<size_t>(n));
+    int rc = dev_->query_batch(n, slots.data(), dirs, distances, q.data(), kernel_ms, err);
+    for (int k = 0; k < n; ++k) {
+        const QueryResult &r = q[size_t(k)];
+        mcacg_contact &c = out[k];
+        c.distance = r.distance;
+        c.moving_sphere = -1;
+        c.other_sphere = -1;
+        c.moving_aggregate = -1;
+        c.other_aggregate = -1;
+        if (rc == ST_OK && r.moving_sphere >= 0) {
+            c.moving_sphere = r.moving_sphere;
+            c.other_sphere = r.other_sphere;
+            c.moving_aggregate = labels[k];
+            c.other_aggregate = label_of(r.other_slot);
+        }
+    }
+    return rc;
+}
+
 int HostBox::translate(int64_t label, const double v[3], std::string *err) {
     if (label < 0 || label >= int64_t(alive_.size())) {
         if (err) *err = "label out of range";
@@ -522,46 +556,58 @@ void HostBox::sort_time_steps(double factor) {
     //
     // factor/time_step is non-increasing in time_step (correctly rounded
     // division is monotone), so the aggregates ordered by decreasing time
-    // step are in non-decreasing weight order. When every weight in that
-    // order is strictly greater than the previous one, that order is the only
-    // sorted order, so it is exactly what std::sort returns; the order is kept
-    // up to date at every merge instead of re-sorting. Any tie (identical
-    // monomers, or two time steps rounding to one weight) takes the full
-    // std::sort path, whose element order among ties is the reference's.
+    // step are in non-decreasing weight order; that order is kept up to date
+    // at every merge instead of re-sorting. Every sorted order has the same
+    // sequence of weights, hence the same cumulative sums, bit for bit: the
+    // orders differ only in which label sits at each position of a run of
+    // equal weights. So the cumulative sums come from the kept order, and the
+    // reference's own order (std::sort's placement of equal keys) is only
+    // needed when a pick lands inside such a run (pick_random); it is then
+    // computed from the weights as they were at this call.
     const size_t n = alive_.size();
     if (!dt_order_valid_ || by_dt_.size() != n) build_dt_order();
     if (slot_label_.size() != size_t(nslots_)) slot_label_.assign(size_t(nslots_), -1);
     for (size_t l = 0; l < n; ++l) slot_label_[size_t(alive_[l])] = int(l);
     index_sorted_.resize(n);
     cumulative_.resize(n);
-    bool strict = true;
+    weights_.resize(n);
+    tp_by_label_.resize(n);
+    ties_ = false;
+    ref_order_valid_ = false;
     double prev = -std::numeric_limits<double>::infinity();
     for (size_t k = 0; k < n; ++k) {
         const int slot = by_dt_[k].second;
         const double tp = factor / F(AGG_TIME_STEP, slot);
-        if (!(tp > prev)) {
-            strict = false;
-            break;
-        }
+        ties_ = ties_ || !(tp > prev);
         prev = tp;
-        index_sorted_[k] = size_t(slot_label_[size_t(slot)]);
+        const int label = slot_label_[size_t(slot)];
+        index_sorted_[k] = size_t(label);
+        weights_[k] = tp;
+        tp_by_label_[size_t(label)] = tp;
         cumulative_[k] = (k == 0) ? tp : cumulative_[k - 1] + tp;
     }
-    if (strict) return;
-    std::vector<double> tp(n);
-    for (size_t i = 0; i < n; i++) tp[i] = factor / F(AGG_TIME_STEP, alive_[i]);
-    index_sorted_.resize(n);
-    std::iota(index_sorted_.begin(), index_sorted_.end(), 0);
-    std::sort(index_sorted_.begin(), index_sorted_.end(), [&tp](size_t a, size_t b) { return tp[a] < tp[b]; });
-    cumulative_.resize(n);
-    cumulative_[0] = tp[index_sorted_[0]];
-    for (size_t i = 1; i < n; i++) cumulative_[i] = cumulative_[i - 1] + tp[index_sorted_[i]];
+}
+
+void HostBox::reference_sort_order() {
+    // aggregat_list.cpp:109-123: indices 0..n-1 sorted by weight with std::sort
+    const size_t n = tp_by_label_.size();
+    index_ref_.resize(n);
+    std::iota(index_ref_.begin(), index_ref_.end(), size_t(0));
+    const std::vector<double> &tp = tp_by_label_;
+    std::sort(index_ref_.begin(), index_ref_.end(), [&tp](size_t a, size_t b) { return tp[a] < tp[b]; });
+    ref_order_valid_ = true;
 }
 
 int64_t HostBox::pick_random() {
+    // aggregat_list.cpp:59-66
     double val = random_uniform() * cumulative_[alive_.size() - 1];
-    long n = std::lower_bound(cumulative_.begin(), cumulative_.end(), val) - cumulative_.begin();
-    return int64_t(index_sorted_[size_t(n)]);
+    size_t k = size_t(std::lower_bound(cumulative_.begin(), cumulative_.end(), val) - cumulative_.begin());
+    if (k >= cumulative_.size()) k = cumulative_.size() - 1;  // unreachable for finite weights
+    const bool in_run = ties_ && ((k > 0 && weights_[k - 1] == weights_[k]) ||
+                                  (k + 1 < weights_.size() && weights_[k + 1] == weights_[k]));
+    if (!in_run) return int64_t(index_sorted_[k]);
+    if (!ref_order_valid_) reference_sort_order();
+    return int64_t(index_ref_[k]);
 }
 
 void HostBox::refresh() {

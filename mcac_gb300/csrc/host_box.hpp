@@ -35,12 +35,16 @@ class HostBox {
     // per-step interface
     int distance_to_next_contact(int64_t label, const double dir[3], double distance, mcacg_contact *out,
                                  std::string *err);
+    // n independent queries on the current state, run concurrently on the
+    // device; *kernel_ms (may be null) gets the kernel time.
+    int distance_to_next_contacts(int n, const int64_t *labels, const double *dirs, const double *distances,
+                                  mcacg_contact *out, double *kernel_ms, std::string *err);
     int translate(int64_t label, const double v[3], std::string *err);
     int time_forward(int64_t label, double dt, std::string *err);
     int merge(const mcacg_contact &c, int32_t *merged, std::string *err);
     void sort_time_steps(double factor);
     int64_t pick_random();
-    double get_time_step(double max) const { return max / cumulative_.back(); }
+    double get_time_step(double max) const { return max / cumulative_[alive_.size() - 1]; }
     double max_time_step() const { return max_time_step_; }
     double avg_npp() const { return avg_npp_; }
     void refresh();
@@ -89,6 +93,11 @@ class HostBox {
     double max_time_step_ = 0, avg_npp_ = 1;
     std::vector<size_t> index_sorted_;
     std::vector<double> cumulative_;
+    std::vector<double> weights_;      // weights in sorted order
+    std::vector<double> tp_by_label_;  // weights by label at the last sort
+    std::vector<size_t> index_ref_;    // the reference's std::sort order, on demand
+    bool ties_ = false, ref_order_valid_ = false;
+    void reference_sort_order();
     // live slots ordered by decreasing time step (kept across merges)
     std::vector<std::pair<double, int>> by_dt_;
     bool dt_order_valid_ = false;
@@ -117,5 +126,13 @@ int state_to_host(const mcacg_state &in, HostState *out, std::string *err);
 // position-independent proper time and charge, and raises 'maxradius'.
 int host_update_aggregate(const mcacg_params &p, const HostState &st, const std::vector<int> &members,
                           double fields[21], double *maxradius);
+
+// A seeded synthetic snapshot for the contact-search benchmark:
+// p.n_monomeres spheres (diameters drawn like initialisation_mode=lognormal)
+// in n_aggregates aggregates of 1..max_size spheres grown by ballistic
+// sticking, placed without overlap in a periodic cube whose length makes the
+// sphere volume fraction p.volume_fraction. Deterministic for a given
+// p.random_seed (workloads.cpp).
+int make_synthetic_state(const mcacg_params &p, int n_aggregates, int max_size, HostState *st, std::string *err);
 
 }  // namespace mcacg

@@ -67,3 +67,56 @@ def test_monodisperse_run_matches_oracle():
            "initialisation_mode = lognormal\n[environment]\nvolume_fraction = 3e-3\ntemperature = 1800\n"
            "[limits]\nnumber_of_aggregates = 20\n[numerics]\nrandom_seed = 1005\nwith_domain_duplication = false\n")
     compare_runs(ini)
+
+
+@pytest.mark.gpu
+def test_partly_tied_weights_run_matches_oracle():
+    """Distinct weights with a few runs of equal ones: the pick order comes
+    from the kept time-step order, and from std::sort's order of equal keys
+    only when a pick lands inside a run. Forty monomers are given the radius
+    (and so every aggregate field but the position) of monomer 0."""
+    import ctypes
+
+    from mcac_gb300 import init_state
+    from mcac_gb300.snapshot import A, S
+    ini = ("[monomers]\nnumber = 1500\nmean_diameter = 30\ndispersion_diameter = 1.25\n"
+           "initialisation_mode = normal\n[environment]\nvolume_fraction = 2e-3\ntemperature = 1700\n"
+           "[limits]\nnumber_of_aggregates = 200\n[numerics]\nrandom_seed = 77\nwith_domain_duplication = false\n")
+    pm = PhysicalModel(text=ini)
+    snap = init_state(pm).to_snapshot()
+    L = snap.box_length
+    pos = snap.spheres[[S["x"], S["y"], S["z"]]].T
+    r = snap.spheres[S["r"]]
+    keep_pos = [A["x"], A["y"], A["z"], A["rx"], A["ry"], A["rz"], A["time"]]
+    chosen = []
+    for m in range(1, len(r)):
+        d = pos - pos[m]
+        d -= L * np.floor(d / L + 0.5)
+        dist = np.sqrt((d ** 2).sum(1))
+        dist[m] = np.inf
+        if np.all(dist - (r + r[0]) > 1e-8):  # room for the new radius
+            chosen.append(m)
+        if len(chosen) == 40:
+            break
+    for m in chosen:
+        s = snap.members[snap.member_offsets()[m]]
+        for f in ("r", "volume", "surface"):
+            snap.spheres[S[f], s] = snap.spheres[S[f], 0]
+        for f in range(21):
+            if f not in keep_pos:
+                snap.aggregates[f, m] = snap.aggregates[f, 0]
+    libc = ctypes.CDLL(None)
+    libc.srand(77)
+    ob = O.OracleBox(ini, snap)
+    ost, otr = ob.calcul(max_steps=30000, trace=True, trace_capacity=30000)
+    libc.srand(77)
+    with AggregatList(pm, snap) as box:
+        st, tr = box.calcul(max_steps=30000, trace=True, trace_capacity=30000)
+        assert (st.steps, st.events) == (ost.steps, ost.events)
+        for f in FIELDS:
+            np.testing.assert_array_equal(tr[f], otr[f], err_msg=f)
+        for f in DFIELDS:
+            np.testing.assert_array_equal(tr[f].view(np.int64), otr[f].view(np.int64), err_msg=f)
+        assert digest(box.store()) == digest(ob.store())
+    assert len(chosen) == 40
+    assert st.events > 100

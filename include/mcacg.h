@@ -235,6 +235,22 @@ int mcacg_distance_to_next_contact(mcacg_box *box, int64_t source, const double 
  * counterpart in the reference, which answers one query at a time. */
 int mcacg_distance_to_next_contacts(mcacg_box *box, int32_t n, const int64_t *sources, const double *directions,
                                     const double *distances, mcacg_contact *out, double *kernel_ms);
+/* The queries of mcacg_distance_to_next_contacts with no device memory
+ * allocated: for callers that cannot allocate while they run (a loop that
+ * gave the device to its own memory pool, one that must not take the
+ * device-wide synchronisation of cudaMalloc/cudaFree, one under a fixed
+ * memory budget). All device scratch is one 32 MiB __device__ array of the
+ * library. At most 65536 queries per call (MCACG_ERR_CAPACITY beyond); a box
+ * whose per-block candidate lists (40 bytes per aggregate slot) do not fit
+ * it is refused with MCACG_ERR_CAPACITY. The first call on each device, with
+ * that device current, looks the array up (cudaGetSymbolAddress); make it
+ * before any stream capture begins. Each call zeroes its query counter and
+ * status word, copies the queries in, runs on the box's stream and waits for
+ * it. The array is shared by all boxes on a device: overlapping calls would
+ * race on it, so the library serialises them with a lock. No counterpart in
+ * the reference. */
+int mcacg_distance_to_next_contacts_static(mcacg_box *box, int32_t n, const int64_t *sources,
+                                           const double *directions, const double *distances, mcacg_contact *out);
 /* Aggregate::translate (aggregat.hpp:108, aggregat.cpp:148-161). */
 int mcacg_translate(mcacg_box *box, int64_t label, const double vector[3]);
 /* Aggregate::time_forward (aggregat.cpp:106-108). */

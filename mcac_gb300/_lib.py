@@ -94,6 +94,8 @@ SIGNATURES = {
     "mcacg_distance_to_next_contact": [vp, i64, C.POINTER(f64), f64, C.POINTER(Contact)],
     "mcacg_distance_to_next_contacts": [vp, i32, C.POINTER(i64), C.POINTER(f64), C.POINTER(f64),
                                         C.POINTER(Contact), C.POINTER(f64)],
+    "mcacg_distance_to_next_contacts_static": [vp, i32, C.POINTER(i64), C.POINTER(f64), C.POINTER(f64),
+                                               C.POINTER(Contact)],
     "mcacg_translate": [vp, i64, C.POINTER(f64)],
     "mcacg_time_forward": [vp, i64, f64],
     "mcacg_merge": [vp, C.POINTER(Contact), C.POINTER(i32)],

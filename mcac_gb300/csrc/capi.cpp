@@ -19,6 +19,7 @@
 #include "batch.hpp"
 #include "host_box.hpp"
 #include "physics.hpp"
+#include "static_query.hpp"
 
 struct mcacg_box {
     std::unique_ptr<mcacg::HostBox> impl;
@@ -309,6 +310,18 @@ int mcacg_distance_to_next_contacts(mcacg_box *box, int32_t n, const int64_t *so
             return fail(MCACG_ERR_BAD_ARGUMENT, "null argument or negative count");
         std::string err;
         return finish(box->impl->distance_to_next_contacts(n, sources, directions, distances, out, kernel_ms, &err),
+                      err);
+    });
+}
+
+int mcacg_distance_to_next_contacts_static(mcacg_box *box, int32_t n, const int64_t *sources,
+                                           const double *directions, const double *distances, mcacg_contact *out) {
+    return guarded([&] {
+        if (!box || n < 0 || (n > 0 && (!sources || !directions || !distances || !out)))
+            return fail(MCACG_ERR_BAD_ARGUMENT, "null argument or negative count");
+        std::string err;
+        return finish(mcacg::query_batch_static(box->impl->device(), box->impl->size(), n, sources, directions,
+                                                distances, out, &err),
                       err);
     });
 }

@@ -9,12 +9,13 @@ loop; the metric is MC steps per second summed over replicas.
 
 Arms:
   --impl ours       (default) R independent replicas of the box (seeds 1..,
-                    skipping DEGENERATE_SEEDS; R = one per SM unless
-                    --replicas) advanced by the
+                    skipping DEGENERATE_SEEDS; R = the boxes the GPU keeps
+                    resident at once unless --replicas) advanced by the
                     device-resident loop, one thread block per box; value is
                     timed with CUDA events on the launching stream; e2e goes
                     through the C-ABI from host buffers: upload of the R
-                    states, the steps, download of the R states. The line
+                    states, --e2e-steps bench steps (statistics read back
+                    after each), download of the R states. The line
                     also reports the plain host-driven single-box path
                     (the bit-exact drop-in form) and a one-core CPU sample.
   --impl reference  the CPU restatement of the reference algorithm (oracle/)
@@ -27,7 +28,11 @@ exchange): value = total steps of all ranks / max time.
 --workload contact-search times the contact-search microbenchmark instead:
 10,000 queries on a 1,000,000-sphere synthetic snapshot per bench step, all
 in one batched launch (metric: contact queries/s; the reference arm is the
-oracle on one core).
+oracle on one core). --workload ensemble runs the 512-box ensemble to
+completion (or --cap-seconds) and reports boxes/hour, with the oracle's MC
+steps/s on one box per host core beside it. --workload serve feeds a seeded
+Poisson stream of runs to the continuous-batching server and reports p50/p99
+run latency (arrival to completion).
 """
 from __future__ import annotations
 
@@ -151,6 +156,13 @@ def query_bytes(prof: dict) -> float:
 DEGENERATE_SEEDS = frozenset({257})
 
 
+def phase_share(prof: dict) -> dict:
+    """Share of the device loop's SM cycles per phase of the MC step."""
+    keys = ("cycles_pick", "cycles_query", "cycles_move", "cycles_merge")
+    tot = sum(prof.get(k, 0) for k in keys)
+    return {k[7:]: (prof.get(k, 0) / tot if tot else None) for k in keys}
+
+
 def replica_seeds(n: int, first: int) -> list[int]:
     """n seeds from 'first' upwards, skipping the degenerate ones."""
     seeds, s = [], first
@@ -173,11 +185,15 @@ def replica_models(n: int, rank: int = 0):
     return models
 
 
-def host_states(models):
-    """The reference placement of every replica, on the host. Sequential: it
-    draws from the C library's single random stream."""
-    from mcac_gb300 import init_state
-    return [init_state(m) for m in models]
+def host_states(models, stream):
+    """The reference placement of every replica as host arrays: placed by a
+    batch (parallel host threads, each with its own copy of the C library
+    stream) and read back before any step."""
+    from mcac_gb300 import Batch
+    from mcac_gb300._lib import StateBuffers
+    with Batch(models, stream=stream) as b0:
+        snaps = b0.store_all()
+    return [StateBuffers.from_snapshot(sn) for sn in snaps]
 
 
 def plain_single_box(args, stream) -> dict:
@@ -207,15 +223,16 @@ def plain_single_box(args, stream) -> dict:
 def run_ours(args, rank: int, world: int) -> dict | None:
     import torch
 
-    from mcac_gb300 import Batch
+    from mcac_gb300 import Batch, resident_boxes
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
-    R = args.replicas or torch.cuda.get_device_properties(dev).multi_processor_count
+    R = args.replicas or resident_boxes(64)  # the most boxes one wave holds
     models = replica_models(R, rank)
     t0 = time.perf_counter()
     batch = Batch(models, stream=stream.cuda_stream)
+    batch.threads = args.threads
     setup_s = time.perf_counter() - t0
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     M = args.mc_steps
@@ -241,28 +258,36 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     torch.cuda.synchronize()
     clocks = sampler.stop()
     st = batch.stats()
+    threads_used = batch.threads
     steps_done = int(st["steps"].sum()) - steps0
     work1 = batch.work()
     prof = {k: work1[k] - work0[k] for k in work1}
     n_alive = st["n_aggregates"].tolist()
     batch.close()
     del flush
-    # end to end through the C-ABI from host buffers: upload R states, M steps
-    # per box, download R states
-    states = host_states(models)
-    h2d = sum(int(b.spheres.nbytes + b.sphere_label.nbytes + b.aggregates.nbytes + b.n_spheres.nbytes
-                  + b.members.nbytes) for b in states)
-    e2e_steps, e2e_s, d2h = 0, 0.0, 0
-    for _ in range(max(1, args.e2e_steps)):
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        with Batch(models, stream=stream.cuda_stream, states=states) as b2:
+    # end to end through the C-ABI from host buffers: the R host states are
+    # uploaded, advanced by K bench steps of M MC steps each (the per-box
+    # statistics read back after every bench step), and downloaded
+    states = host_states(models, stream.cuda_stream)
+    state_bytes = sum(int(b.spheres.nbytes + b.sphere_label.nbytes + b.aggregates.nbytes + b.n_spheres.nbytes
+                          + b.members.nbytes) for b in states)
+    K = max(1, args.e2e_steps)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    stats_bytes = 0
+    with Batch(models, stream=stream.cuda_stream, states=states) as b2:
+        b2.threads = threads_used
+        for _ in range(K):
             b2.run(max_steps=M, steps_per_launch=M)
-            outs = [b2.store(k) for k in range(R)]
-            e2e_steps += int(b2.stats()["steps"].sum())
-        e2e_s += time.perf_counter() - t
-        d2h = sum(int(o.spheres.nbytes + o.sphere_label.nbytes + o.aggregates.nbytes + o.n_spheres.nbytes
-                      + o.members.nbytes) for o in outs)
+            st2 = b2.stats()
+            stats_bytes += int(st2.nbytes)
+        e2e_steps = int(st2["steps"].sum())
+        outs = b2.store_all()
+    e2e_s = time.perf_counter() - t
+    out_bytes = sum(int(o.spheres.nbytes + o.sphere_label.nbytes + o.aggregates.nbytes + o.n_spheres.nbytes
+                        + o.members.nbytes) for o in outs)
+    h2d = state_bytes // K
+    d2h = (out_bytes + stats_bytes) // K
     times = torch.tensor([total_ms / 1000.0, float(steps_done), e2e_s, float(e2e_steps)], device="cuda",
                          dtype=torch.float64)
     if world > 1:
@@ -291,16 +316,20 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                    "path": "device-resident MC loop, one thread block per box, one launch per bench step",
                    "parallelism": f"{R} independent replicas per GPU x {world} GPU",
                    "l2": "flushed (256 MB write) between timed iterations", "setup_s": round(setup_s, 2),
+                   "threads_per_box": threads_used,
                    "aggregates_left": [min(n_alive), max(n_alive)]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None, "kernel": "k_run (batched MC loop)",
                      "bytes_per_launch": qbytes / max(1, launches), "us_per_launch": 1000.0 * total_ms / max(1, launches),
                      "bytes_model": "per contact query: 16 B x moving spheres + 36 B x aggregates scanned + 8 B x cells "
                                     "+ 16 B x candidate spheres + 64 B x FP64-refined pairs"},
-        "e2e": {"value": e2e_all / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_all / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "bench_steps": K, "note": "host states uploaded, K bench steps with per-box statistics read back "
+                                          "after each, final states downloaded; bytes are per bench step"},
         "gpu_launches": launches,
         "clocks": clocks,
         "work": prof,
+        "phase_share": phase_share(prof),
     }
     if not args.no_plain:
         out["plain_single_box"] = plain_single_box(args, stream)
@@ -437,6 +466,219 @@ def cpu_baseline_sample(args) -> dict | None:
     return oracle_py.bench_sample(C2_INI, seconds=args.cpu_seconds, processes=1)
 
 
+ENS_WORKLOAD = ("batched ensemble: 512 independent boxes, seed 1000+b, N ~ round(exp(U[ln 256, ln 16384])), "
+                "50/50 monodisperse 30 nm or LogNormal(30 nm, 1.25), volume fraction ~ U[100, 5000] ppm, "
+                "T ~ U[1500, 1900] K, stop at 1 aggregate or 10000 steps without an event")
+
+
+def ensemble_inis(n_boxes: int = 512, first_seed: int = 1000) -> list[str]:
+    """Parameter files of the ensemble (seeded with numpy's PCG64 per box)."""
+    import numpy as np
+    inis = []
+    for b in range(n_boxes):
+        rng = np.random.Generator(np.random.PCG64(first_seed + b))
+        n = int(round(np.exp(rng.uniform(np.log(256), np.log(16384)))))
+        disp = 1.0 if rng.random() < 0.5 else 1.25
+        fv = rng.uniform(100e-6, 5000e-6)
+        temp = rng.uniform(1500, 1900)
+        inis.append(f"[monomers]\nnumber = {n}\nmean_diameter = 30\ndispersion_diameter = {disp}\n"
+                    f"initialisation_mode = lognormal\ndensity = 1800\n[environment]\nvolume_fraction = {fv!r}\n"
+                    f"temperature = {temp!r}\npressure = 101300\nfractal_prefactor = 1.4\nfractal_dimension = 1.8\n"
+                    f"[limits]\nnumber_of_aggregates = 1\nn_iter_without_event = 10000\n"
+                    f"[numerics]\nrandom_seed = {first_seed + b}\nwith_domain_duplication = false\n")
+    return inis
+
+
+def run_ensemble(args, rank: int, world: int) -> dict | None:
+    """The 512-box ensemble to completion (or --cap-seconds): boxes/hour."""
+    import numpy as np
+    import torch
+
+    from mcac_gb300 import Batch, PhysicalModel
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    inis = ensemble_inis(args.boxes)[rank::world]  # boxes are sharded across ranks
+    models = [PhysicalModel(text=t) for t in inis]
+    t0 = time.perf_counter()
+    batch = Batch(models, stream=stream.cuda_stream)
+    batch.threads = args.threads
+    setup_s = time.perf_counter() - t0
+    done_at = np.full(len(models), np.nan)
+    sampler = ClockSampler(dev)
+    sampler.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    kernel_ms, launches = 0.0, 0
+    while True:
+        batch.run(max_steps=args.mc_steps, steps_per_launch=args.mc_steps)
+        ms, nl = batch.last_run()
+        kernel_ms += ms
+        launches += nl
+        st = batch.stats()
+        now = time.perf_counter() - t0
+        fin = (st["finished"] == 1) | (st["status"] != 0)
+        done_at[fin & np.isnan(done_at)] = now
+        if fin.all() or now > args.cap_seconds:
+            break
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    st = batch.stats()
+    steps = int(st["steps"].sum())
+    n_done = int(np.isfinite(done_at).sum())
+    failed = int((st["status"] != 0).sum())
+    work = batch.work()
+    threads_used = batch.threads
+    batch.close()
+    vals = torch.tensor([wall, float(steps), float(n_done), kernel_ms / 1000.0], device="cuda",
+                        dtype=torch.float64)
+    if world > 1:
+        import torch.distributed as dist
+        tmax, tsum = vals.clone(), vals.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        wall, steps, n_done = float(tmax[0]), int(tsum[1]), int(tsum[2])
+    if rank != 0:
+        return None
+    fin_times = np.sort(done_at[np.isfinite(done_at)])
+    res = {
+        "metric": "boxes/hour", "value": n_done / wall * 3600.0, "unit": "boxes/h", "n_gpus": world,
+        "steps": launches, "warmup": 0, "ms_per_step": 1000.0 * wall / max(1, launches),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": ENS_WORKLOAD, "boxes": args.boxes, "finished": n_done, "failed": failed,
+                   "wall_s": wall, "cap_s": args.cap_seconds, "setup_s": round(setup_s, 2),
+                   "mc_steps_per_launch": args.mc_steps, "threads_per_box": threads_used,
+                   "time_to_finish_s": {q: float(np.quantile(fin_times, p)) for q, p in
+                                        (("p50", 0.5), ("p90", 0.9), ("max", 1.0))} if len(fin_times) else None},
+        "mc_steps_per_s": steps / wall,
+        "kernel_s": kernel_ms / 1000.0,
+        "clocks": clocks,
+        "gpu_launches": launches,
+        "work": work,
+        "phase_share": phase_share(work),
+    }
+    if not args.no_cpu_baseline:
+        res["cpu_baseline"] = ensemble_cpu_sample(inis, args.cpu_seconds)
+    return res
+
+
+def _ens_worker(job):
+    ini, seconds = job
+    from oracle import oracle_py
+    box = oracle_py.OracleBox(ini)
+    steps, t0 = 0, time.perf_counter()
+    finished = False
+    while time.perf_counter() - t0 < seconds:
+        st, _ = box.calcul(max_steps=500)
+        steps += int(st.steps)
+        if st.finished:
+            finished = True
+            break
+    dt = time.perf_counter() - t0
+    box.close()
+    return steps, dt, finished
+
+
+def ensemble_cpu_sample(inis, seconds: float) -> dict:
+    """The oracle on all host cores: one box per core from the start of the
+    ensemble, each advanced for at most 'seconds'; MC steps/s summed."""
+    import multiprocessing as mp
+    procs = os.cpu_count() or 1
+    jobs = [(ini, seconds) for ini in inis[:procs]]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        res = pool.map(_ens_worker, jobs)
+    return {"value": sum(r[0] / r[1] for r in res), "unit": "MC steps/s", "cores": procs, "kind": "port",
+            "sample": f"the first {len(jobs)} boxes of the ensemble, one per core, up to {seconds:.0f} s each "
+                      f"({sum(r[2] for r in res)} finished in that time)"}
+
+
+SERVE_WORKLOAD = ("serving stream: seeded Poisson arrivals at --rate runs/s for --serve-seconds, "
+                  "N ~ round(exp(U[ln 500, ln --serve-nmax])), LogNormal(30 nm, sigma_geo ~ U[1.1, 1.6]), "
+                  "volume fraction ~ U[100, 5000] ppm, 1700 K, stop at 1 aggregate or 60 s of physical time")
+
+
+def serve_requests(seconds: float, rate: float, nmax: int, seed: int = 5000) -> list[tuple[float, str, bool]]:
+    """(arrival time, parameter file, surface-growth flag) of each request."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out, t, k = [], 0.0, 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            return out
+        n = int(round(np.exp(rng.uniform(np.log(500), np.log(nmax)))))
+        fv = rng.uniform(100e-6, 5000e-6)
+        sg = rng.uniform(1.1, 1.6)
+        growth = bool(rng.random() < 0.3)
+        ini = (f"[monomers]\nnumber = {n}\nmean_diameter = 30\ndispersion_diameter = {sg!r}\n"
+               f"initialisation_mode = lognormal\n[environment]\nvolume_fraction = {fv!r}\ntemperature = 1700\n"
+               f"[limits]\nnumber_of_aggregates = 1\nphysical_time = 60\n"
+               f"[numerics]\nrandom_seed = {seed + 1 + k}\nwith_domain_duplication = false\n")
+        out.append((t, ini, growth))
+        k += 1
+
+
+def run_serve(args, rank: int, world: int) -> dict | None:
+    """Continuous batching of a seeded request stream: p50/p99 latency."""
+    import numpy as np
+    import torch
+
+    from mcac_gb300 import PhysicalModel, Server, resident_boxes
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    reqs = serve_requests(args.serve_seconds, args.rate, args.serve_nmax, seed=5000 + rank)
+    models = [PhysicalModel(text=ini) for _, ini, _ in reqs]
+    capacity = resident_boxes(256)
+    budget = int(0.5 * torch.cuda.get_device_properties(dev).total_memory)
+    lat, steps_done, finished = [], 0, 0
+    sampler = ClockSampler(dev)
+    with Server(capacity=capacity, memory_budget=budget, stream=stream.cuda_stream) as srv:
+        sampler.start()
+        t0 = time.perf_counter()
+        nxt = 0
+        while True:
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and reqs[nxt][0] <= now:
+                srv.submit(models[nxt])
+                nxt += 1
+            active, pending = srv.step(args.epoch_steps)
+            for c in srv.poll():
+                lat.append(float(c["finish_s"] - c["submit_s"]))
+                steps_done += int(c["steps"])
+                finished += int(c["finished"] == 1 and c["status"] == 0)
+            if nxt == len(reqs) and active == 0 and pending == 0:
+                break
+            if now > args.serve_seconds + args.cap_seconds:
+                break
+            if active == 0 and pending == 0 and nxt < len(reqs):
+                time.sleep(max(0.0, min(0.01, reqs[nxt][0] - (time.perf_counter() - t0))))
+        wall = time.perf_counter() - t0
+        kernel_ms, launches = srv.kernel_time()
+        clocks = sampler.stop()
+    if rank != 0:
+        return None
+    lat = np.array(lat)
+    q = (lambda p: float(np.quantile(lat, p)) if len(lat) else None)
+    return {
+        "metric": "run latency p50/p99", "value": q(0.5), "unit": "s", "n_gpus": world, "steps": launches,
+        "warmup": 0, "ms_per_step": kernel_ms / max(1, launches), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "latency_s": {"p50": q(0.5), "p90": q(0.9), "p99": q(0.99), "max": q(1.0)},
+        "config": {"workload": SERVE_WORKLOAD, "rate_per_s": args.rate, "arrival_seconds": args.serve_seconds,
+                   "n_max": args.serve_nmax, "requests": len(reqs), "completed": int(len(lat)),
+                   "finished_to_criterion": finished, "capacity_slots": capacity,
+                   "memory_budget_bytes": budget, "epoch_steps": args.epoch_steps, "wall_s": wall,
+                   "surface_growth_requests": int(sum(g for _, _, g in reqs)),
+                   "surface_growth": "not in the device loop: the requests drawn with surface growth run without it"},
+        "throughput": {"runs_per_s": len(lat) / wall, "mc_steps_per_s": steps_done / wall},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+
+
 def run_reference(args) -> dict:
     try:
         from oracle import oracle_py
@@ -463,14 +705,22 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mc-steps", type=int, default=2000, help="MC steps per box per bench step")
-    ap.add_argument("--replicas", type=int, default=0, help="boxes per GPU (0: one per SM)")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--replicas", type=int, default=0, help="boxes per GPU (0: as many as stay resident)")
+    ap.add_argument("--threads", type=int, default=0, help="threads per box (64/128/256; 0: timed at the first run)")
+    ap.add_argument("--e2e-steps", type=int, default=5, help="bench steps between upload and download (e2e)")
     ap.add_argument("--plain-steps", type=int, default=500)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "contact-search"],
-                    help="c2: replicas of the 100k-monomer box (headline); contact-search: batched queries")
+    ap.add_argument("--workload", default="c2", choices=["c2", "contact-search", "ensemble", "serve"],
+                    help="c2: replicas of the 100k-monomer box (headline); contact-search: batched queries; "
+                         "ensemble: the 512-box ensemble to completion (boxes/hour)")
+    ap.add_argument("--boxes", type=int, default=512, help="ensemble boxes")
+    ap.add_argument("--cap-seconds", type=float, default=240.0, help="ensemble / serving wall-time cap")
+    ap.add_argument("--rate", type=float, default=50.0, help="serving arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=30.0, help="serving arrival window")
+    ap.add_argument("--serve-nmax", type=int, default=5000, help="serving: largest request (monomers)")
+    ap.add_argument("--epoch-steps", type=int, default=1000, help="serving: MC steps per box per epoch")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -485,7 +735,9 @@ def main() -> int:
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    out = (run_contact_search if args.workload == "contact-search" else run_ours)(args, rank, world)
+    runner = {"c2": run_ours, "contact-search": run_contact_search, "ensemble": run_ensemble,
+              "serve": run_serve}[args.workload]
+    out = runner(args, rank, world)
     if out is not None:
         print(json.dumps(out))
     if world > 1:

@@ -158,6 +158,10 @@ typedef struct mcacg_profile {
     int64_t cand_spheres; /* spheres of those candidates */
     int64_t refined;      /* sphere pairs evaluated in FP64 */
     int64_t merged_spheres, merge_pairs;
+    /* device-resident loop only: SM clock cycles its thread blocks spent in
+     * each phase of the MC step (pick + direction, contact query,
+     * translation + time, merge + pick-tree update), summed over boxes */
+    int64_t cycles_pick, cycles_query, cycles_move, cycles_merge;
 } mcacg_profile;
 
 typedef struct mcacg_box mcacg_box;
@@ -241,7 +245,7 @@ int mcacg_distance_to_next_contacts(mcacg_box *box, int32_t n, const int64_t *so
  * device-wide synchronisation of cudaMalloc/cudaFree, one under a fixed
  * memory budget). All device scratch is one 32 MiB __device__ array of the
  * library. At most 65536 queries per call (MCACG_ERR_CAPACITY beyond); a box
- * whose per-block candidate lists (40 bytes per aggregate slot) do not fit
+ * whose per-block candidate lists (44 bytes per aggregate slot) do not fit
  * it is refused with MCACG_ERR_CAPACITY. The first call on each device, with
  * that device current, looks the array up (cudaGetSymbolAddress); make it
  * before any stream capture begins. Each call zeroes its query counter and
@@ -305,6 +309,16 @@ int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_s
 int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state *states, int32_t n_boxes,
                                    void *cuda_stream, mcacg_batch **batch);
 int mcacg_batch_destroy(mcacg_batch *batch);
+/* Boxes the device-resident loop runs at once on the current device with
+ * 'threads' threads per box (64, 128, 256 or 512): its thread blocks per SM x
+ * SMs. Batches up to this size take one wave. */
+int mcacg_resident_boxes(int32_t threads, int32_t *boxes);
+/* Threads per box of the batch's loop: 64, 128, 256 or 512, or 0 (the
+ * default) to let mcacg_batch_run time each on a short slice of the run and
+ * keep the fastest, and choose again when half of the running boxes have
+ * finished (runs to the stop criteria). Results do not depend on it. */
+int mcacg_batch_set_threads(mcacg_batch *batch, int32_t threads);
+int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads);
 /* Advances every unfinished box by at most max_steps steps (<= 0: until all
  * meet their stop criteria) in kernel launches of steps_per_launch steps. */
 int mcacg_batch_run(mcacg_batch *batch, int64_t max_steps, int64_t steps_per_launch);
@@ -313,6 +327,9 @@ int mcacg_batch_stats(mcacg_batch *batch, mcacg_run_stats *stats);
 int mcacg_batch_size(const mcacg_batch *batch, int32_t *n_boxes);
 int mcacg_batch_box_sizes(mcacg_batch *batch, int32_t box, int64_t *n_spheres, int64_t *n_aggregates);
 int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state);
+/* mcacg_batch_store_state for every box at once (states[i] for box i, all
+ * n_boxes of them), the conversions spread over the host's cores. */
+int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_boxes);
 /* Work counters of all boxes since creation, summed (the query and merge
  * fields of mcacg_profile; times are left at 0). */
 int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out);

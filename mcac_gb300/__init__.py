@@ -5,5 +5,5 @@ the CUDA kernels for sm_103a and the C++ host layer; this package binds it
 with ctypes and mirrors the reference's C++ interface (see ``api``).
 """
 from .api import (CONTACT_DTYPE, AggregateContactInfo, AggregatList, Batch, PhysicalModel, Server,  # noqa: F401
-                  calcul, device_count, init_state, run_device, synthetic_state)
+                  calcul, device_count, init_state, resident_boxes, run_device, synthetic_state)
 from .snapshot import Snapshot  # noqa: F401

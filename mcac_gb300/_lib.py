@@ -68,7 +68,8 @@ class RunStats(C.Structure):
 class Profile(C.Structure):
     _fields_ = [("queries", i64), ("merges", i64), ("translates", i64), ("query_ms", f64), ("merge_ms", f64),
                 ("mov_spheres", i64), ("scanned", i64), ("cells", i64), ("candidates", i64),
-                ("cand_spheres", i64), ("refined", i64), ("merged_spheres", i64), ("merge_pairs", i64)]
+                ("cand_spheres", i64), ("refined", i64), ("merged_spheres", i64), ("merge_pairs", i64),
+                ("cycles_pick", i64), ("cycles_query", i64), ("cycles_move", i64), ("cycles_merge", i64)]
 
 
 # every exported symbol with its argument types (restype is int unless noted)
@@ -114,11 +115,15 @@ SIGNATURES = {
     "mcacg_batch_create": [C.POINTER(Params), i32, vp, C.POINTER(vp)],
     "mcacg_batch_create_from_states": [C.POINTER(Params), C.POINTER(State), i32, vp, C.POINTER(vp)],
     "mcacg_batch_destroy": [vp],
+    "mcacg_resident_boxes": [i32, C.POINTER(i32)],
+    "mcacg_batch_set_threads": [vp, i32],
+    "mcacg_batch_threads": [vp, C.POINTER(i32)],
     "mcacg_batch_run": [vp, i64, i64],
     "mcacg_batch_stats": [vp, C.POINTER(RunStats)],
     "mcacg_batch_size": [vp, C.POINTER(i32)],
     "mcacg_batch_box_sizes": [vp, i32, C.POINTER(i64), C.POINTER(i64)],
     "mcacg_batch_store_state": [vp, i32, C.POINTER(State)],
+    "mcacg_batch_store_states": [vp, C.POINTER(State), i32],
     "mcacg_batch_last_run": [vp, C.POINTER(f64), C.POINTER(i32)],
     "mcacg_batch_work": [vp, C.POINTER(Profile)],
     "mcacg_server_create": [i32, i64, vp, i32, C.POINTER(vp)],

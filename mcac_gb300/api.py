@@ -297,6 +297,14 @@ def device_count() -> int:
     return n.value
 
 
+def resident_boxes(threads: int = 256) -> int:
+    """Boxes the device-resident loop runs at once on the current device with
+    'threads' threads per box."""
+    n = C.c_int32(0)
+    check(lib().mcacg_resident_boxes(int(threads), C.byref(n)))
+    return n.value
+
+
 def _run_stats(box_run) -> RunStats:
     return box_run
 
@@ -342,6 +350,17 @@ class Batch:
     def __len__(self) -> int:
         return len(self.models)
 
+    @property
+    def threads(self) -> int:
+        """Threads per box of the loop (0 until chosen by the first run)."""
+        n = C.c_int32(0)
+        check(lib().mcacg_batch_threads(self._b, C.byref(n)))
+        return n.value
+
+    @threads.setter
+    def threads(self, value: int) -> None:
+        check(lib().mcacg_batch_set_threads(self._b, int(value)))
+
     def run(self, max_steps: int = 0, steps_per_launch: int = 20000) -> None:
         check(lib().mcacg_batch_run(self._b, int(max_steps), int(steps_per_launch)))
 
@@ -364,6 +383,21 @@ class Batch:
         ms, n = C.c_double(), C.c_int32()
         check(lib().mcacg_batch_last_run(self._b, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def store_all(self) -> list[Snapshot]:
+        """The state of every box (one call, converted in parallel)."""
+        bufs = []
+        for box in range(len(self.models)):
+            ns, na = C.c_int64(), C.c_int64()
+            check(lib().mcacg_batch_box_sizes(self._b, box, C.byref(ns), C.byref(na)))
+            bufs.append(StateBuffers(ns.value, max(na.value, 1)))
+        arr = (_lib.State * len(bufs))(*[b.state for b in bufs])
+        check(lib().mcacg_batch_store_states(self._b, arr, len(bufs)))
+        out = []
+        for k, b in enumerate(bufs):
+            b.state = arr[k]
+            out.append(b.to_snapshot(volsurf_method=int(self.models[k].params.volsurf_method)))
+        return out
 
     def store(self, box: int) -> Snapshot:
         ns, na = C.c_int64(), C.c_int64()

@@ -8,28 +8,53 @@
 #include <thread>
 
 #include "batch.hpp"
+#include "host_parallel.hpp"
 #include "host_box.hpp"
 #include "run.cuh"
 
 namespace mcacg {
 
-constexpr int kRunThreads = 256;
+constexpr int kRunThreads = 256;  // serving loop
+// Block sizes of the batched loop. Most of an MC step is a chain of
+// dependent loads and block barriers, so smaller blocks (more boxes per SM)
+// often finish more steps per second; BatchRunner::run picks one by timing.
+// Every variant keeps to 128 registers a thread (512 / NT blocks per SM).
+// Large blocks pay off late in a run, when few boxes are left and each holds
+// big aggregates (long pair searches and merges).
+constexpr int kRunThreadChoices[] = {64, 128, 256, 512};
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_run(const BoxRun *runs, int n, long long max_steps) {
+__global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n, long long max_steps) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RunSmem &sm = *reinterpret_cast<RunSmem *>(smem_raw);
     __shared__ __align__(16) BoxRun R;
+    __shared__ __align__(16) RunState st;  // the box's loop state, kept on chip for the launch
     const int box = blockIdx.x;
     if (box >= n) return;
-    if (runs[box].st == nullptr) return;  // an empty serving slot
-    const int words = int(sizeof(BoxRun) / sizeof(int));
-    const int *src = reinterpret_cast<const int *>(&runs[box]);
-    int *dst = reinterpret_cast<int *>(&R);
-    for (int k = threadIdx.x; k < words; k += NT) dst[k] = src[k];
+    RunState *st_global = runs[box].st;
+    if (st_global == nullptr) return;  // an empty serving slot
+    {
+        const int words = int(sizeof(BoxRun) / sizeof(int));
+        const int *src = reinterpret_cast<const int *>(&runs[box]);
+        int *dst = reinterpret_cast<int *>(&R);
+        for (int k = threadIdx.x; k < words; k += NT) dst[k] = src[k];
+        const int swords = int(sizeof(RunState) / sizeof(int));
+        const int *ssrc = reinterpret_cast<const int *>(st_global);
+        int *sdst = reinterpret_cast<int *>(&st);
+        for (int k = threadIdx.x; k < swords; k += NT) sdst[k] = ssrc[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) R.st = &st;
     __syncthreads();
     for (long long s = 0; s < max_steps; ++s)
         if (!block_mc_step(R, sm)) break;
+    __syncthreads();
+    {
+        const int swords = int(sizeof(RunState) / sizeof(int));
+        const int *ssrc = reinterpret_cast<const int *>(&st);
+        int *sdst = reinterpret_cast<int *>(st_global);
+        for (int k = threadIdx.x; k < swords; k += NT) sdst[k] = ssrc[k];
+    }
 }
 
 namespace {
@@ -38,6 +63,39 @@ bool ok_cuda(cudaError_t e, std::string *err, const char *what) {
     if (e == cudaSuccess) return true;
     if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
     return false;
+}
+
+template <int NT>
+cudaError_t prepare_k_run() {
+    cudaError_t e = cudaFuncSetAttribute(k_run<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RunSmem)));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_run<NT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+cudaError_t prepare_all_k_run() {
+    cudaError_t e = prepare_k_run<64>();
+    if (e == cudaSuccess) e = prepare_k_run<128>();
+    if (e == cudaSuccess) e = prepare_k_run<256>();
+    if (e == cudaSuccess) e = prepare_k_run<512>();
+    return e;
+}
+cudaError_t launch_k_run(int nt, int grid, cudaStream_t s, const BoxRun *runs, int n, long long steps) {
+    switch (nt) {
+        case 64: k_run<64><<<grid, 64, sizeof(RunSmem), s>>>(runs, n, steps); break;
+        case 128: k_run<128><<<grid, 128, sizeof(RunSmem), s>>>(runs, n, steps); break;
+        case 512: k_run<512><<<grid, 512, sizeof(RunSmem), s>>>(runs, n, steps); break;
+        default: k_run<256><<<grid, 256, sizeof(RunSmem), s>>>(runs, n, steps); break;
+    }
+    return cudaGetLastError();
+}
+int occupancy_k_run(int nt, int *per_sm) {
+    cudaError_t e;
+    switch (nt) {
+        case 64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_run<64>, 64, sizeof(RunSmem)); break;
+        case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_run<128>, 128, sizeof(RunSmem)); break;
+        case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_run<512>, 512, sizeof(RunSmem)); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_run<256>, 256, sizeof(RunSmem)); break;
+    }
+    return e == cudaSuccess ? ST_OK : ST_CUDA;
 }
 
 // 32-ary sum tree over per-slot weights (leaves first, top level <= 32 entries).
@@ -126,6 +184,24 @@ BatchRunner::~BatchRunner() {
     if (own_stream_ && stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
 }
 
+int BatchRunner::resident_boxes(int threads, int *boxes, std::string *err) {
+    if (threads != 64 && threads != 128 && threads != 256 && threads != 512) {
+        if (err) *err = "threads per box must be 64, 128, 256 or 512";
+        return ST_BAD_ARGUMENT;
+    }
+    int dev = 0, n_sm = 0, per_sm = 0;
+    if (!ok_cuda(cudaGetDevice(&dev), err, "cudaGetDevice") ||
+        !ok_cuda(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), err, "device attribute") ||
+        !ok_cuda(prepare_all_k_run(), err, "cudaFuncSetAttribute"))
+        return ST_CUDA;
+    if (occupancy_k_run(threads, &per_sm) != ST_OK) {
+        if (err) *err = "occupancy query failed";
+        return ST_CUDA;
+    }
+    *boxes = std::max(1, per_sm) * n_sm;
+    return ST_OK;
+}
+
 int BatchRunner::create(const std::vector<mcacg_params> &params, std::vector<HostState> &&states, void *stream,
                         std::unique_ptr<BatchRunner> *out, std::string *err) {
     if (params.size() != states.size() || params.empty()) {
@@ -133,18 +209,36 @@ int BatchRunner::create(const std::vector<mcacg_params> &params, std::vector<Hos
         return ST_BAD_ARGUMENT;
     }
     std::unique_ptr<BatchRunner> r(new BatchRunner());
-    std::vector<double> times;
-    for (size_t i = 0; i < states.size(); ++i) {
-        DeviceBox *d = nullptr;
-        int rc = DeviceBox::create(states[i], stream, &d, err);
-        if (rc != ST_OK) return rc;
-        r->owned_.emplace_back(d);
-        r->boxes_.push_back(d);
-        times.push_back(states[i].time);
-        states[i] = HostState();  // release host memory early
+    const int n = int(states.size());
+    std::vector<double> times(states.size());
+    std::vector<DeviceBox *> made(states.size(), nullptr);
+    std::vector<int> rcs(states.size(), ST_OK);
+    std::vector<std::string> errs(states.size());
+    // boxes are built in parallel, each on a stream of its own, then moved to
+    // the batch's stream
+    parallel_for(n, [&](int i) {
+        rcs[size_t(i)] = DeviceBox::create(states[size_t(i)], nullptr, &made[size_t(i)], &errs[size_t(i)]);
+        times[size_t(i)] = states[size_t(i)].time;
+        states[size_t(i)] = HostState();  // release host memory early
+    });
+    for (int i = 0; i < n; ++i) {
+        if (made[size_t(i)]) {
+            r->owned_.emplace_back(made[size_t(i)]);
+            r->boxes_.push_back(made[size_t(i)]);
+        }
     }
+    for (int i = 0; i < n; ++i)
+        if (rcs[size_t(i)] != ST_OK) {
+            if (err) *err = "box " + std::to_string(i) + ": " + errs[size_t(i)];
+            return rcs[size_t(i)];
+        }
     int rc = r->init_stream(stream, err);
     if (rc != ST_OK) return rc;
+    for (DeviceBox *d : r->boxes_)
+        if (d->set_stream(r->stream_) != ST_OK) {
+            if (err) *err = "could not move a box to the batch stream";
+            return ST_CUDA;
+        }
     rc = r->init(params, times, err);
     if (rc != ST_OK) return rc;
     *out = std::move(r);
@@ -204,51 +298,125 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
     if (!ok_cuda(cudaMemcpyAsync(states_dev_, states.data(), sizeof(RunState) * size_t(n), cudaMemcpyHostToDevice, s),
                  err, "upload"))
         return ST_CUDA;
-    if (!ok_cuda(cudaFuncSetAttribute(k_run<kRunThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(sizeof(RunSmem))), err, "cudaFuncSetAttribute"))
-        return ST_CUDA;
+    if (!ok_cuda(prepare_all_k_run(), err, "cudaFuncSetAttribute")) return ST_CUDA;
     if (!ok_cuda(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
     return ST_OK;
+}
+
+int BatchRunner::set_threads(int threads) {
+    if (threads != 0 && threads != 64 && threads != 128 && threads != 256 && threads != 512) return ST_BAD_ARGUMENT;
+    threads_ = threads;
+    auto_threads_ = threads == 0;
+    return ST_OK;
+}
+
+// Times each block size on a short slice of the run (results do not depend
+// on the block size) and keeps the fastest. Returns the MC steps done.
+int BatchRunner::tune(int64_t budget, int64_t *done, float *ms_total, std::string *err) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    const int n = int(boxes_.size());
+    const BoxRun *runs = static_cast<const BoxRun *>(runs_dev_);
+    const int64_t probe = 32;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_ms = 0.f;
+    int best = threads_ ? threads_ : 256;
+    int rc = ST_OK;
+    for (int nt : kRunThreadChoices) {
+        if (budget > 0 && *done + probe > budget) break;
+        cudaEventRecord(e0, s);
+        if (!ok_cuda(launch_k_run(nt, n, s, runs, n, (long long)probe), err, "k_run")) {
+            rc = ST_CUDA;
+            break;
+        }
+        cudaEventRecord(e1, s);
+        if (!ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {
+            rc = ST_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *ms_total += ms;
+        ++launches_;
+        *done += probe;
+        if (best_ms == 0.f || ms < best_ms) {
+            best_ms = ms;
+            best = nt;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == ST_OK && best_ms > 0.f) threads_ = best;
+    return rc;
 }
 
 int BatchRunner::run(int64_t max_steps, int64_t chunk, std::string *err) {
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
     const int n = int(boxes_.size());
+    const BoxRun *runs = static_cast<const BoxRun *>(runs_dev_);
     if (chunk <= 0) chunk = 20000;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, s);
     launches_ = 0;
     int64_t done = 0;
     int rc = ST_OK;
+    float ms_total = 0.f;
+    auto count_active = [&](int *active) -> int {
+        std::vector<BoxRunStats> st;
+        int r = stats(&st, err);
+        if (r != ST_OK) return r;
+        int a = 0;
+        for (const auto &x : st) a += !(x.finished || x.status != ST_OK);
+        *active = a;
+        return ST_OK;
+    };
+    if (auto_threads_ && threads_ == 0) {
+        rc = count_active(&tuned_active_);
+        if (rc == ST_OK) rc = tune(max_steps, &done, &ms_total, err);
+        if (rc != ST_OK) return rc;
+    }
+    const float ms_tune = ms_total;
+    ms_total = 0.f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
     for (;;) {
         int64_t steps = max_steps > 0 ? std::min(chunk, max_steps - done) : chunk;
         if (steps <= 0) break;
-        k_run<kRunThreads><<<n, kRunThreads, sizeof(RunSmem), s>>>(static_cast<const BoxRun *>(runs_dev_), n,
-                                                                   (long long)steps);
-        ++launches_;
-        if (!ok_cuda(cudaGetLastError(), err, "k_run")) {
+        const int nt = threads_ ? threads_ : 256;
+        cudaEventRecord(e0, s);
+        if (!ok_cuda(launch_k_run(nt, n, s, runs, n, (long long)steps), err, "k_run")) {
             rc = ST_CUDA;
             break;
         }
+        cudaEventRecord(e1, s);
+        if (!ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {
+            rc = ST_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms_total += ms;
+        ++launches_;
         done += steps;
         if (max_steps > 0 && done >= max_steps) break;
         if (max_steps <= 0) {
-            // until every box has met its stop criterion (or failed)
-            std::vector<BoxRunStats> st;
-            rc = stats(&st, err);
+            // until every box has met its stop criterion (or failed); when
+            // half of the boxes running at the last tuning have finished, the
+            // block size is chosen again
+            int active = 0;
+            rc = count_active(&active);
             if (rc != ST_OK) break;
-            bool all = true;
-            for (const auto &x : st) all = all && (x.finished || x.status != ST_OK);
-            if (all) break;
+            if (active == 0) break;
+            if (auto_threads_ && active * 2 <= tuned_active_) {
+                tuned_active_ = active;
+                float mt = 0.f;
+                rc = tune(0, &done, &mt, err);
+                ms_total += mt;
+                if (rc != ST_OK) break;
+            }
         }
     }
-    cudaEventRecord(e1, s);
-    if (!ok_cuda(cudaEventSynchronize(e1), err, "k_run")) rc = ST_CUDA;
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    last_ms_ = ms;
+    last_ms_ = ms_total + ms_tune;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
@@ -288,6 +456,10 @@ int BatchRunner::stats(std::vector<BoxRunStats> *out, std::string *err) {
         o.refined = r.c_refined;
         o.merged_spheres = r.c_merged_spheres;
         o.merge_pairs = r.c_merge_pairs;
+        o.cyc_pick = r.cyc_pick;
+        o.cyc_query = r.cyc_query;
+        o.cyc_move = r.cyc_move;
+        o.cyc_merge = r.cyc_merge;
     }
     return ST_OK;
 }
@@ -296,10 +468,24 @@ int BatchRunner::download(int box, HostState *st, std::string *err) {
     if (box < 0 || box >= size()) return ST_BAD_ARGUMENT;
     int rc = boxes_[size_t(box)]->download(st, err);
     if (rc != ST_OK) return rc;
-    std::vector<BoxRunStats> s;
-    rc = stats(&s, err);
-    if (rc != ST_OK) return rc;
-    st->time = s[size_t(box)].time;
+    RunState r;
+    if (!ok_cuda(cudaMemcpy(&r, static_cast<RunState *>(states_dev_) + box, sizeof(r), cudaMemcpyDeviceToHost), err,
+                 "download"))
+        return ST_CUDA;
+    st->time = r.time;
+    return ST_OK;
+}
+
+int BatchRunner::times(std::vector<double> *out, std::string *err) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    const int n = size();
+    std::vector<RunState> st(static_cast<size_t>(n));
+    if (!ok_cuda(cudaMemcpyAsync(st.data(), states_dev_, sizeof(RunState) * size_t(n), cudaMemcpyDeviceToHost, s),
+                 err, "download") ||
+        !ok_cuda(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
+    out->resize(size_t(n));
+    for (int i = 0; i < n; ++i) (*out)[size_t(i)] = st[size_t(i)].time;
     return ST_OK;
 }
 
@@ -312,7 +498,8 @@ int64_t Server::footprint(const mcacg_params &p) {
     // device bytes of one box (DeviceBox::create's arrays plus the sum tree)
     const int64_t n = p.n_monomeres;
     const int64_t cells = p.n_verlet_divisions * p.n_verlet_divisions * p.n_verlet_divisions;
-    return n * 860 + cells * 4 * 80 + (1 << 20);
+    const int64_t fine_cells = int64_t(kFineMaxDiv) * kFineMaxDiv * kFineMaxDiv;  // upper bound
+    return n * 876 + cells * 4 * 80 + fine_cells * 4 + (1 << 20);
 }
 
 int Server::create(int capacity, int64_t memory_budget, void *stream, bool keep_final_states,

@@ -17,6 +17,7 @@ struct BoxRunStats {
     int finished, status;
     // work counters since creation
     int64_t queries, mov, scanned, cells, candidates, cand_spheres, refined, merged_spheres, merge_pairs;
+    int64_t cyc_pick, cyc_query, cyc_move, cyc_merge;  // SM cycles per phase of the step
 };
 
 class BatchRunner {
@@ -30,6 +31,13 @@ class BatchRunner {
                       const std::vector<double> &times, void *stream, std::unique_ptr<BatchRunner> *out,
                       std::string *err);
     ~BatchRunner();
+    // Boxes the device loop keeps resident at once on the current device
+    // (thread blocks per SM at its register and shared-memory use x SMs).
+    static int resident_boxes(int threads, int *boxes, std::string *err);
+    // Threads per box (64, 128, 256 or 512; 0: chosen by timing at the next
+    // run, and again when half of the running boxes have finished).
+    int set_threads(int threads);
+    int threads() const { return threads_; }
 
     int size() const { return int(boxes_.size()); }
     // Advances every unfinished box by at most max_steps MC steps (<= 0: until
@@ -37,6 +45,8 @@ class BatchRunner {
     int run(int64_t max_steps, int64_t chunk, std::string *err);
     int stats(std::vector<BoxRunStats> *out, std::string *err);
     int download(int box, HostState *st, std::string *err);
+    // Physical time of every box.
+    int times(std::vector<double> *out, std::string *err);
     DeviceBox &box(int i) { return *boxes_[size_t(i)]; }
     // Kernel time of the last run() (CUDA events on the stream).
     double last_kernel_ms() const { return last_ms_; }
@@ -55,6 +65,10 @@ class BatchRunner {
     std::vector<void *> trees_;
     double last_ms_ = 0;
     int launches_ = 0;
+    int threads_ = 0;
+    bool auto_threads_ = true;
+    int tuned_active_ = 0;  // unfinished boxes at the last tuning
+    int tune(int64_t budget, int64_t *done, float *ms_total, std::string *err);
 };
 
 // Continuous-batching request loop: 'capacity' block slots; between kernel

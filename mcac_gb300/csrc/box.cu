@@ -33,19 +33,22 @@ struct BatchScratch {
     size_t stride;  // candidate entries per block (nslots + 1)
     int surv_cap;   // HBM survivors per block
     double *cand_db;
-    int *cand_flat, *cand_slot, *cand_order, *cand_prefix;
+    long long *cand_key;
+    int *cand_slot, *cand_order, *cand_prefix;
     unsigned long long *best_res, *best_ij;
     int4 *surv;
     double *surv_res;
 };
-__global__ void __launch_bounds__(kQueryThreads) k_query_batch(DevBox b, BatchScratch s, int n, const QueryIn *in,
-                                                               QueryOut *out) {
+constexpr int kBatchThreads = 256;  // two blocks per SM at 128 registers a thread
+template <int NT>
+__global__ void __launch_bounds__(NT) k_query_batch(DevBox b, BatchScratch s, int n, const QueryIn *in,
+                                                    QueryOut *out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     QuerySmem &sm = *reinterpret_cast<QuerySmem *>(smem_raw);
     __shared__ int q_cur;
     const size_t c0 = size_t(blockIdx.x) * s.stride;
     b.cand_db = s.cand_db + c0;
-    b.cand_flat = s.cand_flat + c0;
+    b.cand_key = s.cand_key + c0;
     b.cand_slot = s.cand_slot + c0;
     b.cand_order = s.cand_order + c0;
     b.cand_prefix = s.cand_prefix + c0;
@@ -86,11 +89,17 @@ __global__ void k_set_fields(DevBox b, int slot, FieldUpdate u, unsigned mask) {
     if (f < AGG_NFIELDS && (mask >> f) & 1u) A(b, f, slot) = u.v[f];
 }
 
-// Verlet grid from the aggregate positions, in three grid-wide passes:
-// clear the cells, drop every live slot into its cell, sort each cell by slot
-// (the reference's std::set order).
+// Verlet and fine grids from the aggregate positions: clear the cells, drop
+// every live slot into its cells (in any order: the scan key restores the
+// reference's order), then link the fine lists backwards.
 __global__ void k_grid_clear(DevBox b) {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < b.n_cells; c += gridDim.x * blockDim.x) b.cell_n[c] = 0;
+    const int stride = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int c = t; c < b.n_cells; c += stride) b.cell_n[c] = 0;
+    if (b.fine_div > 0) {
+        const int nf3 = b.fine_div * b.fine_div * b.fine_div;
+        for (int c = t; c < nf3; c += stride) b.fine_head[c] = -1;
+        for (int a = t; a < b.nslots; a += stride) b.fine_cell[a] = -1;
+    }
 }
 __global__ void k_grid_fill(DevBox b) {
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nslots; a += gridDim.x * blockDim.x) {
@@ -102,10 +111,26 @@ __global__ void k_grid_fill(DevBox b) {
         const int k = atomicAdd(&b.cell_n[c], 1);
         if (k < b.cell_cap) {
             b.cell_items[size_t(c) * b.cell_cap + k] = a;
+            b.cell_pos[a] = k;
         } else {
             b.sc->cell_overflow = 1;
             b.sc->status = ST_CAPACITY;
         }
+        if (b.fine_div > 0) {
+            const int fc = fine_cell_of(b, agg_pos(b, a));
+            b.fine_cell[a] = fc;
+            b.fine_next[a] = atomicExch(&b.fine_head[fc], a);
+        }
+    }
+}
+// back links of the fine lists built by k_grid_fill
+__global__ void k_fine_link(DevBox b) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nslots; a += gridDim.x * blockDim.x) {
+        const int c = b.fine_cell[a];
+        if (c < 0) continue;
+        const int n = b.fine_next[a];
+        if (n >= 0) b.fine_prev[n] = a;
+        if (b.fine_head[c] == a) b.fine_prev[a] = -1;
     }
 }
 __global__ void k_refresh_f4(DevBox b) {
@@ -113,25 +138,6 @@ __global__ void k_refresh_f4(DevBox b) {
         b.agg_f4[a] = make_float4(float(A(b, AGG_X, a)), float(A(b, AGG_Y, a)), float(A(b, AGG_Z, a)),
                                   float(A(b, AGG_RMAX, a)));
 }
-__global__ void k_grid_sort(DevBox b) {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < b.n_cells; c += gridDim.x * blockDim.x) {
-        int n = b.cell_n[c];
-        if (n > b.cell_cap) {
-            n = b.cell_cap;
-            b.cell_n[c] = n;
-        }
-        int *items = b.cell_items + size_t(c) * b.cell_cap;
-        for (int x = 1; x < n; ++x) {
-            int v = items[x], y = x;
-            while (y > 0 && items[y - 1] > v) {
-                items[y] = items[y - 1];
-                --y;
-            }
-            items[y] = v;
-        }
-    }
-}
-
 // ------------------------------------------------------------------- host
 namespace {
 
@@ -172,6 +178,25 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     for (int a = 0; a < st.nslots; ++a)
         if (st.agg_n[a] > 0) rmax_all = std::max(rmax_all, st.agg[size_t(AGG_RMAX) * st.nslots + a]);
     b.margin = (3.0 * st.box_length + 4.0 * rmax_all) * (1.0 / 131072.0);
+    // fine discovery grid, when finer than the Verlet grid: a query visits
+    // the cells covering its swept box, about lpm/2 + 2 (r_max + max r_max)
+    // per axis on average; cells of 0.6 of that balance the cells visited
+    // against the aggregates screened. At least 2 max r_max and L/128.
+    {
+        double lpm_sum = 0.0, rmax_sum = 0.0;
+        int live = 0;
+        for (int a = 0; a < st.nslots; ++a)
+            if (st.agg_n[a] > 0) {
+                lpm_sum += st.agg[size_t(AGG_LPM) * st.nslots + a];
+                rmax_sum += st.agg[size_t(AGG_RMAX) * st.nslots + a];
+                ++live;
+            }
+        const double extent = live ? 0.5 * lpm_sum / live + 2.0 * (rmax_sum / live + rmax_all) : 0.0;
+        const double h = std::max({2.0 * rmax_all, st.box_length / double(kFineMaxDiv), 0.6 * extent});
+        const double nf = std::floor(st.box_length / h);
+        b.fine_div = (nf > double(st.n_div) && nf <= double(kFineMaxDiv)) ? int(nf) : 0;
+        b.fine_step = b.fine_div > 0 ? double(b.fine_div) / st.box_length : 0.0;
+    }
     // grid capacity
     std::vector<int> cell_n(size_t(b.n_cells), 0);
     int maxc = 0;
@@ -229,6 +254,14 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
         ok = ok && alloc((void **)&b.pool_pos[k], sizeof(float4) * size_t(b.pool_cap));
     }
     ok = ok && alloc((void **)&b.cell_n, sizeof(int) * size_t(b.n_cells));
+    ok = ok && alloc((void **)&b.cell_pos, sizeof(int) * size_t(st.nslots));
+    if (b.fine_div > 0) {
+        const size_t nf3 = size_t(b.fine_div) * size_t(b.fine_div) * size_t(b.fine_div);
+        ok = ok && alloc((void **)&b.fine_head, sizeof(int) * nf3);
+        ok = ok && alloc((void **)&b.fine_next, sizeof(int) * size_t(st.nslots));
+        ok = ok && alloc((void **)&b.fine_prev, sizeof(int) * size_t(st.nslots));
+        ok = ok && alloc((void **)&b.fine_cell, sizeof(int) * size_t(st.nslots));
+    }
     ok = ok && alloc((void **)&b.cell_items, sizeof(int) * size_t(b.n_cells) * size_t(b.cell_cap));
     ok = ok && alloc((void **)&b.sc, sizeof(DevScalars));
     ok = ok && alloc((void **)&b.surv, sizeof(int4) * size_t(b.surv_cap));
@@ -244,7 +277,7 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     ok = ok && alloc((void **)&b.counters, sizeof(int) * 8);
     const size_t nc1 = size_t(st.nslots) + 1;
     ok = ok && alloc((void **)&b.cand_db, sizeof(double) * nc1);
-    ok = ok && alloc((void **)&b.cand_flat, sizeof(int) * nc1);
+    ok = ok && alloc((void **)&b.cand_key, sizeof(long long) * nc1);
     ok = ok && alloc((void **)&b.cand_slot, sizeof(int) * nc1);
     ok = ok && alloc((void **)&b.cand_order, sizeof(int) * nc1);
     ok = ok && alloc((void **)&b.cand_prefix, sizeof(int) * nc1);
@@ -401,11 +434,12 @@ int DeviceBox::rebuild_grid(int cap, std::string *err) {
     sc.cell_overflow = 0;
     if (sc.status == ST_CAPACITY) sc.status = ST_OK;
     if (!cuda_ok(cudaMemcpyAsync(b.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, s), err, "status")) return ST_CUDA;
-    const int cells_blocks = std::min(1024, (b.n_cells + 255) / 256);
     const int slot_blocks = std::min(1024, (b.nslots + 255) / 256);
-    k_grid_clear<<<cells_blocks, 256, 0, s>>>(b);
+    const int nf3 = b.fine_div * b.fine_div * b.fine_div;
+    const int clear_blocks = std::min(1024, (std::max({b.n_cells, nf3, b.nslots}) + 255) / 256);
+    k_grid_clear<<<clear_blocks, 256, 0, s>>>(b);
     k_grid_fill<<<slot_blocks, 256, 0, s>>>(b);
-    k_grid_sort<<<cells_blocks, 256, 0, s>>>(b);
+    if (b.fine_div > 0) k_fine_link<<<slot_blocks, 256, 0, s>>>(b);
     if (!cuda_ok(cudaGetLastError(), err, "grid build")) return ST_CUDA;
     int st = check_status(err);
     if (st == ST_CAPACITY) return rebuild_grid(cap * 2, err);
@@ -465,7 +499,7 @@ int DeviceBox::query_batch(int n, const int *slots, const double *dirs, const do
     if (!cuda_ok(cudaGetDevice(&dev), err, "cudaGetDevice")) return ST_CUDA;
     if (!cuda_ok(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), err, "device attribute"))
         return ST_CUDA;
-    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_query_batch, kQueryThreads,
+    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_query_batch<kBatchThreads>, kBatchThreads,
                                                                sizeof(QuerySmem)),
                  err, "occupancy"))
         return ST_CUDA;
@@ -484,7 +518,7 @@ int DeviceBox::query_batch(int n, const int *slots, const double *dirs, const do
         return at;
     };
     const size_t o_next = carve(sizeof(int)), o_in = carve(sizeof(QueryIn) * size_t(n)),
-                 o_out = carve(sizeof(QueryOut) * size_t(n)), o_db = carve(8 * ncand), o_flat = carve(4 * ncand),
+                 o_out = carve(sizeof(QueryOut) * size_t(n)), o_db = carve(8 * ncand), o_key = carve(8 * ncand),
                  o_slot = carve(4 * ncand), o_order = carve(4 * ncand), o_prefix = carve(4 * ncand),
                  o_res = carve(8 * ncand), o_ij = carve(8 * ncand), o_surv = carve(sizeof(int4) * nsurv),
                  o_sres = carve(8 * nsurv);
@@ -501,7 +535,7 @@ int DeviceBox::query_batch(int n, const int *slots, const double *dirs, const do
     char *base = static_cast<char *>(batch_mem_);
     sc.next = reinterpret_cast<int *>(base + o_next);
     sc.cand_db = reinterpret_cast<double *>(base + o_db);
-    sc.cand_flat = reinterpret_cast<int *>(base + o_flat);
+    sc.cand_key = reinterpret_cast<long long *>(base + o_key);
     sc.cand_slot = reinterpret_cast<int *>(base + o_slot);
     sc.cand_order = reinterpret_cast<int *>(base + o_order);
     sc.cand_prefix = reinterpret_cast<int *>(base + o_prefix);
@@ -527,7 +561,7 @@ int DeviceBox::query_batch(int n, const int *slots, const double *dirs, const do
               cuda_ok(cudaMemsetAsync(sc.next, 0, sizeof(int), s), err, "query counter");
     if (ok) {
         cudaEventRecord(e0, s);
-        k_query_batch<<<blocks, kQueryThreads, sizeof(QuerySmem), s>>>(b, sc, n, d_in, d_out);
+        k_query_batch<kBatchThreads><<<blocks, kBatchThreads, sizeof(QuerySmem), s>>>(b, sc, n, d_in, d_out);
         cudaEventRecord(e1, s);
         ok = cuda_ok(cudaGetLastError(), err, "k_query_batch") &&
              cuda_ok(cudaMemcpyAsync(hout.data(), d_out, sizeof(QueryOut) * size_t(n), cudaMemcpyDeviceToHost, s),

@@ -13,8 +13,14 @@
 //               and an FP32 (x, y, z, r) copy used by the screening passes;
 //               merges append keep++removed at the pool top, a compaction
 //               pass reclaims space
-//   Verlet grid n_div^3 cells of slot lists kept in ascending slot order
-//               (the reference's std::set<size_t> of labels, verlet.hpp:29)
+//   Verlet grid n_div^3 cells of unordered slot lists (+ each slot's place in
+//               its list, so moves are O(1)); the reference's order inside a
+//               cell (std::set<size_t> of labels, verlet.hpp:29) is restored
+//               by the scan key (cell rank in the scan, slot)
+//   fine grid   fine_div^3 cells (fine_div > n_div) of doubly linked slot
+//               lists, used only to find the neighbours of a query faster;
+//               which neighbours count, and their order, stay the Verlet
+//               grid's
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -29,6 +35,9 @@ constexpr int kQueryThreads = 512;
 constexpr int kCellChunk = 1024;       // Verlet cells scanned per chunk
 constexpr int kMoveTile = 512;         // moving spheres staged per pass
 constexpr int kMaxSurvivorsSmem = 256; // refined pairs kept in shared memory (the rest in HBM)
+constexpr int kFineMaxCells = 4096;    // fine cells a query may visit before the Verlet cells are used
+constexpr int kFineMaxDiv = 128;       // fine cells per axis at most
+constexpr int kCullCands = 16;         // candidates whose extents cull the moving spheres
 
 // Mutable per-box scalars, in device memory.
 struct DevScalars {
@@ -65,7 +74,13 @@ struct DevBox {
     int *pool_id[2];
     float4 *pool_pos[2];
     int *cell_n;     // [n_cells]
-    int *cell_items; // [n_cells][cell_cap]
+    int *cell_items; // [n_cells][cell_cap], unordered
+    int *cell_pos;   // [nslots] index of each live slot in its cell's list
+    int fine_div;    // fine grid cells per axis (0: no fine grid)
+    double fine_step;  // fine_div / box_length
+    int *fine_head;  // [fine_div^3] first slot of each fine cell, -1 if empty
+    int *fine_next, *fine_prev;  // [nslots] list links, -1 at the ends
+    int *fine_cell;  // [nslots] fine cell of each live slot, -1 if none
     DevScalars *sc;
     // global scratch (one box handled by one block at a time)
     int4 *surv;          // survivors: candidate, i, j, unused
@@ -79,7 +94,8 @@ struct DevBox {
     int *counters;       // [8]
     // contact-query candidates (at most one per aggregate slot)
     double *cand_db;
-    int *cand_flat, *cand_slot, *cand_order, *cand_prefix;
+    long long *cand_key;  // Verlet scan position: cell rank in the scan x nslots + slot
+    int *cand_slot, *cand_order, *cand_prefix;
     unsigned long long *best_res, *best_ij;
 };
 
@@ -206,13 +222,17 @@ struct QuerySmem {
     int cell_lin[kCellChunk];
     // candidate arrays live in the machine's HBM scratch (one entry per slot at most)
     double *cand_db;
-    int *cand_flat;
+    long long *cand_key;
     int *cand_slot;
     int *cand_order;   // sorted position -> candidate
     int *cand_prefix;
     unsigned long long *best_res;
     unsigned long long *best_ij;
     float4 mov[kMoveTile];
+    short mov_sel[kMoveTile];  // moving spheres of the tile that can reach a candidate
+    float4 cand_c[kCullCands];  // candidate centre (FP32)
+    float cand_ext[kCullCands]; // candidate extent from that centre (max |q - c| + r_q)
+    int n_sel;
     int4 surv[kMaxSurvivorsSmem];
     double surv_res[kMaxSurvivorsSmem];
     int warp_tmp[32];
@@ -222,6 +242,8 @@ struct QuerySmem {
     int found_source;
     int flat_base;
     int n_refined;
+    int use_fine;     // neighbours found through the fine grid
+    int fine_lo[3], fine_n[3];
     float mov_reach;
     CellRange range;
     QueryOut out;
@@ -252,6 +274,32 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
         double mindist = rmax_src + sc->maxradius;
         Vec3 vec{dist * dir.x, dist * dir.y, dist * dir.z};
         sm.range = neighborhood_range(sp, vec, mindist, b.n_div, b.L);
+        // The fine grid finds the same neighbours when every aggregate that
+        // can pass the bounding-sphere filter lies in the fine cells visited:
+        // its centre is within rmax_src + rmax <= mindist of the path. The
+        // range is widened by 1e-6 of a fine cell, far above the rounding of
+        // these bounds and of the periodic images (~1e-13 of a cell). Used
+        // when it visits fewer cells and aggregates.
+        sm.use_fine = 0;
+        if (b.fine_div > 0) {
+            const double pos[3] = {sp.x, sp.y, sp.z}, v[3] = {vec.x, vec.y, vec.z};
+            const double hf = 1e-6 / b.fine_step;
+            double n_fine = 1.0, n_coarse = 1.0;
+            for (int l = 0; l < 3; ++l) {
+                const double lo = floor((pos[l] - mindist + dmin(v[l], 0.) - hf) * b.fine_step);
+                const double hi = floor((pos[l] + mindist + dmax(v[l], 0.) + hf) * b.fine_step);
+                const bool part = (hi - lo + 1.0 < double(b.fine_div)) && lo > -1e9 && hi < 1e9;
+                sm.fine_lo[l] = part ? int(lo) : 0;
+                sm.fine_n[l] = part ? int(hi - lo + 1.0) : b.fine_div;
+                n_fine *= double(sm.fine_n[l]);
+                n_coarse *= double(sm.range.hi[l] - sm.range.lo[l] + 1);
+            }
+            const double alive = double(sc->n_alive);
+            const double nf3 = double(b.fine_div) * double(b.fine_div) * double(b.fine_div);
+            const double cost_fine = n_fine * (1.0 + alive / nf3);
+            const double cost_coarse = n_coarse * (1.0 + alive / double(b.n_cells));
+            sm.use_fine = (n_fine <= double(kFineMaxCells)) && (cost_fine < cost_coarse);
+        }
         sm.n_cand = 0;
         sm.n_surv = 0;
         sm.found_source = 0;
@@ -269,7 +317,7 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
         sm.out.n_cand_spheres = 0;
         sm.out.n_mov = b.agg_n[src];
         sm.cand_db = b.cand_db;
-        sm.cand_flat = b.cand_flat;
+        sm.cand_key = b.cand_key;
         sm.cand_slot = b.cand_slot;
         sm.cand_order = b.cand_order;
         sm.cand_prefix = b.cand_prefix;
@@ -300,6 +348,69 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     const CellRange rg = sm.range;
     const int nx = rg.hi[0] - rg.lo[0] + 1, ny = rg.hi[1] - rg.lo[1] + 1, nz = rg.hi[2] - rg.lo[2] + 1;
     const int n_scan = nx * ny * nz;
+    // bounding-sphere filter of one neighbour; 'key' is its position in the
+    // reference's neighbour list order (Verlet cell rank in the scan, then slot)
+    auto consider = [&](int slot, long long key, float4 of) {
+        if (!capsule_hit(w, of.x, of.y, of.z, float(rmax_src) + of.w + margin)) return;
+        const double ox = A(b, AGG_X, slot), oy = A(b, AGG_Y, slot), oz = A(b, AGG_Z, slot);
+        const double orm = A(b, AGG_RMAX, slot);
+        double db = sweep_contact_distance(sp, rmax_src, Vec3{ox, oy, oz}, orm, dir, dist, b.L);
+        if (db < dist) {
+            int k = atomicAdd(&sm.n_cand, 1);  // < nslots: one entry per aggregate
+            sm.cand_db[k] = db;
+            sm.cand_key[k] = key;
+            sm.cand_slot[k] = slot;
+        }
+    };
+    int n_cells_visited = n_scan;
+    if (sm.use_fine) {
+        // walk the fine cells; keep the aggregates whose Verlet cell is in
+        // the reference's neighbourhood
+        const int fny = sm.fine_n[1], fnz = sm.fine_n[2];
+        const int n_f = sm.fine_n[0] * fny * fnz;
+        const int nf = b.fine_div, nd = b.n_div;
+        n_cells_visited = n_f;
+        int visited = 0;
+        constexpr int kHeads = 4;  // list heads fetched together per thread
+        for (int g0 = 0; g0 < n_f; g0 += kHeads * NT) {
+            int heads[kHeads];
+#pragma unroll
+            for (int u = 0; u < kHeads; ++u) {
+                const int g = g0 + u * NT + tid;
+                heads[u] = -1;
+                if (g < n_f) {
+                    const int a = g / (fny * fnz), r = g % (fny * fnz), bb = r / fnz, c = r % fnz;
+                    const int fi = periodic_cell(sm.fine_lo[0] + a, nf);
+                    const int fj = periodic_cell(sm.fine_lo[1] + bb, nf);
+                    const int fk = periodic_cell(sm.fine_lo[2] + c, nf);
+                    heads[u] = b.fine_head[(size_t(fi) * nf + fj) * nf + fk];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kHeads; ++u) {
+                int slot = heads[u];
+                for (int guard = 0; slot >= 0 && guard < b.nslots; ++guard) {
+                    // the three loads of a list entry are independent
+                    const int nxt = b.fine_next[slot];
+                    const int lin = b.agg_cell[slot];
+                    const float4 of = b.agg_f4[slot];
+                    ++visited;
+                    if (slot == src) {
+                        sm.found_source = 1;
+                    } else {
+                        const int oa = periodic_cell(lin / (nd * nd) - rg.lo[0], nd);
+                        const int ob = periodic_cell((lin / nd) % nd - rg.lo[1], nd);
+                        const int oc = periodic_cell(lin % nd - rg.lo[2], nd);
+                        if (oa < nx && ob < ny && oc < nz)
+                            consider(slot, (long long)((oa * ny + ob) * nz + oc) * b.nslots + slot, of);
+                    }
+                    slot = nxt;
+                }
+            }
+        }
+        if (visited) atomicAdd(&sm.flat_base, visited);
+        __syncthreads();
+    } else {
     for (int c0 = 0; c0 < n_scan; c0 += kCellChunk) {
         const int nch = min(kCellChunk, n_scan - c0);
         int cnt_local = 0;
@@ -346,25 +457,16 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
                 sm.found_source = 1;
                 continue;
             }
-            const float4 of = b.agg_f4[slot];
-            if (!capsule_hit(w, of.x, of.y, of.z, float(rmax_src) + of.w + margin)) continue;
-            const double ox = A(b, AGG_X, slot), oy = A(b, AGG_Y, slot), oz = A(b, AGG_Z, slot);
-            const double orm = A(b, AGG_RMAX, slot);
-            double db = sweep_contact_distance(sp, rmax_src, Vec3{ox, oy, oz}, orm, dir, dist, b.L);
-            if (db < dist) {
-                int k = atomicAdd(&sm.n_cand, 1);  // < nslots: one entry per aggregate
-                sm.cand_db[k] = db;
-                sm.cand_flat[k] = sm.flat_base + f;
-                sm.cand_slot[k] = slot;
-            }
+            consider(slot, (long long)(c0 + lo) * b.nslots + slot, b.agg_f4[slot]);
         }
         __syncthreads();
         if (tid == 0) sm.flat_base += total;
         __syncthreads();
     }
+    }
     if (tid == 0) {
         sm.out.n_scanned = sm.flat_base;
-        sm.out.n_cells = n_scan;
+        sm.out.n_cells = n_cells_visited;
         sm.out.n_candidates = sm.n_cand;
     }
     if (!sm.found_source) {
@@ -381,11 +483,11 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     // order candidates by (d_b, scan position): rank sort
     for (int k = tid; k < nc; k += NT) {
         double dk = sm.cand_db[k];
-        int fk = sm.cand_flat[k];
+        long long fk = sm.cand_key[k];
         int rank = 0;
         for (int m = 0; m < nc; ++m) {
             double dm = sm.cand_db[m];
-            rank += (dm < dk) || (dm == dk && sm.cand_flat[m] < fk);
+            rank += (dm < dk) || (dm == dk && sm.cand_key[m] < fk);
         }
         sm.cand_order[rank] = k;
     }
@@ -410,6 +512,35 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     const int off_m = b.agg_off[src];
     const int n_other = sm.cand_prefix[nc];
     if (tid == 0) sm.out.n_cand_spheres = n_other;
+    // With few candidates and a large moving aggregate, the moving spheres
+    // that cannot come within reach of any candidate's spheres are dropped
+    // before the pair loop. Each candidate's extent is measured from its own
+    // FP32 spheres (the stored r_max of a monomer can be smaller than its
+    // radius), and the test keeps two screening margins: a moving sphere
+    // whose sweep reaches a candidate sphere always reaches the ball around
+    // the candidate centre that holds all its spheres.
+    const bool cull = nc <= kCullCands && n_mov >= 8;
+    if (cull) {
+        for (int r = tid; r < nc; r += NT) {
+            sm.cand_c[r] = b.agg_f4[sm.cand_slot[sm.cand_order[r]]];
+            sm.cand_ext[r] = 0.f;
+        }
+        __syncthreads();
+        for (int f = tid; f < n_other; f += NT) {
+            int r = 0;
+            while (r + 1 < nc && sm.cand_prefix[r + 1] <= f) ++r;
+            const int cslot = sm.cand_slot[sm.cand_order[r]];
+            const float4 q = pool_pos[b.agg_off[cslot] + (f - sm.cand_prefix[r])];
+            const float4 c = sm.cand_c[r];
+            float ex = q.x - c.x, ey = q.y - c.y, ez = q.z - c.z;
+            ex -= w.L * rintf(ex * w.invL);
+            ey -= w.L * rintf(ey * w.invL);
+            ez -= w.L * rintf(ez * w.invL);
+            const float e = sqrtf(ex * ex + ey * ey + ez * ez) + q.w;
+            atomicMax(reinterpret_cast<int *>(&sm.cand_ext[r]), __float_as_int(e));  // e >= 0
+        }
+        __syncthreads();
+    }
     for (int t0 = 0; t0 < n_mov; t0 += kMoveTile) {
         const int nt = min(kMoveTile, n_mov - t0);
         float reach_local = 0.f;
@@ -435,7 +566,28 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
         }
         __syncthreads();
         const float mov_reach = sm.mov_reach + margin;
-        for (int f = tid; f < n_other; f += NT) {
+        int n_sel = nt;
+        if (cull) {
+            if (tid == 0) sm.n_sel = 0;
+            __syncthreads();
+            for (int i = tid; i < nt; i += NT) {
+                const float4 p = sm.mov[i];
+                Sweep32 wi = w;
+                wi.px = p.x;
+                wi.py = p.y;
+                wi.pz = p.z;
+                bool hit = false;
+                for (int r = 0; r < nc && !hit; ++r) {
+                    const float4 c = sm.cand_c[r];
+                    const float e = sm.cand_ext[r];
+                    hit = !(e < 0.25f * w.L) || capsule_hit(wi, c.x, c.y, c.z, p.w + e + 2.f * margin);
+                }
+                if (hit) sm.mov_sel[atomicAdd(&sm.n_sel, 1)] = short(i);
+            }
+            __syncthreads();
+            n_sel = sm.n_sel;
+        }
+        for (int f = tid; f < n_other && n_sel > 0; f += NT) {
             int lo = 0, hi = nc - 1;
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
@@ -449,7 +601,8 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
             // can any moving sphere reach this one?
             if (!capsule_hit(w, q.x, q.y, q.z, mov_reach + q.w)) continue;
             Sweep32 wi = w;
-            for (int i = 0; i < nt; ++i) {
+            for (int ii = 0; ii < n_sel; ++ii) {
+                const int i = cull ? int(sm.mov_sel[ii]) : ii;
                 const float4 p = sm.mov[i];
                 wi.px = p.x;
                 wi.py = p.y;
@@ -522,40 +675,82 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
 }
 
 // ------------------------------------------------------------- Verlet grid
-// Remove / insert a slot in a cell kept in ascending order (one thread).
+// Remove / insert a slot in a cell's unordered list (one thread, O(1)).
 __device__ __forceinline__ void cell_remove(const DevBox &b, int cell, int slot) {
-    int n = b.cell_n[cell];
+    const int n = b.cell_n[cell];
     int *items = b.cell_items + size_t(cell) * b.cell_cap;
-    int k = 0;
-    while (k < n && items[k] != slot) ++k;
-    if (k == n) return;
-    for (; k + 1 < n; ++k) items[k] = items[k + 1];
+    int k = b.cell_pos[slot];
+    if (k < 0 || k >= n || items[k] != slot) {  // not where recorded: search
+        k = 0;
+        while (k < n && items[k] != slot) ++k;
+        if (k == n) return;
+    }
+    const int last = items[n - 1];
+    items[k] = last;
+    b.cell_pos[last] = k;
+    b.cell_pos[slot] = -1;
     b.cell_n[cell] = n - 1;
 }
 __device__ __forceinline__ void cell_insert(const DevBox &b, int cell, int slot) {
-    int n = b.cell_n[cell];
+    const int n = b.cell_n[cell];
     if (n >= b.cell_cap) {
         b.sc->cell_overflow = 1;
         b.sc->status = ST_CAPACITY;
         return;
     }
-    int *items = b.cell_items + size_t(cell) * b.cell_cap;
-    int k = n;
-    while (k > 0 && items[k - 1] > slot) {
-        items[k] = items[k - 1];
-        --k;
-    }
-    items[k] = slot;
+    b.cell_items[size_t(cell) * b.cell_cap + n] = slot;
+    b.cell_pos[slot] = n;
     b.cell_n[cell] = n + 1;
 }
-// Aggregate::update_verlet (aggregat.cpp:706-717) for a new position.
+// Fine grid cell of a position (clamped into the grid).
+// Periodic fine cell index of one coordinate (a position of exactly L falls
+// in cell 0, its periodic image).
+__device__ __forceinline__ int fine_index(double x, double step, int n) {
+    double f = floor(x * step);
+    if (!(f > -1e9 && f < 1e9)) f = 0.0;
+    return periodic_cell(static_cast<int>(f), n);
+}
+__device__ __forceinline__ int fine_cell_of(const DevBox &b, Vec3 p) {
+    const int n = b.fine_div;
+    const int ix = fine_index(p.x, b.fine_step, n);
+    const int iy = fine_index(p.y, b.fine_step, n);
+    const int iz = fine_index(p.z, b.fine_step, n);
+    return (ix * n + iy) * n + iz;
+}
+// Take a slot out of its fine cell's list / put it at the head of one (one thread).
+__device__ __forceinline__ void fine_unlink(const DevBox &b, int slot) {
+    const int c = b.fine_cell[slot];
+    if (c < 0) return;
+    const int p = b.fine_prev[slot], n = b.fine_next[slot];
+    if (p >= 0) b.fine_next[p] = n; else b.fine_head[c] = n;
+    if (n >= 0) b.fine_prev[n] = p;
+    b.fine_cell[slot] = -1;
+}
+__device__ __forceinline__ void fine_link(const DevBox &b, int slot, int c) {
+    const int n = b.fine_head[c];
+    b.fine_next[slot] = n;
+    b.fine_prev[slot] = -1;
+    if (n >= 0) b.fine_prev[n] = slot;
+    b.fine_head[c] = slot;
+    b.fine_cell[slot] = c;
+}
+// Aggregate::update_verlet (aggregat.cpp:706-717) for a new position, and
+// the same move in the fine grid.
 __device__ __forceinline__ void regrid(const DevBox &b, int slot) {
-    int c = cell_of(b, agg_pos(b, slot));
+    const Vec3 p = agg_pos(b, slot);
+    int c = cell_of(b, p);
     int old = b.agg_cell[slot];
     if (c != old) {
         cell_remove(b, old, slot);
         cell_insert(b, c, slot);
         b.agg_cell[slot] = c;
+    }
+    if (b.fine_div > 0) {
+        const int fc = fine_cell_of(b, p);
+        if (fc != b.fine_cell[slot]) {
+            fine_unlink(b, slot);
+            fine_link(b, slot, fc);
+        }
     }
 }
 

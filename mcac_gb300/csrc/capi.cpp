@@ -20,6 +20,7 @@
 #include "host_box.hpp"
 #include "physics.hpp"
 #include "static_query.hpp"
+#include "host_parallel.hpp"
 
 struct mcacg_box {
     std::unique_ptr<mcacg::HostBox> impl;
@@ -470,16 +471,9 @@ int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_s
         std::vector<mcacg::HostState> states(static_cast<size_t>(n_boxes));
         std::vector<int> rcs(static_cast<size_t>(n_boxes), 0);
         std::vector<std::string> errs(static_cast<size_t>(n_boxes));
-        std::atomic<int> next{0};
-        unsigned nthreads = std::max(1u, std::min(std::thread::hardware_concurrency(), unsigned(n_boxes)));
-        std::vector<std::thread> pool;
-        for (unsigned t = 0; t < nthreads; ++t)
-            pool.emplace_back([&] {
-                for (int i = next++; i < n_boxes; i = next++)
-                    rcs[size_t(i)] = mcacg::init_random_state_private(ps[size_t(i)], &states[size_t(i)],
-                                                                      &errs[size_t(i)]);
-            });
-        for (auto &th : pool) th.join();
+        mcacg::parallel_for(n_boxes, [&](int i) {
+            rcs[size_t(i)] = mcacg::init_random_state_private(ps[size_t(i)], &states[size_t(i)], &errs[size_t(i)]);
+        });
         for (int i = 0; i < n_boxes; ++i)
             if (rcs[size_t(i)] != 0) return fail(rcs[size_t(i)], "box " + std::to_string(i) + ": " + errs[size_t(i)]);
         std::unique_ptr<mcacg_batch> b(new mcacg_batch());
@@ -499,13 +493,16 @@ int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state
         *batch = nullptr;
         std::vector<mcacg_params> ps(params, params + n_boxes);
         std::vector<mcacg::HostState> hs(static_cast<size_t>(n_boxes));
-        std::string err;
-        for (int i = 0; i < n_boxes; ++i) {
-            int rc = mcacg::state_to_host(states[i], &hs[size_t(i)], &err);
-            if (rc != 0) return fail(rc, "box " + std::to_string(i) + ": " + err);
+        std::vector<int> rcs(static_cast<size_t>(n_boxes), 0);
+        std::vector<std::string> errs(static_cast<size_t>(n_boxes));
+        mcacg::parallel_for(n_boxes, [&](int i) {
+            rcs[size_t(i)] = mcacg::state_to_host(states[i], &hs[size_t(i)], &errs[size_t(i)]);
             ps[size_t(i)].box_length = states[i].box_length;
             ps[size_t(i)].n_verlet_divisions = states[i].n_verlet_divisions;
-        }
+        });
+        for (int i = 0; i < n_boxes; ++i)
+            if (rcs[size_t(i)] != 0) return fail(rcs[size_t(i)], "box " + std::to_string(i) + ": " + errs[size_t(i)]);
+        std::string err;
         std::unique_ptr<mcacg_batch> b(new mcacg_batch());
         int rc = mcacg::BatchRunner::create(ps, std::move(hs), cuda_stream, &b->impl, &err);
         if (rc != 0) return finish(rc, err);
@@ -582,6 +579,57 @@ int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state)
     });
 }
 
+int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_boxes) {
+    return guarded([&] {
+        if (!batch || !states || n_boxes != batch->impl->size()) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
+        std::vector<int> rcs(static_cast<size_t>(n_boxes), 0);
+        std::vector<std::string> errs(static_cast<size_t>(n_boxes));
+        std::vector<double> times;
+        std::string err;
+        int rc = batch->impl->times(&times, &err);
+        if (rc != 0) return finish(rc, err);
+        mcacg::parallel_for(n_boxes, [&](int i) {
+            mcacg::HostState st;
+            rcs[size_t(i)] = batch->impl->box(i).download(&st, &errs[size_t(i)]);
+            if (rcs[size_t(i)] != 0) return;
+            st.time = times[size_t(i)];
+            rcs[size_t(i)] = store_host_state(st, &states[i], &errs[size_t(i)]);
+        });
+        for (int i = 0; i < n_boxes; ++i)
+            if (rcs[size_t(i)] != 0) return fail(rcs[size_t(i)], "box " + std::to_string(i) + ": " + errs[size_t(i)]);
+        return 0;
+    });
+}
+
+int mcacg_resident_boxes(int32_t threads, int32_t *boxes) {
+    return guarded([&] {
+        if (!boxes) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        int n = 0;
+        std::string err;
+        int rc = mcacg::BatchRunner::resident_boxes(threads, &n, &err);
+        if (rc != 0) return finish(rc, err);
+        *boxes = n;
+        return 0;
+    });
+}
+
+int mcacg_batch_set_threads(mcacg_batch *batch, int32_t threads) {
+    return guarded([&] {
+        if (!batch) return fail(MCACG_ERR_BAD_ARGUMENT, "null batch");
+        if (batch->impl->set_threads(threads) != 0)
+            return fail(MCACG_ERR_BAD_ARGUMENT, "threads per box must be 0, 64, 128, 256 or 512");
+        return 0;
+    });
+}
+
+int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads) {
+    return guarded([&] {
+        if (!batch || !threads) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *threads = batch->impl->threads();
+        return 0;
+    });
+}
+
 int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out) {
     return guarded([&] {
         if (!batch || !out) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
@@ -602,6 +650,10 @@ int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out) {
             out->refined += x.refined;
             out->merged_spheres += x.merged_spheres;
             out->merge_pairs += x.merge_pairs;
+            out->cycles_pick += x.cyc_pick;
+            out->cycles_query += x.cyc_query;
+            out->cycles_move += x.cyc_move;
+            out->cycles_merge += x.cyc_merge;
         }
         return 0;
     });

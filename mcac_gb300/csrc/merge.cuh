@@ -5,7 +5,8 @@
 // The reference accumulates every aggregate sum sequentially in sphere-list
 // order. To stay bit-identical the per-sphere terms are formed in parallel
 // (one rounding each, as in the reference) and each sum is then accumulated
-// in list order by one thread; distinct sums run on distinct warps. The
+// in list order by one thread; the seven sums run on seven lanes of the
+// first warp, in step (any block size of 32 threads or more works). The
 // O(n^2) intra-aggregate contact search is screened in FP32 and refined in
 // FP64; its pairs are put back in (i, j) order before they are summed.
 #pragma once
@@ -335,9 +336,8 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
     }
     __syncthreads();
     {
-        // seven independent ordered sums, one per warp
-        const int wid = tid >> 5, lane = tid & 31;
-        if (lane == 0 && wid < 7) sm.sums[wid] = ordered_sum(wv + size_t(wid) * W, n);
+        // seven independent ordered sums, one per lane of the first warp
+        if (tid < 7) sm.sums[tid] = ordered_sum(wv + size_t(tid) * W, n);
         if (tid == 0) {
             // overlapping: sequential over (i, j)-ordered pairs
             double ov = 0.0;
@@ -419,6 +419,7 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
         b.agg_f4[keep] = make_float4(float(x), float(y), float(z), float(rmax));
         regrid(b, keep);
         cell_remove(b, b.agg_cell[removed], removed);
+        if (b.fine_div > 0) fine_unlink(b, removed);
         if (rmax > sc->maxradius) sc->maxradius = rmax;
         out->merged = 1;
         out->status = ST_OK;

@@ -47,7 +47,10 @@ struct RunState {
     // work counters of the contact queries and merges (algorithmic bytes)
     long long c_queries, c_mov, c_scanned, c_cells, c_candidates, c_cand_spheres, c_refined;
     long long c_merged_spheres, c_merge_pairs;
+    // SM clock cycles spent by the block in each phase of the step
+    long long cyc_pick, cyc_query, cyc_move, cyc_merge;
 };
+static_assert(sizeof(RunState) % sizeof(int) == 0, "RunState is copied as ints");
 
 struct BoxRun {
     DevBox box;
@@ -165,7 +168,9 @@ __device__ inline bool block_mc_step(const BoxRun &R, RunSmem &sm) {
     const int tid = threadIdx.x;
     const DevBox &b = R.box;
     RunState &st = *R.st;
+    long long t_phase = 0;
     if (tid == 0) {
+        t_phase = clock64();
         sm.stop = st.finished || st.status != ST_OK;
         if (!sm.stop && run_finished(R, st, b.sc->n_alive)) {
             st.finished = 1;
@@ -198,6 +203,11 @@ __device__ inline bool block_mc_step(const BoxRun &R, RunSmem &sm) {
     }
     __syncthreads();
     if (sm.stop) return false;
+    if (tid == 0) {
+        const long long t = clock64();
+        st.cyc_pick += t - t_phase;
+        t_phase = t;
+    }
     const int slot = sm.slot;
     const Vec3 dir{sm.dir[0], sm.dir[1], sm.dir[2]};
     if (R.lim.with_collisions) {
@@ -227,9 +237,17 @@ __device__ inline bool block_mc_step(const BoxRun &R, RunSmem &sm) {
     }
     __syncthreads();
     if (sm.stop) return false;
+    if (tid == 0) {
+        const long long t = clock64();
+        st.cyc_query += t - t_phase;
+        t_phase = t;
+    }
     const int ms = sm.ms, os = sm.os, oslot = sm.oslot;
     block_translate(b, slot, Vec3{dir.x * sm.move, dir.y * sm.move, dir.z * sm.move}, sm.refpos);
     if (tid == 0) {
+        const long long t = clock64();
+        st.cyc_move += t - t_phase;
+        t_phase = t;
         double dt = sm.dt * (sm.move / sm.full + 0.0);
         A(b, AGG_TIME, slot) += dt;
         st.time = st.time + dt;
@@ -269,6 +287,7 @@ __device__ inline bool block_mc_step(const BoxRun &R, RunSmem &sm) {
         }
     }
     if (tid == 0) {
+        st.cyc_merge += clock64() - t_phase;
         st.steps += 1;
         if (sm.merged) {
             st.events += 1;

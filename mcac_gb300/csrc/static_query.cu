@@ -12,7 +12,7 @@
 // routine on this path.
 //
 // Limits: at most kStaticMaxQueries queries per call; a box whose candidate
-// lists (40 bytes per aggregate slot per block) do not fit the array even
+// lists (44 bytes per aggregate slot per block) do not fit the array even
 // for one block is refused; fewer blocks run concurrently than on the
 // allocating path when the box is large.
 //
@@ -57,7 +57,7 @@ struct StaticScratch {
     size_t stride;  // candidate entries per block (nslots + 1)
     char *blocks;   // per-block slices
     size_t block_bytes;
-    size_t o_flat, o_slot, o_order, o_prefix, o_res, o_ij, o_surv, o_sres;
+    size_t o_key, o_slot, o_order, o_prefix, o_res, o_ij, o_surv, o_sres;
 };
 
 // Slot of the live aggregate with the given label: labels are the ranks of
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_static(DevBox b, Static
     __shared__ int warp_tmp[32];
     char *mine = s.blocks + size_t(blockIdx.x) * s.block_bytes;
     b.cand_db = reinterpret_cast<double *>(mine);
-    b.cand_flat = reinterpret_cast<int *>(mine + s.o_flat);
+    b.cand_key = reinterpret_cast<long long *>(mine + s.o_key);
     b.cand_slot = reinterpret_cast<int *>(mine + s.o_slot);
     b.cand_order = reinterpret_cast<int *>(mine + s.o_order);
     b.cand_prefix = reinterpret_cast<int *>(mine + s.o_prefix);
@@ -203,8 +203,8 @@ int query_batch_static(DeviceBox &dev, int n_alive, int n, const int64_t *source
     off += round256(sizeof(mcacg_contact) * size_t(n));
     s.stride = size_t(dev.nslots()) + 1;
     size_t bo = round256(8 * s.stride);
-    s.o_flat = bo;
-    bo += round256(4 * s.stride);
+    s.o_key = bo;
+    bo += round256(8 * s.stride);
     s.o_slot = bo;
     bo += round256(4 * s.stride);
     s.o_order = bo;

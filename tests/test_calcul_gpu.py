@@ -120,3 +120,14 @@ def test_partly_tied_weights_run_matches_oracle():
         assert digest(box.store()) == digest(ob.store())
     assert len(chosen) == 40
     assert st.events > 100
+
+
+@pytest.mark.gpu
+def test_dense_box_run_matches_oracle_step_by_step():
+    """100,000 monomers: the fine neighbour grid is used and kept up to date
+    through translations and merges; 4,000 steps stay the oracle's."""
+    ini = ("[monomers]\nnumber = 100000\nmean_diameter = 30\ndispersion_diameter = 1.25\n"
+           "initialisation_mode = lognormal\n[environment]\nvolume_fraction = 1e-3\ntemperature = 1700\n"
+           "[limits]\nnumber_of_aggregates = 100\n[numerics]\nrandom_seed = 1\nwith_domain_duplication = false\n")
+    st = compare_runs(ini, max_steps=4000)
+    assert st.events > 100

@@ -15,7 +15,7 @@ import pytest
 from conftest import load_golden
 from mcac_gb300 import AggregatList, PhysicalModel
 from mcac_gb300._lib import MCACError
-from mcac_gb300.snapshot import Snapshot
+from mcac_gb300.snapshot import A, Snapshot
 from mcac_gb300.workloads import contact_search_case
 from oracle import oracle_py as O
 
@@ -116,3 +116,44 @@ def test_contact_search_full_size_matches_oracle():
         out, ms = box.distance_to_next_contacts(case.sources, case.directions, case.distances)
     ref = check_against_oracle(case, out)
     assert (ref["ms"] >= 0).sum() > 100
+
+
+DENSE_INI = ("[monomers]\nnumber = 100000\nmean_diameter = 30\ndispersion_diameter = 1.25\n"
+             "initialisation_mode = lognormal\n[environment]\nvolume_fraction = 1e-3\ntemperature = 1700\n"
+             "[limits]\nnumber_of_aggregates = 100\n[numerics]\nrandom_seed = 1\nwith_domain_duplication = false\n")
+
+
+@pytest.mark.gpu
+def test_fine_grid_queries_match_oracle_on_dense_box():
+    """100,000 monomers, 100 per Verlet cell: neighbours are found through
+    the fine grid (few aggregates visited per query), and the answers are
+    still the oracle's, bit for bit. Queries four times as long mix both
+    ways of finding neighbours."""
+    from mcac_gb300 import init_state
+    from mcac_gb300.workloads import random_directions
+    pm = PhysicalModel(text=DENSE_INI)
+    snap = init_state(pm).to_snapshot()
+    rng = np.random.Generator(np.random.PCG64(7))
+    src = rng.integers(0, snap.na, 3000).astype(np.int64)
+    dirs = random_directions(rng, 3000)
+    lpm = snap.aggregates[A["lpm"], src]
+    ob = O.OracleBox(DENSE_INI, snap)
+    with AggregatList(pm, snap) as box:
+        for scale in (1.0, 4.0):
+            dist = scale * lpm
+            box.set_profiling(True)
+            out, _ = box.distance_to_next_contacts(src, dirs, dist)
+            prof = box.take_profile()
+            box.set_profiling(False)
+            if scale == 1.0:
+                # the Verlet cells alone hold ~1,000 aggregates per query
+                assert prof["scanned"] / prof["queries"] < 200
+            for k in range(200):
+                one = box.distance_to_next_contact(int(src[k]), dirs[k], float(dist[k]))
+                assert bits(one.distance) == bits(out["distance"][k])
+            for k in range(len(src)):
+                c = ob.distance_to_next_contact(src[k], dirs[k], dist[k])
+                assert bits(c.distance) == bits(out["distance"][k]), (scale, k)
+                assert (c.moving_sphere, c.other_sphere, c.other_aggregate) == (
+                    out["moving_sphere"][k], out["other_sphere"][k], out["other_aggregate"][k]), (scale, k)
+            assert (out["moving_sphere"] >= 0).sum() > (20 if scale == 1.0 else 50)

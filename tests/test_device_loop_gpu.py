@@ -87,10 +87,13 @@ def test_batch_keeps_valid_states():
         st = b.stats()
         assert np.all(st["status"] == 0)
         assert np.all(st["steps"] > 0)
+        every = b.store_all()
         for k in range(len(models)):
             snap = b.store(k)
             assert snap.na == models[k].params.n_monomeres - st["events"][k]
             check_state(snap)
+            assert np.array_equal(every[k].spheres.view(np.int64), snap.spheres.view(np.int64))
+            assert np.array_equal(every[k].members, snap.members) and every[k].time == snap.time
 
 
 @pytest.mark.gpu
@@ -176,3 +179,25 @@ def test_ensemble_statistics_match_oracle():
     assert abs(dg - dc) < 0.15, (dg, dc)     # fractal dimension
     assert abs(np.log(kg / kc)) < 0.3, (kg, kc)  # prefactor
     assert abs(mg / mc - 1) < 0.1, (mg, mc)
+
+
+@pytest.mark.gpu
+def test_results_do_not_depend_on_threads_per_box():
+    models = [PhysicalModel(text=small_ini(n, 70 + k, mode="lognormal", disp=1.3, fv=4e-3))
+              for k, n in enumerate([300, 650, 1200])]
+    snaps = {}
+    for nt in (64, 128, 256, 512):
+        with Batch(models) as b:
+            b.threads = nt
+            b.run(max_steps=3000, steps_per_launch=1000)
+            assert b.threads == nt
+            assert np.all(b.stats()["status"] == 0)
+            snaps[nt] = [b.store(k) for k in range(len(models))]
+    for nt in (64, 128, 512):
+        for s1, s2 in zip(snaps[nt], snaps[256]):
+            assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
+            assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64))
+            assert np.array_equal(s1.members, s2.members)
+    with Batch(models[:1]) as b:
+        with pytest.raises(Exception):
+            b.threads = 96

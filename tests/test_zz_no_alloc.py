@@ -57,7 +57,7 @@ def test_static_scratch_limits():
 
 @pytest.mark.gpu
 def test_static_scratch_refuses_a_box_too_large_for_it():
-    # 1,000,000 aggregate slots need 40 MB of candidate lists per block
+    # 1,000,000 aggregate slots need 44 MB of candidate lists per block
     from mcac_gb300 import PhysicalModel, synthetic_state
     from mcac_gb300.workloads import contact_search_ini
     pm = PhysicalModel(text=contact_search_ini(1_000_000, seed=3, sigma_geo=1.25, volume_fraction=1e-3))

@@ -512,7 +512,8 @@ def run_ensemble(args, rank: int, world: int) -> dict | None:
     t0 = time.perf_counter()
     kernel_ms, launches = 0.0, 0
     while True:
-        batch.run(max_steps=args.mc_steps, steps_per_launch=args.mc_steps)
+        # each box as fast as it goes; finish times read every second
+        batch.run_timed(1000.0)
         ms, nl = batch.last_run()
         kernel_ms += ms
         launches += nl
@@ -530,6 +531,23 @@ def run_ensemble(args, rank: int, world: int) -> dict | None:
     failed = int((st["status"] != 0).sum())
     work = batch.work()
     threads_used = batch.threads
+    # where the boxes with the most device time spend it
+    box_work = [batch.box_work(k) for k in range(len(models))]
+    box_cycles = np.array([sum(bw[c] for c in ("cycles_pick", "cycles_query", "cycles_move", "cycles_merge"))
+                           for bw in box_work], dtype=np.float64)
+    order = np.argsort(box_cycles)[::-1][:8]
+    slowest = []
+    for k in order:
+        bw = box_work[int(k)]
+        q = max(1, bw["queries"])
+        cyc = sum(bw[c] for c in ("cycles_pick", "cycles_query", "cycles_move", "cycles_merge"))
+        slowest.append({"box": int(k), "n_monomers": int(models[k].params.n_monomeres),
+                        "aggregates_left": int(st["n_aggregates"][k]), "steps": int(st["steps"][k]),
+                        "done_s": None if not np.isfinite(done_at[k]) else float(done_at[k]),
+                        "cycles_per_step": cyc / q, "device_s": cyc / 2.07e9, "phase_share": phase_share(bw),
+                        "per_query": {f: bw[f] / q for f in ("mov_spheres", "scanned", "cells", "candidates",
+                                                             "cand_spheres", "refined")},
+                        "per_merge": {f: bw[f] / max(1, bw["merges"]) for f in ("merged_spheres", "merge_pairs")}})
     batch.close()
     vals = torch.tensor([wall, float(steps), float(n_done), kernel_ms / 1000.0], device="cuda",
                         dtype=torch.float64)
@@ -548,7 +566,8 @@ def run_ensemble(args, rank: int, world: int) -> dict | None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": ENS_WORKLOAD, "boxes": args.boxes, "finished": n_done, "failed": failed,
                    "wall_s": wall, "cap_s": args.cap_seconds, "setup_s": round(setup_s, 2),
-                   "mc_steps_per_launch": args.mc_steps, "threads_per_box": threads_used,
+                   "launches": "at most 200 ms each, every box doing as many steps as fit",
+                   "threads_per_box": threads_used,
                    "time_to_finish_s": {q: float(np.quantile(fin_times, p)) for q, p in
                                         (("p50", 0.5), ("p90", 0.9), ("max", 1.0))} if len(fin_times) else None},
         "mc_steps_per_s": steps / wall,
@@ -557,6 +576,7 @@ def run_ensemble(args, rank: int, world: int) -> dict | None:
         "gpu_launches": launches,
         "work": work,
         "phase_share": phase_share(work),
+        "slowest_boxes": slowest,
     }
     if not args.no_cpu_baseline:
         res["cpu_baseline"] = ensemble_cpu_sample(inis, args.cpu_seconds)
@@ -631,11 +651,14 @@ def run_serve(args, rank: int, world: int) -> dict | None:
     stream = torch.cuda.current_stream()
     reqs = serve_requests(args.serve_seconds, args.rate, args.serve_nmax, seed=5000 + rank)
     models = [PhysicalModel(text=ini) for _, ini, _ in reqs]
-    capacity = resident_boxes(256)
+    threads = args.threads or 64
+    capacity = resident_boxes(threads)
     budget = int(0.5 * torch.cuda.get_device_properties(dev).total_memory)
     lat, steps_done, finished = [], 0, 0
     sampler = ClockSampler(dev)
     with Server(capacity=capacity, memory_budget=budget, stream=stream.cuda_stream) as srv:
+        srv.set_threads(threads)
+        srv.set_epoch_ms(args.epoch_ms)
         sampler.start()
         t0 = time.perf_counter()
         nxt = 0
@@ -669,8 +692,9 @@ def run_serve(args, rank: int, world: int) -> dict | None:
         "latency_s": {"p50": q(0.5), "p90": q(0.9), "p99": q(0.99), "max": q(1.0)},
         "config": {"workload": SERVE_WORKLOAD, "rate_per_s": args.rate, "arrival_seconds": args.serve_seconds,
                    "n_max": args.serve_nmax, "requests": len(reqs), "completed": int(len(lat)),
-                   "finished_to_criterion": finished, "capacity_slots": capacity,
-                   "memory_budget_bytes": budget, "epoch_steps": args.epoch_steps, "wall_s": wall,
+                   "finished_to_criterion": finished, "capacity_slots": capacity, "threads_per_box": threads,
+                   "memory_budget_bytes": budget, "epoch_steps": args.epoch_steps, "epoch_ms": args.epoch_ms,
+                   "wall_s": wall,
                    "surface_growth_requests": int(sum(g for _, _, g in reqs)),
                    "surface_growth": "not in the device loop: the requests drawn with surface growth run without it"},
         "throughput": {"runs_per_s": len(lat) / wall, "mc_steps_per_s": steps_done / wall},
@@ -720,7 +744,8 @@ def main() -> int:
     ap.add_argument("--rate", type=float, default=50.0, help="serving arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=30.0, help="serving arrival window")
     ap.add_argument("--serve-nmax", type=int, default=5000, help="serving: largest request (monomers)")
-    ap.add_argument("--epoch-steps", type=int, default=1000, help="serving: MC steps per box per epoch")
+    ap.add_argument("--epoch-steps", type=int, default=100000, help="serving: most MC steps per box per epoch")
+    ap.add_argument("--epoch-ms", type=float, default=100.0, help="serving: wall-time cap of an epoch")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

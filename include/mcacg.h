@@ -322,6 +322,11 @@ int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads);
 /* Advances every unfinished box by at most max_steps steps (<= 0: until all
  * meet their stop criteria) in kernel launches of steps_per_launch steps. */
 int mcacg_batch_run(mcacg_batch *batch, int64_t max_steps, int64_t steps_per_launch);
+/* Advances every unfinished box for about wall_ms milliseconds: launches of
+ * at most 200 ms in which each box does as many steps as fit, so boxes of
+ * very different cost never wait for one another. Returns early once every
+ * box has met its stop criteria. */
+int mcacg_batch_run_timed(mcacg_batch *batch, double wall_ms);
 /* Per-box counters since creation (arrays of n_boxes). */
 int mcacg_batch_stats(mcacg_batch *batch, mcacg_run_stats *stats);
 int mcacg_batch_size(const mcacg_batch *batch, int32_t *n_boxes);
@@ -333,6 +338,8 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
 /* Work counters of all boxes since creation, summed (the query and merge
  * fields of mcacg_profile; times are left at 0). */
 int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out);
+/* The same counters for one box of the batch. */
+int mcacg_batch_box_work(mcacg_batch *batch, int32_t box, mcacg_profile *out);
 /* GPU time (CUDA events) and kernel launches of the last mcacg_batch_run. */
 int mcacg_batch_last_run(const mcacg_batch *batch, double *kernel_ms, int32_t *launches);
 
@@ -356,6 +363,13 @@ typedef struct mcacg_completion {
 int mcacg_server_create(int32_t capacity, int64_t memory_budget_bytes, void *cuda_stream, int32_t keep_final_states,
                         mcacg_server **server);
 int mcacg_server_destroy(mcacg_server *server);
+/* Threads per box of the server's epochs: 64, 128, 256 (default) or 512.
+ * With smaller blocks more slots fit on the GPU at once
+ * (mcacg_resident_boxes); results do not depend on it. */
+int mcacg_server_set_threads(mcacg_server *server, int32_t threads);
+/* Wall-time cap of one epoch in milliseconds: each box then does as many of
+ * its epoch_steps as fit (0, the default: every box does epoch_steps). */
+int mcacg_server_set_epoch_ms(mcacg_server *server, double ms);
 int mcacg_server_submit(mcacg_server *server, const mcacg_params *params, int64_t *id);
 int mcacg_server_step(mcacg_server *server, int64_t epoch_steps, int32_t *n_active, int32_t *n_pending);
 /* Moves up to 'capacity' completions (oldest first) into 'out'. */

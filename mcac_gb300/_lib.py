@@ -119,6 +119,7 @@ SIGNATURES = {
     "mcacg_batch_set_threads": [vp, i32],
     "mcacg_batch_threads": [vp, C.POINTER(i32)],
     "mcacg_batch_run": [vp, i64, i64],
+    "mcacg_batch_run_timed": [vp, f64],
     "mcacg_batch_stats": [vp, C.POINTER(RunStats)],
     "mcacg_batch_size": [vp, C.POINTER(i32)],
     "mcacg_batch_box_sizes": [vp, i32, C.POINTER(i64), C.POINTER(i64)],
@@ -126,8 +127,11 @@ SIGNATURES = {
     "mcacg_batch_store_states": [vp, C.POINTER(State), i32],
     "mcacg_batch_last_run": [vp, C.POINTER(f64), C.POINTER(i32)],
     "mcacg_batch_work": [vp, C.POINTER(Profile)],
+    "mcacg_batch_box_work": [vp, i32, C.POINTER(Profile)],
     "mcacg_server_create": [i32, i64, vp, i32, C.POINTER(vp)],
     "mcacg_server_destroy": [vp],
+    "mcacg_server_set_threads": [vp, i32],
+    "mcacg_server_set_epoch_ms": [vp, f64],
     "mcacg_server_submit": [vp, C.POINTER(Params), C.POINTER(i64)],
     "mcacg_server_step": [vp, i64, C.POINTER(i32), C.POINTER(i32)],
     "mcacg_server_poll": [vp, C.c_void_p, i32, C.POINTER(i32)],

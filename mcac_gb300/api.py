@@ -361,6 +361,11 @@ class Batch:
     def threads(self, value: int) -> None:
         check(lib().mcacg_batch_set_threads(self._b, int(value)))
 
+    def run_timed(self, wall_ms: float) -> None:
+        """Runs every unfinished box for about wall_ms of wall time, each as
+        fast as it goes (returns early when all are done)."""
+        check(lib().mcacg_batch_run_timed(self._b, float(wall_ms)))
+
     def run(self, max_steps: int = 0, steps_per_launch: int = 20000) -> None:
         check(lib().mcacg_batch_run(self._b, int(max_steps), int(steps_per_launch)))
 
@@ -373,6 +378,12 @@ class Batch:
         for i, s in enumerate(arr):
             out[i] = (s.steps, s.events, s.n_aggregates, s.time, s.finished, s.reserved)
         return out
+
+    def box_work(self, box: int) -> dict:
+        """Work counters and phase cycles of one box since creation."""
+        p = _lib.Profile()
+        check(lib().mcacg_batch_box_work(self._b, int(box), C.byref(p)))
+        return {name: getattr(p, name) for name, _ in _lib.Profile._fields_}
 
     def work(self) -> dict:
         p = _lib.Profile()
@@ -432,6 +443,14 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+    def set_threads(self, threads: int) -> None:
+        """Threads per box of the epochs (64, 128, 256 or 512)."""
+        check(lib().mcacg_server_set_threads(self._s, int(threads)))
+
+    def set_epoch_ms(self, ms: float) -> None:
+        """Wall-time cap of an epoch (0: each box does all its epoch steps)."""
+        check(lib().mcacg_server_set_epoch_ms(self._s, float(ms)))
 
     def submit(self, model: PhysicalModel) -> int:
         rid = C.c_int64()

@@ -22,9 +22,21 @@ constexpr int kRunThreads = 256;  // serving loop
 // Large blocks pay off late in a run, when few boxes are left and each holds
 // big aggregates (long pair searches and merges).
 constexpr int kRunThreadChoices[] = {64, 128, 256, 512};
+// wall time of one launch when boxes run to their stop criteria
+constexpr long long kRunLaunchBudgetNs = 200LL * 1000 * 1000;
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Each block advances its box by at most max_steps steps; with budget_ns > 0
+// it also stops after that much wall time, so that boxes of very different
+// cost do not wait for one another between launches.
 template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n, long long max_steps) {
+__global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n, long long max_steps,
+                                                      long long budget_ns) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RunSmem &sm = *reinterpret_cast<RunSmem *>(smem_raw);
     __shared__ __align__(16) BoxRun R;
@@ -43,11 +55,23 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
         int *sdst = reinterpret_cast<int *>(&st);
         for (int k = threadIdx.x; k < swords; k += NT) sdst[k] = ssrc[k];
     }
+    __shared__ unsigned long long t_start;
+    __shared__ int out_of_time;
     __syncthreads();
-    if (threadIdx.x == 0) R.st = &st;
+    if (threadIdx.x == 0) {
+        R.st = &st;
+        t_start = global_ns();
+        out_of_time = 0;
+    }
     __syncthreads();
-    for (long long s = 0; s < max_steps; ++s)
+    for (long long s = 0; s < max_steps; ++s) {
+        if (budget_ns > 0 && (s & 15) == 0) {
+            if (threadIdx.x == 0) out_of_time = global_ns() - t_start >= (unsigned long long)budget_ns;
+            __syncthreads();
+            if (out_of_time) break;
+        }
         if (!block_mc_step(R, sm)) break;
+    }
     __syncthreads();
     {
         const int swords = int(sizeof(RunState) / sizeof(int));
@@ -78,12 +102,13 @@ cudaError_t prepare_all_k_run() {
     if (e == cudaSuccess) e = prepare_k_run<512>();
     return e;
 }
-cudaError_t launch_k_run(int nt, int grid, cudaStream_t s, const BoxRun *runs, int n, long long steps) {
+cudaError_t launch_k_run(int nt, int grid, cudaStream_t s, const BoxRun *runs, int n, long long steps,
+                         long long budget_ns = 0) {
     switch (nt) {
-        case 64: k_run<64><<<grid, 64, sizeof(RunSmem), s>>>(runs, n, steps); break;
-        case 128: k_run<128><<<grid, 128, sizeof(RunSmem), s>>>(runs, n, steps); break;
-        case 512: k_run<512><<<grid, 512, sizeof(RunSmem), s>>>(runs, n, steps); break;
-        default: k_run<256><<<grid, 256, sizeof(RunSmem), s>>>(runs, n, steps); break;
+        case 64: k_run<64><<<grid, 64, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
+        case 128: k_run<128><<<grid, 128, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
+        case 512: k_run<512><<<grid, 512, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
+        default: k_run<256><<<grid, 256, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
     }
     return cudaGetLastError();
 }
@@ -383,8 +408,11 @@ int BatchRunner::run(int64_t max_steps, int64_t chunk, std::string *err) {
         int64_t steps = max_steps > 0 ? std::min(chunk, max_steps - done) : chunk;
         if (steps <= 0) break;
         const int nt = threads_ ? threads_ : 256;
+        // to the stop criteria: launches of a fixed wall time, each box
+        // doing as many steps as it can in it
+        const long long budget = max_steps <= 0 ? kRunLaunchBudgetNs : 0;
         cudaEventRecord(e0, s);
-        if (!ok_cuda(launch_k_run(nt, n, s, runs, n, (long long)steps), err, "k_run")) {
+        if (!ok_cuda(launch_k_run(nt, n, s, runs, n, (long long)steps, budget), err, "k_run")) {
             rc = ST_CUDA;
             break;
         }
@@ -417,6 +445,70 @@ int BatchRunner::run(int64_t max_steps, int64_t chunk, std::string *err) {
         }
     }
     last_ms_ = ms_total + ms_tune;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+int BatchRunner::run_timed(double wall_ms, std::string *err) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    const int n = int(boxes_.size());
+    const BoxRun *runs = static_cast<const BoxRun *>(runs_dev_);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto elapsed_ms = [&] {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    };
+    launches_ = 0;
+    float ms_total = 0.f;
+    int64_t done = 0;
+    auto count_active = [&](int *active) -> int {
+        std::vector<BoxRunStats> st;
+        int r = stats(&st, err);
+        if (r != ST_OK) return r;
+        int a = 0;
+        for (const auto &x : st) a += !(x.finished || x.status != ST_OK);
+        *active = a;
+        return ST_OK;
+    };
+    int active = 0;
+    int rc = count_active(&active);
+    if (rc != ST_OK) return rc;
+    if (auto_threads_ && (threads_ == 0 || active * 2 <= tuned_active_) && active > 0) {
+        tuned_active_ = active;
+        rc = tune(0, &done, &ms_total, err);
+        if (rc != ST_OK) return rc;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    while (active > 0) {
+        const double left = wall_ms - elapsed_ms();
+        if (left <= 0.0) break;
+        const long long budget = std::max(1LL, std::min(kRunLaunchBudgetNs, (long long)(left * 1e6)));
+        const int nt = threads_ ? threads_ : 256;
+        cudaEventRecord(e0, s);
+        if (!ok_cuda(launch_k_run(nt, n, s, runs, n, 1LL << 50, budget), err, "k_run")) {
+            rc = ST_CUDA;
+            break;
+        }
+        cudaEventRecord(e1, s);
+        if (!ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {
+            rc = ST_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms_total += ms;
+        ++launches_;
+        rc = count_active(&active);
+        if (rc != ST_OK) break;
+        if (auto_threads_ && active > 0 && active * 2 <= tuned_active_) {
+            tuned_active_ = active;
+            rc = tune(0, &done, &ms_total, err);
+            if (rc != ST_OK) break;
+        }
+    }
+    last_ms_ = ms_total;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
@@ -526,10 +618,14 @@ int Server::create(int capacity, int64_t memory_budget, void *stream, bool keep_
     if (!ok_cuda(cudaMalloc(&s->runs_dev_, sizeof(BoxRun) * size_t(capacity)), err, "cudaMalloc")) return ST_CUDA;
     if (!ok_cuda(cudaMalloc(&s->states_dev_, sizeof(RunState) * size_t(capacity)), err, "cudaMalloc")) return ST_CUDA;
     if (!ok_cuda(cudaMemset(s->runs_dev_, 0, sizeof(BoxRun) * size_t(capacity)), err, "cudaMemset")) return ST_CUDA;
-    if (!ok_cuda(cudaFuncSetAttribute(k_run<kRunThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(sizeof(RunSmem))), err, "cudaFuncSetAttribute"))
-        return ST_CUDA;
+    if (!ok_cuda(prepare_all_k_run(), err, "cudaFuncSetAttribute")) return ST_CUDA;
     *out = std::move(s);
+    return ST_OK;
+}
+
+int Server::set_threads(int threads) {
+    if (threads != 64 && threads != 128 && threads != 256 && threads != 512) return ST_BAD_ARGUMENT;
+    threads_ = threads;
     return ST_OK;
 }
 
@@ -676,11 +772,11 @@ int Server::step(int64_t epoch_steps, std::string *err) {
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, s);
-        k_run<kRunThreads><<<capacity_, kRunThreads, sizeof(RunSmem), s>>>(static_cast<const BoxRun *>(runs_dev_),
-                                                                           capacity_, (long long)epoch_steps);
+        const cudaError_t le = launch_k_run(threads_, capacity_, s, static_cast<const BoxRun *>(runs_dev_),
+                                            capacity_, (long long)epoch_steps, epoch_budget_ns_);
         ++launches_;
         cudaEventRecord(e1, s);
-        if (!ok_cuda(cudaGetLastError(), err, "k_run") || !ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {
+        if (!ok_cuda(le, err, "k_run") || !ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             return ST_CUDA;

@@ -43,6 +43,10 @@ class BatchRunner {
     // Advances every unfinished box by at most max_steps MC steps (<= 0: until
     // every box meets its stop criterion) in launches of 'chunk' steps.
     int run(int64_t max_steps, int64_t chunk, std::string *err);
+    // Runs every unfinished box for about wall_ms milliseconds of wall time
+    // (launches of at most 200 ms in which each box does as many steps as
+    // fit), returning early when all have met their stop criteria.
+    int run_timed(double wall_ms, std::string *err);
     int stats(std::vector<BoxRunStats> *out, std::string *err);
     int download(int box, HostState *st, std::string *err);
     // Physical time of every box.
@@ -91,6 +95,10 @@ class Server {
     int submit(const mcacg_params &p, int64_t *id, std::string *err);
     // admit, one kernel epoch of at most 'epoch_steps' steps per box, retire
     int step(int64_t epoch_steps, std::string *err);
+    // Threads per box of the epochs (64, 128, 256 or 512; default 256).
+    int set_threads(int threads);
+    // Wall-time cap of an epoch in milliseconds (0: epochs end by steps only).
+    void set_epoch_ms(double ms) { epoch_budget_ns_ = ms > 0 ? (long long)(ms * 1e6) : 0; }
     int n_active() const;
     int n_pending() const { return int(pending_.size()); }
     std::vector<Completion> poll();
@@ -118,6 +126,8 @@ class Server {
     int admit(std::string *err);
     int retire(std::string *err);
     int capacity_ = 0;
+    int threads_ = 256;
+    long long epoch_budget_ns_ = 0;  // wall-time cap of an epoch (0: steps only)
     int64_t budget_ = 0, mem_in_use_ = 0, next_id_ = 0;
     bool keep_ = false;
     void *stream_ = nullptr;

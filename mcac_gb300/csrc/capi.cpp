@@ -527,6 +527,14 @@ int mcacg_batch_run(mcacg_batch *batch, int64_t max_steps, int64_t steps_per_lau
     });
 }
 
+int mcacg_batch_run_timed(mcacg_batch *batch, double wall_ms) {
+    return guarded([&] {
+        if (!batch || !(wall_ms >= 0.0)) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
+        std::string err;
+        return finish(batch->impl->run_timed(wall_ms, &err), err);
+    });
+}
+
 int mcacg_batch_stats(mcacg_batch *batch, mcacg_run_stats *stats) {
     return guarded([&] {
         if (!batch || !stats) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
@@ -630,6 +638,26 @@ int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads) {
     });
 }
 
+namespace {
+void add_work(const mcacg::BoxRunStats &x, mcacg_profile *out) {
+    out->queries += x.queries;
+    out->merges += x.events;
+    out->translates += x.steps;
+    out->mov_spheres += x.mov;
+    out->scanned += x.scanned;
+    out->cells += x.cells;
+    out->candidates += x.candidates;
+    out->cand_spheres += x.cand_spheres;
+    out->refined += x.refined;
+    out->merged_spheres += x.merged_spheres;
+    out->merge_pairs += x.merge_pairs;
+    out->cycles_pick += x.cyc_pick;
+    out->cycles_query += x.cyc_query;
+    out->cycles_move += x.cyc_move;
+    out->cycles_merge += x.cyc_merge;
+}
+}  // namespace
+
 int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out) {
     return guarded([&] {
         if (!batch || !out) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
@@ -638,23 +666,20 @@ int mcacg_batch_work(mcacg_batch *batch, mcacg_profile *out) {
         int rc = batch->impl->stats(&s, &err);
         if (rc != 0) return finish(rc, err);
         *out = mcacg_profile{};
-        for (const auto &x : s) {
-            out->queries += x.queries;
-            out->merges += x.events;
-            out->translates += x.steps;
-            out->mov_spheres += x.mov;
-            out->scanned += x.scanned;
-            out->cells += x.cells;
-            out->candidates += x.candidates;
-            out->cand_spheres += x.cand_spheres;
-            out->refined += x.refined;
-            out->merged_spheres += x.merged_spheres;
-            out->merge_pairs += x.merge_pairs;
-            out->cycles_pick += x.cyc_pick;
-            out->cycles_query += x.cyc_query;
-            out->cycles_move += x.cyc_move;
-            out->cycles_merge += x.cyc_merge;
-        }
+        for (const auto &x : s) add_work(x, out);
+        return 0;
+    });
+}
+
+int mcacg_batch_box_work(mcacg_batch *batch, int32_t box, mcacg_profile *out) {
+    return guarded([&] {
+        if (!batch || !out || box < 0 || box >= batch->impl->size()) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
+        std::vector<mcacg::BoxRunStats> s;
+        std::string err;
+        int rc = batch->impl->stats(&s, &err);
+        if (rc != 0) return finish(rc, err);
+        *out = mcacg_profile{};
+        add_work(s[size_t(box)], out);
         return 0;
     });
 }
@@ -677,6 +702,23 @@ int mcacg_server_create(int32_t capacity, int64_t memory_budget_bytes, void *cud
 int mcacg_server_destroy(mcacg_server *server) {
     return guarded([&] {
         delete server;
+        return 0;
+    });
+}
+
+int mcacg_server_set_epoch_ms(mcacg_server *server, double ms) {
+    return guarded([&] {
+        if (!server || !(ms >= 0.0)) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
+        server->impl->set_epoch_ms(ms);
+        return 0;
+    });
+}
+
+int mcacg_server_set_threads(mcacg_server *server, int32_t threads) {
+    return guarded([&] {
+        if (!server) return fail(MCACG_ERR_BAD_ARGUMENT, "null server");
+        if (server->impl->set_threads(threads) != 0)
+            return fail(MCACG_ERR_BAD_ARGUMENT, "threads per box must be 64, 128, 256 or 512");
         return 0;
     });
 }

@@ -201,3 +201,25 @@ def test_results_do_not_depend_on_threads_per_box():
     with Batch(models[:1]) as b:
         with pytest.raises(Exception):
             b.threads = 96
+
+
+@pytest.mark.gpu
+def test_timed_runs_give_the_same_boxes():
+    """Launches cut by wall time (each box as many steps as fit) leave every
+    trajectory as it is."""
+    models = [PhysicalModel(text=small_ini(n, 80 + k, fv=5e-3, nagg=4)) for k, n in enumerate([180, 420, 260])]
+    with Batch(models) as b:
+        b.run(max_steps=0, steps_per_launch=4000)
+        ref = b.store_all()
+        ref_steps = b.stats()["steps"].copy()
+    with Batch(models) as b:
+        for _ in range(1000):
+            b.run_timed(3.0)
+            st = b.stats()
+            if np.all(st["finished"] == 1):
+                break
+        assert np.all(st["finished"] == 1) and np.all(st["status"] == 0)
+        assert np.array_equal(st["steps"], ref_steps)
+        for s1, s2 in zip(b.store_all(), ref):
+            assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
+            assert np.array_equal(s1.members, s2.members)

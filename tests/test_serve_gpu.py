@@ -69,3 +69,27 @@ def test_memory_budget_limits_concurrency():
             if seen == 4 and pending == 0 and active == 0:
                 break
         assert seen == 4 and max_active <= 1
+
+
+@pytest.mark.gpu
+def test_time_capped_epochs_give_the_same_runs():
+    """Epochs cut by wall time (each box does as many steps as fit) change
+    how far a box gets per epoch, never its trajectory."""
+    models = [PhysicalModel(text=req_ini(n, 950 + k)) for k, n in enumerate([260, 520, 380])]
+    done = {}
+    with Server(capacity=2, keep_final_states=True) as srv:
+        srv.set_epoch_ms(2.0)
+        srv.set_threads(64)
+        ids = [srv.submit(m) for m in models]
+        for _ in range(100_000):
+            active, pending = srv.step(1_000_000)
+            for c in srv.poll():
+                done[int(c["id"])] = c
+            if len(done) == len(models) and active == 0 and pending == 0:
+                break
+        finals = {rid: srv.final_state(rid) for rid in ids}
+    for k, rid in enumerate(ids):
+        with Batch([models[k]]) as b:
+            b.run(max_steps=0, steps_per_launch=5000)
+            assert int(b.stats()["steps"][0]) == int(done[rid]["steps"])
+            assert same_state(b.store(0), finals[rid])

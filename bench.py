@@ -160,7 +160,11 @@ def phase_share(prof: dict) -> dict:
     """Share of the device loop's SM cycles per phase of the MC step."""
     keys = ("cycles_pick", "cycles_query", "cycles_move", "cycles_merge")
     tot = sum(prof.get(k, 0) for k in keys)
-    return {k[7:]: (prof.get(k, 0) / tot if tot else None) for k in keys}
+    out = {k[7:]: (prof.get(k, 0) / tot if tot else None) for k in keys}
+    # the query's own split: neighbourhood + filter, pairs + walk
+    for k in ("cycles_query_scan", "cycles_query_pairs"):
+        out[k[7:]] = prof.get(k, 0) / tot if tot else None
+    return out
 
 
 def replica_seeds(n: int, first: int) -> list[int]:
@@ -276,13 +280,16 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     t = time.perf_counter()
     stats_bytes = 0
     with Batch(models, stream=stream.cuda_stream, states=states) as b2:
+        t_up = time.perf_counter() - t
         b2.threads = threads_used
         for _ in range(K):
             b2.run(max_steps=M, steps_per_launch=M)
             st2 = b2.stats()
             stats_bytes += int(st2.nbytes)
         e2e_steps = int(st2["steps"].sum())
-        outs = b2.store_all()
+        t_run = time.perf_counter() - t - t_up
+        outs = b2.store_all(raw=True)  # the final states in host arrays
+        t_down = time.perf_counter() - t - t_up - t_run
     e2e_s = time.perf_counter() - t
     out_bytes = sum(int(o.spheres.nbytes + o.sphere_label.nbytes + o.aggregates.nbytes + o.n_spheres.nbytes
                         + o.members.nbytes) for o in outs)
@@ -325,7 +332,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                                     "+ 16 B x candidate spheres + 64 B x FP64-refined pairs"},
         "e2e": {"value": e2e_all / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "bench_steps": K, "note": "host states uploaded, K bench steps with per-box statistics read back "
-                                          "after each, final states downloaded; bytes are per bench step"},
+                                          "after each, final states downloaded; bytes are per bench step",
+                "upload_s": round(t_up, 3), "steps_s": round(t_run, 3), "download_s": round(t_down, 3)},
         "gpu_launches": launches,
         "clocks": clocks,
         "work": prof,

@@ -162,6 +162,9 @@ typedef struct mcacg_profile {
      * each phase of the MC step (pick + direction, contact query,
      * translation + time, merge + pick-tree update), summed over boxes */
     int64_t cycles_pick, cycles_query, cycles_move, cycles_merge;
+    /* the query cycles split: neighbourhood + bounding-sphere filter, and
+     * candidate order + sphere-pair search + ordered walk */
+    int64_t cycles_query_scan, cycles_query_pairs;
 } mcacg_profile;
 
 typedef struct mcacg_box mcacg_box;

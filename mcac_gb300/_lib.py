@@ -69,7 +69,8 @@ class Profile(C.Structure):
     _fields_ = [("queries", i64), ("merges", i64), ("translates", i64), ("query_ms", f64), ("merge_ms", f64),
                 ("mov_spheres", i64), ("scanned", i64), ("cells", i64), ("candidates", i64),
                 ("cand_spheres", i64), ("refined", i64), ("merged_spheres", i64), ("merge_pairs", i64),
-                ("cycles_pick", i64), ("cycles_query", i64), ("cycles_move", i64), ("cycles_merge", i64)]
+                ("cycles_pick", i64), ("cycles_query", i64), ("cycles_move", i64), ("cycles_merge", i64),
+                ("cycles_query_scan", i64), ("cycles_query_pairs", i64)]
 
 
 # every exported symbol with its argument types (restype is int unless noted)

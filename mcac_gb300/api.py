@@ -395,8 +395,10 @@ class Batch:
         check(lib().mcacg_batch_last_run(self._b, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
-    def store_all(self) -> list[Snapshot]:
-        """The state of every box (one call, converted in parallel)."""
+    def store_all(self, raw: bool = False) -> list:
+        """The state of every box (one call, converted in parallel): as
+        Snapshots, or with raw=True as the filled host arrays
+        (StateBuffers), without further copies."""
         bufs = []
         for box in range(len(self.models)):
             ns, na = C.c_int64(), C.c_int64()
@@ -404,11 +406,11 @@ class Batch:
             bufs.append(StateBuffers(ns.value, max(na.value, 1)))
         arr = (_lib.State * len(bufs))(*[b.state for b in bufs])
         check(lib().mcacg_batch_store_states(self._b, arr, len(bufs)))
-        out = []
         for k, b in enumerate(bufs):
             b.state = arr[k]
-            out.append(b.to_snapshot(volsurf_method=int(self.models[k].params.volsurf_method)))
-        return out
+        if raw:
+            return bufs
+        return [b.to_snapshot(volsurf_method=int(self.models[k].params.volsurf_method)) for k, b in enumerate(bufs)]
 
     def store(self, box: int) -> Snapshot:
         ns, na = C.c_int64(), C.c_int64()

@@ -552,6 +552,8 @@ int BatchRunner::stats(std::vector<BoxRunStats> *out, std::string *err) {
         o.cyc_query = r.cyc_query;
         o.cyc_move = r.cyc_move;
         o.cyc_merge = r.cyc_merge;
+        o.cyc_qscan = r.cyc_qscan;
+        o.cyc_qpairs = r.cyc_qpairs;
     }
     return ST_OK;
 }

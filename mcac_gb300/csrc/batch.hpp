@@ -18,6 +18,7 @@ struct BoxRunStats {
     // work counters since creation
     int64_t queries, mov, scanned, cells, candidates, cand_spheres, refined, merged_spheres, merge_pairs;
     int64_t cyc_pick, cyc_query, cyc_move, cyc_merge;  // SM cycles per phase of the step
+    int64_t cyc_qscan, cyc_qpairs;                     // parts of cyc_query
 };
 
 class BatchRunner {

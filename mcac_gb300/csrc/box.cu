@@ -709,11 +709,9 @@ int DeviceBox::download(HostState *st, std::string *err) {
     if (!cuda_ok(cudaMemcpy(pool.data(), b.pool_id[sc.pool_sel], sizeof(int) * size_t(b.pool_cap), cudaMemcpyDeviceToHost),
                  err, "download"))
         return ST_CUDA;
-    st->members.assign(size_t(b.nslots), {});
-    for (int a = 0; a < b.nslots; ++a) {
-        int n = st->agg_n[size_t(a)];
-        st->members[size_t(a)].assign(pool.begin() + off[size_t(a)], pool.begin() + off[size_t(a)] + n);
-    }
+    st->members.clear();
+    st->members.reserve(size_t(b.nslots), size_t(b.ns));
+    for (int a = 0; a < b.nslots; ++a) st->members.push_list(pool.data() + off[size_t(a)], st->agg_n[size_t(a)]);
     st->maxradius = sc.maxradius;
     st->time = sc.time;
     return ST_OK;

@@ -119,6 +119,8 @@ struct QueryOut {
     int n_cells;          // Verlet cells scanned
     int n_cand_spheres;   // spheres of the candidates
     int n_mov;            // spheres of the moving aggregate
+    long long cyc_scan;   // SM cycles: neighbourhood and bounding-sphere filter
+    long long cyc_pairs;  // SM cycles: candidate order, pair search, walk
 };
 
 // Merge result returned to the host (geometry; physics done by the caller).
@@ -233,16 +235,22 @@ struct QuerySmem {
     float4 cand_c[kCullCands];  // candidate centre (FP32)
     float cand_ext[kCullCands]; // candidate extent from that centre (max |q - c| + r_q)
     int n_sel;
+    // 2D grid of a moving tile across the direction of motion
+    float grid_h, grid_half, grid_rmax, grid_span;
+    int grid_g, grid_on;
+    float basis[6];  // two unit vectors orthogonal to the direction
     int4 surv[kMaxSurvivorsSmem];
     double surv_res[kMaxSurvivorsSmem];
     int warp_tmp[32];
     float warp_f[32];
+    float warp_f2[32];
     int n_cand;
     int n_surv;
     int found_source;
     int flat_base;
     int n_refined;
     int use_fine;     // neighbours found through the fine grid
+    long long t_q0;   // clock at the start of the query
     int fine_lo[3], fine_n[3];
     float mov_reach;
     CellRange range;
@@ -316,6 +324,9 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
         sm.out.n_cells = 0;
         sm.out.n_cand_spheres = 0;
         sm.out.n_mov = b.agg_n[src];
+        sm.out.cyc_scan = 0;
+        sm.out.cyc_pairs = 0;
+        sm.t_q0 = clock64();
         sm.cand_db = b.cand_db;
         sm.cand_key = b.cand_key;
         sm.cand_slot = b.cand_slot;
@@ -466,6 +477,7 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     }
     if (tid == 0) {
         sm.out.n_scanned = sm.flat_base;
+        sm.out.cyc_scan = clock64() - sm.t_q0;
         sm.out.n_cells = n_cells_visited;
         sm.out.n_candidates = sm.n_cand;
     }
@@ -541,33 +553,150 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
         }
         __syncthreads();
     }
+    // one candidate sphere against one moving sphere of the tile: FP32
+    // capsule screen, exact FP64 swept test, the candidate's running minimum
+    auto try_pair = [&](int t0, int i, const float4 &q, int pj, int r, int jl) {
+        const float4 p = sm.mov[i];
+        Sweep32 wi = w;
+        wi.px = p.x;
+        wi.py = p.y;
+        wi.pz = p.z;
+        if (!capsule_hit(wi, q.x, q.y, q.z, p.w + q.w + margin)) return;
+        const int si = pool_id[off_m + t0 + i];
+        const int sj = pool_id[pj];
+        double res = sweep_contact_distance(sph_pos(b, si), S(b, SPH_R, si), sph_pos(b, sj), S(b, SPH_R, sj), dir,
+                                            dist, b.L);
+        atomicAdd(&sm.n_refined, 1);
+        if (!(res < CUDART_INF)) return;
+        unsigned long long key = dkey(res);
+        atomicMin(&sm.best_res[r], key);
+        int k = atomicAdd(&sm.n_surv, 1);
+        int4 rec = make_int4(r, t0 + i, jl, 0);
+        if (k < kMaxSurvivorsSmem) {
+            sm.surv[k] = rec;
+            sm.surv_res[k] = res;
+        } else if (k - kMaxSurvivorsSmem < b.surv_cap) {
+            b.surv[k - kMaxSurvivorsSmem] = rec;
+            b.surv_res[k - kMaxSurvivorsSmem] = res;
+        }
+    };
+    if (tid == 0) {
+        // basis across the motion: u1 = dir x (axis least aligned), u2 = dir x u1
+        const float ax = fabsf(w.ux), ay = fabsf(w.uy), az = fabsf(w.uz);
+        float ex = 0.f, ey = 0.f, ez = 0.f;
+        if (ax <= ay && ax <= az) ex = 1.f; else if (ay <= az) ey = 1.f; else ez = 1.f;
+        float u1x = w.uy * ez - w.uz * ey, u1y = w.uz * ex - w.ux * ez, u1z = w.ux * ey - w.uy * ex;
+        const float inv = rsqrtf(u1x * u1x + u1y * u1y + u1z * u1z);
+        u1x *= inv;
+        u1y *= inv;
+        u1z *= inv;
+        sm.basis[0] = u1x;
+        sm.basis[1] = u1y;
+        sm.basis[2] = u1z;
+        sm.basis[3] = w.uy * u1z - w.uz * u1y;
+        sm.basis[4] = w.uz * u1x - w.ux * u1z;
+        sm.basis[5] = w.ux * u1y - w.uy * u1x;
+    }
     for (int t0 = 0; t0 < n_mov; t0 += kMoveTile) {
         const int nt = min(kMoveTile, n_mov - t0);
-        float reach_local = 0.f;
+        float reach_local = 0.f, rad_local = 0.f, span_local = 0.f;
         for (int i = tid; i < nt; i += NT) {
             float4 p = pool_pos[off_m + t0 + i];
             sm.mov[i] = p;
             // distance of this moving sphere from the source centre, + radius
             float ex = p.x - w.px, ey = p.y - w.py, ez = p.z - w.pz;
+            // unreduced: member positions are stored around the centre
+            span_local = fmaxf(span_local, sqrtf(ex * ex + ey * ey + ez * ez) + p.w);
             ex -= w.L * rintf(ex * w.invL);
             ey -= w.L * rintf(ey * w.invL);
             ez -= w.L * rintf(ez * w.invL);
             reach_local = fmaxf(reach_local, sqrtf(ex * ex + ey * ey + ez * ez) + p.w);
+            rad_local = fmaxf(rad_local, p.w);
         }
-        // block max of the moving tile's extent
+        // block max of the moving tile's extent and of its radii
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) reach_local = fmaxf(reach_local, __shfl_xor_sync(0xffffffffu, reach_local, o));
-        if ((tid & 31) == 0) sm.warp_f[tid >> 5] = reach_local;
+        for (int o = 16; o > 0; o >>= 1) {
+            reach_local = fmaxf(reach_local, __shfl_xor_sync(0xffffffffu, reach_local, o));
+            rad_local = fmaxf(rad_local, __shfl_xor_sync(0xffffffffu, rad_local, o));
+            span_local = fmaxf(span_local, __shfl_xor_sync(0xffffffffu, span_local, o));
+        }
+        if ((tid & 31) == 0) {
+            sm.warp_f[tid >> 5] = reach_local;
+            sm.warp_tmp[tid >> 5] = __float_as_int(rad_local);  // non-negative: int order is float order
+            sm.warp_f2[tid >> 5] = span_local;
+        }
         __syncthreads();
         if (tid == 0) {
-            float m = 0.f;
-            for (int k = 0; k < NT / 32; ++k) m = fmaxf(m, sm.warp_f[k]);
+            float m = 0.f, rr = 0.f, sp = 0.f;
+            for (int k = 0; k < NT / 32; ++k) {
+                m = fmaxf(m, sm.warp_f[k]);
+                rr = fmaxf(rr, __int_as_float(sm.warp_tmp[k]));
+                sp = fmaxf(sp, sm.warp_f2[k]);
+            }
             sm.mov_reach = m;
+            sm.grid_span = sp;
+            // Moving spheres binned on a grid across the motion. A pair can
+            // pass the capsule test only if the candidate sphere lies within
+            // r_p + r_q + margin of the moving sphere's line of motion, so
+            // with cells at least that wide the 3 x 3 cells around the
+            // candidate's position hold every moving sphere it can meet.
+            // Used for large pair counts; at most 32 x 32 cells.
+            const bool big = nt >= 32 && (long long)nt * n_other >= 16384;
+            sm.grid_on = big;
+            if (big) {
+                const float h = (2.f * rr + margin) * 1.001f + margin;
+                const float span = 2.f * (sp + margin);
+                const int g = max(1, min(32, int(span / h) + 1));
+                sm.grid_g = g;
+                sm.grid_h = fmaxf(h, span / float(g));
+                sm.grid_half = 0.5f * float(g) * sm.grid_h;
+                sm.grid_rmax = rr;
+            }
         }
         __syncthreads();
         const float mov_reach = sm.mov_reach + margin;
+        const bool grid = sm.grid_on;
         int n_sel = nt;
-        if (cull) {
+        if (grid) {
+            // counting sort of the tile's spheres by grid cell
+            const int g = sm.grid_g, g2 = g * g;
+            const float gh = sm.grid_h, ghalf = sm.grid_half;
+            const float b0 = sm.basis[0], b1 = sm.basis[1], b2 = sm.basis[2];
+            const float b3 = sm.basis[3], b4 = sm.basis[4], b5 = sm.basis[5];
+            auto cell_of_mov = [&](int i) {
+                // member positions are stored unwrapped around the aggregate
+                // centre, so p - centre is the true offset
+                const float4 p = sm.mov[i];
+                const float ex = p.x - w.px, ey = p.y - w.py, ez = p.z - w.pz;
+                const float a1 = ex * b0 + ey * b1 + ez * b2, a2 = ex * b3 + ey * b4 + ez * b5;
+                const int c1 = min(g - 1, max(0, int(floorf((a1 + ghalf) / gh))));
+                const int c2 = min(g - 1, max(0, int(floorf((a2 + ghalf) / gh))));
+                return c1 * g + c2;
+            };
+            for (int c = tid; c <= g2; c += NT) sm.cell_prefix[c] = 0;
+            __syncthreads();
+            for (int i = tid; i < nt; i += NT) atomicAdd(&sm.cell_prefix[cell_of_mov(i)], 1);
+            __syncthreads();
+            {
+                const int per = (g2 + NT - 1) / NT, my0 = tid * per;
+                int cnt = 0;
+                for (int k = 0; k < per; ++k)
+                    if (my0 + k < g2) cnt += sm.cell_prefix[my0 + k];
+                int total;
+                int run = block_exclusive_scan(cnt, sm.warp_tmp, total);
+                for (int k = 0; k < per; ++k)
+                    if (my0 + k < g2) {
+                        const int v = sm.cell_prefix[my0 + k];
+                        sm.cell_prefix[my0 + k] = run;
+                        sm.cell_lin[my0 + k] = run;
+                        run += v;
+                    }
+                if (tid == 0) sm.cell_prefix[g2] = total;
+            }
+            __syncthreads();
+            for (int i = tid; i < nt; i += NT) sm.mov_sel[atomicAdd(&sm.cell_lin[cell_of_mov(i)], 1)] = short(i);
+            __syncthreads();
+        } else if (cull) {
             if (tid == 0) sm.n_sel = 0;
             __syncthreads();
             for (int i = tid; i < nt; i += NT) {
@@ -600,31 +729,44 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
             const float4 q = pool_pos[pj];
             // can any moving sphere reach this one?
             if (!capsule_hit(w, q.x, q.y, q.z, mov_reach + q.w)) continue;
-            Sweep32 wi = w;
-            for (int ii = 0; ii < n_sel; ++ii) {
-                const int i = cull ? int(sm.mov_sel[ii]) : ii;
-                const float4 p = sm.mov[i];
-                wi.px = p.x;
-                wi.py = p.y;
-                wi.pz = p.z;
-                if (!capsule_hit(wi, q.x, q.y, q.z, p.w + q.w + margin)) continue;
-                const int si = pool_id[off_m + t0 + i];
-                const int sj = pool_id[pj];
-                double res = sweep_contact_distance(sph_pos(b, si), S(b, SPH_R, si), sph_pos(b, sj),
-                                                    S(b, SPH_R, sj), dir, dist, b.L);
-                atomicAdd(&sm.n_refined, 1);
-                if (!(res < CUDART_INF)) continue;
-                unsigned long long key = dkey(res);
-                atomicMin(&sm.best_res[r], key);
-                int k = atomicAdd(&sm.n_surv, 1);
-                int4 rec = make_int4(r, t0 + i, jl, 0);
-                if (k < kMaxSurvivorsSmem) {
-                    sm.surv[k] = rec;
-                    sm.surv_res[k] = res;
-                } else if (k - kMaxSurvivorsSmem < b.surv_cap) {
-                    b.surv[k - kMaxSurvivorsSmem] = rec;
-                    b.surv_res[k - kMaxSurvivorsSmem] = res;
-                }
+            // the grid needs the pair's reach within a cell, and a swept zone
+            // short of the box (else the capsule test passes every pair)
+            if (grid && q.w <= sm.grid_rmax + margin &&
+                w.zmax + 2.f * (sm.grid_rmax + q.w + margin) + 8.f * margin < w.L) {
+                const int g = sm.grid_g;
+                const float mr = sm.grid_span + 2.f * margin;  // bound of |moving sphere - centre|
+                const float dx = q.x - w.px, dy = q.y - w.py, dz = q.z - w.pz;
+                // periodic shifts k the capsule test can give this sphere
+                // against a moving sphere: rint((q - p_i - c) / L), p_i within mr
+                const int kx0 = int(rintf((dx - w.cx - mr) * w.invL)), kx1 = int(rintf((dx - w.cx + mr) * w.invL));
+                const int ky0 = int(rintf((dy - w.cy - mr) * w.invL)), ky1 = int(rintf((dy - w.cy + mr) * w.invL));
+                const int kz0 = int(rintf((dz - w.cz - mr) * w.invL)), kz1 = int(rintf((dz - w.cz + mr) * w.invL));
+                for (int kx = kx0; kx <= kx1; ++kx)
+                    for (int ky = ky0; ky <= ky1; ++ky)
+                        for (int kz = kz0; kz <= kz1; ++kz) {
+                            const float ex = dx - w.L * float(kx), ey = dy - w.L * float(ky), ez = dz - w.L * float(kz);
+                            const float a1 = ex * sm.basis[0] + ey * sm.basis[1] + ez * sm.basis[2];
+                            const float a2 = ex * sm.basis[3] + ey * sm.basis[4] + ez * sm.basis[5];
+                            const int c1 = int(floorf((a1 + sm.grid_half) / sm.grid_h));
+                            const int c2 = int(floorf((a2 + sm.grid_half) / sm.grid_h));
+                            for (int x1 = max(0, c1 - 1); x1 <= min(g - 1, c1 + 1); ++x1)
+                                for (int x2 = max(0, c2 - 1); x2 <= min(g - 1, c2 + 1); ++x2) {
+                                    const int cell = x1 * g + x2;
+                                    for (int k = sm.cell_prefix[cell]; k < sm.cell_prefix[cell + 1]; ++k) {
+                                        const int i = int(sm.mov_sel[k]);
+                                        const float4 p = sm.mov[i];
+                                        // the shift the capsule test will use for this pair
+                                        // (same expression): each pair is tried once
+                                        if (int(rintf(((q.x - p.x) - w.cx) * w.invL)) != kx ||
+                                            int(rintf(((q.y - p.y) - w.cy) * w.invL)) != ky ||
+                                            int(rintf(((q.z - p.z) - w.cz) * w.invL)) != kz)
+                                            continue;
+                                        try_pair(t0, i, q, pj, r, jl);
+                                    }
+                                }
+                        }
+            } else {
+                for (int ii = 0; ii < n_sel; ++ii) try_pair(t0, (cull && !grid) ? int(sm.mov_sel[ii]) : ii, q, pj, r, jl);
             }
         }
         __syncthreads();
@@ -670,6 +812,7 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
             sm.out.other_slot = cslot;
         }
         sm.out.n_pairs_refined = sm.n_refined;
+        sm.out.cyc_pairs = clock64() - sm.t_q0 - sm.out.cyc_scan;
     }
     __syncthreads();
 }

@@ -655,6 +655,8 @@ void add_work(const mcacg::BoxRunStats &x, mcacg_profile *out) {
     out->cycles_query += x.cyc_query;
     out->cycles_move += x.cyc_move;
     out->cycles_merge += x.cyc_merge;
+    out->cycles_query_scan += x.cyc_qscan;
+    out->cycles_query_pairs += x.cyc_qpairs;
 }
 }  // namespace
 

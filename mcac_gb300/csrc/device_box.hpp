@@ -10,6 +10,39 @@ namespace mcacg {
 struct QueryOut;
 struct MergeOut;
 
+// Member lists of all aggregate slots in one array (list a is
+// ids[off[a] .. off[a+1]), in list order); built slot by slot in order.
+struct MemberLists {
+    std::vector<int> off{0};
+    std::vector<int> ids;
+    struct View {
+        const int *p;
+        int n;
+        int size() const { return n; }
+        const int &operator[](size_t k) const { return p[k]; }
+        const int *begin() const { return p; }
+        const int *end() const { return p + n; }
+    };
+    View operator[](size_t a) const { return View{ids.data() + off[a], off[a + 1] - off[a]}; }
+    size_t count() const { return off.size() - 1; }
+    void clear() {
+        off.assign(1, 0);
+        ids.clear();
+    }
+    void reserve(size_t lists, size_t items) {
+        off.reserve(lists + 1);
+        ids.reserve(items);
+    }
+    void push_list(const int *b, int n) {
+        ids.insert(ids.end(), b, b + n);
+        off.push_back(int(ids.size()));
+    }
+    void push_single(int x) {
+        ids.push_back(x);
+        off.push_back(int(ids.size()));
+    }
+};
+
 // Complete box state in host memory, by stable aggregate slot.
 struct HostState {
     int n_div = 10;
@@ -22,7 +55,7 @@ struct HostState {
     std::vector<int> sph_slot;        // [ns]
     std::vector<double> agg;          // [21][nslots]
     std::vector<int> agg_n;           // [nslots], 0 for a dead slot
-    std::vector<std::vector<int>> members;  // per slot, list order
+    MemberLists members;              // per slot, list order
 };
 
 struct QueryResult {

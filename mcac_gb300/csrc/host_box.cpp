@@ -63,9 +63,9 @@ struct PlacementGrid {
 
 }  // namespace
 
-int host_update_aggregate(const mcacg_params &p, const HostState &st, const std::vector<int> &members,
-                          double fields[21], double *maxradius) {
-    const int n = int(members.size());
+int host_update_aggregate(const mcacg_params &p, const HostState &st, MemberLists::View members, double fields[21],
+                          double *maxradius) {
+    const int n = members.size();
     // update_distances_and_overlapping (aggregat.cpp:719-764)
     double overlapping = 0.0, coordination = 0.0;
     int intersections = 0;
@@ -181,7 +181,8 @@ int init_random_state(const mcacg_params &p, HostState *st, std::string *err) {
     st->sph_slot.assign(size_t(N), -1);
     st->agg.assign(21 * size_t(N), 0.);
     st->agg_n.assign(size_t(N), 0);
-    st->members.assign(size_t(N), {});
+    st->members.clear();
+    st->members.reserve(size_t(N), size_t(N));
     PlacementGrid grid;
     grid.init(L, 4.0 * p.mean_diameter * 1e-9, N);
     for (int i = 0; i < N; ++i) {
@@ -223,7 +224,7 @@ int init_random_state(const mcacg_params &p, HostState *st, std::string *err) {
             SF(*st, SPH_RZ, i) = 0.;
             SF(*st, SPH_VOLUME, i) = volume_factor * std::pow(radius, 3);
             SF(*st, SPH_SURFACE, i) = surface_factor * std::pow(radius, 2);
-            st->members[size_t(i)] = {i};
+            st->members.push_single(i);
             st->agg_n[size_t(i)] = 1;
             AF(*st, AGG_D_M, i) = diameter;
             double f[21];
@@ -360,7 +361,8 @@ int state_to_host(const mcacg_state &in, HostState *out, std::string *err) {
     }
     st.agg.assign(in.aggregates, in.aggregates + 21 * size_t(st.nslots));
     st.agg_n.resize(size_t(st.nslots));
-    st.members.resize(size_t(st.nslots));
+    st.members.off.resize(size_t(st.nslots) + 1);
+    st.members.off[0] = 0;
     int64_t off = 0;
     for (int a = 0; a < st.nslots; ++a) {
         int64_t n = in.n_spheres_per_aggregate[a];
@@ -369,19 +371,27 @@ int state_to_host(const mcacg_state &in, HostState *out, std::string *err) {
             return ST_BAD_ARGUMENT;
         }
         st.agg_n[size_t(a)] = int(n);
-        for (int64_t k = 0; k < n; ++k) {
-            int64_t s = in.members[off + k];
-            if (s < 0 || s >= st.ns || st.sph_slot[size_t(s)] != a) {
-                if (err) *err = "member list inconsistent with sphere labels";
-                return ST_BAD_ARGUMENT;
-            }
-            st.members[size_t(a)].push_back(int(s));
-        }
         off += n;
+        if (off > st.ns) {
+            if (err) *err = "member lists do not cover every sphere once";
+            return ST_BAD_ARGUMENT;
+        }
+        st.members.off[size_t(a) + 1] = int(off);
     }
     if (off != st.ns) {
         if (err) *err = "member lists do not cover every sphere once";
         return ST_BAD_ARGUMENT;
+    }
+    st.members.ids.resize(size_t(st.ns));
+    for (int a = 0; a < st.nslots; ++a) {
+        for (int k = st.members.off[size_t(a)]; k < st.members.off[size_t(a) + 1]; ++k) {
+            int64_t s = in.members[k];
+            if (s < 0 || s >= st.ns || st.sph_slot[size_t(s)] != a) {
+                if (err) *err = "member list inconsistent with sphere labels";
+                return ST_BAD_ARGUMENT;
+            }
+            st.members.ids[size_t(k)] = int(s);
+        }
     }
     return ST_OK;
 }

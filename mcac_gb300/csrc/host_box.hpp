@@ -124,8 +124,8 @@ int state_to_host(const mcacg_state &in, HostState *out, std::string *err);
 // Aggregate::update for an aggregate given by its members (host, used for
 // initial monomers and for loading states): writes all 21 fields except the
 // position-independent proper time and charge, and raises 'maxradius'.
-int host_update_aggregate(const mcacg_params &p, const HostState &st, const std::vector<int> &members,
-                          double fields[21], double *maxradius);
+int host_update_aggregate(const mcacg_params &p, const HostState &st, MemberLists::View members, double fields[21],
+                          double *maxradius);
 
 // A seeded synthetic snapshot for the contact-search benchmark:
 // p.n_monomeres spheres (diameters drawn like initialisation_mode=lognormal)

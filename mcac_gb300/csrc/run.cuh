@@ -49,6 +49,7 @@ struct RunState {
     long long c_merged_spheres, c_merge_pairs;
     // SM clock cycles spent by the block in each phase of the step
     long long cyc_pick, cyc_query, cyc_move, cyc_merge;
+    long long cyc_qscan, cyc_qpairs;  // parts of cyc_query
 };
 static_assert(sizeof(RunState) % sizeof(int) == 0, "RunState is copied as ints");
 
@@ -230,6 +231,8 @@ __device__ inline bool block_mc_step(const BoxRun &R, RunSmem &sm) {
             st.c_candidates += q.n_candidates;
             st.c_cand_spheres += q.n_cand_spheres;
             st.c_refined += q.n_pairs_refined;
+            st.cyc_qscan += q.cyc_scan;
+            st.cyc_qpairs += q.cyc_pairs;
         }
     } else if (tid == 0) {
         sm.contact = 0;

@@ -144,7 +144,8 @@ int make_synthetic_state(const mcacg_params &p, int n_aggregates, int max_size, 
     st->sph_slot.assign(size_t(ns), 0);
     st->agg.assign(21 * size_t(n_aggregates), 0.0);
     st->agg_n.assign(size_t(n_aggregates), 0);
-    st->members.assign(size_t(n_aggregates), {});
+    st->members.clear();
+    st->members.reserve(size_t(n_aggregates), size_t(ns));
     for (int a = 0; a < n_aggregates; ++a) {
         const auto &g = aggs[size_t(a)];
         bool ok = false;
@@ -200,8 +201,10 @@ int make_synthetic_state(const mcacg_params &p, int n_aggregates, int max_size, 
             S(SPH_RY) = g[k].y - g[0].y;
             S(SPH_RZ) = g[k].z - g[0].z;
             st->sph_slot[size_t(s_id)] = a;
-            st->members[size_t(a)].push_back(s_id);
         }
+        // this aggregate's spheres are the last g.size() ids placed, in order
+        for (int k = 0; k < int(g.size()); ++k) st->members.ids.push_back(int(used) - int(g.size()) + k);
+        st->members.off.push_back(int(st->members.ids.size()));
         st->agg_n[size_t(a)] = int(g.size());
         double f[21] = {0};
         f[AGG_TIME] = p.initial_time;

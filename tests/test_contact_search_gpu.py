@@ -157,3 +157,42 @@ def test_fine_grid_queries_match_oracle_on_dense_box():
                 assert (c.moving_sphere, c.other_sphere, c.other_aggregate) == (
                     out["moving_sphere"][k], out["other_sphere"][k], out["other_aggregate"][k]), (scale, k)
             assert (out["moving_sphere"] >= 0).sum() > (20 if scale == 1.0 else 50)
+
+
+@pytest.mark.gpu
+def test_large_aggregate_queries_match_oracle():
+    """A box taken to four aggregates of ~750 spheres, each about as wide as
+    half the box: the sphere-pair search meets the cross-motion grid and
+    several periodic images. Queries of 5 to 200 mean free paths, bit for
+    bit against the oracle."""
+    from mcac_gb300 import Batch
+    from mcac_gb300.workloads import random_directions
+    ini = ("[monomers]\nnumber = 3000\nmean_diameter = 30\ndispersion_diameter = 1.25\n"
+           "initialisation_mode = lognormal\n[environment]\nvolume_fraction = 4e-3\ntemperature = 1700\n"
+           "[limits]\nnumber_of_aggregates = 4\n[numerics]\nrandom_seed = 31\nwith_domain_duplication = false\n")
+    pm = PhysicalModel(text=ini)
+    with Batch([pm]) as b:
+        b.run(max_steps=0, steps_per_launch=20000)
+        assert b.stats()["finished"][0] == 1
+        snap = b.store(0)
+    assert snap.na <= 4 and snap.aggregates[A["rmax"]].max() > 0.2 * snap.box_length
+    rng = np.random.Generator(np.random.PCG64(99))
+    n = 300
+    src = rng.integers(0, snap.na, n).astype(np.int64)
+    dirs = random_directions(rng, n)
+    # late in a run a mean free path is a few nm against gaps of ~100 nm
+    dist = snap.aggregates[A["lpm"], src] * np.exp(rng.uniform(np.log(5.0), np.log(200.0), n))
+    ob = O.OracleBox(ini, snap)
+    with AggregatList(pm, snap) as box:
+        box.set_profiling(True)
+        out, _ = box.distance_to_next_contacts(src, dirs, dist)
+        prof = box.take_profile()
+    assert prof["cand_spheres"] > 100 * n  # large candidates: the pair search is exercised
+    hits = 0
+    for k in range(n):
+        c = ob.distance_to_next_contact(src[k], dirs[k], dist[k])
+        assert bits(c.distance) == bits(out["distance"][k]), k
+        assert (c.moving_sphere, c.other_sphere, c.other_aggregate) == (
+            out["moving_sphere"][k], out["other_sphere"][k], out["other_aggregate"][k]), k
+        hits += c.moving_sphere >= 0
+    assert hits > 20

@@ -395,19 +395,29 @@ class Batch:
         check(lib().mcacg_batch_last_run(self._b, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
-    def store_all(self, raw: bool = False) -> list:
+    def store_all(self, raw: bool = False, out: list | None = None) -> list:
         """The state of every box (one call, converted in parallel): as
         Snapshots, or with raw=True as the filled host arrays
-        (StateBuffers), without further copies."""
-        bufs = []
-        for box in range(len(self.models)):
-            ns, na = C.c_int64(), C.c_int64()
-            check(lib().mcacg_batch_box_sizes(self._b, box, C.byref(ns), C.byref(na)))
-            bufs.append(StateBuffers(ns.value, max(na.value, 1)))
+        (StateBuffers), without further copies. 'out' may supply the
+        StateBuffers to fill (one per box, large enough), e.g. buffers kept
+        from an earlier call."""
+        if out is not None:
+            bufs = list(out)
+            for b in bufs:
+                b.state.n_spheres, b.state.n_aggregates = b.spheres.shape[1], b.aggregates.shape[1]
+        else:
+            bufs = []
+            for box in range(len(self.models)):
+                ns, na = C.c_int64(), C.c_int64()
+                check(lib().mcacg_batch_box_sizes(self._b, box, C.byref(ns), C.byref(na)))
+                bufs.append(StateBuffers(ns.value, max(na.value, 1)))
         arr = (_lib.State * len(bufs))(*[b.state for b in bufs])
         check(lib().mcacg_batch_store_states(self._b, arr, len(bufs)))
         for k, b in enumerate(bufs):
             b.state = arr[k]
+            na = int(b.state.n_aggregates)
+            if na != b.aggregates.shape[1]:  # the table is stored packed as [21][na]
+                b.aggregates = b.aggregates.reshape(-1)[:21 * na].reshape(21, na)
         if raw:
             return bufs
         return [b.to_snapshot(volsurf_method=int(self.models[k].params.volsurf_method)) for k, b in enumerate(bufs)]

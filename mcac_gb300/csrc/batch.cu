@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 
 #include "batch.hpp"
 #include "host_parallel.hpp"
@@ -21,7 +22,12 @@ constexpr int kRunThreads = 256;  // serving loop
 // Every variant keeps to 128 registers a thread (512 / NT blocks per SM).
 // Large blocks pay off late in a run, when few boxes are left and each holds
 // big aggregates (long pair searches and merges).
-constexpr int kRunThreadChoices[] = {64, 128, 256, 512};
+constexpr int kRunThreadChoices[] = {32, 64, 128, 256, 512};
+
+// One warp per box uses the small shared-memory plan, so that 16 boxes fit
+// an SM (shared memory being the limit there, not registers).
+template <int NT>
+using RunSmemFor = typename std::conditional<(NT <= 32), RunSmemSmall, RunSmem>::type;
 // wall time of one launch when boxes run to their stop criteria
 constexpr long long kRunLaunchBudgetNs = 200LL * 1000 * 1000;
 
@@ -38,7 +44,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n, long long max_steps,
                                                       long long budget_ns) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    RunSmem &sm = *reinterpret_cast<RunSmem *>(smem_raw);
+    RunSmemFor<NT> &sm = *reinterpret_cast<RunSmemFor<NT> *>(smem_raw);
     __shared__ __align__(16) BoxRun R;
     __shared__ __align__(16) RunState st;  // the box's loop state, kept on chip for the launch
     const int box = blockIdx.x;
@@ -91,12 +97,14 @@ bool ok_cuda(cudaError_t e, std::string *err, const char *what) {
 
 template <int NT>
 cudaError_t prepare_k_run() {
-    cudaError_t e = cudaFuncSetAttribute(k_run<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RunSmem)));
+    cudaError_t e =
+        cudaFuncSetAttribute(k_run<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RunSmemFor<NT>)));
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_run<NT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 cudaError_t prepare_all_k_run() {
-    cudaError_t e = prepare_k_run<64>();
+    cudaError_t e = prepare_k_run<32>();
+    if (e == cudaSuccess) e = prepare_k_run<64>();
     if (e == cudaSuccess) e = prepare_k_run<128>();
     if (e == cudaSuccess) e = prepare_k_run<256>();
     if (e == cudaSuccess) e = prepare_k_run<512>();
@@ -105,6 +113,7 @@ cudaError_t prepare_all_k_run() {
 cudaError_t launch_k_run(int nt, int grid, cudaStream_t s, const BoxRun *runs, int n, long long steps,
                          long long budget_ns = 0) {
     switch (nt) {
+        case 32: k_run<32><<<grid, 32, sizeof(RunSmemFor<32>), s>>>(runs, n, steps, budget_ns); break;
         case 64: k_run<64><<<grid, 64, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
         case 128: k_run<128><<<grid, 128, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
         case 512: k_run<512><<<grid, 512, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
@@ -115,6 +124,7 @@ cudaError_t launch_k_run(int nt, int grid, cudaStream_t s, const BoxRun *runs, i
 int occupancy_k_run(int nt, int *per_sm) {
     cudaError_t e;
     switch (nt) {
+        case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_run<32>, 32, sizeof(RunSmemFor<32>)); break;
         case 64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_run<64>, 64, sizeof(RunSmem)); break;
         case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_run<128>, 128, sizeof(RunSmem)); break;
         case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_run<512>, 512, sizeof(RunSmem)); break;
@@ -210,8 +220,8 @@ BatchRunner::~BatchRunner() {
 }
 
 int BatchRunner::resident_boxes(int threads, int *boxes, std::string *err) {
-    if (threads != 64 && threads != 128 && threads != 256 && threads != 512) {
-        if (err) *err = "threads per box must be 64, 128, 256 or 512";
+    if (threads != 32 && threads != 64 && threads != 128 && threads != 256 && threads != 512) {
+        if (err) *err = "threads per box must be 32, 64, 128, 256 or 512";
         return ST_BAD_ARGUMENT;
     }
     int dev = 0, n_sm = 0, per_sm = 0;
@@ -329,7 +339,8 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
 }
 
 int BatchRunner::set_threads(int threads) {
-    if (threads != 0 && threads != 64 && threads != 128 && threads != 256 && threads != 512) return ST_BAD_ARGUMENT;
+    if (threads != 0 && threads != 32 && threads != 64 && threads != 128 && threads != 256 && threads != 512)
+        return ST_BAD_ARGUMENT;
     threads_ = threads;
     auto_threads_ = threads == 0;
     return ST_OK;
@@ -626,7 +637,7 @@ int Server::create(int capacity, int64_t memory_budget, void *stream, bool keep_
 }
 
 int Server::set_threads(int threads) {
-    if (threads != 64 && threads != 128 && threads != 256 && threads != 512) return ST_BAD_ARGUMENT;
+    if (threads != 32 && threads != 64 && threads != 128 && threads != 256 && threads != 512) return ST_BAD_ARGUMENT;
     threads_ = threads;
     return ST_OK;
 }

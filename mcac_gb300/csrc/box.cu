@@ -683,9 +683,10 @@ int DeviceBox::upload_aggregates(const std::vector<double> &agg, std::string *er
     return ST_OK;
 }
 
-int DeviceBox::download(HostState *st, std::string *err) {
+int DeviceBox::download(HostState *st, std::string *err, void *copy_stream) {
     DevBox &b = *static_cast<DevBox *>(devbox_);
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    cudaStream_t cs = copy_stream ? static_cast<cudaStream_t>(copy_stream) : s;
     if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
     DevScalars sc;
     st->ns = b.ns;
@@ -696,19 +697,20 @@ int DeviceBox::download(HostState *st, std::string *err) {
     st->sph_slot.resize(size_t(b.ns));
     st->agg.resize(21 * size_t(b.nslots));
     st->agg_n.resize(size_t(b.nslots));
-    std::vector<int> off(size_t(b.nslots));
-    bool ok = true;
-    ok = ok && cuda_ok(cudaMemcpy(&sc, b.sc, sizeof(sc), cudaMemcpyDeviceToHost), err, "download");
-    ok = ok && cuda_ok(cudaMemcpy(st->sph.data(), b.sph, sizeof(double) * 9 * size_t(b.ns), cudaMemcpyDeviceToHost), err, "download");
-    ok = ok && cuda_ok(cudaMemcpy(st->sph_slot.data(), b.sph_slot, sizeof(int) * size_t(b.ns), cudaMemcpyDeviceToHost), err, "download");
-    ok = ok && cuda_ok(cudaMemcpy(st->agg.data(), b.agg, sizeof(double) * 21 * size_t(b.nslots), cudaMemcpyDeviceToHost), err, "download");
-    ok = ok && cuda_ok(cudaMemcpy(st->agg_n.data(), b.agg_n, sizeof(int) * size_t(b.nslots), cudaMemcpyDeviceToHost), err, "download");
-    ok = ok && cuda_ok(cudaMemcpy(off.data(), b.agg_off, sizeof(int) * size_t(b.nslots), cudaMemcpyDeviceToHost), err, "download");
+    std::vector<int> off(static_cast<size_t>(b.nslots));
+    auto get = [&](void *dst, const void *src, size_t bytes) {
+        return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, cs), err, "download");
+    };
+    bool ok = get(&sc, b.sc, sizeof(sc)) && cuda_ok(cudaStreamSynchronize(cs), err, "download") &&
+              get(st->sph.data(), b.sph, sizeof(double) * 9 * size_t(b.ns)) &&
+              get(st->sph_slot.data(), b.sph_slot, sizeof(int) * size_t(b.ns)) &&
+              get(st->agg.data(), b.agg, sizeof(double) * 21 * size_t(b.nslots)) &&
+              get(st->agg_n.data(), b.agg_n, sizeof(int) * size_t(b.nslots)) &&
+              get(off.data(), b.agg_off, sizeof(int) * size_t(b.nslots));
+    std::vector<int> pool(static_cast<size_t>(b.pool_cap));
+    ok = ok && get(pool.data(), b.pool_id[sc.pool_sel], sizeof(int) * size_t(b.pool_cap)) &&
+         cuda_ok(cudaStreamSynchronize(cs), err, "download");
     if (!ok) return ST_CUDA;
-    std::vector<int> pool(size_t(b.pool_cap));
-    if (!cuda_ok(cudaMemcpy(pool.data(), b.pool_id[sc.pool_sel], sizeof(int) * size_t(b.pool_cap), cudaMemcpyDeviceToHost),
-                 err, "download"))
-        return ST_CUDA;
     st->members.clear();
     st->members.reserve(size_t(b.nslots), size_t(b.ns));
     for (int a = 0; a < b.nslots; ++a) st->members.push_list(pool.data() + off[size_t(a)], st->agg_n[size_t(a)]);

@@ -32,9 +32,6 @@
 namespace mcacg {
 
 constexpr int kQueryThreads = 512;
-constexpr int kCellChunk = 1024;       // Verlet cells scanned per chunk
-constexpr int kMoveTile = 512;         // moving spheres staged per pass
-constexpr int kMaxSurvivorsSmem = 256; // refined pairs kept in shared memory (the rest in HBM)
 constexpr int kFineMaxCells = 4096;    // fine cells a query may visit before the Verlet cells are used
 constexpr int kFineMaxDiv = 128;       // fine cells per axis at most
 constexpr int kCullCands = 16;         // candidates whose extents cull the moving spheres
@@ -219,7 +216,17 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tmp, int &t
 }
 
 // ------------------------------------------------------ shared memory plans
-struct QuerySmem {
+// CellChunk: Verlet cells scanned per chunk (also the cross-motion grid's
+// room); MoveTile: moving spheres staged per pass; SurvSmem: refined pairs
+// kept in shared memory (the rest in HBM). The small plan lets 16 boxes
+// share an SM.
+template <int CellChunk, int MoveTile, int SurvSmem>
+struct QuerySmemT {
+    static constexpr int kCellChunk = CellChunk;
+    static constexpr int kMoveTile = MoveTile;
+    static constexpr int kSurv = SurvSmem;
+    static constexpr int kGridMax = CellChunk >= 1024 ? 32 : 16;  // cross-motion grid cells per axis
+    static_assert(kGridMax * kGridMax <= CellChunk, "grid must fit the cell arrays");
     int cell_prefix[kCellChunk + 1];
     int cell_lin[kCellChunk];
     // candidate arrays live in the machine's HBM scratch (one entry per slot at most)
@@ -239,8 +246,8 @@ struct QuerySmem {
     float grid_h, grid_half, grid_rmax, grid_span;
     int grid_g, grid_on;
     float basis[6];  // two unit vectors orthogonal to the direction
-    int4 surv[kMaxSurvivorsSmem];
-    double surv_res[kMaxSurvivorsSmem];
+    int4 surv[kSurv];
+    double surv_res[kSurv];
     int warp_tmp[32];
     float warp_f[32];
     float warp_f2[32];
@@ -256,6 +263,8 @@ struct QuerySmem {
     CellRange range;
     QueryOut out;
 };
+using QuerySmem = QuerySmemT<1024, 512, 256>;
+using QuerySmemSmall = QuerySmemT<256, 256, 128>;
 
 // -------------------------------------------------------------- the query
 // AggregatList::distance_to_next_contact (aggregats/aggregat_list.cpp:447-532):
@@ -269,7 +278,11 @@ struct QuerySmem {
 //  4. the candidates are walked in filter order with the reference's two
 //     early exits.
 // Must be called by all threads of the block.
-__device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double dist, QuerySmem &sm) {
+template <class SM>
+__device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double dist, SM &sm) {
+    constexpr int kCellChunk = SM::kCellChunk;
+    constexpr int kMoveTile = SM::kMoveTile;
+    constexpr int kMaxSurvivorsSmem = SM::kSurv;
     const int tid = threadIdx.x;
     const int NT = blockDim.x;
     const DevScalars *sc = b.sc;
@@ -640,13 +653,13 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
             // r_p + r_q + margin of the moving sphere's line of motion, so
             // with cells at least that wide the 3 x 3 cells around the
             // candidate's position hold every moving sphere it can meet.
-            // Used for large pair counts; at most 32 x 32 cells.
+            // Used for large pair counts; at most kGridMax^2 cells.
             const bool big = nt >= 32 && (long long)nt * n_other >= 16384;
             sm.grid_on = big;
             if (big) {
                 const float h = (2.f * rr + margin) * 1.001f + margin;
                 const float span = 2.f * (sp + margin);
-                const int g = max(1, min(32, int(span / h) + 1));
+                const int g = max(1, min(SM::kGridMax, int(span / h) + 1));
                 sm.grid_g = g;
                 sm.grid_h = fmaxf(h, span / float(g));
                 sm.grid_half = 0.5f * float(g) * sm.grid_h;
@@ -878,22 +891,59 @@ __device__ __forceinline__ void fine_link(const DevBox &b, int slot, int c) {
     b.fine_cell[slot] = c;
 }
 // Aggregate::update_verlet (aggregat.cpp:706-717) for a new position, and
-// the same move in the fine grid.
-__device__ __forceinline__ void regrid(const DevBox &b, int slot) {
-    const Vec3 p = agg_pos(b, slot);
-    int c = cell_of(b, p);
-    int old = b.agg_cell[slot];
+// the same move in the fine grid (one thread). The loads that do not depend
+// on one another are issued first: a move costs three rounds of memory
+// latency instead of one per list operation.
+__device__ __forceinline__ void regrid(const DevBox &b, int slot, Vec3 p) {
+    const int c = cell_of(b, p);
+    const bool fine = b.fine_div > 0;
+    const int fc = fine ? fine_cell_of(b, p) : -1;
+    // round 1: everything indexed by the slot or by the new cells
+    const int old = b.agg_cell[slot];
+    const int k = b.cell_pos[slot];
+    const int n_new = b.cell_n[c];
+    const int fold = fine ? b.fine_cell[slot] : -1;
+    const int fprev = fine ? b.fine_prev[slot] : -1;
+    const int fnext = fine ? b.fine_next[slot] : -1;
+    const int fhead = fine ? b.fine_head[fc] : -1;
     if (c != old) {
-        cell_remove(b, old, slot);
-        cell_insert(b, c, slot);
+        // round 2 and 3: the old cell's length, then its last item
+        const int n_old = b.cell_n[old];
+        int *items = b.cell_items + size_t(old) * b.cell_cap;
+        int kk = k;
+        if (kk < 0 || kk >= n_old || items[kk] != slot) {  // not where recorded: search
+            kk = 0;
+            while (kk < n_old && items[kk] != slot) ++kk;
+        }
+        if (kk < n_old) {
+            const int last = items[n_old - 1];
+            items[kk] = last;
+            b.cell_pos[last] = kk;
+            b.cell_n[old] = n_old - 1;
+        }
+        if (n_new >= b.cell_cap) {
+            b.sc->cell_overflow = 1;
+            b.sc->status = ST_CAPACITY;
+            b.cell_pos[slot] = -1;
+        } else {
+            b.cell_items[size_t(c) * b.cell_cap + n_new] = slot;
+            b.cell_pos[slot] = n_new;
+            b.cell_n[c] = n_new + 1;
+        }
         b.agg_cell[slot] = c;
     }
-    if (b.fine_div > 0) {
-        const int fc = fine_cell_of(b, p);
-        if (fc != b.fine_cell[slot]) {
-            fine_unlink(b, slot);
-            fine_link(b, slot, fc);
+    if (fine && fc != fold) {
+        // unlink from the old fine cell, link at the head of the new one (the
+        // two lists are distinct, so the loads above stay valid)
+        if (fold >= 0) {
+            if (fprev >= 0) b.fine_next[fprev] = fnext; else b.fine_head[fold] = fnext;
+            if (fnext >= 0) b.fine_prev[fnext] = fprev;
         }
+        b.fine_next[slot] = fhead;
+        b.fine_prev[slot] = -1;
+        if (fhead >= 0) b.fine_prev[fhead] = slot;
+        b.fine_head[fc] = slot;
+        b.fine_cell[slot] = fc;
     }
 }
 
@@ -912,7 +962,7 @@ __device__ inline void block_translate(const DevBox &b, int slot, Vec3 v, double
         refpos_sm[0] = x - A(b, AGG_RX, slot);
         refpos_sm[1] = y - A(b, AGG_RY, slot);
         refpos_sm[2] = z - A(b, AGG_RZ, slot);
-        regrid(b, slot);
+        regrid(b, slot, Vec3{x, y, z});
     }
     __syncthreads();
     const double rx = refpos_sm[0], ry = refpos_sm[1], rz = refpos_sm[2];

@@ -596,9 +596,18 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
         std::string err;
         int rc = batch->impl->times(&times, &err);
         if (rc != 0) return finish(rc, err);
+        // one copy stream per worker thread, so boxes come back concurrently
+        struct CopyStream {
+            cudaStream_t s = nullptr;
+            ~CopyStream() {
+                if (s) cudaStreamDestroy(s);
+            }
+        };
         mcacg::parallel_for(n_boxes, [&](int i) {
+            thread_local CopyStream cs;
+            if (!cs.s) cudaStreamCreateWithFlags(&cs.s, cudaStreamNonBlocking);
             mcacg::HostState st;
-            rcs[size_t(i)] = batch->impl->box(i).download(&st, &errs[size_t(i)]);
+            rcs[size_t(i)] = batch->impl->box(i).download(&st, &errs[size_t(i)], cs.s);
             if (rcs[size_t(i)] != 0) return;
             st.time = times[size_t(i)];
             rcs[size_t(i)] = store_host_state(st, &states[i], &errs[size_t(i)]);

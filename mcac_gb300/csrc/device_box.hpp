@@ -106,8 +106,10 @@ class DeviceBox {
     int set_fields(int slot, const double fields[21], unsigned mask, std::string *err);
     // Overwrites the whole aggregate table ([21][nslots], slot order).
     int upload_aggregates(const std::vector<double> &agg, std::string *err);
-    // Copies the whole state back (spheres, aggregates, members, scalars).
-    int download(HostState *st, std::string *err);
+    // Copies the whole state back (spheres, aggregates, members, scalars),
+    // on copy_stream when given (so several boxes can come back at once),
+    // else on the box's stream.
+    int download(HostState *st, std::string *err, void *copy_stream = nullptr);
     // Rebuilds the Verlet grid from the aggregate positions with 'cap' rooms per cell.
     int rebuild_grid(int cap, std::string *err);
     int sync(std::string *err);

@@ -14,10 +14,12 @@
 
 namespace mcacg {
 
-constexpr int kPairTile = 1024;
 constexpr int kSumSeries = 8;
 
-struct MergeSmem {
+// PairTile: spheres staged per pass of the intra-aggregate pair search.
+template <int PairTile>
+struct MergeSmemT {
+    static constexpr int kPairTile = PairTile;
     double refpos[3];
     double diffpos[3];
     double r_cm[3];
@@ -33,6 +35,8 @@ struct MergeSmem {
     int merged;
     float margin;
 };
+using MergeSmem = MergeSmemT<1024>;
+using MergeSmemSmall = MergeSmemT<256>;
 
 // exclusive scan of a global int array in place (block-wide, chunked);
 // returns the total.
@@ -113,7 +117,9 @@ __device__ __forceinline__ double ordered_sum(const double *v, int n) {
 // ms / os: moving / other sphere; mslot / oslot: their aggregates at query
 // time. The physics fields (f_agg, d_m, time_step, lpm, dg_over_dp), the
 // proper time and the charge are left to the caller.
-__device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, int oslot, MergeSmem &sm, MergeOut *out) {
+template <class SM>
+__device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, int oslot, SM &sm, MergeOut *out) {
+    constexpr int kPairTile = SM::kPairTile;
     const int tid = threadIdx.x, NT = blockDim.x;
     DevScalars *sc = b.sc;
     if (tid == 0) {
@@ -417,7 +423,7 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
         A(b, AGG_OVERLAPPING, keep) = overlapping;
         A(b, AGG_COORDINATION_NUMBER, keep) = coordination;
         b.agg_f4[keep] = make_float4(float(x), float(y), float(z), float(rmax));
-        regrid(b, keep);
+        regrid(b, keep, Vec3{x, y, z});
         cell_remove(b, b.agg_cell[removed], removed);
         if (b.fine_div > 0) fine_unlink(b, removed);
         if (rmax > sc->maxradius) sc->maxradius = rmax;

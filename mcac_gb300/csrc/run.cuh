@@ -64,10 +64,11 @@ struct BoxRun {
     int tree_len[kMaxTreeLevels];
 };
 
-struct RunSmem {
+template <class QS, class MS>
+struct RunSmemT {
     union {
-        QuerySmem q;
-        MergeSmem m;
+        QS q;
+        MS m;
     } u;
     MergeOut mout;
     double refpos[3];
@@ -77,6 +78,8 @@ struct RunSmem {
     int keep, removed;
     int ms, os, oslot;  // contact of this step: spheres and the other slot
 };
+using RunSmem = RunSmemT<QuerySmem, MergeSmem>;
+using RunSmemSmall = RunSmemT<QuerySmemSmall, MergeSmemSmall>;
 
 // ------------------------------------------------------------ sum tree
 // Warp 0: descend from the top level to a leaf holding the target 't'.
@@ -165,7 +168,8 @@ __device__ __forceinline__ bool run_finished(const BoxRun &R, const RunState &st
 
 // One MC step of one box by the whole block. Returns false when the box is
 // finished or in error (then nothing was done).
-__device__ inline bool block_mc_step(const BoxRun &R, RunSmem &sm) {
+template <class RS>
+__device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
     const int tid = threadIdx.x;
     const DevBox &b = R.box;
     RunState &st = *R.st;

@@ -88,6 +88,14 @@ def test_batch_keeps_valid_states():
         assert np.all(st["status"] == 0)
         assert np.all(st["steps"] > 0)
         every = b.store_all()
+        # into buffers sized for the initial state (more room than needed)
+        from mcac_gb300._lib import StateBuffers
+        bufs = [StateBuffers(m.params.n_monomeres, m.params.n_monomeres) for m in models]
+        again = [x.to_snapshot() for x in b.store_all(raw=True, out=bufs)]
+        for s1, s2 in zip(again, every):
+            assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64))
+            assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
+            assert np.array_equal(s1.members, s2.members) and np.array_equal(s1.n_spheres, s2.n_spheres)
         for k in range(len(models)):
             snap = b.store(k)
             assert snap.na == models[k].params.n_monomeres - st["events"][k]

@@ -242,7 +242,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
-    R = args.replicas or resident_boxes(64)  # the most boxes one wave holds
+    R = args.replicas or resident_boxes(32)  # the most boxes one wave holds
     models = replica_models(R, rank)
     t0 = time.perf_counter()
     batch = Batch(models, stream=stream.cuda_stream)
@@ -683,7 +683,7 @@ def run_serve(args, rank: int, world: int) -> dict | None:
     stream = torch.cuda.current_stream()
     reqs = serve_requests(args.serve_seconds, args.rate, args.serve_nmax, seed=5000 + rank)
     models = [PhysicalModel(text=ini) for _, ini, _ in reqs]
-    threads = args.threads or 64
+    threads = args.threads or 32
     capacity = resident_boxes(threads)
     budget = int(0.5 * torch.cuda.get_device_properties(dev).total_memory)
     lat, steps_done, finished = [], 0, 0

@@ -313,10 +313,10 @@ int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state
                                    void *cuda_stream, mcacg_batch **batch);
 int mcacg_batch_destroy(mcacg_batch *batch);
 /* Boxes the device-resident loop runs at once on the current device with
- * 'threads' threads per box (64, 128, 256 or 512): its thread blocks per SM x
+ * 'threads' threads per box (32, 64, 128, 256 or 512): its thread blocks per SM x
  * SMs. Batches up to this size take one wave. */
 int mcacg_resident_boxes(int32_t threads, int32_t *boxes);
-/* Threads per box of the batch's loop: 64, 128, 256 or 512, or 0 (the
+/* Threads per box of the batch's loop: 32, 64, 128, 256 or 512, or 0 (the
  * default) to let mcacg_batch_run time each on a short slice of the run and
  * keep the fastest, and choose again when half of the running boxes have
  * finished (runs to the stop criteria). Results do not depend on it. */
@@ -366,7 +366,7 @@ typedef struct mcacg_completion {
 int mcacg_server_create(int32_t capacity, int64_t memory_budget_bytes, void *cuda_stream, int32_t keep_final_states,
                         mcacg_server **server);
 int mcacg_server_destroy(mcacg_server *server);
-/* Threads per box of the server's epochs: 64, 128, 256 (default) or 512.
+/* Threads per box of the server's epochs: 32, 64, 128, 256 (default) or 512.
  * With smaller blocks more slots fit on the GPU at once
  * (mcacg_resident_boxes); results do not depend on it. */
 int mcacg_server_set_threads(mcacg_server *server, int32_t threads);

@@ -604,7 +604,7 @@ int64_t Server::footprint(const mcacg_params &p) {
     const int64_t n = p.n_monomeres;
     const int64_t cells = p.n_verlet_divisions * p.n_verlet_divisions * p.n_verlet_divisions;
     const int64_t fine_cells = int64_t(kFineMaxDiv) * kFineMaxDiv * kFineMaxDiv;  // upper bound
-    return n * 876 + cells * 4 * 80 + fine_cells * 4 + (1 << 20);
+    return n * 760 + cells * 4 * 80 + fine_cells * 4 + (3 << 20);
 }
 
 int Server::create(int capacity, int64_t memory_budget, void *stream, bool keep_final_states,

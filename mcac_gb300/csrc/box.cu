@@ -214,7 +214,10 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     b.cell_cap = std::max({64, 2 * maxc, 8 * avg});
     b.pool_cap = 2 * st.ns + 1024;
     b.surv_cap = 1 << 16;
-    b.pair_cap = 16 * st.ns + 1024;
+    // contact pairs inside one aggregate: equal spheres touch at most 12
+    // others (the kissing number), so at most 6 pairs per sphere; the
+    // merge reports a capacity error beyond 8 per sphere
+    b.pair_cap = 8 * st.ns + 1024;
 
     // all arrays of the box are carved from one allocation: a sizing pass,
     // one cudaMalloc, then the carving pass

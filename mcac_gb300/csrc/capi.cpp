@@ -634,7 +634,7 @@ int mcacg_batch_set_threads(mcacg_batch *batch, int32_t threads) {
     return guarded([&] {
         if (!batch) return fail(MCACG_ERR_BAD_ARGUMENT, "null batch");
         if (batch->impl->set_threads(threads) != 0)
-            return fail(MCACG_ERR_BAD_ARGUMENT, "threads per box must be 0, 64, 128, 256 or 512");
+            return fail(MCACG_ERR_BAD_ARGUMENT, "threads per box must be 0, 32, 64, 128, 256 or 512");
         return 0;
     });
 }
@@ -729,7 +729,7 @@ int mcacg_server_set_threads(mcacg_server *server, int32_t threads) {
     return guarded([&] {
         if (!server) return fail(MCACG_ERR_BAD_ARGUMENT, "null server");
         if (server->impl->set_threads(threads) != 0)
-            return fail(MCACG_ERR_BAD_ARGUMENT, "threads per box must be 64, 128, 256 or 512");
+            return fail(MCACG_ERR_BAD_ARGUMENT, "threads per box must be 32, 64, 128, 256 or 512");
         return 0;
     });
 }

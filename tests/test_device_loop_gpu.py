@@ -191,17 +191,17 @@ def test_ensemble_statistics_match_oracle():
 
 @pytest.mark.gpu
 def test_results_do_not_depend_on_threads_per_box():
-    models = [PhysicalModel(text=small_ini(n, 70 + k, mode="lognormal", disp=1.3, fv=4e-3))
+    models = [PhysicalModel(text=small_ini(n, 70 + k, mode="lognormal", disp=1.3, fv=4e-3, nagg=20))
               for k, n in enumerate([300, 650, 1200])]
     snaps = {}
-    for nt in (64, 128, 256, 512):
+    for nt in (32, 64, 128, 256, 512):
         with Batch(models) as b:
             b.threads = nt
-            b.run(max_steps=3000, steps_per_launch=1000)
+            b.run(max_steps=0, steps_per_launch=5000)  # to 20 aggregates: large tiles and merges
             assert b.threads == nt
             assert np.all(b.stats()["status"] == 0)
             snaps[nt] = [b.store(k) for k in range(len(models))]
-    for nt in (64, 128, 512):
+    for nt in (32, 64, 128, 512):  # 32: the small shared-memory plan
         for s1, s2 in zip(snaps[nt], snaps[256]):
             assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
             assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64))

@@ -57,7 +57,7 @@ def test_requests_admitted_as_slots_free_and_match_alone():
 def test_memory_budget_limits_concurrency():
     models = [PhysicalModel(text=req_ini(300, 50 + k)) for k in range(4)]
     # the server's footprint model for one box (fine grid at its 128^3 bound)
-    one_box = 300 * 876 + 1000 * 4 * 80 + 128 ** 3 * 4 + (1 << 20)
+    one_box = 300 * 760 + 1000 * 4 * 80 + 128 ** 3 * 4 + (3 << 20)
     with Server(capacity=4, memory_budget=int(one_box * 1.5)) as srv:
         for m in models:
             srv.submit(m)

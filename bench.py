@@ -647,7 +647,8 @@ def ensemble_cpu_sample(inis, seconds: float) -> dict:
 
 SERVE_WORKLOAD = ("serving stream: seeded Poisson arrivals at --rate runs/s for --serve-seconds, "
                   "N ~ round(exp(U[ln 500, ln --serve-nmax])), LogNormal(30 nm, sigma_geo ~ U[1.1, 1.6]), "
-                  "volume fraction ~ U[100, 5000] ppm, 1700 K, stop at 1 aggregate or 60 s of physical time")
+                  "volume fraction ~ U[100, 5000] ppm, 1700 K, 30% with surface growth (flux 1e-3), "
+                  "stop at 1 aggregate or 60 s of physical time")
 
 
 def serve_requests(seconds: float, rate: float, nmax: int, seed: int = 5000) -> list[tuple[float, str, bool]]:
@@ -663,9 +664,11 @@ def serve_requests(seconds: float, rate: float, nmax: int, seed: int = 5000) -> 
         fv = rng.uniform(100e-6, 5000e-6)
         sg = rng.uniform(1.1, 1.6)
         growth = bool(rng.random() < 0.3)
+        growth_section = ("[surface_growth]\nwith_surface_reactions = true\nflux_surfgrowth = 1e-3\n"
+                          if growth else "")
         ini = (f"[monomers]\nnumber = {n}\nmean_diameter = 30\ndispersion_diameter = {sg!r}\n"
                f"initialisation_mode = lognormal\n[environment]\nvolume_fraction = {fv!r}\ntemperature = 1700\n"
-               f"[limits]\nnumber_of_aggregates = 1\nphysical_time = 60\n"
+               f"{growth_section}[limits]\nnumber_of_aggregates = 1\nphysical_time = 60\n"
                f"[numerics]\nrandom_seed = {seed + 1 + k}\nwith_domain_duplication = false\n")
         out.append((t, ini, growth))
         k += 1
@@ -728,7 +731,8 @@ def run_serve(args, rank: int, world: int) -> dict | None:
                    "memory_budget_bytes": budget, "epoch_steps": args.epoch_steps, "epoch_ms": args.epoch_ms,
                    "wall_s": wall,
                    "surface_growth_requests": int(sum(g for _, _, g in reqs)),
-                   "surface_growth": "not in the device loop: the requests drawn with surface growth run without it"},
+                   "surface_growth": "flux_surfgrowth = 1e-3 kg/m^2/s on those requests (xsurfgrowth has no "
+                                     "counterpart in the reference's parameters)"},
         "throughput": {"runs_per_s": len(lat) / wall, "mc_steps_per_s": steps_done / wall},
         "gpu_launches": launches,
         "clocks": clocks,

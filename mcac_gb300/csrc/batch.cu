@@ -192,7 +192,9 @@ int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *
     state->weight_total = total;
     std::memset(run, 0, sizeof(*run));
     run->box = b;
-    run->phys = PhysParams{p.viscosity, p.gaz_mean_free_path, p.fractal_dimension, p.density, p.temperature};
+    run->phys = PhysParams{p.viscosity, p.gaz_mean_free_path, p.fractal_dimension, p.density, p.temperature,
+                           p.with_surface_reactions ? p.u_sg : 0.0, p.with_surface_reactions ? 1 : 0,
+                           int(std::max<int64_t>(1, p.full_aggregate_update_frequency))};
     run->lim.number_of_aggregates_limit = p.number_of_aggregates_limit;
     run->lim.n_iter_without_event_limit = p.n_iter_without_event_limit;
     run->lim.mean_monomere_per_aggregate_limit = p.mean_monomere_per_aggregate_limit;
@@ -311,6 +313,8 @@ int BatchRunner::init_stream(void *stream, std::string *err) {
 
 int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector<double> &times, std::string *err) {
     const int n = int(boxes_.size());
+    growth_.assign(static_cast<size_t>(n), 0);
+    for (int i = 0; i < n; ++i) growth_[size_t(i)] = params[size_t(i)].with_surface_reactions ? 1 : 0;
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
     for (DeviceBox *d : boxes_)
         if (d->sync(err) != ST_OK) return ST_CUDA;
@@ -573,6 +577,7 @@ int BatchRunner::download(int box, HostState *st, std::string *err) {
     if (box < 0 || box >= size()) return ST_BAD_ARGUMENT;
     int rc = boxes_[size_t(box)]->download(st, err);
     if (rc != ST_OK) return rc;
+    if (grows(box)) host_refresh_overlap(st);
     RunState r;
     if (!ok_cuda(cudaMemcpy(&r, static_cast<RunState *>(states_dev_) + box, sizeof(r), cudaMemcpyDeviceToHost), err,
                  "download"))
@@ -654,8 +659,8 @@ Server::~Server() {
 
 int Server::submit(const mcacg_params &p, int64_t *id, std::string *err) {
     if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges ||
-        p.with_surface_reactions) {
-        if (err) *err = "served boxes cover the collision-only configuration";
+        (p.with_surface_reactions && (p.u_sg < 0.0 || p.individual_surf_reactions))) {
+        if (err) *err = "served boxes cover collisions with optional surface growth (u_sg >= 0, not individual)";
         return ST_INPUT;
     }
     if (footprint(p) > budget_) {
@@ -728,6 +733,7 @@ int Server::admit(std::string *err) {
             !ok_cuda(cudaStreamSynchronize(s), err, "sync"))
             return ST_CUDA;
         sl.id = take[i].id;
+        sl.growth = take[i].p.with_surface_reactions != 0;
         sl.bytes = footprint(take[i].p);
         sl.submit_s = take[i].submit_s;
         sl.admit_s = t_admit;
@@ -753,6 +759,7 @@ int Server::retire(std::string *err) {
         HostState final_state;
         if (keep_) {
             int rc = sl.box->download(&final_state, err);
+            if (rc == ST_OK && sl.growth) host_refresh_overlap(&final_state);
             if (rc != ST_OK) return rc;
             final_state.time = r.time;
         }

@@ -52,6 +52,8 @@ class BatchRunner {
     int download(int box, HostState *st, std::string *err);
     // Physical time of every box.
     int times(std::vector<double> *out, std::string *err);
+    // Box i grows by surface reactions (its overlap fields are refreshed on read-back).
+    bool grows(int i) const { return growth_.size() > size_t(i) && growth_[size_t(i)]; }
     DeviceBox &box(int i) { return *boxes_[size_t(i)]; }
     // Kernel time of the last run() (CUDA events on the stream).
     double last_kernel_ms() const { return last_ms_; }
@@ -72,6 +74,7 @@ class BatchRunner {
     int launches_ = 0;
     int threads_ = 0;
     bool auto_threads_ = true;
+    std::vector<char> growth_;  // per box: surface reactions on
     int tuned_active_ = 0;  // unfinished boxes at the last tuning
     int tune(int64_t budget, int64_t *done, float *ms_total, std::string *err);
 };
@@ -123,6 +126,7 @@ class Server {
         int64_t id = -1;
         int64_t bytes = 0;
         double submit_s = 0, admit_s = 0;
+        bool growth = false;
     };
     int admit(std::string *err);
     int retire(std::string *err);

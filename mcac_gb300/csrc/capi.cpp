@@ -464,8 +464,9 @@ int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_s
         std::vector<mcacg_params> ps(params, params + n_boxes);
         for (const auto &p : ps)
             if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges ||
-                p.with_surface_reactions)
-                return fail(mcacg::ST_INPUT, "batched boxes cover the collision-only configuration");
+                (p.with_surface_reactions && (p.u_sg < 0.0 || p.individual_surf_reactions)))
+                return fail(mcacg::ST_INPUT,
+                            "batched boxes cover collisions with optional surface growth (u_sg >= 0, not individual)");
         // placements in parallel: each box draws from its own copy of the C
         // library stream, so the result equals a sequential placement
         std::vector<mcacg::HostState> states(static_cast<size_t>(n_boxes));
@@ -609,6 +610,7 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
             mcacg::HostState st;
             rcs[size_t(i)] = batch->impl->box(i).download(&st, &errs[size_t(i)], cs.s);
             if (rcs[size_t(i)] != 0) return;
+            if (batch->impl->grows(i)) mcacg::host_refresh_overlap(&st);
             st.time = times[size_t(i)];
             rcs[size_t(i)] = store_host_state(st, &states[i], &errs[size_t(i)]);
         });

@@ -63,10 +63,10 @@ struct PlacementGrid {
 
 }  // namespace
 
-int host_update_aggregate(const mcacg_params &p, const HostState &st, MemberLists::View members, double fields[21],
-                          double *maxradius) {
+namespace {
+// update_distances_and_overlapping (aggregat.cpp:719-764)
+void overlap_fields(const HostState &st, MemberLists::View members, double *overlapping_out, double *coordination_out) {
     const int n = members.size();
-    // update_distances_and_overlapping (aggregat.cpp:719-764)
     double overlapping = 0.0, coordination = 0.0;
     int intersections = 0;
     for (int i = 0; i < n; i++) {
@@ -89,6 +89,26 @@ int host_update_aggregate(const mcacg_params &p, const HostState &st, MemberList
         overlapping /= static_cast<double>(intersections);
         coordination = static_cast<double>(intersections) / static_cast<double>(n);
     }
+    *overlapping_out = overlapping;
+    *coordination_out = coordination;
+}
+}  // namespace
+
+void host_refresh_overlap(HostState *st) {
+    for (int a = 0; a < st->nslots; ++a) {
+        if (st->agg_n[size_t(a)] == 0) continue;
+        double ov = 0.0, co = 0.0;
+        overlap_fields(*st, st->members[size_t(a)], &ov, &co);
+        AF(*st, AGG_OVERLAPPING, a) = ov;
+        AF(*st, AGG_COORDINATION_NUMBER, a) = co;
+    }
+}
+
+int host_update_aggregate(const mcacg_params &p, const HostState &st, MemberLists::View members, double fields[21],
+                          double *maxradius) {
+    const int n = members.size();
+    double overlapping = 0.0, coordination = 0.0;
+    overlap_fields(st, members, &overlapping, &coordination);
     if (p.volsurf_method != VS_NONE) return ST_INPUT;  // other methods are device-only
     // compute_volume_surface (aggregat.cpp:321-430), method "none"
     double volume = 0.0, surface = 0.0;

@@ -127,6 +127,11 @@ int state_to_host(const mcacg_state &in, HostState *out, std::string *err);
 int host_update_aggregate(const mcacg_params &p, const HostState &st, MemberLists::View members, double fields[21],
                           double *maxradius);
 
+// The overlap and coordination fields of every live aggregate from its
+// spheres (update_distances_and_overlapping, aggregat.cpp:719-764): the
+// device loop with surface growth leaves them to the read-back.
+void host_refresh_overlap(HostState *st);
+
 // A seeded synthetic snapshot for the contact-search benchmark:
 // p.n_monomeres spheres (diameters drawn like initialisation_mode=lognormal)
 // in n_aggregates aggregates of 1..max_size spheres grown by ballistic

@@ -26,6 +26,9 @@ constexpr int kMaxTreeLevels = 8;
 
 struct PhysParams {
     double viscosity, lambda, fractal_dimension, density, temperature;
+    double u_sg;        // surface growth velocity dr/dt (m/s)
+    int growth;         // with_surface_reactions
+    int full_update_every;  // full_aggregate_update_frequency
 };
 
 struct RunLimits {
@@ -64,6 +67,8 @@ struct BoxRun {
     int tree_len[kMaxTreeLevels];
 };
 
+constexpr int kMovedCap = 64;  // grid moves listed per update of all aggregates
+
 template <class QS, class MS>
 struct RunSmemT {
     union {
@@ -77,6 +82,10 @@ struct RunSmemT {
     int slot, contact, stop, merged;
     int keep, removed;
     int ms, os, oslot;  // contact of this step: spheres and the other slot
+    unsigned long long tree_tmp;  // block reduction scratch
+    double step_dt;               // this step's time increment
+    int n_moved;                  // slots whose grid cell changed in the update of all aggregates
+    int moved[kMovedCap];
 };
 using RunSmem = RunSmemT<QuerySmem, MergeSmem>;
 using RunSmemSmall = RunSmemT<QuerySmemSmall, MergeSmemSmall>;
@@ -168,6 +177,173 @@ __device__ __forceinline__ bool run_finished(const BoxRun &R, const RunState &st
 
 // One MC step of one box by the whole block. Returns false when the box is
 // finished or in error (then nothing was done).
+// ------------------------------------------------------ surface growth
+// Sphere::croissance_surface (sphere.cpp:113-120) for every sphere of the box:
+// r += u_sg dt, volume and surface from the new radius. Each sphere is found
+// once through the live segments of the member pool, whose FP32 copy is
+// refreshed too.
+__device__ inline void block_grow_spheres(const BoxRun &R, double dt) {
+    const DevBox &b = R.box;
+    const double pi = pi_value();
+    const double vf = 4. * pi / 3., sf = 4. * pi;
+    const int *pool_id = b.pool_id[b.sc->pool_sel];
+    float4 *pool_pos = b.pool_pos[b.sc->pool_sel];
+    const int top = b.sc->pool_top;
+    for (int k = threadIdx.x; k < top; k += blockDim.x) {
+        const int s = pool_id[k];
+        if (s < 0 || s >= b.ns) continue;
+        const int a = b.sph_slot[s];
+        const int rel = k - b.agg_off[a];
+        if (b.agg_n[a] == 0 || rel < 0 || rel >= b.agg_n[a]) continue;  // a stale pool entry
+        const double r = S(b, SPH_R, s) + R.phys.u_sg * dt;                // PhysicalModel::grow
+        const double r2 = r * r, r3 = r2 * r;
+        S(b, SPH_R, s) = r;
+        S(b, SPH_VOLUME, s) = vf * r3;
+        S(b, SPH_SURFACE, s) = sf * r2;
+        pool_pos[k].w = float(r);
+    }
+}
+
+// Aggregate::update / update_partial (aggregat.cpp:247-288) of one slot by
+// one thread, sums in list order; 'full' also recomputes volume and surface
+// (volsurf method "none": sums of the sphere values). The overlap and
+// coordination fields, which need every pair of the aggregate and do not
+// act on the dynamics, are left to the merge and to the read-back.
+__device__ inline double thread_update_aggregate(const BoxRun &R, int a, bool full) {
+    const DevBox &b = R.box;
+    const int n = b.agg_n[a];
+    const int *mem = b.pool_id[b.sc->pool_sel] + b.agg_off[a];
+    double volume = A(b, AGG_VOLUME, a);
+    if (full) {
+        double v = 0.0, sfc = 0.0;
+        for (int i = 0; i < n; ++i) {
+            v = v + S(b, SPH_VOLUME, mem[i]);
+            sfc = sfc + S(b, SPH_SURFACE, mem[i]);
+        }
+        volume = v;
+        A(b, AGG_VOLUME, a) = v;
+        A(b, AGG_SURFACE, a) = sfc;
+    }
+    // compute_mass_center (aggregat.cpp:431-452)
+    double rx = 0., ry = 0., rz = 0.;
+    for (int i = 0; i < n; ++i) {
+        const int s = mem[i];
+        const double vol = S(b, SPH_VOLUME, s);
+        rx += S(b, SPH_RX, s) * vol;
+        ry += S(b, SPH_RY, s) * vol;
+        rz += S(b, SPH_RZ, s) * vol;
+    }
+    rx /= volume;
+    ry /= volume;
+    rz /= volume;
+    // compute_max_radius, compute_giration_radius (aggregat.cpp:453-483)
+    double rmax = 0.0, arg = 0., brg = 0., dp = 0., vol_pp = 0.;
+    for (int i = 0; i < n; ++i) {
+        const int s = mem[i];
+        const double dx = S(b, SPH_RX, s) - rx, dy = S(b, SPH_RY, s) - ry, dz = S(b, SPH_RZ, s) - rz;
+        const double dc = sqrt(dx * dx + dy * dy + dz * dz);
+        const double rs = S(b, SPH_R, s), vol = S(b, SPH_VOLUME, s);
+        rmax = dmax(rmax, rs + dc);
+        arg = arg + vol * (dc * dc);
+        brg = brg + vol * (rs * rs);
+        vol_pp += vol;
+        dp += rs;
+    }
+    const double rg = sqrt(fabs((arg + (3. / 5.) * brg) / volume));
+    dp = 2 * dp / double(n);
+    vol_pp = vol_pp / double(n);
+    // the aggregate's position (aggregat.cpp:431-452, as in the merge)
+    const int s0 = mem[0];
+    const double x = periodic_position(S(b, SPH_X, s0) + rx, b.L);
+    const double y = periodic_position(S(b, SPH_Y, s0) + ry, b.L);
+    const double z = periodic_position(S(b, SPH_Z, s0) + rz, b.L);
+    A(b, AGG_RX, a) = rx;
+    A(b, AGG_RY, a) = ry;
+    A(b, AGG_RZ, a) = rz;
+    A(b, AGG_X, a) = x;
+    A(b, AGG_Y, a) = y;
+    A(b, AGG_Z, a) = z;
+    A(b, AGG_RMAX, a) = rmax;
+    A(b, AGG_RG, a) = rg;
+    A(b, AGG_DP, a) = dp;
+    b.agg_f4[a] = make_float4(float(x), float(y), float(z), float(rmax));
+    double f, dm, ts, lpm, dgdp;
+    device_physics(R.phys, volume, vol_pp, dp, rg, &f, &dm, &ts, &lpm, &dgdp);
+    A(b, AGG_F_AGG, a) = f;
+    A(b, AGG_D_M, a) = dm;
+    A(b, AGG_TIME_STEP, a) = ts;
+    A(b, AGG_LPM, a) = lpm;
+    A(b, AGG_DG_OVER_DP, a) = dgdp;
+    return rmax;
+}
+
+// The per-step update of every aggregate after growth (calcul.cpp:180-206):
+// fields, Verlet and fine cells (centres move as spheres grow unevenly),
+// maxradius, and the pick tree rebuilt from the new time steps.
+template <class RS>
+__device__ inline void block_update_all(const BoxRun &R, RS &sm, bool full) {
+    const DevBox &b = R.box;
+    const int tid = threadIdx.x, NT = blockDim.x;
+    double rmax_d = 0.0;
+    if (tid == 0) sm.n_moved = 0;
+    __syncthreads();
+    for (int a = tid; a < b.nslots; a += NT) {
+        if (b.agg_n[a] == 0) continue;
+        const double rm = thread_update_aggregate(R, a, full);
+        rmax_d = dmax(rmax_d, rm);
+        // the centre moves a little when spheres grow unevenly: note the
+        // slots whose Verlet or fine cell changed
+        const Vec3 pa = agg_pos(b, a);
+        if (cell_of(b, pa) != b.agg_cell[a] || (b.fine_div > 0 && fine_cell_of(b, pa) != b.fine_cell[a])) {
+            const int k = atomicAdd(&sm.n_moved, 1);
+            if (k < kMovedCap) sm.moved[k] = a;
+        }
+    }
+    // block max of r_max (bits of a non-negative double order like integers)
+    unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(rmax_d));
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
+        bits = other > bits ? other : bits;
+    }
+    if (tid == 0) sm.tree_tmp = 0ULL;
+    __syncthreads();
+    if ((tid & 31) == 0) atomicMax(&sm.tree_tmp, bits);
+    __syncthreads();
+    if (tid == 0) {
+        const double m = __longlong_as_double(static_cast<long long>(sm.tree_tmp));
+        if (m > b.sc->maxradius) b.sc->maxradius = m;
+        // the grid lists change one slot at a time, as in the translation
+        if (sm.n_moved <= kMovedCap) {
+            for (int k = 0; k < sm.n_moved; ++k) regrid(b, sm.moved[k], agg_pos(b, sm.moved[k]));
+        } else {
+            for (int a = 0; a < b.nslots; ++a)
+                if (b.agg_n[a] > 0) regrid(b, a, agg_pos(b, a));
+        }
+    }
+    // pick tree: leaves 1/time_step, then each level from the one below
+    for (int a = tid; a < R.tree_len[0]; a += NT)
+        R.tree[R.tree_off[0] + a] = (a < b.nslots && b.agg_n[a] > 0) ? 1.0 / A(b, AGG_TIME_STEP, a) : 0.0;
+    __syncthreads();
+    for (int lev = 1; lev < R.tree_levels; ++lev) {
+        for (int g = tid; g < R.tree_len[lev]; g += NT) {
+            double sum = 0.0;
+            for (int k = 0; k < kTreeFan; ++k) {
+                const int c = g * kTreeFan + k;
+                if (c < R.tree_len[lev - 1]) sum += R.tree[R.tree_off[lev - 1] + c];
+            }
+            R.tree[R.tree_off[lev] + g] = sum;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const int top = R.tree_levels - 1;
+        double total = 0.0;
+        for (int k = 0; k < R.tree_len[top]; ++k) total += R.tree[R.tree_off[top] + k];
+        R.st->weight_total = total;
+    }
+    __syncthreads();
+}
+
 template <class RS>
 __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
     const int tid = threadIdx.x;
@@ -259,7 +435,11 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
         A(b, AGG_TIME, slot) += dt;
         st.time = st.time + dt;
         sm.merged = 0;
+        sm.step_dt = dt;
     }
+    __syncthreads();
+    // surface reactions before the merge (calcul.cpp:157-172)
+    if (R.phys.growth) block_grow_spheres(R, sm.step_dt);
     __syncthreads();
     if (sm.contact) {
         block_merge(b, ms, os, slot, oslot, sm.u.m, &sm.mout);
@@ -287,11 +467,19 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
         }
         __syncthreads();
         if (sm.stop) return false;
-        if (sm.merged && tid < 32) {
+        if (sm.merged && tid < 32 && !R.phys.growth) {
             tree_set(R, sm.removed, 0.0);
             double total = tree_set(R, sm.keep, 1.0 / A(b, AGG_TIME_STEP, sm.keep));
             if (tid == 0) st.weight_total = total;
         }
+    }
+    if (R.phys.growth) {
+        // every aggregate after growth (and merge): update() on every
+        // full_aggregate_update_frequency-th step without event, else
+        // update_partial() (calcul.cpp:180-206)
+        __syncthreads();
+        const long long every = R.phys.full_update_every > 0 ? R.phys.full_update_every : 1;
+        block_update_all(R, sm, st.n_iter_without_event % every == 0);
     }
     if (tid == 0) {
         st.cyc_merge += clock64() - t_phase;

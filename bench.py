@@ -286,13 +286,9 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     state_bytes = sum(int(b.spheres.nbytes + b.sphere_label.nbytes + b.aggregates.nbytes + b.n_spheres.nbytes
                           + b.members.nbytes) for b in states)
     K = max(1, args.e2e_steps)
-    # output host arrays prepared (and touched) before the timed region, like
-    # the pinned input buffers of a serving loop
-    from mcac_gb300._lib import StateBuffers
-    outs = [StateBuffers(b.spheres.shape[1], b.aggregates.shape[1]) for b in states]
-    for o in outs:
-        for a in (o.spheres, o.sphere_label, o.aggregates, o.n_spheres, o.members):
-            a.fill(0)
+    # the results come back into the input arrays (already resident in host
+    # memory; the upload has finished when the batch exists)
+    outs = states
     torch.cuda.synchronize()
     t = time.perf_counter()
     stats_bytes = 0

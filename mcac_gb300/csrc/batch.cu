@@ -20,6 +20,8 @@ constexpr int kRunThreads = 256;  // serving loop
 // dependent loads and block barriers, so smaller blocks (more boxes per SM)
 // often finish more steps per second; BatchRunner::run picks one by timing.
 // Every variant keeps to 128 registers a thread (512 / NT blocks per SM).
+// (Holding one warp per box to fewer registers, for 20 boxes per SM, spilled
+// and ran slower.)
 // Large blocks pay off late in a run, when few boxes are left and each holds
 // big aggregates (long pair searches and merges).
 constexpr int kRunThreadChoices[] = {32, 64, 128, 256, 512};

@@ -225,7 +225,7 @@ struct QuerySmemT {
     static constexpr int kCellChunk = CellChunk;
     static constexpr int kMoveTile = MoveTile;
     static constexpr int kSurv = SurvSmem;
-    static constexpr int kGridMax = CellChunk >= 1024 ? 32 : 16;  // cross-motion grid cells per axis
+    static constexpr int kGridMax = CellChunk >= 1024 ? 32 : (CellChunk >= 256 ? 16 : 11);  // grid cells per axis
     static_assert(kGridMax * kGridMax <= CellChunk, "grid must fit the cell arrays");
     int cell_prefix[kCellChunk + 1];
     int cell_lin[kCellChunk];

@@ -72,6 +72,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
         out_of_time = 0;
     }
     __syncthreads();
+    tree_cache_load(R, sm.tree);
     for (long long s = 0; s < max_steps; ++s) {
         if (budget_ns > 0 && (s & 15) == 0) {
             if (threadIdx.x == 0) out_of_time = global_ns() - t_start >= (unsigned long long)budget_ns;

@@ -69,6 +69,17 @@ struct BoxRun {
 
 constexpr int kMovedCap = 64;  // grid moves listed per update of all aggregates
 
+// The top levels of a box's pick tree (up to kTreeCache entries) are kept in
+// shared memory for a launch: the descent then reads global memory only for
+// the lower levels. coff[lev] is the level's offset in the copy, -1 if the
+// level is not kept.
+constexpr int kTreeCache = 128;
+struct TreeCache {
+    double v[kTreeCache];
+    int coff[kMaxTreeLevels];
+};
+
+
 template <class QS, class MS>
 struct RunSmemT {
     union {
@@ -86,19 +97,41 @@ struct RunSmemT {
     double step_dt;               // this step's time increment
     int n_moved;                  // slots whose grid cell changed in the update of all aggregates
     int moved[kMovedCap];
+    TreeCache tree;               // top levels of the pick tree
 };
 using RunSmem = RunSmemT<QuerySmem, MergeSmem>;
 using RunSmemSmall = RunSmemT<QuerySmemSmall, MergeSmemSmall>;
 
 // ------------------------------------------------------------ sum tree
+// Marks the kept levels and copies them (all threads).
+__device__ inline void tree_cache_load(const BoxRun &R, TreeCache &c) {
+    if (threadIdx.x == 0) {
+        int used = 0;
+        for (int lev = kMaxTreeLevels - 1; lev >= 0; --lev) c.coff[lev] = -1;
+        for (int lev = R.tree_levels - 1; lev >= 0; --lev) {
+            if (used + R.tree_len[lev] > kTreeCache) break;
+            c.coff[lev] = used;
+            used += R.tree_len[lev];
+        }
+    }
+    __syncthreads();
+    for (int lev = 0; lev < R.tree_levels; ++lev) {
+        if (c.coff[lev] < 0) continue;
+        for (int k = threadIdx.x; k < R.tree_len[lev]; k += blockDim.x) c.v[c.coff[lev] + k] = R.tree[R.tree_off[lev] + k];
+    }
+    __syncthreads();
+}
+
 // Warp 0: descend from the top level to a leaf holding the target 't'.
-__device__ inline int tree_sample(const BoxRun &R, double t) {
+__device__ inline int tree_sample(const BoxRun &R, const TreeCache &c, double t) {
     const int lane = threadIdx.x & 31;
     int node = 0;  // index within the current level
     for (int lev = R.tree_levels - 1; lev >= 0; --lev) {
         const int base = node * kTreeFan;
         const int len = R.tree_len[lev];
-        double v = (base + lane < len) ? R.tree[R.tree_off[lev] + base + lane] : 0.0;
+        const int co = c.coff[lev];
+        double v = (base + lane < len) ? (co >= 0 ? c.v[co + base + lane] : R.tree[R.tree_off[lev] + base + lane])
+                                       : 0.0;
         // inclusive scan over the 32 children (fixed order)
         double incl = v;
 #pragma unroll
@@ -116,21 +149,30 @@ __device__ inline int tree_sample(const BoxRun &R, double t) {
     return node;
 }
 
-// Warp 0: set leaf 'slot' to 'w' and refresh its ancestors; returns the new total.
-__device__ inline double tree_set(const BoxRun &R, int slot, double w) {
+// Warp 0: set leaf 'slot' to 'w' and refresh its ancestors (in global
+// memory and in the kept copy); returns the new total.
+__device__ inline double tree_set(const BoxRun &R, TreeCache &c, int slot, double w) {
     const int lane = threadIdx.x & 31;
-    if (lane == 0) R.tree[R.tree_off[0] + slot] = w;
+    if (lane == 0) {
+        R.tree[R.tree_off[0] + slot] = w;
+        if (c.coff[0] >= 0) c.v[c.coff[0] + slot] = w;
+    }
     __syncwarp();
     int idx = slot;
     double total = 0.0;
     for (int lev = 0; lev < R.tree_levels; ++lev) {
         const int g = idx / kTreeFan;
         const int len = R.tree_len[lev];
-        double v = (g * kTreeFan + lane < len) ? R.tree[R.tree_off[lev] + g * kTreeFan + lane] : 0.0;
+        const int co = c.coff[lev];
+        const int k = g * kTreeFan + lane;
+        double v = (k < len) ? (co >= 0 ? c.v[co + k] : R.tree[R.tree_off[lev] + k]) : 0.0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lev + 1 < R.tree_levels) {
-            if (lane == 0) R.tree[R.tree_off[lev + 1] + g] = v;
+            if (lane == 0) {
+                R.tree[R.tree_off[lev + 1] + g] = v;
+                if (c.coff[lev + 1] >= 0) c.v[c.coff[lev + 1] + g] = v;
+            }
             __syncwarp();
         } else {
             total = v;
@@ -342,6 +384,7 @@ __device__ inline void block_update_all(const BoxRun &R, RS &sm, bool full) {
         R.st->weight_total = total;
     }
     __syncthreads();
+    tree_cache_load(R, sm.tree);
 }
 
 template <class RS>
@@ -362,7 +405,7 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
     __syncthreads();
     if (sm.stop) return false;
     if (tid < 32) {
-        int slot = tree_sample(R, sm.t_pick);
+        int slot = tree_sample(R, sm.tree, sm.t_pick);
         if (tid == 0) {
             if (slot < 0 || slot >= b.nslots || b.agg_n[slot] == 0) {
                 st.status = ST_UNKNOWN;  // the tree lost a live slot: stop this box
@@ -372,11 +415,16 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
             sm.slot = slot;
             sm.dt = 1.0 / st.weight_total;
             sm.full = A(b, AGG_LPM, slot);
-            double theta = st.rng.uniform() * 2 * pi_value();
-            double phi = acos(1 - 2 * st.rng.uniform());
-            double sp, cp, sth, cth;
-            sincos(phi, &sp, &cp);
-            sincos(theta, &sth, &cth);
+            // random_direction (tools.cpp:82-89): theta = 2 pi u1, phi =
+            // acos(1 - 2 u2). cos(phi) is 1 - 2 u2 itself and sin(phi) =
+            // 2 sqrt(u2 (1 - u2)), which saves the acos and one sincos
+            // (slow in FP64) on every step; same distribution, last bits
+            // aside (the device loop follows the reference statistically)
+            const double u1 = st.rng.uniform(), u2 = st.rng.uniform();
+            const double cp = 1 - 2 * u2;
+            const double sp = 2 * sqrt(u2 * (1 - u2));
+            double sth, cth;
+            sincospi(2 * u1, &sth, &cth);
             sm.dir[0] = sp * cth;
             sm.dir[1] = sp * sth;
             sm.dir[2] = cp;
@@ -468,8 +516,8 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
         __syncthreads();
         if (sm.stop) return false;
         if (sm.merged && tid < 32 && !R.phys.growth) {
-            tree_set(R, sm.removed, 0.0);
-            double total = tree_set(R, sm.keep, 1.0 / A(b, AGG_TIME_STEP, sm.keep));
+            tree_set(R, sm.tree, sm.removed, 0.0);
+            double total = tree_set(R, sm.tree, sm.keep, 1.0 / A(b, AGG_TIME_STEP, sm.keep));
             if (tid == 0) st.weight_total = total;
         }
     }

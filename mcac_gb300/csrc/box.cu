@@ -322,25 +322,24 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     int alive = 0;
     for (int a = 0; a < st.nslots; ++a) alive += st.agg_n[a] > 0;
     sc.n_alive = alive;
+    // copies on the box's own stream (boxes of a batch are built in parallel,
+    // each on a stream of its own); the host arrays stay alive until the
+    // grid build below synchronises the stream
     cudaStream_t s = static_cast<cudaStream_t>(d->stream_);
-    ok = ok && cuda_ok(cudaMemcpy(b.sph, st.sph.data(), sizeof(double) * 9 * size_t(st.ns), cudaMemcpyHostToDevice), err, "upload");
-    ok = ok && cuda_ok(cudaMemcpy(b.sph_slot, st.sph_slot.data(), sizeof(int) * size_t(st.ns), cudaMemcpyHostToDevice), err, "upload");
-    ok = ok && cuda_ok(cudaMemcpy(b.agg, st.agg.data(), sizeof(double) * 21 * size_t(st.nslots), cudaMemcpyHostToDevice), err, "upload");
-    ok = ok && cuda_ok(cudaMemcpy(b.agg_n, st.agg_n.data(), sizeof(int) * size_t(st.nslots), cudaMemcpyHostToDevice), err, "upload");
-    ok = ok && cuda_ok(cudaMemcpy(b.agg_off, off.data(), sizeof(int) * size_t(st.nslots), cudaMemcpyHostToDevice), err, "upload");
-    ok = ok && cuda_ok(cudaMemcpy(b.pool_id[0], pool_id.data(), sizeof(int) * size_t(b.pool_cap), cudaMemcpyHostToDevice), err, "upload");
-    ok = ok && cuda_ok(cudaMemcpy(b.pool_pos[0], pool_pos.data(), sizeof(float4) * size_t(b.pool_cap), cudaMemcpyHostToDevice), err, "upload");
-    ok = ok && cuda_ok(cudaMemcpy(b.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice), err, "upload");
+    auto put = [&](void *dst, const void *src, size_t bytes) {
+        return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s), err, "upload");
+    };
+    ok = ok && put(b.sph, st.sph.data(), sizeof(double) * 9 * size_t(st.ns)) &&
+         put(b.sph_slot, st.sph_slot.data(), sizeof(int) * size_t(st.ns)) &&
+         put(b.agg, st.agg.data(), sizeof(double) * 21 * size_t(st.nslots)) &&
+         put(b.agg_n, st.agg_n.data(), sizeof(int) * size_t(st.nslots)) &&
+         put(b.agg_off, off.data(), sizeof(int) * size_t(st.nslots)) &&
+         put(b.pool_id[0], pool_id.data(), sizeof(int) * size_t(b.pool_cap)) &&
+         put(b.pool_pos[0], pool_pos.data(), sizeof(float4) * size_t(b.pool_cap)) && put(b.sc, &sc, sizeof(sc));
     if (!ok) {
         delete d;
         return ST_CUDA;
     }
-    ok = ok && cuda_ok(cudaHostAlloc(&d->host_out_, sizeof(OutBuffers), cudaHostAllocMapped), err, "cudaHostAlloc");
-    ok = ok && cuda_ok(cudaHostGetDevicePointer(&d->dev_out_, d->host_out_, 0), err, "cudaHostGetDevicePointer");
-    ok = ok && cuda_ok(cudaFuncSetAttribute(k_query, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(QuerySmem))),
-                       err, "cudaFuncSetAttribute");
-    ok = ok && cuda_ok(cudaFuncSetAttribute(k_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(MergeSmem))),
-                       err, "cudaFuncSetAttribute");
     d->devbox_ = new DevBox(b);
     if (!ok) {
         delete d;
@@ -449,7 +448,30 @@ int DeviceBox::rebuild_grid(int cap, std::string *err) {
     return st;
 }
 
+// The mapped host buffer of the one-at-a-time query and merge results, made
+// on first use (a batch's boxes never need one), and the kernels' shared
+// memory limits, set once per process.
+int DeviceBox::ensure_out_buffers(std::string *err) {
+    if (host_out_) return ST_OK;
+    static bool attrs = false;
+    if (!attrs) {
+        if (!cuda_ok(cudaFuncSetAttribute(k_query, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(QuerySmem))),
+                     err, "cudaFuncSetAttribute") ||
+            !cuda_ok(cudaFuncSetAttribute(k_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(MergeSmem))),
+                     err, "cudaFuncSetAttribute"))
+            return ST_CUDA;
+        attrs = true;
+    }
+    if (!cuda_ok(cudaHostAlloc(&host_out_, sizeof(OutBuffers), cudaHostAllocMapped), err, "cudaHostAlloc")) {
+        host_out_ = nullptr;
+        return ST_CUDA;
+    }
+    if (!cuda_ok(cudaHostGetDevicePointer(&dev_out_, host_out_, 0), err, "cudaHostGetDevicePointer")) return ST_CUDA;
+    return ST_OK;
+}
+
 int DeviceBox::query(int src_slot, const double dir[3], double dist, QueryResult *out, std::string *err) {
+    if (ensure_out_buffers(err) != ST_OK) return ST_CUDA;
     DevBox &b = *static_cast<DevBox *>(devbox_);
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
     OutBuffers *ho = static_cast<OutBuffers *>(host_out_);
@@ -620,6 +642,7 @@ int DeviceBox::translate(int slot, const double v[3], std::string *err) {
 }
 
 int DeviceBox::merge(int ms, int os, int mslot, int oslot, MergeResult *out, std::string *err) {
+    if (ensure_out_buffers(err) != ST_OK) return ST_CUDA;
     DevBox &b = *static_cast<DevBox *>(devbox_);
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
     OutBuffers *ho = static_cast<OutBuffers *>(host_out_);

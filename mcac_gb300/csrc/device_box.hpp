@@ -122,6 +122,7 @@ class DeviceBox {
   private:
     DeviceBox() = default;
     int check_status(std::string *err);
+    int ensure_out_buffers(std::string *err);
     void *devbox_ = nullptr;  // DevBox (host copy with device pointers)
     void *stream_ = nullptr;
     bool own_stream_ = false;

@@ -200,14 +200,12 @@ def replica_models(n: int, rank: int = 0):
 
 
 def host_states(models, stream):
-    """The reference placement of every replica as host arrays: placed by a
-    batch (parallel host threads, each with its own copy of the C library
-    stream) and read back before any step."""
+    """The reference placement of every replica as page-locked host arrays:
+    placed by a batch (parallel host threads, each with its own copy of the C
+    library stream) and read back before any step."""
     from mcac_gb300 import Batch
-    from mcac_gb300._lib import StateBuffers
     with Batch(models, stream=stream) as b0:
-        snaps = b0.store_all()
-    return [StateBuffers.from_snapshot(sn) for sn in snaps]
+        return b0.store_all(raw=True, pinned=True)
 
 
 def plain_single_box(args, stream) -> dict:

@@ -308,9 +308,16 @@ int mcacg_run_device(mcacg_box *box, int64_t max_steps, mcacg_run_stats *stats);
  * with params[i] (size, seed, physics and stop criteria per box). */
 int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_stream, mcacg_batch **batch);
 /* n_boxes boxes from host states (states[i] as for mcacg_box_create_from_state);
- * params[i] gives box i's physics, stop criteria and device stream seed. */
+ * params[i] gives box i's physics, stop criteria and device stream seed. The
+ * arrays are read in place (by DMA when they are page-locked, e.g. from
+ * mcacg_host_alloc) and checked on the device: an inconsistent state gives
+ * MCACG_ERR_BAD_ARGUMENT. */
 int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state *states, int32_t n_boxes,
                                    void *cuda_stream, mcacg_batch **batch);
+/* Page-locked host memory (freed by mcacg_host_free), for state arrays that
+ * are loaded and stored by DMA. */
+int mcacg_host_alloc(int64_t bytes, void **ptr);
+int mcacg_host_free(void *ptr);
 int mcacg_batch_destroy(mcacg_batch *batch);
 /* Boxes the device-resident loop runs at once on the current device with
  * 'threads' threads per box (32, 64, 128, 256 or 512): its thread blocks per SM x

@@ -116,6 +116,8 @@ SIGNATURES = {
     "mcacg_batch_create": [C.POINTER(Params), i32, vp, C.POINTER(vp)],
     "mcacg_batch_create_from_states": [C.POINTER(Params), C.POINTER(State), i32, vp, C.POINTER(vp)],
     "mcacg_batch_destroy": [vp],
+    "mcacg_host_alloc": [i64, C.POINTER(vp)],
+    "mcacg_host_free": [vp],
     "mcacg_resident_boxes": [i32, C.POINTER(i32)],
     "mcacg_batch_set_threads": [vp, i32],
     "mcacg_batch_threads": [vp, C.POINTER(i32)],
@@ -202,22 +204,57 @@ def ptr(arr: np.ndarray, ctype):
     return arr.ctypes.data_as(C.POINTER(ctype))
 
 
-class StateBuffers:
-    """Host arrays behind an mcacg_state (keeps them alive)."""
+class _PinnedBlock:
+    """Page-locked host memory from the library, freed with the last array
+    that views it."""
 
-    def __init__(self, n_spheres: int, n_aggregates: int):
-        self.spheres = np.zeros((9, n_spheres), dtype=np.float64)
-        self.sphere_label = np.zeros(n_spheres, dtype=np.int64)
-        self.aggregates = np.zeros((21, n_aggregates), dtype=np.float64)
-        self.n_spheres = np.zeros(n_aggregates, dtype=np.int64)
-        self.members = np.zeros(n_spheres, dtype=np.int64)
-        self.state = State(n_spheres, n_aggregates, 0, 0.0, 0.0, 0.0,
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        check(lib().mcacg_host_alloc(int(nbytes), C.byref(p)))
+        self.ptr, self.nbytes = p.value, int(nbytes)
+
+    def __del__(self):
+        if self.ptr:
+            lib().mcacg_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+    def buffer(self):
+        buf = (C.c_char * self.nbytes).from_address(self.ptr)
+        buf._owner = self  # the numpy views keep the block alive through buf
+        return buf
+
+
+class StateBuffers:
+    """Host arrays behind an mcacg_state (keeps them alive). With
+    pinned=True they sit in one page-locked block, so loading and storing
+    the state moves them by DMA."""
+
+    def __init__(self, n_spheres: int, n_aggregates: int, pinned: bool = False):
+        ns, na = int(n_spheres), int(n_aggregates)
+        if pinned:
+            layout = [("spheres", np.float64, (9, ns)), ("sphere_label", np.int64, (ns,)),
+                      ("aggregates", np.float64, (21, na)), ("n_spheres", np.int64, (na,)),
+                      ("members", np.int64, (ns,))]
+            total = sum(8 * int(np.prod(shape)) for _, _, shape in layout)
+            buf = _PinnedBlock(max(total, 8)).buffer()
+            off = 0
+            for name, dt, shape in layout:
+                count = int(np.prod(shape))
+                setattr(self, name, np.frombuffer(buf, dtype=dt, count=count, offset=off).reshape(shape))
+                off += 8 * count
+        else:
+            self.spheres = np.zeros((9, ns), dtype=np.float64)
+            self.sphere_label = np.zeros(ns, dtype=np.int64)
+            self.aggregates = np.zeros((21, na), dtype=np.float64)
+            self.n_spheres = np.zeros(na, dtype=np.int64)
+            self.members = np.zeros(ns, dtype=np.int64)
+        self.state = State(ns, na, 0, 0.0, 0.0, 0.0,
                            ptr(self.spheres, f64), ptr(self.sphere_label, i64), ptr(self.aggregates, f64),
                            ptr(self.n_spheres, i64), ptr(self.members, i64))
 
     @classmethod
-    def from_snapshot(cls, snap) -> "StateBuffers":
-        sb = cls(snap.ns, snap.na)
+    def from_snapshot(cls, snap, pinned: bool = False) -> "StateBuffers":
+        sb = cls(snap.ns, snap.na, pinned=pinned)
         sb.spheres[...] = snap.spheres
         sb.sphere_label[...] = snap.sphere_label
         sb.aggregates[...] = snap.aggregates

@@ -395,22 +395,24 @@ class Batch:
         check(lib().mcacg_batch_last_run(self._b, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
-    def store_all(self, raw: bool = False, out: list | None = None) -> list:
+    def box_sizes(self, box: int) -> tuple[int, int]:
+        """(spheres, live aggregates) of one box: the sizes its stored state needs."""
+        ns, na = C.c_int64(), C.c_int64()
+        check(lib().mcacg_batch_box_sizes(self._b, int(box), C.byref(ns), C.byref(na)))
+        return ns.value, max(na.value, 1)
+
+    def store_all(self, raw: bool = False, out: list | None = None, pinned: bool = False) -> list:
         """The state of every box (one call, converted in parallel): as
         Snapshots, or with raw=True as the filled host arrays
         (StateBuffers), without further copies. 'out' may supply the
         StateBuffers to fill (one per box, large enough), e.g. buffers kept
-        from an earlier call."""
+        from an earlier call; new buffers are page-locked with pinned=True."""
         if out is not None:
             bufs = list(out)
             for b in bufs:
                 b.state.n_spheres, b.state.n_aggregates = b.spheres.shape[1], b.aggregates.shape[1]
         else:
-            bufs = []
-            for box in range(len(self.models)):
-                ns, na = C.c_int64(), C.c_int64()
-                check(lib().mcacg_batch_box_sizes(self._b, box, C.byref(ns), C.byref(na)))
-                bufs.append(StateBuffers(ns.value, max(na.value, 1)))
+            bufs = [StateBuffers(*self.box_sizes(box), pinned=pinned) for box in range(len(self.models))]
         arr = (_lib.State * len(bufs))(*[b.state for b in bufs])
         check(lib().mcacg_batch_store_states(self._b, arr, len(bufs)))
         for k, b in enumerate(bufs):
@@ -423,9 +425,7 @@ class Batch:
         return [b.to_snapshot(volsurf_method=int(self.models[k].params.volsurf_method)) for k, b in enumerate(bufs)]
 
     def store(self, box: int) -> Snapshot:
-        ns, na = C.c_int64(), C.c_int64()
-        check(lib().mcacg_batch_box_sizes(self._b, int(box), C.byref(ns), C.byref(na)))
-        sb = StateBuffers(ns.value, max(na.value, 1))
+        sb = StateBuffers(*self.box_sizes(box))
         check(lib().mcacg_batch_store_state(self._b, int(box), C.byref(sb.state)))
         return sb.to_snapshot(volsurf_method=int(self.models[box].params.volsurf_method))
 

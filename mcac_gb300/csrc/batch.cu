@@ -244,6 +244,14 @@ int BatchRunner::resident_boxes(int threads, int *boxes, std::string *err) {
 
 int BatchRunner::create(const std::vector<mcacg_params> &params, std::vector<HostState> &&states, void *stream,
                         std::unique_ptr<BatchRunner> *out, std::string *err) {
+    std::vector<StateView> views(states.size());
+    std::vector<std::vector<int>> compact(states.size());
+    parallel_for(int(states.size()), [&](int i) { views[size_t(i)] = view_of(states[size_t(i)], &compact[size_t(i)]); });
+    return create(params, views, stream, out, err);
+}
+
+int BatchRunner::create(const std::vector<mcacg_params> &params, const std::vector<StateView> &states, void *stream,
+                        std::unique_ptr<BatchRunner> *out, std::string *err) {
     if (params.size() != states.size() || params.empty()) {
         if (err) *err = "one parameter set per state is needed";
         return ST_BAD_ARGUMENT;
@@ -259,7 +267,6 @@ int BatchRunner::create(const std::vector<mcacg_params> &params, std::vector<Hos
     parallel_for(n, [&](int i) {
         rcs[size_t(i)] = DeviceBox::create(states[size_t(i)], nullptr, &made[size_t(i)], &errs[size_t(i)]);
         times[size_t(i)] = states[size_t(i)].time;
-        states[size_t(i)] = HostState();  // release host memory early
     });
     for (int i = 0; i < n; ++i) {
         if (made[size_t(i)]) {

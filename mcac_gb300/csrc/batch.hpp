@@ -27,6 +27,10 @@ class BatchRunner {
     // seed (its device rand() stream is seeded with params[i].random_seed).
     static int create(const std::vector<mcacg_params> &params, std::vector<HostState> &&states, void *stream,
                       std::unique_ptr<BatchRunner> *out, std::string *err);
+    // The same from states in host memory that the caller keeps (page-locked
+    // arrays are copied by DMA, without a host-side copy).
+    static int create(const std::vector<mcacg_params> &params, const std::vector<StateView> &states, void *stream,
+                      std::unique_ptr<BatchRunner> *out, std::string *err);
     // Runs existing device boxes (owned elsewhere) with the device loop.
     static int attach(const std::vector<mcacg_params> &params, const std::vector<DeviceBox *> &boxes,
                       const std::vector<double> &times, void *stream, std::unique_ptr<BatchRunner> *out,

@@ -138,6 +138,173 @@ __global__ void k_refresh_f4(DevBox b) {
         b.agg_f4[a] = make_float4(float(A(b, AGG_X, a)), float(A(b, AGG_Y, a)), float(A(b, AGG_Z, a)),
                                   float(A(b, AGG_RMAX, a)));
 }
+
+// Loading a state: the sphere and aggregate tables go straight to their
+// places; the integer arrays (owning slot per sphere, spheres per slot,
+// member lists in slot order) are staged as 32- or 64-bit values and
+// converted here, with the pool built from the member lists. Inconsistent
+// input is flagged (sc->pad[0] = the LoadError, status BAD_ARGUMENT) and
+// never read out of bounds.
+enum LoadError { LOAD_OK = 0, LOAD_LABEL = 1, LOAD_COUNT = 2, LOAD_COVER = 3, LOAD_MEMBER = 4 };
+struct LoadStage {
+    const void *label, *count, *members;
+    int wide;     // 64-bit integers
+    int dead_ok;  // slots without spheres are allowed
+};
+__device__ __forceinline__ long long load_int(const void *p, int wide, int i) {
+    return wide ? static_cast<const long long *>(p)[i] : static_cast<long long>(static_cast<const int *>(p)[i]);
+}
+__device__ __forceinline__ void load_fail(DevBox &b, int code) {
+    atomicCAS(&b.sc->pad[0], 0, code);
+    b.sc->status = ST_BAD_ARGUMENT;
+}
+constexpr int kLoadScanThreads = 1024;
+// spheres per slot, pool offsets (exclusive sum in slot order), live count
+__global__ void __launch_bounds__(kLoadScanThreads) k_load_counts(DevBox b, LoadStage in) {
+    __shared__ long long part[kLoadScanThreads];
+    __shared__ int alive[kLoadScanThreads];
+    __shared__ int bad;
+    const int t = threadIdx.x;
+    if (t == 0) bad = 0;
+    __syncthreads();
+    const int chunk = (b.nslots + kLoadScanThreads - 1) / kLoadScanThreads;
+    const int a0 = min(b.nslots, t * chunk), a1 = min(b.nslots, a0 + chunk);
+    long long sum = 0;
+    int live = 0, flag = 0;
+    for (int a = a0; a < a1; ++a) {
+        long long n = load_int(in.count, in.wide, a);
+        if (n < 0 || n > b.ns || (n == 0 && !in.dead_ok)) {
+            flag = 1;
+            n = 0;
+        }
+        sum += n;
+        live += n > 0;
+    }
+    part[t] = sum;
+    alive[t] = live;
+    if (flag) atomicOr(&bad, 1);
+    __syncthreads();
+    if (t == 0) {
+        if (bad) load_fail(b, LOAD_COUNT);
+        long long run = 0;
+        int n_alive = 0;
+        for (int k = 0; k < kLoadScanThreads; ++k) {
+            const long long v = part[k];
+            part[k] = run;
+            run += v;
+            n_alive += alive[k];
+        }
+        b.sc->n_alive = n_alive;
+        b.sc->pool_top = b.ns;
+        if (run != b.ns) load_fail(b, LOAD_COVER);
+    }
+    __syncthreads();
+    long long off = part[t];
+    for (int a = a0; a < a1; ++a) {
+        long long n = load_int(in.count, in.wide, a);
+        if (n < 0 || n > b.ns || (n == 0 && !in.dead_ok)) n = 0;
+        b.agg_n[a] = int(n);
+        b.agg_off[a] = int(min(off, (long long)b.ns));
+        off += n;
+    }
+}
+// owning slots, pool ids and pool positions (pool entry k = member k)
+__global__ void k_load_spheres(DevBox b, LoadStage in) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < b.ns; s += gridDim.x * blockDim.x) {
+        long long l = load_int(in.label, in.wide, s);
+        if (l < 0 || l >= b.nslots) {
+            load_fail(b, LOAD_LABEL);
+            l = 0;
+        }
+        b.sph_slot[s] = int(l);
+        long long m = load_int(in.members, in.wide, s);
+        if (m < 0 || m >= b.ns) {
+            load_fail(b, LOAD_MEMBER);
+            m = 0;
+        }
+        b.pool_id[0][s] = int(m);
+        b.pool_pos[0][s] = make_float4(float(S(b, SPH_X, int(m))), float(S(b, SPH_Y, int(m))),
+                                       float(S(b, SPH_Z, int(m))), float(S(b, SPH_R, int(m))));
+    }
+    for (int k = b.ns + blockIdx.x * blockDim.x + threadIdx.x; k < b.pool_cap; k += gridDim.x * blockDim.x) {
+        b.pool_id[0][k] = 0;
+        b.pool_pos[0][k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+// Storing a state: the live slots are packed in slot order (label = rank
+// among the live slots, as the reference's list has them), with their member
+// lists back to back, into the staging area; the host copies the pieces out.
+struct PackStage {
+    double *agg;       // [21][na]
+    long long *count;  // [na]
+    long long *label;  // [ns]
+    long long *members;// [ns]
+    int *rank;         // [nslots]
+    int *moff;         // [nslots] first member of the slot in 'members'
+    int na;
+    int sel;           // live pool buffer
+};
+__global__ void __launch_bounds__(kLoadScanThreads) k_pack_ranks(DevBox b, PackStage out) {
+    __shared__ int live_part[kLoadScanThreads];
+    __shared__ int mem_part[kLoadScanThreads];
+    const int t = threadIdx.x;
+    const int chunk = (b.nslots + kLoadScanThreads - 1) / kLoadScanThreads;
+    const int a0 = min(b.nslots, t * chunk), a1 = min(b.nslots, a0 + chunk);
+    int live = 0, mem = 0;
+    for (int a = a0; a < a1; ++a) {
+        const int n = b.agg_n[a];
+        live += n > 0;
+        mem += n;
+    }
+    live_part[t] = live;
+    mem_part[t] = mem;
+    __syncthreads();
+    if (t == 0) {
+        int rl = 0, rm = 0;
+        for (int k = 0; k < kLoadScanThreads; ++k) {
+            const int l = live_part[k], m = mem_part[k];
+            live_part[k] = rl;
+            mem_part[k] = rm;
+            rl += l;
+            rm += m;
+        }
+    }
+    __syncthreads();
+    int r = live_part[t], o = mem_part[t];
+    for (int a = a0; a < a1; ++a) {
+        const int n = b.agg_n[a];
+        out.rank[a] = n > 0 ? r : -1;
+        out.moff[a] = o;
+        r += n > 0;
+        o += n;
+    }
+}
+__global__ void k_pack(DevBox b, PackStage out) {
+    const int stride = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int *pool = b.pool_id[out.sel];
+    for (int a = t; a < b.nslots; a += stride) {
+        const int r = out.rank[a];
+        if (r < 0 || r >= out.na) continue;
+        const int n = b.agg_n[a];
+        out.count[r] = n;
+        for (int f = 0; f < AGG_NFIELDS; ++f) out.agg[size_t(f) * out.na + r] = A(b, f, a);
+        const int src = b.agg_off[a], dst = out.moff[a];
+        for (int k = 0; k < n && dst + k < b.ns && src + k < b.pool_cap; ++k) out.members[dst + k] = pool[src + k];
+    }
+    for (int s = t; s < b.ns; s += stride) out.label[s] = out.rank[b.sph_slot[s]];
+}
+
+// every member of slot a is owned by slot a
+__global__ void k_load_check(DevBox b) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nslots; a += gridDim.x * blockDim.x) {
+        const int o = b.agg_off[a], e = min(b.ns, o + b.agg_n[a]);
+        for (int k = o; k < e; ++k)
+            if (b.sph_slot[b.pool_id[0][k]] != a) {
+                load_fail(b, LOAD_MEMBER);
+                break;
+            }
+    }
+}
 // ------------------------------------------------------------------- host
 namespace {
 
@@ -154,12 +321,56 @@ struct OutBuffers {
 
 }  // namespace
 
+StateView view_of(const HostState &st, std::vector<int> *compact) {
+    StateView v;
+    v.n_div = st.n_div;
+    v.box_length = st.box_length;
+    v.maxradius = st.maxradius;
+    v.time = st.time;
+    v.ns = st.ns;
+    v.nslots = st.nslots;
+    v.sph = st.sph.data();
+    v.agg = st.agg.data();
+    v.sph_slot = st.sph_slot.data();
+    v.agg_n = st.agg_n.data();
+    v.wide = false;
+    v.dead_slots = true;
+    // the member lists are usually stored back to back in slot order, dead
+    // slots empty; otherwise they are gathered
+    bool packed = st.members.count() == size_t(st.nslots) && st.members.ids.size() == size_t(st.ns);
+    for (int a = 0; packed && a < st.nslots; ++a)
+        packed = st.members[size_t(a)].size() == st.agg_n[size_t(a)];
+    if (packed) {
+        v.members = st.members.ids.data();
+    } else {
+        compact->clear();
+        compact->reserve(size_t(st.ns));
+        for (int a = 0; a < st.nslots && a < int(st.members.count()); ++a)
+            if (st.agg_n[size_t(a)] > 0)
+                for (int s : st.members[size_t(a)]) compact->push_back(s);
+        compact->resize(size_t(st.ns), -1);  // a short list is flagged by the load check
+        v.members = compact->data();
+    }
+    return v;
+}
+
 int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::string *err) {
+    std::vector<int> compact;
+    const StateView v = view_of(st, &compact);
+    return create(v, stream, out, err);
+}
+
+int DeviceBox::create(const StateView &st, void *stream, DeviceBox **out, std::string *err) {
     *out = nullptr;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         if (err) *err = "no CUDA device";
         return ST_NO_DEVICE;
+    }
+    if (st.ns <= 0 || st.nslots <= 0 || st.nslots > st.ns || !st.sph || !st.agg || !st.sph_slot || !st.agg_n ||
+        !st.members || !(st.box_length > 0.0) || st.n_div <= 0) {
+        if (err) *err = "incomplete state";
+        return ST_BAD_ARGUMENT;
     }
     DeviceBox *d = new DeviceBox();
     d->ns_ = st.ns;
@@ -171,26 +382,34 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     b.n_cells = st.n_div * st.n_div * st.n_div;
     b.ns = st.ns;
     b.nslots = st.nslots;
+    const double *agg = st.agg;
+    auto AF = [&](int f, int a) { return agg[size_t(f) * size_t(st.nslots) + size_t(a)]; };
     // FP32 screening margin: coordinates are bounded by the box plus the
     // largest aggregate; 2^-17 of that bound is >10x the FP32 error of the
     // capsule test.
-    double rmax_all = st.maxradius;
-    for (int a = 0; a < st.nslots; ++a)
-        if (st.agg_n[a] > 0) rmax_all = std::max(rmax_all, st.agg[size_t(AGG_RMAX) * st.nslots + a]);
+    // one pass over the live slots: largest r_max, the means of lpm and
+    // r_max, and the Verlet cell counts (for the cell capacity)
+    double rmax_all = st.maxradius, lpm_sum = 0.0, rmax_sum = 0.0;
+    int live = 0, maxc = 0;
+    std::vector<int> cell_n(size_t(b.n_cells), 0);
+    for (int a = 0; a < st.nslots; ++a) {
+        if (st.count(a) <= 0) continue;
+        const double rm = AF(AGG_RMAX, a);
+        rmax_all = std::max(rmax_all, rm);
+        lpm_sum += AF(AGG_LPM, a);
+        rmax_sum += rm;
+        ++live;
+        const int ix = std::min(std::max(verlet_coord(AF(AGG_X, a), b.step), 0), b.n_div - 1);
+        const int iy = std::min(std::max(verlet_coord(AF(AGG_Y, a), b.step), 0), b.n_div - 1);
+        const int iz = std::min(std::max(verlet_coord(AF(AGG_Z, a), b.step), 0), b.n_div - 1);
+        maxc = std::max(maxc, ++cell_n[size_t((ix * b.n_div + iy) * b.n_div + iz)]);
+    }
     b.margin = (3.0 * st.box_length + 4.0 * rmax_all) * (1.0 / 131072.0);
     // fine discovery grid, when finer than the Verlet grid: a query visits
     // the cells covering its swept box, about lpm/2 + 2 (r_max + max r_max)
     // per axis on average; cells of 0.6 of that balance the cells visited
     // against the aggregates screened. At least 2 max r_max and L/128.
     {
-        double lpm_sum = 0.0, rmax_sum = 0.0;
-        int live = 0;
-        for (int a = 0; a < st.nslots; ++a)
-            if (st.agg_n[a] > 0) {
-                lpm_sum += st.agg[size_t(AGG_LPM) * st.nslots + a];
-                rmax_sum += st.agg[size_t(AGG_RMAX) * st.nslots + a];
-                ++live;
-            }
         const double extent = live ? 0.5 * lpm_sum / live + 2.0 * (rmax_sum / live + rmax_all) : 0.0;
         const double h = std::max({2.0 * rmax_all, st.box_length / double(kFineMaxDiv), 0.6 * extent});
         const double nf = std::floor(st.box_length / h);
@@ -198,18 +417,6 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
         b.fine_step = b.fine_div > 0 ? double(b.fine_div) / st.box_length : 0.0;
     }
     // grid capacity
-    std::vector<int> cell_n(size_t(b.n_cells), 0);
-    int maxc = 0;
-    for (int a = 0; a < st.nslots; ++a) {
-        if (st.agg_n[a] == 0) continue;
-        const double *ag = st.agg.data();
-        double x = ag[size_t(AGG_X) * st.nslots + a], y = ag[size_t(AGG_Y) * st.nslots + a],
-               z = ag[size_t(AGG_Z) * st.nslots + a];
-        int ix = std::min(std::max(verlet_coord(x, b.step), 0), b.n_div - 1);
-        int iy = std::min(std::max(verlet_coord(y, b.step), 0), b.n_div - 1);
-        int iz = std::min(std::max(verlet_coord(z, b.step), 0), b.n_div - 1);
-        maxc = std::max(maxc, ++cell_n[size_t((ix * b.n_div + iy) * b.n_div + iz)]);
-    }
     int avg = (st.nslots + b.n_cells - 1) / b.n_cells;
     b.cell_cap = std::max({64, 2 * maxc, 8 * avg});
     b.pool_cap = 2 * st.ns + 1024;
@@ -269,12 +476,21 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     ok = ok && alloc((void **)&b.sc, sizeof(DevScalars));
     ok = ok && alloc((void **)&b.surv, sizeof(int4) * size_t(b.surv_cap));
     ok = ok && alloc((void **)&b.surv_res, sizeof(double) * size_t(b.surv_cap));
-    ok = ok && alloc((void **)&b.pair_i, sizeof(int) * size_t(b.pair_cap));
-    ok = ok && alloc((void **)&b.pair_j, sizeof(int) * size_t(b.pair_cap));
-    ok = ok && alloc((void **)&b.pair_d, sizeof(double) * size_t(b.pair_cap));
-    ok = ok && alloc((void **)&b.pair_tmp_i, sizeof(int) * size_t(b.pair_cap));
-    ok = ok && alloc((void **)&b.pair_tmp_j, sizeof(int) * size_t(b.pair_cap));
-    ok = ok && alloc((void **)&b.pair_tmp_d, sizeof(double) * size_t(b.pair_cap));
+    // the merge's pair scratch is one block (32 B per pair), which also
+    // stages a packed state on its way to the host
+    {
+        char *pairs = nullptr;
+        const size_t pc = size_t(b.pair_cap);
+        ok = ok && alloc((void **)&pairs, 32 * pc);
+        b.pair_i = reinterpret_cast<int *>(pairs);
+        b.pair_j = b.pair_i + pc;
+        b.pair_tmp_i = b.pair_j + pc;
+        b.pair_tmp_j = b.pair_tmp_i + pc;
+        b.pair_d = reinterpret_cast<double *>(pairs + 16 * pc);
+        b.pair_tmp_d = b.pair_d + pc;
+        d->stage_ = pairs;
+        d->stage_bytes_ = 32 * pc;
+    }
     ok = ok && alloc((void **)&b.row_cnt, sizeof(int) * (size_t(std::max(st.ns, st.nslots)) + 2));
     ok = ok && alloc((void **)&b.work, sizeof(double) * 8 * size_t(st.ns));
     ok = ok && alloc((void **)&b.counters, sizeof(int) * 8);
@@ -298,54 +514,59 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
         d->stream_ = s;
         d->own_stream_ = true;
     }
-    // upload
-    std::vector<int> off(size_t(st.nslots), 0), pool_id(size_t(b.pool_cap), 0);
-    std::vector<float4> pool_pos(size_t(b.pool_cap));
-    int top = 0;
-    for (int a = 0; a < st.nslots; ++a) {
-        off[size_t(a)] = top;
-        if (st.agg_n[a] == 0) continue;
-        for (int s : st.members[size_t(a)]) {
-            pool_id[size_t(top)] = s;
-            pool_pos[size_t(top)] = make_float4(float(st.sph[size_t(SPH_X) * st.ns + s]),
-                                                float(st.sph[size_t(SPH_Y) * st.ns + s]),
-                                                float(st.sph[size_t(SPH_Z) * st.ns + s]),
-                                                float(st.sph[size_t(SPH_R) * st.ns + s]));
-            ++top;
-        }
-    }
+    // upload: the tables straight to their places, the integer arrays to
+    // the box's work area (64 B per sphere; 16 B per sphere and 8 B per slot
+    // at most are needed), converted and checked there by the load kernels
     DevScalars sc{};
     sc.maxradius = st.maxradius;
     sc.time = st.time;
-    sc.pool_top = top;
     sc.pool_sel = 0;
-    int alive = 0;
-    for (int a = 0; a < st.nslots; ++a) alive += st.agg_n[a] > 0;
-    sc.n_alive = alive;
+    const size_t iw = st.wide ? 8 : 4;
+    char *stage = reinterpret_cast<char *>(b.work);
+    LoadStage in{stage, stage + 2 * iw * size_t(st.ns), stage + iw * size_t(st.ns), st.wide ? 1 : 0,
+                 st.dead_slots ? 1 : 0};
     // copies on the box's own stream (boxes of a batch are built in parallel,
     // each on a stream of its own); the host arrays stay alive until the
-    // grid build below synchronises the stream
+    // status read below synchronises the stream
     cudaStream_t s = static_cast<cudaStream_t>(d->stream_);
-    auto put = [&](void *dst, const void *src, size_t bytes) {
-        return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s), err, "upload");
+    auto put = [&](const void *dst, const void *src, size_t bytes) {
+        return cuda_ok(cudaMemcpyAsync(const_cast<void *>(dst), src, bytes, cudaMemcpyHostToDevice, s), err, "upload");
     };
-    ok = ok && put(b.sph, st.sph.data(), sizeof(double) * 9 * size_t(st.ns)) &&
-         put(b.sph_slot, st.sph_slot.data(), sizeof(int) * size_t(st.ns)) &&
-         put(b.agg, st.agg.data(), sizeof(double) * 21 * size_t(st.nslots)) &&
-         put(b.agg_n, st.agg_n.data(), sizeof(int) * size_t(st.nslots)) &&
-         put(b.agg_off, off.data(), sizeof(int) * size_t(st.nslots)) &&
-         put(b.pool_id[0], pool_id.data(), sizeof(int) * size_t(b.pool_cap)) &&
-         put(b.pool_pos[0], pool_pos.data(), sizeof(float4) * size_t(b.pool_cap)) && put(b.sc, &sc, sizeof(sc));
+    ok = ok && put(b.sph, st.sph, sizeof(double) * 9 * size_t(st.ns)) &&
+         put(b.agg, st.agg, sizeof(double) * 21 * size_t(st.nslots)) && put(in.label, st.sph_slot, iw * size_t(st.ns)) &&
+         put(in.members, st.members, iw * size_t(st.ns)) && put(in.count, st.agg_n, iw * size_t(st.nslots)) &&
+         put(b.sc, &sc, sizeof(sc));
     if (!ok) {
         delete d;
         return ST_CUDA;
+    }
+    {
+        const int blocks = std::min(1024, (std::max(st.ns, st.nslots) + 255) / 256);
+        k_load_counts<<<1, kLoadScanThreads, 0, s>>>(b, in);
+        k_load_spheres<<<blocks, 256, 0, s>>>(b, in);
+        k_load_check<<<blocks, 256, 0, s>>>(b);
+        if (!cuda_ok(cudaGetLastError(), err, "state load")) {
+            delete d;
+            return ST_CUDA;
+        }
+        DevScalars got;
+        if (!cuda_ok(cudaMemcpyAsync(&got, b.sc, sizeof(got), cudaMemcpyDeviceToHost, s), err, "status") ||
+            !cuda_ok(cudaStreamSynchronize(s), err, "sync")) {
+            delete d;
+            return ST_CUDA;
+        }
+        if (got.status != ST_OK) {
+            static const char *const what[] = {"state rejected", "sphere label out of range",
+                                                "bad sphere count of an aggregate",
+                                                "member lists do not cover every sphere once",
+                                                "member list inconsistent with sphere labels"};
+            const int code = got.pad[0];
+            if (err) *err = what[(code >= 0 && code <= LOAD_MEMBER) ? code : 0];
+            delete d;
+            return ST_BAD_ARGUMENT;
+        }
     }
     d->devbox_ = new DevBox(b);
-    if (!ok) {
-        delete d;
-        return ST_CUDA;
-    }
-    (void)s;
     int rc = d->rebuild_grid(b.cell_cap, err);
     if (rc != ST_OK) {
         delete d;
@@ -742,6 +963,61 @@ int DeviceBox::download(HostState *st, std::string *err, void *copy_stream) {
     for (int a = 0; a < b.nslots; ++a) st->members.push_list(pool.data() + off[size_t(a)], st->agg_n[size_t(a)]);
     st->maxradius = sc.maxradius;
     st->time = sc.time;
+    return ST_OK;
+}
+
+int DeviceBox::store(mcacg_state *out, std::string *err, void *copy_stream) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    cudaStream_t cs = copy_stream ? static_cast<cudaStream_t>(copy_stream) : s;
+    if (!out->spheres || !out->sphere_label || !out->aggregates || !out->n_spheres_per_aggregate || !out->members) {
+        if (err) *err = "incomplete state buffers";
+        return ST_BAD_ARGUMENT;
+    }
+    if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
+    DevScalars sc;
+    if (!cuda_ok(cudaMemcpyAsync(&sc, b.sc, sizeof(sc), cudaMemcpyDeviceToHost, cs), err, "store") ||
+        !cuda_ok(cudaStreamSynchronize(cs), err, "store"))
+        return ST_CUDA;
+    const int na = sc.n_alive;
+    if (out->n_spheres < b.ns || out->n_aggregates < na || na < 1) {
+        if (err) *err = "state buffers too small";
+        return ST_BAD_ARGUMENT;
+    }
+    const size_t need = 176 * size_t(na) + 16 * size_t(b.ns) + 8 * size_t(b.nslots);
+    if (need > stage_bytes_) {
+        if (err) *err = "store staging area too small";
+        return ST_CAPACITY;
+    }
+    char *p = static_cast<char *>(stage_);
+    PackStage ps;
+    ps.agg = reinterpret_cast<double *>(p);
+    ps.count = reinterpret_cast<long long *>(p + 168 * size_t(na));
+    ps.label = reinterpret_cast<long long *>(p + 176 * size_t(na));
+    ps.members = ps.label + b.ns;
+    ps.rank = reinterpret_cast<int *>(ps.members + b.ns);
+    ps.moff = ps.rank + b.nslots;
+    ps.na = na;
+    ps.sel = sc.pool_sel;
+    const int blocks = std::min(1024, (std::max(b.ns, b.nslots) + 255) / 256);
+    k_pack_ranks<<<1, kLoadScanThreads, 0, cs>>>(b, ps);
+    k_pack<<<blocks, 256, 0, cs>>>(b, ps);
+    if (!cuda_ok(cudaGetLastError(), err, "store")) return ST_CUDA;
+    auto get = [&](void *dst, const void *src, size_t bytes) {
+        return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, cs), err, "store");
+    };
+    const bool ok = get(out->spheres, b.sph, sizeof(double) * 9 * size_t(b.ns)) &&
+                    get(out->sphere_label, ps.label, 8 * size_t(b.ns)) &&
+                    get(out->aggregates, ps.agg, 168 * size_t(na)) &&
+                    get(out->n_spheres_per_aggregate, ps.count, 8 * size_t(na)) &&
+                    get(out->members, ps.members, 8 * size_t(b.ns)) && cuda_ok(cudaStreamSynchronize(cs), err, "store");
+    if (!ok) return ST_CUDA;
+    out->n_spheres = b.ns;
+    out->n_aggregates = na;
+    out->n_verlet_divisions = b.n_div;
+    out->box_length = b.L;
+    out->maxradius = sc.maxradius;
+    out->time = sc.time;
     return ST_OK;
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <atomic>
 #include <thread>
 #include <vector>
@@ -493,19 +494,36 @@ int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state
         if (!params || !states || !batch || n_boxes <= 0) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
         *batch = nullptr;
         std::vector<mcacg_params> ps(params, params + n_boxes);
-        std::vector<mcacg::HostState> hs(static_cast<size_t>(n_boxes));
-        std::vector<int> rcs(static_cast<size_t>(n_boxes), 0);
-        std::vector<std::string> errs(static_cast<size_t>(n_boxes));
-        mcacg::parallel_for(n_boxes, [&](int i) {
-            rcs[size_t(i)] = mcacg::state_to_host(states[i], &hs[size_t(i)], &errs[size_t(i)]);
-            ps[size_t(i)].box_length = states[i].box_length;
-            ps[size_t(i)].n_verlet_divisions = states[i].n_verlet_divisions;
-        });
-        for (int i = 0; i < n_boxes; ++i)
-            if (rcs[size_t(i)] != 0) return fail(rcs[size_t(i)], "box " + std::to_string(i) + ": " + errs[size_t(i)]);
+        // the boxes load straight from the caller's arrays (by DMA when they
+        // are page-locked); the device checks labels, counts and member lists
+        std::vector<mcacg::StateView> views(static_cast<size_t>(n_boxes));
+        for (int i = 0; i < n_boxes; ++i) {
+            const mcacg_state &in = states[i];
+            if (in.n_spheres <= 0 || in.n_aggregates <= 0 || in.n_spheres > INT32_MAX ||
+                in.n_aggregates > in.n_spheres || !in.spheres || !in.sphere_label || !in.aggregates ||
+                !in.n_spheres_per_aggregate || !in.members || in.n_verlet_divisions <= 0 ||
+                in.n_verlet_divisions > 1024 || !(in.box_length > 0.0))
+                return fail(mcacg::ST_BAD_ARGUMENT, "box " + std::to_string(i) + ": incomplete state");
+            mcacg::StateView &v = views[size_t(i)];
+            v.n_div = int(in.n_verlet_divisions);
+            v.box_length = in.box_length;
+            v.maxradius = in.maxradius;
+            v.time = in.time;
+            v.ns = int(in.n_spheres);
+            v.nslots = int(in.n_aggregates);
+            v.sph = in.spheres;
+            v.agg = in.aggregates;
+            v.sph_slot = in.sphere_label;
+            v.agg_n = in.n_spheres_per_aggregate;
+            v.members = in.members;
+            v.wide = true;
+            v.dead_slots = false;
+            ps[size_t(i)].box_length = in.box_length;
+            ps[size_t(i)].n_verlet_divisions = in.n_verlet_divisions;
+        }
         std::string err;
         std::unique_ptr<mcacg_batch> b(new mcacg_batch());
-        int rc = mcacg::BatchRunner::create(ps, std::move(hs), cuda_stream, &b->impl, &err);
+        int rc = mcacg::BatchRunner::create(ps, views, cuda_stream, &b->impl, &err);
         if (rc != 0) return finish(rc, err);
         b->params = ps;
         *batch = b.release();
@@ -580,8 +598,15 @@ int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state)
     return guarded([&] {
         if (!batch || !state || box < 0 || box >= batch->impl->size())
             return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
-        mcacg::HostState st;
         std::string err;
+        if (!batch->impl->grows(box)) {
+            std::vector<double> times;
+            int rc = batch->impl->times(&times, &err);
+            if (rc == 0) rc = batch->impl->box(box).store(state, &err);
+            if (rc == 0) state->time = times[size_t(box)];
+            return finish(rc, err);
+        }
+        mcacg::HostState st;
         int rc = batch->impl->download(box, &st, &err);
         if (rc != 0) return finish(rc, err);
         return finish(store_host_state(st, state, &err), err);
@@ -607,15 +632,42 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
         mcacg::parallel_for(n_boxes, [&](int i) {
             thread_local CopyStream cs;
             if (!cs.s) cudaStreamCreateWithFlags(&cs.s, cudaStreamNonBlocking);
+            if (!batch->impl->grows(i)) {
+                // packed on the device and copied straight into the caller's arrays
+                rcs[size_t(i)] = batch->impl->box(i).store(&states[i], &errs[size_t(i)], cs.s);
+                states[i].time = times[size_t(i)];
+                return;
+            }
+            // growing boxes: overlap and coordination refreshed on the host
             mcacg::HostState st;
             rcs[size_t(i)] = batch->impl->box(i).download(&st, &errs[size_t(i)], cs.s);
             if (rcs[size_t(i)] != 0) return;
-            if (batch->impl->grows(i)) mcacg::host_refresh_overlap(&st);
+            mcacg::host_refresh_overlap(&st);
             st.time = times[size_t(i)];
             rcs[size_t(i)] = store_host_state(st, &states[i], &errs[size_t(i)]);
         });
         for (int i = 0; i < n_boxes; ++i)
             if (rcs[size_t(i)] != 0) return fail(rcs[size_t(i)], "box " + std::to_string(i) + ": " + errs[size_t(i)]);
+        return 0;
+    });
+}
+
+int mcacg_host_alloc(int64_t bytes, void **ptr) {
+    return guarded([&] {
+        if (!ptr || bytes <= 0) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
+        *ptr = nullptr;
+        cudaError_t e = cudaHostAlloc(ptr, size_t(bytes), cudaHostAllocPortable);
+        if (e != cudaSuccess) {
+            *ptr = nullptr;
+            return fail(mcacg::ST_CUDA, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+        }
+        return 0;
+    });
+}
+
+int mcacg_host_free(void *ptr) {
+    return guarded([&] {
+        if (ptr) cudaFreeHost(ptr);
         return 0;
     });
 }

@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include "../../include/mcacg.h"
+
 namespace mcacg {
 
 struct QueryOut;
@@ -58,6 +60,32 @@ struct HostState {
     MemberLists members;              // per slot, list order
 };
 
+// A box state in host memory, not owned: the tables of HostState or of an
+// mcacg_state. The integer arrays are 32-bit (HostState) or 64-bit
+// (mcacg_state, wide). Page-locked arrays are copied by DMA.
+struct StateView {
+    int n_div = 10;
+    double box_length = 0;
+    double maxradius = 0;
+    double time = 0;
+    int ns = 0;
+    int nslots = 0;
+    const double *sph = nullptr;    // [9][ns]
+    const double *agg = nullptr;    // [21][nslots]
+    const void *sph_slot = nullptr; // [ns] owning slot
+    const void *agg_n = nullptr;    // [nslots] spheres per slot (0: dead slot)
+    const void *members = nullptr;  // [ns] member lists of the slots, concatenated in slot order
+    bool wide = false;
+    bool dead_slots = true;         // slots without spheres are allowed
+    long long count(int a) const {
+        return wide ? static_cast<const long long *>(agg_n)[a] : static_cast<const int *>(agg_n)[a];
+    }
+};
+
+// The view of a HostState; 'compact' receives the member ids when the lists
+// are not stored back to back in slot order.
+StateView view_of(const HostState &st, std::vector<int> *compact);
+
 struct QueryResult {
     double distance;
     int moving_sphere, other_sphere, other_slot;
@@ -85,8 +113,11 @@ struct MergeResult {
 
 class DeviceBox {
   public:
-    // Uploads 'st' to the current device. Returns a status code.
+    // Uploads a state to the current device. Returns a status code; an
+    // inconsistent state (labels, counts, member lists) gives BAD_ARGUMENT.
+    // The host arrays must stay valid until this returns.
     static int create(const HostState &st, void *stream, DeviceBox **out, std::string *err);
+    static int create(const StateView &v, void *stream, DeviceBox **out, std::string *err);
     ~DeviceBox();
     DeviceBox(const DeviceBox &) = delete;
     DeviceBox &operator=(const DeviceBox &) = delete;
@@ -110,6 +141,13 @@ class DeviceBox {
     // on copy_stream when given (so several boxes can come back at once),
     // else on the box's stream.
     int download(HostState *st, std::string *err, void *copy_stream = nullptr);
+    // Stores the state straight into caller arrays in the layout of
+    // mcacg_state (live aggregates packed in slot order, labels = their
+    // ranks): packed on the device, then copied (by DMA into page-locked
+    // arrays). The overlap and coordination fields are those on the device.
+    // Capacities are out->n_spheres and out->n_aggregates; the scalars are
+    // set on return.
+    int store(mcacg_state *out, std::string *err, void *copy_stream = nullptr);
     // Rebuilds the Verlet grid from the aggregate positions with 'cap' rooms per cell.
     int rebuild_grid(int cap, std::string *err);
     int sync(std::string *err);
@@ -134,6 +172,8 @@ class DeviceBox {
     void *ev_[2] = {nullptr, nullptr};
     void *batch_mem_ = nullptr;  // query_batch scratch, grown on demand
     size_t batch_bytes_ = 0;
+    void *stage_ = nullptr;      // the merge's pair scratch, also the store staging area
+    size_t stage_bytes_ = 0;
     Profile prof_;
 };
 

@@ -231,3 +231,53 @@ def test_timed_runs_give_the_same_boxes():
         for s1, s2 in zip(b.store_all(), ref):
             assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
             assert np.array_equal(s1.members, s2.members)
+
+
+@pytest.mark.gpu
+def test_batch_loads_host_states_in_place():
+    """A batch made from host states (page-locked or not) holds them bit for
+    bit, continues them identically, and rejects inconsistent ones with the
+    reference's InputError-style status instead of reading out of bounds."""
+    from mcac_gb300._lib import MCACError, StateBuffers
+    models = [PhysicalModel(text=small_ini(n, 90 + k, mode="lognormal", disp=1.3, fv=4e-3))
+              for k, n in enumerate([240, 510, 330])]
+    with Batch(models) as b:
+        b.run(max_steps=1500, steps_per_launch=1500)
+        mid = b.store_all()
+        pinned = b.store_all(raw=True, pinned=True)
+    plain = [StateBuffers.from_snapshot(s) for s in mid]
+    finals = []
+    for states in (pinned, plain):
+        with Batch(models, states=states) as b:
+            for s1, s2 in zip(b.store_all(), mid):  # held exactly
+                assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
+                assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64))
+                assert np.array_equal(s1.members, s2.members) and np.array_equal(s1.sphere_label, s2.sphere_label)
+                assert s1.time == s2.time
+            b.run(max_steps=1000, steps_per_launch=1000)
+            assert np.all(b.stats()["status"] == 0)
+            finals.append(b.store_all())
+    for s1, s2 in zip(*finals):
+        assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
+        assert np.array_equal(s1.members, s2.members)
+    check_state(finals[0][0])
+
+    def broken(edit):
+        sb = StateBuffers.from_snapshot(mid[0])
+        edit(sb)
+        return sb
+
+    na = mid[0].na
+    first = int(mid[0].members[0])
+    other = int(mid[0].members[mid[0].n_spheres[0]])  # first member of aggregate 1
+    cases = [
+        (lambda sb: sb.sphere_label.__setitem__(3, na), "sphere label out of range"),
+        (lambda sb: sb.n_spheres.__setitem__(0, 0), "bad sphere count"),
+        (lambda sb: sb.n_spheres.__setitem__(1, sb.n_spheres[1] + 1), "cover every sphere"),
+        (lambda sb: sb.members.__setitem__(0, -7), "inconsistent"),
+        (lambda sb: sb.members.__setitem__(0, other), "inconsistent"),
+    ]
+    assert first != other
+    for edit, what in cases:
+        with pytest.raises(MCACError, match=what):
+            Batch(models[:1], states=[broken(edit)])

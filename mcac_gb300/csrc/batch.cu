@@ -90,6 +90,13 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
     }
 }
 
+// The pick trees of n boxes from their time steps, one block per box
+// (block_tree_build); the total weight goes to each box's loop state.
+__global__ void __launch_bounds__(256) k_tree_build(const BoxRun *runs, int n) {
+    if (int(blockIdx.x) >= n) return;
+    block_tree_build(runs[blockIdx.x]);
+}
+
 namespace {
 
 bool ok_cuda(cudaError_t e, std::string *err, const char *what) {
@@ -158,41 +165,16 @@ TreeLayout tree_layout(int nslots) {
     return t;
 }
 
-// Builds the sum tree (uploaded to a new device allocation), the loop state
-// and the run descriptor of one box.
+// The loop state and the launch record of one box; 'tree' (tree_layout's
+// total doubles of device memory) receives the sum tree, built by
+// k_tree_build from the box's time steps once the records are on the device.
 int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *state_dev, BoxRun *run,
-                 RunState *state, void **tree_dev, std::string *err) {
-    std::vector<double> ts(size_t(b.nslots));
-    std::vector<int> alive(size_t(b.nslots));
-    if (!ok_cuda(cudaMemcpy(ts.data(), b.agg + size_t(AGG_TIME_STEP) * b.nslots, sizeof(double) * ts.size(),
-                            cudaMemcpyDeviceToHost), err, "download"))
-        return ST_CUDA;
-    if (!ok_cuda(cudaMemcpy(alive.data(), b.agg_n, sizeof(int) * alive.size(), cudaMemcpyDeviceToHost), err,
-                 "download"))
-        return ST_CUDA;
-    TreeLayout tl = tree_layout(b.nslots);
-    std::vector<double> tree(size_t(tl.total), 0.0);
-    for (int a = 0; a < b.nslots; ++a) tree[size_t(a)] = alive[size_t(a)] > 0 ? 1.0 / ts[size_t(a)] : 0.0;
-    for (int lev = 1; lev < tl.levels; ++lev)
-        for (int g = 0; g < tl.len[lev]; ++g) {
-            double sum = 0.0;
-            for (int k = 0; k < kTreeFan; ++k) {
-                int c = g * kTreeFan + k;
-                if (c < tl.len[lev - 1]) sum += tree[size_t(tl.off[lev - 1] + c)];
-            }
-            tree[size_t(tl.off[lev] + g)] = sum;
-        }
-    double total = 0.0;
-    for (int k = 0; k < tl.len[tl.levels - 1]; ++k) total += tree[size_t(tl.off[tl.levels - 1] + k)];
-    *tree_dev = nullptr;
-    if (!ok_cuda(cudaMalloc(tree_dev, sizeof(double) * tree.size()), err, "cudaMalloc")) return ST_CUDA;
-    if (!ok_cuda(cudaMemcpy(*tree_dev, tree.data(), sizeof(double) * tree.size(), cudaMemcpyHostToDevice), err,
-                 "upload"))
-        return ST_CUDA;
+                 RunState *state, double *tree) {
+    const TreeLayout tl = tree_layout(b.nslots);
     std::memset(state, 0, sizeof(*state));
     state->rng.seed(uint32_t(p.random_seed < 0 ? 0 : p.random_seed));
     state->time = time;
-    state->weight_total = total;
+    state->weight_total = 0.0;  // set by k_tree_build
     std::memset(run, 0, sizeof(*run));
     run->box = b;
     run->phys = PhysParams{p.viscosity, p.gaz_mean_free_path, p.fractal_dimension, p.density, p.temperature,
@@ -204,7 +186,7 @@ int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *
     run->lim.physical_time_limit = p.physical_time_limit;
     run->lim.with_collisions = p.with_collisions;
     run->st = state_dev;
-    run->tree = static_cast<double *>(*tree_dev);
+    run->tree = tree;
     run->tree_levels = tl.levels;
     for (int k = 0; k < kMaxTreeLevels; ++k) {
         run->tree_off[k] = tl.off[k];
@@ -257,35 +239,15 @@ int BatchRunner::create(const std::vector<mcacg_params> &params, const std::vect
         return ST_BAD_ARGUMENT;
     }
     std::unique_ptr<BatchRunner> r(new BatchRunner());
-    const int n = int(states.size());
-    std::vector<double> times(states.size());
-    std::vector<DeviceBox *> made(states.size(), nullptr);
-    std::vector<int> rcs(states.size(), ST_OK);
-    std::vector<std::string> errs(states.size());
-    // boxes are built in parallel, each on a stream of its own, then moved to
-    // the batch's stream
-    parallel_for(n, [&](int i) {
-        rcs[size_t(i)] = DeviceBox::create(states[size_t(i)], nullptr, &made[size_t(i)], &errs[size_t(i)]);
-        times[size_t(i)] = states[size_t(i)].time;
-    });
-    for (int i = 0; i < n; ++i) {
-        if (made[size_t(i)]) {
-            r->owned_.emplace_back(made[size_t(i)]);
-            r->boxes_.push_back(made[size_t(i)]);
-        }
-    }
-    for (int i = 0; i < n; ++i)
-        if (rcs[size_t(i)] != ST_OK) {
-            if (err) *err = "box " + std::to_string(i) + ": " + errs[size_t(i)];
-            return rcs[size_t(i)];
-        }
     int rc = r->init_stream(stream, err);
     if (rc != ST_OK) return rc;
-    for (DeviceBox *d : r->boxes_)
-        if (d->set_stream(r->stream_) != ST_OK) {
-            if (err) *err = "could not move a box to the batch stream";
-            return ST_CUDA;
-        }
+    rc = DeviceBox::create_many(states, r->stream_, &r->owned_, err);
+    if (rc != ST_OK) return rc;
+    std::vector<double> times(states.size());
+    for (size_t i = 0; i < states.size(); ++i) {
+        times[i] = states[i].time;
+        r->boxes_.push_back(r->owned_[i].get());
+    }
     rc = r->init(params, times, err);
     if (rc != ST_OK) return rc;
     *out = std::move(r);
@@ -333,12 +295,19 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
     if (!ok_cuda(cudaMalloc(&runs_dev_, sizeof(BoxRun) * size_t(n)), err, "cudaMalloc")) return ST_CUDA;
     if (!ok_cuda(cudaMalloc(&states_dev_, sizeof(RunState) * size_t(n)), err, "cudaMalloc")) return ST_CUDA;
     RunState *states_dev = static_cast<RunState *>(states_dev_);
+    // the pick trees of all boxes in one allocation, built on the device
+    std::vector<size_t> tree_off(static_cast<size_t>(n) + 1, 0);
     for (int i = 0; i < n; ++i) {
         const DevBox &b = *static_cast<DevBox *>(boxes_[size_t(i)]->devbox_ptr());
-        void *tree_dev = nullptr;
+        tree_off[size_t(i) + 1] = tree_off[size_t(i)] + size_t(tree_layout(b.nslots).total);
+    }
+    void *trees = nullptr;
+    if (!ok_cuda(cudaMalloc(&trees, sizeof(double) * tree_off[size_t(n)]), err, "cudaMalloc")) return ST_CUDA;
+    trees_.push_back(trees);
+    for (int i = 0; i < n; ++i) {
+        const DevBox &b = *static_cast<DevBox *>(boxes_[size_t(i)]->devbox_ptr());
         int rc = make_box_run(b, params[size_t(i)], times[size_t(i)], states_dev + i, &runs[size_t(i)],
-                              &states[size_t(i)], &tree_dev, err);
-        if (tree_dev) trees_.push_back(tree_dev);
+                              &states[size_t(i)], static_cast<double *>(trees) + tree_off[size_t(i)]);
         if (rc != ST_OK) return rc;
     }
     if (!ok_cuda(cudaMemcpyAsync(runs_dev_, runs.data(), sizeof(BoxRun) * size_t(n), cudaMemcpyHostToDevice, s), err,
@@ -347,6 +316,8 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
     if (!ok_cuda(cudaMemcpyAsync(states_dev_, states.data(), sizeof(RunState) * size_t(n), cudaMemcpyHostToDevice, s),
                  err, "upload"))
         return ST_CUDA;
+    k_tree_build<<<n, 256, 0, s>>>(static_cast<const BoxRun *>(runs_dev_), n);
+    if (!ok_cuda(cudaGetLastError(), err, "k_tree_build")) return ST_CUDA;
     if (!ok_cuda(prepare_all_k_run(), err, "cudaFuncSetAttribute")) return ST_CUDA;
     if (!ok_cuda(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
     return ST_OK;
@@ -735,12 +706,16 @@ int Server::admit(std::string *err) {
         sl.box.reset(d);
         BoxRun run;
         RunState st;
-        rc = make_box_run(*static_cast<DevBox *>(d->devbox_ptr()), take[i].p, states[i].time, states_dev + slot, &run,
-                          &st, &sl.tree, err);
+        const DevBox &db = *static_cast<DevBox *>(d->devbox_ptr());
+        if (!ok_cuda(cudaMalloc(&sl.tree, sizeof(double) * size_t(tree_layout(db.nslots).total)), err, "cudaMalloc"))
+            return ST_CUDA;
+        rc = make_box_run(db, take[i].p, states[i].time, states_dev + slot, &run, &st, static_cast<double *>(sl.tree));
         if (rc != ST_OK) return rc;
         if (!ok_cuda(cudaMemcpyAsync(states_dev + slot, &st, sizeof(st), cudaMemcpyHostToDevice, s), err, "upload") ||
-            !ok_cuda(cudaMemcpyAsync(runs_dev + slot, &run, sizeof(run), cudaMemcpyHostToDevice, s), err, "upload") ||
-            !ok_cuda(cudaStreamSynchronize(s), err, "sync"))
+            !ok_cuda(cudaMemcpyAsync(runs_dev + slot, &run, sizeof(run), cudaMemcpyHostToDevice, s), err, "upload"))
+            return ST_CUDA;
+        k_tree_build<<<1, 256, 0, s>>>(runs_dev + slot, 1);
+        if (!ok_cuda(cudaGetLastError(), err, "k_tree_build") || !ok_cuda(cudaStreamSynchronize(s), err, "sync"))
             return ST_CUDA;
         sl.id = take[i].id;
         sl.growth = take[i].p.with_surface_reactions != 0;

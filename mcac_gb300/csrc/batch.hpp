@@ -59,6 +59,7 @@ class BatchRunner {
     // Box i grows by surface reactions (its overlap fields are refreshed on read-back).
     bool grows(int i) const { return growth_.size() > size_t(i) && growth_[size_t(i)]; }
     DeviceBox &box(int i) { return *boxes_[size_t(i)]; }
+    void *stream() const { return stream_; }
     // Kernel time of the last run() (CUDA events on the stream).
     double last_kernel_ms() const { return last_ms_; }
     int launches() const { return launches_; }

@@ -3,10 +3,13 @@
 
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <string>
+#include <vector>
 
 #include "box.cuh"
 #include "device_box.hpp"
+#include "host_parallel.hpp"
 #include "merge.cuh"
 
 namespace mcacg {
@@ -89,11 +92,15 @@ __global__ void k_set_fields(DevBox b, int slot, FieldUpdate u, unsigned mask) {
     if (f < AGG_NFIELDS && (mask >> f) & 1u) A(b, f, slot) = u.v[f];
 }
 
+// The kernels below run on one box (single-box launches) or on many boxes at
+// once (k_boxes: per_box blocks for each box, whose DevBox is read into
+// shared memory). Their bodies take the thread's index among the box's
+// threads and the number of those threads.
+//
 // Verlet and fine grids from the aggregate positions: clear the cells, drop
 // every live slot into its cells (in any order: the scan key restores the
 // reference's order), then link the fine lists backwards.
-__global__ void k_grid_clear(DevBox b) {
-    const int stride = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void grid_clear_range(const DevBox &b, int t, int stride) {
     for (int c = t; c < b.n_cells; c += stride) b.cell_n[c] = 0;
     if (b.fine_div > 0) {
         const int nf3 = b.fine_div * b.fine_div * b.fine_div;
@@ -101,8 +108,8 @@ __global__ void k_grid_clear(DevBox b) {
         for (int a = t; a < b.nslots; a += stride) b.fine_cell[a] = -1;
     }
 }
-__global__ void k_grid_fill(DevBox b) {
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nslots; a += gridDim.x * blockDim.x) {
+__device__ void grid_fill_range(const DevBox &b, int t, int stride) {
+    for (int a = t; a < b.nslots; a += stride) {
         if (b.agg_n[a] == 0) continue;
         const int c = cell_of(b, agg_pos(b, a));
         b.agg_cell[a] = c;
@@ -123,9 +130,10 @@ __global__ void k_grid_fill(DevBox b) {
         }
     }
 }
-// back links of the fine lists built by k_grid_fill
-__global__ void k_fine_link(DevBox b) {
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nslots; a += gridDim.x * blockDim.x) {
+// back links of the fine lists built by grid_fill_range
+__device__ void fine_link_range(const DevBox &b, int t, int stride) {
+    if (b.fine_div == 0) return;
+    for (int a = t; a < b.nslots; a += stride) {
         const int c = b.fine_cell[a];
         if (c < 0) continue;
         const int n = b.fine_next[a];
@@ -141,33 +149,40 @@ __global__ void k_refresh_f4(DevBox b) {
 
 // Loading a state: the sphere and aggregate tables go straight to their
 // places; the integer arrays (owning slot per sphere, spheres per slot,
-// member lists in slot order) are staged as 32- or 64-bit values and
-// converted here, with the pool built from the member lists. Inconsistent
-// input is flagged (sc->pad[0] = the LoadError, status BAD_ARGUMENT) and
-// never read out of bounds.
+// member lists in slot order) are staged in the box's work area (64 B per
+// sphere; 16 B per sphere and 8 B per slot at most are used) as 32- or 64-bit
+// values and converted here, with the pool built from the member lists.
+// Inconsistent input is flagged (sc->pad[0] = the LoadError, status
+// BAD_ARGUMENT) and never read out of bounds.
 enum LoadError { LOAD_OK = 0, LOAD_LABEL = 1, LOAD_COUNT = 2, LOAD_COVER = 3, LOAD_MEMBER = 4 };
 struct LoadStage {
     const void *label, *count, *members;
     int wide;     // 64-bit integers
     int dead_ok;  // slots without spheres are allowed
 };
+__host__ __device__ inline LoadStage load_stage(const DevBox &b, int wide, int dead_ok) {
+    const size_t iw = wide ? 8 : 4;
+    const char *stage = reinterpret_cast<const char *>(b.work);
+    return LoadStage{stage, stage + 2 * iw * size_t(b.ns), stage + iw * size_t(b.ns), wide, dead_ok};
+}
 __device__ __forceinline__ long long load_int(const void *p, int wide, int i) {
     return wide ? static_cast<const long long *>(p)[i] : static_cast<long long>(static_cast<const int *>(p)[i]);
 }
-__device__ __forceinline__ void load_fail(DevBox &b, int code) {
+__device__ __forceinline__ void load_fail(const DevBox &b, int code) {
     atomicCAS(&b.sc->pad[0], 0, code);
     b.sc->status = ST_BAD_ARGUMENT;
 }
-constexpr int kLoadScanThreads = 1024;
-// spheres per slot, pool offsets (exclusive sum in slot order), live count
-__global__ void __launch_bounds__(kLoadScanThreads) k_load_counts(DevBox b, LoadStage in) {
-    __shared__ long long part[kLoadScanThreads];
-    __shared__ int alive[kLoadScanThreads];
+constexpr int kScanThreads = 1024;
+// spheres per slot, pool offsets (exclusive sum in slot order), live count;
+// one block of kScanThreads threads per box
+__device__ void load_counts_block(const DevBox &b, const LoadStage &in) {
+    __shared__ long long part[kScanThreads];
+    __shared__ int alive[kScanThreads];
     __shared__ int bad;
     const int t = threadIdx.x;
     if (t == 0) bad = 0;
     __syncthreads();
-    const int chunk = (b.nslots + kLoadScanThreads - 1) / kLoadScanThreads;
+    const int chunk = (b.nslots + kScanThreads - 1) / kScanThreads;
     const int a0 = min(b.nslots, t * chunk), a1 = min(b.nslots, a0 + chunk);
     long long sum = 0;
     int live = 0, flag = 0;
@@ -188,7 +203,7 @@ __global__ void __launch_bounds__(kLoadScanThreads) k_load_counts(DevBox b, Load
         if (bad) load_fail(b, LOAD_COUNT);
         long long run = 0;
         int n_alive = 0;
-        for (int k = 0; k < kLoadScanThreads; ++k) {
+        for (int k = 0; k < kScanThreads; ++k) {
             const long long v = part[k];
             part[k] = run;
             run += v;
@@ -209,8 +224,8 @@ __global__ void __launch_bounds__(kLoadScanThreads) k_load_counts(DevBox b, Load
     }
 }
 // owning slots, pool ids and pool positions (pool entry k = member k)
-__global__ void k_load_spheres(DevBox b, LoadStage in) {
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < b.ns; s += gridDim.x * blockDim.x) {
+__device__ void load_spheres_range(const DevBox &b, const LoadStage &in, int t, int stride) {
+    for (int s = t; s < b.ns; s += stride) {
         long long l = load_int(in.label, in.wide, s);
         if (l < 0 || l >= b.nslots) {
             load_fail(b, LOAD_LABEL);
@@ -226,29 +241,52 @@ __global__ void k_load_spheres(DevBox b, LoadStage in) {
         b.pool_pos[0][s] = make_float4(float(S(b, SPH_X, int(m))), float(S(b, SPH_Y, int(m))),
                                        float(S(b, SPH_Z, int(m))), float(S(b, SPH_R, int(m))));
     }
-    for (int k = b.ns + blockIdx.x * blockDim.x + threadIdx.x; k < b.pool_cap; k += gridDim.x * blockDim.x) {
+    for (int k = b.ns + t; k < b.pool_cap; k += stride) {
         b.pool_id[0][k] = 0;
         b.pool_pos[0][k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
+// every member of slot a is owned by slot a
+__device__ void load_check_range(const DevBox &b, int t, int stride) {
+    for (int a = t; a < b.nslots; a += stride) {
+        const int o = b.agg_off[a], e = min(b.ns, o + b.agg_n[a]);
+        for (int k = o; k < e; ++k)
+            if (b.sph_slot[b.pool_id[0][k]] != a) {
+                load_fail(b, LOAD_MEMBER);
+                break;
+            }
+    }
+}
+
 // Storing a state: the live slots are packed in slot order (label = rank
 // among the live slots, as the reference's list has them), with their member
-// lists back to back, into the staging area; the host copies the pieces out.
+// lists back to back, into the merge's pair scratch; the host copies the
+// pieces out (PackLayout gives the offsets).
 struct PackStage {
-    double *agg;       // [21][na]
-    long long *count;  // [na]
-    long long *label;  // [ns]
-    long long *members;// [ns]
-    int *rank;         // [nslots]
-    int *moff;         // [nslots] first member of the slot in 'members'
+    double *agg;         // [21][na]
+    long long *count;    // [na]
+    long long *label;    // [ns]
+    long long *members;  // [ns]
+    int *rank;           // [nslots]
+    int *moff;           // [nslots] first member of the slot in 'members'
     int na;
-    int sel;           // live pool buffer
+    int sel;             // live pool buffer
 };
-__global__ void __launch_bounds__(kLoadScanThreads) k_pack_ranks(DevBox b, PackStage out) {
-    __shared__ int live_part[kLoadScanThreads];
-    __shared__ int mem_part[kLoadScanThreads];
+__host__ __device__ inline PackStage pack_stage(const DevBox &b, int na, int sel) {
+    char *p = reinterpret_cast<char *>(b.pair_i);
+    const PackLayout l = pack_layout(na, b.ns, b.nslots);
+    return PackStage{reinterpret_cast<double *>(p + l.agg),      reinterpret_cast<long long *>(p + l.count),
+                     reinterpret_cast<long long *>(p + l.label), reinterpret_cast<long long *>(p + l.members),
+                     reinterpret_cast<int *>(p + l.rank),        reinterpret_cast<int *>(p + l.moff),
+                     na,
+                     sel};
+}
+// ranks of the live slots and member offsets; one block of kScanThreads
+__device__ void pack_ranks_block(const DevBox &b, const PackStage &out) {
+    __shared__ int live_part[kScanThreads];
+    __shared__ int mem_part[kScanThreads];
     const int t = threadIdx.x;
-    const int chunk = (b.nslots + kLoadScanThreads - 1) / kLoadScanThreads;
+    const int chunk = (b.nslots + kScanThreads - 1) / kScanThreads;
     const int a0 = min(b.nslots, t * chunk), a1 = min(b.nslots, a0 + chunk);
     int live = 0, mem = 0;
     for (int a = a0; a < a1; ++a) {
@@ -261,7 +299,7 @@ __global__ void __launch_bounds__(kLoadScanThreads) k_pack_ranks(DevBox b, PackS
     __syncthreads();
     if (t == 0) {
         int rl = 0, rm = 0;
-        for (int k = 0; k < kLoadScanThreads; ++k) {
+        for (int k = 0; k < kScanThreads; ++k) {
             const int l = live_part[k], m = mem_part[k];
             live_part[k] = rl;
             mem_part[k] = rm;
@@ -279,8 +317,7 @@ __global__ void __launch_bounds__(kLoadScanThreads) k_pack_ranks(DevBox b, PackS
         o += n;
     }
 }
-__global__ void k_pack(DevBox b, PackStage out) {
-    const int stride = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void pack_range(const DevBox &b, const PackStage &out, int t, int stride) {
     const int *pool = b.pool_id[out.sel];
     for (int a = t; a < b.nslots; a += stride) {
         const int r = out.rank[a];
@@ -291,19 +328,52 @@ __global__ void k_pack(DevBox b, PackStage out) {
         const int src = b.agg_off[a], dst = out.moff[a];
         for (int k = 0; k < n && dst + k < b.ns && src + k < b.pool_cap; ++k) out.members[dst + k] = pool[src + k];
     }
-    for (int s = t; s < b.ns; s += stride) out.label[s] = out.rank[b.sph_slot[s]];
+    for (int s = t; s < b.ns; s += stride) {
+        const int a = b.sph_slot[s];
+        out.label[s] = (a >= 0 && a < b.nslots) ? out.rank[a] : -1;
+    }
 }
 
-// every member of slot a is owned by slot a
-__global__ void k_load_check(DevBox b) {
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nslots; a += gridDim.x * blockDim.x) {
-        const int o = b.agg_off[a], e = min(b.ns, o + b.agg_n[a]);
-        for (int k = o; k < e; ++k)
-            if (b.sph_slot[b.pool_id[0][k]] != a) {
-                load_fail(b, LOAD_MEMBER);
-                break;
-            }
+enum BoxOp { OP_GRID_CLEAR, OP_GRID_FILL, OP_FINE_LINK, OP_LOAD_COUNTS, OP_LOAD_SPHERES, OP_LOAD_CHECK, OP_PACK_RANKS,
+             OP_PACK };
+// Per-box arguments of k_boxes: the load flags, or the live count (< 0:
+// skip the box) and live pool buffer of a store.
+struct BoxArg {
+    int a, b;
+};
+template <int OP>
+__device__ __forceinline__ void box_op(const DevBox &b, BoxArg arg, int t, int stride) {
+    if (OP == OP_GRID_CLEAR) grid_clear_range(b, t, stride);
+    if (OP == OP_GRID_FILL) grid_fill_range(b, t, stride);
+    if (OP == OP_FINE_LINK) fine_link_range(b, t, stride);
+    if (OP == OP_LOAD_COUNTS) load_counts_block(b, load_stage(b, arg.a, arg.b));
+    if (OP == OP_LOAD_SPHERES) load_spheres_range(b, load_stage(b, arg.a, arg.b), t, stride);
+    if (OP == OP_LOAD_CHECK) load_check_range(b, t, stride);
+    if (OP == OP_PACK_RANKS) pack_ranks_block(b, pack_stage(b, arg.a, arg.b));
+    if (OP == OP_PACK) pack_range(b, pack_stage(b, arg.a, arg.b), t, stride);
+}
+template <int OP>
+__global__ void __launch_bounds__(kScanThreads) k_box(DevBox b, BoxArg arg) {
+    box_op<OP>(b, arg, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+template <int OP>
+__global__ void __launch_bounds__(kScanThreads) k_boxes(const DevBox *boxes, const BoxArg *args, int n, int per_box) {
+    __shared__ DevBox b;
+    __shared__ BoxArg arg;
+    const int box = blockIdx.x / per_box;
+    if (box >= n) return;  // block-uniform
+    if (threadIdx.x == 0) {
+        b = boxes[box];
+        arg = args[box];
     }
+    __syncthreads();
+    if ((OP == OP_PACK_RANKS || OP == OP_PACK) && arg.a < 0) return;  // block-uniform
+    box_op<OP>(b, arg, (blockIdx.x % per_box) * blockDim.x + threadIdx.x, per_box * blockDim.x);
+}
+// the scalars of many boxes, gathered for one copy to the host
+__global__ void k_gather_scalars(const DevBox *boxes, int n, DevScalars *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = *boxes[i].sc;
 }
 // ------------------------------------------------------------------- host
 namespace {
@@ -360,21 +430,17 @@ int DeviceBox::create(const HostState &st, void *stream, DeviceBox **out, std::s
     return create(v, stream, out, err);
 }
 
-int DeviceBox::create(const StateView &st, void *stream, DeviceBox **out, std::string *err) {
-    *out = nullptr;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-        if (err) *err = "no CUDA device";
-        return ST_NO_DEVICE;
-    }
-    if (st.ns <= 0 || st.nslots <= 0 || st.nslots > st.ns || !st.sph || !st.agg || !st.sph_slot || !st.agg_n ||
-        !st.members || !(st.box_length > 0.0) || st.n_div <= 0) {
-        if (err) *err = "incomplete state";
-        return ST_BAD_ARGUMENT;
-    }
-    DeviceBox *d = new DeviceBox();
-    d->ns_ = st.ns;
-    d->nslots_ = st.nslots;
+namespace {
+
+bool view_ok(const StateView &st) {
+    return st.ns > 0 && st.nslots > 0 && st.nslots <= st.ns && st.sph && st.agg && st.sph_slot && st.agg_n &&
+           st.members && st.box_length > 0.0 && st.n_div > 0 && st.n_div <= 1024;
+}
+
+// Sizes, grids and capacities of a box from its state, by host arithmetic
+// over the live slots: one pass gives the largest r_max, the means of lpm and
+// r_max, and the Verlet cell counts. No pointer is set.
+DevBox plan_box(const StateView &st) {
     DevBox b{};
     b.L = st.box_length;
     b.n_div = st.n_div;
@@ -384,11 +450,6 @@ int DeviceBox::create(const StateView &st, void *stream, DeviceBox **out, std::s
     b.nslots = st.nslots;
     const double *agg = st.agg;
     auto AF = [&](int f, int a) { return agg[size_t(f) * size_t(st.nslots) + size_t(a)]; };
-    // FP32 screening margin: coordinates are bounded by the box plus the
-    // largest aggregate; 2^-17 of that bound is >10x the FP32 error of the
-    // capsule test.
-    // one pass over the live slots: largest r_max, the means of lpm and
-    // r_max, and the Verlet cell counts (for the cell capacity)
     double rmax_all = st.maxradius, lpm_sum = 0.0, rmax_sum = 0.0;
     int live = 0, maxc = 0;
     std::vector<int> cell_n(size_t(b.n_cells), 0);
@@ -404,20 +465,21 @@ int DeviceBox::create(const StateView &st, void *stream, DeviceBox **out, std::s
         const int iz = std::min(std::max(verlet_coord(AF(AGG_Z, a), b.step), 0), b.n_div - 1);
         maxc = std::max(maxc, ++cell_n[size_t((ix * b.n_div + iy) * b.n_div + iz)]);
     }
+    // FP32 screening margin: coordinates are bounded by the box plus the
+    // largest aggregate; 2^-17 of that bound is >10x the FP32 error of the
+    // capsule test.
     b.margin = (3.0 * st.box_length + 4.0 * rmax_all) * (1.0 / 131072.0);
     // fine discovery grid, when finer than the Verlet grid: a query visits
     // the cells covering its swept box, about lpm/2 + 2 (r_max + max r_max)
     // per axis on average; cells of 0.6 of that balance the cells visited
     // against the aggregates screened. At least 2 max r_max and L/128.
-    {
-        const double extent = live ? 0.5 * lpm_sum / live + 2.0 * (rmax_sum / live + rmax_all) : 0.0;
-        const double h = std::max({2.0 * rmax_all, st.box_length / double(kFineMaxDiv), 0.6 * extent});
-        const double nf = std::floor(st.box_length / h);
-        b.fine_div = (nf > double(st.n_div) && nf <= double(kFineMaxDiv)) ? int(nf) : 0;
-        b.fine_step = b.fine_div > 0 ? double(b.fine_div) / st.box_length : 0.0;
-    }
-    // grid capacity
-    int avg = (st.nslots + b.n_cells - 1) / b.n_cells;
+    const double extent = live ? 0.5 * lpm_sum / live + 2.0 * (rmax_sum / live + rmax_all) : 0.0;
+    const double h = std::max({2.0 * rmax_all, st.box_length / double(kFineMaxDiv), 0.6 * extent});
+    const double nf = std::floor(st.box_length / h);
+    b.fine_div = (nf > double(st.n_div) && nf <= double(kFineMaxDiv)) ? int(nf) : 0;
+    b.fine_step = b.fine_div > 0 ? double(b.fine_div) / st.box_length : 0.0;
+    // capacities
+    const int avg = (st.nslots + b.n_cells - 1) / b.n_cells;
     b.cell_cap = std::max({64, 2 * maxc, 8 * avg});
     b.pool_cap = 2 * st.ns + 1024;
     b.surv_cap = 1 << 16;
@@ -425,154 +487,269 @@ int DeviceBox::create(const StateView &st, void *stream, DeviceBox **out, std::s
     // others (the kissing number), so at most 6 pairs per sphere; the
     // merge reports a capacity error beyond 8 per sphere
     b.pair_cap = 8 * st.ns + 1024;
+    return b;
+}
 
-    // all arrays of the box are carved from one allocation: a sizing pass,
-    // one cudaMalloc, then the carving pass
-    size_t arena_bytes = 0;
-    char *arena = nullptr;
-    bool sizing = true;
-    auto alloc = [&](void **p, size_t bytes) -> bool {
-        size_t need = (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
-        if (sizing) {
-            *p = nullptr;
-        } else {
-            *p = arena + arena_bytes;
-        }
-        arena_bytes += need;
-        return true;
+// Places the box's arrays in 'arena' (nullptr: sizes them only, leaving the
+// pointers null) and returns the bytes used; every array starts on a
+// 256-byte boundary.
+size_t carve_box(DevBox &b, char *arena) {
+    size_t used = 0;
+    auto take = [&](void **p, size_t bytes) {
+        *p = arena ? arena + used : nullptr;
+        used += (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
     };
-    bool ok = true;
-    for (int pass = 0; pass < 2; ++pass) {
-    if (pass == 1) {
-        if (!cuda_ok(cudaMalloc((void **)&arena, arena_bytes), err, "cudaMalloc")) {
-            delete d;
-            return ST_CUDA;
-        }
-        d->allocations_.push_back(arena);
-        sizing = false;
-        arena_bytes = 0;
-    }
-    ok = ok && alloc((void **)&b.sph, sizeof(double) * 9 * size_t(st.ns));
-    ok = ok && alloc((void **)&b.sph_slot, sizeof(int) * size_t(st.ns));
-    ok = ok && alloc((void **)&b.agg, sizeof(double) * 21 * size_t(st.nslots));
-    ok = ok && alloc((void **)&b.agg_n, sizeof(int) * size_t(st.nslots));
-    ok = ok && alloc((void **)&b.agg_off, sizeof(int) * size_t(st.nslots));
-    ok = ok && alloc((void **)&b.agg_cell, sizeof(int) * size_t(st.nslots));
-    ok = ok && alloc((void **)&b.agg_f4, sizeof(float4) * size_t(st.nslots));
+    const size_t ns = size_t(b.ns), nslots = size_t(b.nslots);
+    take((void **)&b.sph, sizeof(double) * 9 * ns);
+    take((void **)&b.sph_slot, sizeof(int) * ns);
+    take((void **)&b.agg, sizeof(double) * 21 * nslots);
+    take((void **)&b.agg_n, sizeof(int) * nslots);
+    take((void **)&b.agg_off, sizeof(int) * nslots);
+    take((void **)&b.agg_cell, sizeof(int) * nslots);
+    take((void **)&b.agg_f4, sizeof(float4) * nslots);
     for (int k = 0; k < 2; ++k) {
-        ok = ok && alloc((void **)&b.pool_id[k], sizeof(int) * size_t(b.pool_cap));
-        ok = ok && alloc((void **)&b.pool_pos[k], sizeof(float4) * size_t(b.pool_cap));
+        take((void **)&b.pool_id[k], sizeof(int) * size_t(b.pool_cap));
+        take((void **)&b.pool_pos[k], sizeof(float4) * size_t(b.pool_cap));
     }
-    ok = ok && alloc((void **)&b.cell_n, sizeof(int) * size_t(b.n_cells));
-    ok = ok && alloc((void **)&b.cell_pos, sizeof(int) * size_t(st.nslots));
+    take((void **)&b.cell_n, sizeof(int) * size_t(b.n_cells));
+    take((void **)&b.cell_pos, sizeof(int) * nslots);
     if (b.fine_div > 0) {
         const size_t nf3 = size_t(b.fine_div) * size_t(b.fine_div) * size_t(b.fine_div);
-        ok = ok && alloc((void **)&b.fine_head, sizeof(int) * nf3);
-        ok = ok && alloc((void **)&b.fine_next, sizeof(int) * size_t(st.nslots));
-        ok = ok && alloc((void **)&b.fine_prev, sizeof(int) * size_t(st.nslots));
-        ok = ok && alloc((void **)&b.fine_cell, sizeof(int) * size_t(st.nslots));
+        take((void **)&b.fine_head, sizeof(int) * nf3);
+        take((void **)&b.fine_next, sizeof(int) * nslots);
+        take((void **)&b.fine_prev, sizeof(int) * nslots);
+        take((void **)&b.fine_cell, sizeof(int) * nslots);
     }
-    ok = ok && alloc((void **)&b.cell_items, sizeof(int) * size_t(b.n_cells) * size_t(b.cell_cap));
-    ok = ok && alloc((void **)&b.sc, sizeof(DevScalars));
-    ok = ok && alloc((void **)&b.surv, sizeof(int4) * size_t(b.surv_cap));
-    ok = ok && alloc((void **)&b.surv_res, sizeof(double) * size_t(b.surv_cap));
+    take((void **)&b.cell_items, sizeof(int) * size_t(b.n_cells) * size_t(b.cell_cap));
+    take((void **)&b.sc, sizeof(DevScalars));
+    take((void **)&b.surv, sizeof(int4) * size_t(b.surv_cap));
+    take((void **)&b.surv_res, sizeof(double) * size_t(b.surv_cap));
     // the merge's pair scratch is one block (32 B per pair), which also
     // stages a packed state on its way to the host
     {
         char *pairs = nullptr;
         const size_t pc = size_t(b.pair_cap);
-        ok = ok && alloc((void **)&pairs, 32 * pc);
+        take((void **)&pairs, 32 * pc);
         b.pair_i = reinterpret_cast<int *>(pairs);
-        b.pair_j = b.pair_i + pc;
-        b.pair_tmp_i = b.pair_j + pc;
-        b.pair_tmp_j = b.pair_tmp_i + pc;
-        b.pair_d = reinterpret_cast<double *>(pairs + 16 * pc);
-        b.pair_tmp_d = b.pair_d + pc;
-        d->stage_ = pairs;
-        d->stage_bytes_ = 32 * pc;
+        b.pair_j = pairs ? b.pair_i + pc : nullptr;
+        b.pair_tmp_i = pairs ? b.pair_j + pc : nullptr;
+        b.pair_tmp_j = pairs ? b.pair_tmp_i + pc : nullptr;
+        b.pair_d = pairs ? reinterpret_cast<double *>(pairs + 16 * pc) : nullptr;
+        b.pair_tmp_d = pairs ? b.pair_d + pc : nullptr;
     }
-    ok = ok && alloc((void **)&b.row_cnt, sizeof(int) * (size_t(std::max(st.ns, st.nslots)) + 2));
-    ok = ok && alloc((void **)&b.work, sizeof(double) * 8 * size_t(st.ns));
-    ok = ok && alloc((void **)&b.counters, sizeof(int) * 8);
-    const size_t nc1 = size_t(st.nslots) + 1;
-    ok = ok && alloc((void **)&b.cand_db, sizeof(double) * nc1);
-    ok = ok && alloc((void **)&b.cand_key, sizeof(long long) * nc1);
-    ok = ok && alloc((void **)&b.cand_slot, sizeof(int) * nc1);
-    ok = ok && alloc((void **)&b.cand_order, sizeof(int) * nc1);
-    ok = ok && alloc((void **)&b.cand_prefix, sizeof(int) * nc1);
-    ok = ok && alloc((void **)&b.best_res, sizeof(unsigned long long) * nc1);
-    ok = ok && alloc((void **)&b.best_ij, sizeof(unsigned long long) * nc1);
-    }  // sizing / carving passes
-    if (stream) {
-        d->stream_ = stream;
-    } else {
-        cudaStream_t s;
-        if (!cuda_ok(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), err, "cudaStreamCreate")) {
-            delete d;
-            return ST_CUDA;
-        }
-        d->stream_ = s;
-        d->own_stream_ = true;
-    }
-    // upload: the tables straight to their places, the integer arrays to
-    // the box's work area (64 B per sphere; 16 B per sphere and 8 B per slot
-    // at most are needed), converted and checked there by the load kernels
+    take((void **)&b.row_cnt, sizeof(int) * (std::max(ns, nslots) + 2));
+    take((void **)&b.work, sizeof(double) * 8 * ns);
+    take((void **)&b.counters, sizeof(int) * 8);
+    const size_t nc1 = nslots + 1;
+    take((void **)&b.cand_db, sizeof(double) * nc1);
+    take((void **)&b.cand_key, sizeof(long long) * nc1);
+    take((void **)&b.cand_slot, sizeof(int) * nc1);
+    take((void **)&b.cand_order, sizeof(int) * nc1);
+    take((void **)&b.cand_prefix, sizeof(int) * nc1);
+    take((void **)&b.best_res, sizeof(unsigned long long) * nc1);
+    take((void **)&b.best_ij, sizeof(unsigned long long) * nc1);
+    return used;
+}
+
+// The copies of a state into a carved box on stream s: the tables to their
+// places, the integer arrays to the load stage (load_stage).
+bool upload_state(const DevBox &b, const StateView &st, cudaStream_t s, std::string *err) {
     DevScalars sc{};
     sc.maxradius = st.maxradius;
     sc.time = st.time;
     sc.pool_sel = 0;
     const size_t iw = st.wide ? 8 : 4;
-    char *stage = reinterpret_cast<char *>(b.work);
-    LoadStage in{stage, stage + 2 * iw * size_t(st.ns), stage + iw * size_t(st.ns), st.wide ? 1 : 0,
-                 st.dead_slots ? 1 : 0};
-    // copies on the box's own stream (boxes of a batch are built in parallel,
-    // each on a stream of its own); the host arrays stay alive until the
-    // status read below synchronises the stream
-    cudaStream_t s = static_cast<cudaStream_t>(d->stream_);
+    const LoadStage in = load_stage(b, st.wide ? 1 : 0, st.dead_slots ? 1 : 0);
     auto put = [&](const void *dst, const void *src, size_t bytes) {
         return cuda_ok(cudaMemcpyAsync(const_cast<void *>(dst), src, bytes, cudaMemcpyHostToDevice, s), err, "upload");
     };
-    ok = ok && put(b.sph, st.sph, sizeof(double) * 9 * size_t(st.ns)) &&
-         put(b.agg, st.agg, sizeof(double) * 21 * size_t(st.nslots)) && put(in.label, st.sph_slot, iw * size_t(st.ns)) &&
-         put(in.members, st.members, iw * size_t(st.ns)) && put(in.count, st.agg_n, iw * size_t(st.nslots)) &&
-         put(b.sc, &sc, sizeof(sc));
-    if (!ok) {
-        delete d;
-        return ST_CUDA;
+    return put(b.sph, st.sph, sizeof(double) * 9 * size_t(st.ns)) &&
+           put(b.agg, st.agg, sizeof(double) * 21 * size_t(st.nslots)) && put(in.label, st.sph_slot, iw * size_t(st.ns)) &&
+           put(in.members, st.members, iw * size_t(st.ns)) && put(in.count, st.agg_n, iw * size_t(st.nslots)) &&
+           put(b.sc, &sc, sizeof(sc));
+}
+
+const char *load_error_text(int code) {
+    switch (code) {
+        case LOAD_LABEL: return "sphere label out of range";
+        case LOAD_COUNT: return "bad sphere count of an aggregate";
+        case LOAD_COVER: return "member lists do not cover every sphere once";
+        case LOAD_MEMBER: return "member list inconsistent with sphere labels";
+        default: return "state rejected";
     }
-    {
-        const int blocks = std::min(1024, (std::max(st.ns, st.nslots) + 255) / 256);
-        k_load_counts<<<1, kLoadScanThreads, 0, s>>>(b, in);
-        k_load_spheres<<<blocks, 256, 0, s>>>(b, in);
-        k_load_check<<<blocks, 256, 0, s>>>(b);
-        if (!cuda_ok(cudaGetLastError(), err, "state load")) {
-            delete d;
-            return ST_CUDA;
-        }
-        DevScalars got;
-        if (!cuda_ok(cudaMemcpyAsync(&got, b.sc, sizeof(got), cudaMemcpyDeviceToHost, s), err, "status") ||
-            !cuda_ok(cudaStreamSynchronize(s), err, "sync")) {
-            delete d;
-            return ST_CUDA;
-        }
-        if (got.status != ST_OK) {
-            static const char *const what[] = {"state rejected", "sphere label out of range",
-                                                "bad sphere count of an aggregate",
-                                                "member lists do not cover every sphere once",
-                                                "member list inconsistent with sphere labels"};
-            const int code = got.pad[0];
-            if (err) *err = what[(code >= 0 && code <= LOAD_MEMBER) ? code : 0];
-            delete d;
-            return ST_BAD_ARGUMENT;
-        }
+}
+
+// blocks per box of the many-box kernels: enough to fill the GPU
+int blocks_per_box(int n_boxes, int max_items) {
+    int dev = 0, n_sm = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n_sm <= 0) n_sm = 152;
+    const int want = (8 * n_sm + n_boxes - 1) / std::max(1, n_boxes);
+    return std::max(1, std::min({want, 256, (max_items + 255) / 256}));
+}
+
+}  // namespace
+
+int DeviceBox::create(const StateView &st, void *stream, DeviceBox **out, std::string *err) {
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        if (err) *err = "no CUDA device";
+        return ST_NO_DEVICE;
+    }
+    if (!view_ok(st)) {
+        if (err) *err = "incomplete state";
+        return ST_BAD_ARGUMENT;
+    }
+    DevBox b = plan_box(st);
+    const size_t bytes = carve_box(b, nullptr);
+    std::unique_ptr<DeviceBox> d(new DeviceBox());
+    d->ns_ = st.ns;
+    d->nslots_ = st.nslots;
+    char *arena = nullptr;
+    if (!cuda_ok(cudaMalloc((void **)&arena, bytes), err, "cudaMalloc")) return ST_CUDA;
+    d->allocations_.push_back(arena);
+    carve_box(b, arena);
+    d->stage_ = b.pair_i;
+    d->stage_bytes_ = 32 * size_t(b.pair_cap);
+    if (stream) {
+        d->stream_ = stream;
+    } else {
+        cudaStream_t s;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), err, "cudaStreamCreate")) return ST_CUDA;
+        d->stream_ = s;
+        d->own_stream_ = true;
+    }
+    // the host arrays stay alive until the status read below synchronises
+    cudaStream_t s = static_cast<cudaStream_t>(d->stream_);
+    if (!upload_state(b, st, s, err)) return ST_CUDA;
+    const BoxArg la{st.wide ? 1 : 0, st.dead_slots ? 1 : 0};
+    const int blocks = std::min(1024, (std::max(st.ns, st.nslots) + 255) / 256);
+    k_box<OP_LOAD_COUNTS><<<1, kScanThreads, 0, s>>>(b, la);
+    k_box<OP_LOAD_SPHERES><<<blocks, 256, 0, s>>>(b, la);
+    k_box<OP_LOAD_CHECK><<<blocks, 256, 0, s>>>(b, la);
+    if (!cuda_ok(cudaGetLastError(), err, "state load")) return ST_CUDA;
+    DevScalars got;
+    if (!cuda_ok(cudaMemcpyAsync(&got, b.sc, sizeof(got), cudaMemcpyDeviceToHost, s), err, "status") ||
+        !cuda_ok(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
+    if (got.status != ST_OK) {
+        if (err) *err = load_error_text(got.pad[0]);
+        return ST_BAD_ARGUMENT;
     }
     d->devbox_ = new DevBox(b);
     int rc = d->rebuild_grid(b.cell_cap, err);
-    if (rc != ST_OK) {
-        delete d;
-        return rc;
+    if (rc != ST_OK) return rc;
+    *out = d.release();
+    return ST_OK;
+}
+
+int DeviceBox::create_many(const std::vector<StateView> &views, void *stream,
+                           std::vector<std::unique_ptr<DeviceBox>> *out, std::string *err) {
+    out->clear();
+    const int n = int(views.size());
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        if (err) *err = "no CUDA device";
+        return ST_NO_DEVICE;
     }
-    *out = d;
+    bool same_kind = true;
+    for (int i = 0; i < n; ++i) {
+        if (!view_ok(views[size_t(i)])) {
+            if (err) *err = "box " + std::to_string(i) + ": incomplete state";
+            return ST_BAD_ARGUMENT;
+        }
+        same_kind = same_kind && views[size_t(i)].wide == views[0].wide &&
+                    views[size_t(i)].dead_slots == views[0].dead_slots;
+    }
+    if (n == 0) return ST_OK;
+    if (!same_kind) {
+        if (err) *err = "states of one batch must have the same integer width";
+        return ST_BAD_ARGUMENT;
+    }
+    // plans in parallel, then one allocation for every box
+    std::vector<DevBox> plans(static_cast<size_t>(n));
+    parallel_for(n, [&](int i) { plans[size_t(i)] = plan_box(views[size_t(i)]); });
+    std::vector<size_t> off(static_cast<size_t>(n) + 1, 0);
+    int max_items = 0;
+    for (int i = 0; i < n; ++i) {
+        off[size_t(i) + 1] = off[size_t(i)] + carve_box(plans[size_t(i)], nullptr);
+        max_items = std::max({max_items, plans[size_t(i)].ns, plans[size_t(i)].nslots});
+    }
+    char *arena = nullptr;
+    if (!cuda_ok(cudaMalloc((void **)&arena, off[size_t(n)]), err, "cudaMalloc")) {
+        if (err) *err += " (" + std::to_string(off[size_t(n)] >> 20) + " MiB for " + std::to_string(n) + " boxes)";
+        return ST_CUDA;
+    }
+    std::shared_ptr<void> shared(arena, [](void *p) { cudaFree(p); });
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    std::vector<std::unique_ptr<DeviceBox>> boxes(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i) {
+        DevBox &b = plans[size_t(i)];
+        carve_box(b, arena + off[size_t(i)]);
+        std::unique_ptr<DeviceBox> d(new DeviceBox());
+        d->ns_ = b.ns;
+        d->nslots_ = b.nslots;
+        d->arena_ = shared;
+        d->stage_ = b.pair_i;
+        d->stage_bytes_ = 32 * size_t(b.pair_cap);
+        d->stream_ = s;
+        d->devbox_ = new DevBox(b);
+        boxes[size_t(i)] = std::move(d);
+    }
+    // the copies in one stream (the link is the limit), then the load and
+    // grid kernels over all boxes at once
+    for (int i = 0; i < n; ++i)
+        if (!upload_state(plans[size_t(i)], views[size_t(i)], s, err)) {
+            if (err) *err = "box " + std::to_string(i) + ": " + *err;
+            return ST_CUDA;
+        }
+    const size_t tb = (sizeof(DevBox) * size_t(n) + 255) & ~size_t(255);
+    const size_t ta = (sizeof(BoxArg) * size_t(n) + 255) & ~size_t(255);
+    char *tmp = nullptr;
+    if (!cuda_ok(cudaMalloc((void **)&tmp, tb + ta + sizeof(DevScalars) * size_t(n)), err, "cudaMalloc")) return ST_CUDA;
+    std::unique_ptr<char, void (*)(char *)> tmp_owner(tmp, [](char *p) { cudaFree(p); });
+    DevBox *dboxes = reinterpret_cast<DevBox *>(tmp);
+    BoxArg *dargs = reinterpret_cast<BoxArg *>(tmp + tb);
+    DevScalars *dsc = reinterpret_cast<DevScalars *>(tmp + tb + ta);
+    std::vector<BoxArg> args(static_cast<size_t>(n), BoxArg{views[0].wide ? 1 : 0, views[0].dead_slots ? 1 : 0});
+    std::vector<DevScalars> sc(static_cast<size_t>(n));
+    const int per = blocks_per_box(n, max_items);
+    if (!cuda_ok(cudaMemcpyAsync(dboxes, plans.data(), sizeof(DevBox) * size_t(n), cudaMemcpyHostToDevice, s), err,
+                 "upload") ||
+        !cuda_ok(cudaMemcpyAsync(dargs, args.data(), sizeof(BoxArg) * size_t(n), cudaMemcpyHostToDevice, s), err,
+                 "upload"))
+        return ST_CUDA;
+    k_boxes<OP_LOAD_COUNTS><<<n, kScanThreads, 0, s>>>(dboxes, dargs, n, 1);
+    k_boxes<OP_LOAD_SPHERES><<<n * per, 256, 0, s>>>(dboxes, dargs, n, per);
+    k_boxes<OP_LOAD_CHECK><<<n * per, 256, 0, s>>>(dboxes, dargs, n, per);
+    k_boxes<OP_GRID_CLEAR><<<n * per, 256, 0, s>>>(dboxes, dargs, n, per);
+    k_boxes<OP_GRID_FILL><<<n * per, 256, 0, s>>>(dboxes, dargs, n, per);
+    k_boxes<OP_FINE_LINK><<<n * per, 256, 0, s>>>(dboxes, dargs, n, per);
+    k_gather_scalars<<<(n + 255) / 256, 256, 0, s>>>(dboxes, n, dsc);
+    if (!cuda_ok(cudaGetLastError(), err, "state load") ||
+        !cuda_ok(cudaMemcpyAsync(sc.data(), dsc, sizeof(DevScalars) * size_t(n), cudaMemcpyDeviceToHost, s), err,
+                 "status") ||
+        !cuda_ok(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
+    for (int i = 0; i < n; ++i) {
+        const DevScalars &c = sc[size_t(i)];
+        if (c.status == ST_BAD_ARGUMENT) {
+            if (err) *err = "box " + std::to_string(i) + ": " + load_error_text(c.pad[0]);
+            return ST_BAD_ARGUMENT;
+        }
+        if (c.status == ST_CAPACITY || c.cell_overflow) {  // a crowded Verlet cell: a larger grid for this box
+            int rc = boxes[size_t(i)]->rebuild_grid(2 * plans[size_t(i)].cell_cap, err);
+            if (rc != ST_OK) {
+                if (err) *err = "box " + std::to_string(i) + ": " + *err;
+                return rc;
+            }
+        } else if (c.status != ST_OK) {
+            if (err) *err = "box " + std::to_string(i) + ": status " + std::to_string(c.status);
+            return c.status;
+        }
+    }
+    *out = std::move(boxes);
     return ST_OK;
 }
 
@@ -660,9 +837,9 @@ int DeviceBox::rebuild_grid(int cap, std::string *err) {
     const int slot_blocks = std::min(1024, (b.nslots + 255) / 256);
     const int nf3 = b.fine_div * b.fine_div * b.fine_div;
     const int clear_blocks = std::min(1024, (std::max({b.n_cells, nf3, b.nslots}) + 255) / 256);
-    k_grid_clear<<<clear_blocks, 256, 0, s>>>(b);
-    k_grid_fill<<<slot_blocks, 256, 0, s>>>(b);
-    if (b.fine_div > 0) k_fine_link<<<slot_blocks, 256, 0, s>>>(b);
+    k_box<OP_GRID_CLEAR><<<clear_blocks, 256, 0, s>>>(b, BoxArg{0, 0});
+    k_box<OP_GRID_FILL><<<slot_blocks, 256, 0, s>>>(b, BoxArg{0, 0});
+    if (b.fine_div > 0) k_box<OP_FINE_LINK><<<slot_blocks, 256, 0, s>>>(b, BoxArg{0, 0});
     if (!cuda_ok(cudaGetLastError(), err, "grid build")) return ST_CUDA;
     int st = check_status(err);
     if (st == ST_CAPACITY) return rebuild_grid(cap * 2, err);
@@ -966,6 +1143,17 @@ int DeviceBox::download(HostState *st, std::string *err, void *copy_stream) {
     return ST_OK;
 }
 
+int DeviceBox::n_alive(int *n, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    DevScalars sc;
+    if (!cuda_ok(cudaMemcpyAsync(&sc, b.sc, sizeof(sc), cudaMemcpyDeviceToHost, s), err, "download") ||
+        !cuda_ok(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
+    *n = sc.n_alive;
+    return ST_OK;
+}
+
 int DeviceBox::store(mcacg_state *out, std::string *err, void *copy_stream) {
     DevBox &b = *static_cast<DevBox *>(devbox_);
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
@@ -984,24 +1172,15 @@ int DeviceBox::store(mcacg_state *out, std::string *err, void *copy_stream) {
         if (err) *err = "state buffers too small";
         return ST_BAD_ARGUMENT;
     }
-    const size_t need = 176 * size_t(na) + 16 * size_t(b.ns) + 8 * size_t(b.nslots);
-    if (need > stage_bytes_) {
+    if (pack_layout(na, b.ns, b.nslots).total > stage_bytes_) {
         if (err) *err = "store staging area too small";
         return ST_CAPACITY;
     }
-    char *p = static_cast<char *>(stage_);
-    PackStage ps;
-    ps.agg = reinterpret_cast<double *>(p);
-    ps.count = reinterpret_cast<long long *>(p + 168 * size_t(na));
-    ps.label = reinterpret_cast<long long *>(p + 176 * size_t(na));
-    ps.members = ps.label + b.ns;
-    ps.rank = reinterpret_cast<int *>(ps.members + b.ns);
-    ps.moff = ps.rank + b.nslots;
-    ps.na = na;
-    ps.sel = sc.pool_sel;
+    const PackStage ps = pack_stage(b, na, sc.pool_sel);
+    const BoxArg pa{na, sc.pool_sel};
     const int blocks = std::min(1024, (std::max(b.ns, b.nslots) + 255) / 256);
-    k_pack_ranks<<<1, kLoadScanThreads, 0, cs>>>(b, ps);
-    k_pack<<<blocks, 256, 0, cs>>>(b, ps);
+    k_box<OP_PACK_RANKS><<<1, kScanThreads, 0, cs>>>(b, pa);
+    k_box<OP_PACK><<<blocks, 256, 0, cs>>>(b, pa);
     if (!cuda_ok(cudaGetLastError(), err, "store")) return ST_CUDA;
     auto get = [&](void *dst, const void *src, size_t bytes) {
         return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, cs), err, "store");
@@ -1018,6 +1197,100 @@ int DeviceBox::store(mcacg_state *out, std::string *err, void *copy_stream) {
     out->box_length = b.L;
     out->maxradius = sc.maxradius;
     out->time = sc.time;
+    return ST_OK;
+}
+
+int DeviceBox::store_many(const std::vector<DeviceBox *> &boxes, const std::vector<mcacg_state *> &outs,
+                          void *stream, std::vector<int> *rcs, std::vector<std::string> *errs, std::string *err) {
+    const int n = int(boxes.size());
+    rcs->assign(size_t(n), ST_OK);
+    errs->assign(size_t(n), std::string());
+    if (n == 0) return ST_OK;
+    if (outs.size() != boxes.size()) {
+        if (err) *err = "one state per box is needed";
+        return ST_BAD_ARGUMENT;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    std::vector<DevBox> host_boxes(static_cast<size_t>(n));
+    int max_items = 0;
+    for (int i = 0; i < n; ++i) {
+        if (!cuda_ok(cudaStreamSynchronize(static_cast<cudaStream_t>(boxes[size_t(i)]->stream_)), err, "sync"))
+            return ST_CUDA;
+        host_boxes[size_t(i)] = *static_cast<DevBox *>(boxes[size_t(i)]->devbox_);
+        max_items = std::max({max_items, host_boxes[size_t(i)].ns, host_boxes[size_t(i)].nslots});
+    }
+    const size_t tb = (sizeof(DevBox) * size_t(n) + 255) & ~size_t(255);
+    const size_t ta = (sizeof(BoxArg) * size_t(n) + 255) & ~size_t(255);
+    char *tmp = nullptr;
+    if (!cuda_ok(cudaMalloc((void **)&tmp, tb + ta + sizeof(DevScalars) * size_t(n)), err, "cudaMalloc")) return ST_CUDA;
+    std::unique_ptr<char, void (*)(char *)> tmp_owner(tmp, [](char *p) { cudaFree(p); });
+    DevBox *dboxes = reinterpret_cast<DevBox *>(tmp);
+    BoxArg *dargs = reinterpret_cast<BoxArg *>(tmp + tb);
+    DevScalars *dsc = reinterpret_cast<DevScalars *>(tmp + tb + ta);
+    std::vector<DevScalars> sc(static_cast<size_t>(n));
+    if (!cuda_ok(cudaMemcpyAsync(dboxes, host_boxes.data(), sizeof(DevBox) * size_t(n), cudaMemcpyHostToDevice, s),
+                 err, "store"))
+        return ST_CUDA;
+    k_gather_scalars<<<(n + 255) / 256, 256, 0, s>>>(dboxes, n, dsc);
+    if (!cuda_ok(cudaGetLastError(), err, "store") ||
+        !cuda_ok(cudaMemcpyAsync(sc.data(), dsc, sizeof(DevScalars) * size_t(n), cudaMemcpyDeviceToHost, s), err,
+                 "store") ||
+        !cuda_ok(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
+    // per box: the live count, or -1 for a box that cannot be stored
+    std::vector<BoxArg> args(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i) {
+        const DevBox &b = host_boxes[size_t(i)];
+        const mcacg_state *o = outs[size_t(i)];
+        const int na = sc[size_t(i)].n_alive;
+        args[size_t(i)] = BoxArg{-1, sc[size_t(i)].pool_sel};
+        if (!o || !o->spheres || !o->sphere_label || !o->aggregates || !o->n_spheres_per_aggregate || !o->members) {
+            (*rcs)[size_t(i)] = ST_BAD_ARGUMENT;
+            (*errs)[size_t(i)] = "incomplete state buffers";
+        } else if (o->n_spheres < b.ns || o->n_aggregates < na || na < 1) {
+            (*rcs)[size_t(i)] = ST_BAD_ARGUMENT;
+            (*errs)[size_t(i)] = "state buffers too small";
+        } else if (pack_layout(na, b.ns, b.nslots).total > boxes[size_t(i)]->stage_bytes_) {
+            (*rcs)[size_t(i)] = ST_CAPACITY;
+            (*errs)[size_t(i)] = "store staging area too small";
+        } else {
+            args[size_t(i)].a = na;
+        }
+    }
+    const int per = blocks_per_box(n, max_items);
+    if (!cuda_ok(cudaMemcpyAsync(dargs, args.data(), sizeof(BoxArg) * size_t(n), cudaMemcpyHostToDevice, s), err,
+                 "store"))
+        return ST_CUDA;
+    k_boxes<OP_PACK_RANKS><<<n, kScanThreads, 0, s>>>(dboxes, dargs, n, 1);
+    k_boxes<OP_PACK><<<n * per, 256, 0, s>>>(dboxes, dargs, n, per);
+    if (!cuda_ok(cudaGetLastError(), err, "store")) return ST_CUDA;
+    auto get = [&](void *dst, const void *src, size_t bytes) {
+        return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s), err, "store");
+    };
+    for (int i = 0; i < n; ++i) {
+        const int na = args[size_t(i)].a;
+        if (na < 0) continue;
+        const DevBox &b = host_boxes[size_t(i)];
+        const PackStage ps = pack_stage(b, na, args[size_t(i)].b);
+        mcacg_state *o = outs[size_t(i)];
+        if (!(get(o->spheres, b.sph, sizeof(double) * 9 * size_t(b.ns)) &&
+              get(o->sphere_label, ps.label, 8 * size_t(b.ns)) && get(o->aggregates, ps.agg, 168 * size_t(na)) &&
+              get(o->n_spheres_per_aggregate, ps.count, 8 * size_t(na)) &&
+              get(o->members, ps.members, 8 * size_t(b.ns))))
+            return ST_CUDA;
+    }
+    if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
+    for (int i = 0; i < n; ++i) {
+        if (args[size_t(i)].a < 0) continue;
+        const DevBox &b = host_boxes[size_t(i)];
+        mcacg_state *o = outs[size_t(i)];
+        o->n_spheres = b.ns;
+        o->n_aggregates = args[size_t(i)].a;
+        o->n_verlet_divisions = b.n_div;
+        o->box_length = b.L;
+        o->maxradius = sc[size_t(i)].maxradius;
+        o->time = sc[size_t(i)].time;
+    }
     return ST_OK;
 }
 

@@ -96,6 +96,25 @@ struct DevBox {
     unsigned long long *best_res, *best_ij;
 };
 
+// Byte offsets of a packed state (na live aggregates) in the merge's pair
+// scratch (32 B per pair, 8 ns + 1024 pairs: 200 B per sphere at most are used):
+// aggregates [21][na] f64, sphere counts [na] i64, labels [ns] i64, members
+// [ns] i64, then the ranks and member offsets of the slots [nslots] i32 each.
+struct PackLayout {
+    size_t agg, count, label, members, rank, moff, total;
+};
+__host__ __device__ inline PackLayout pack_layout(int na, int ns, int nslots) {
+    PackLayout l;
+    l.agg = 0;
+    l.count = 168 * size_t(na);
+    l.label = 176 * size_t(na);
+    l.members = l.label + 8 * size_t(ns);
+    l.rank = l.members + 8 * size_t(ns);
+    l.moff = l.rank + 4 * size_t(nslots);
+    l.total = l.moff + 4 * size_t(nslots);
+    return l;
+}
+
 __device__ __forceinline__ double &A(const DevBox &b, int field, int slot) {
     return b.agg[size_t(field) * size_t(b.nslots) + size_t(slot)];
 }

@@ -584,12 +584,12 @@ int mcacg_batch_size(const mcacg_batch *batch, int32_t *n_boxes) {
 int mcacg_batch_box_sizes(mcacg_batch *batch, int32_t box, int64_t *n_spheres, int64_t *n_aggregates) {
     return guarded([&] {
         if (!batch || box < 0 || box >= batch->impl->size()) return fail(MCACG_ERR_BAD_ARGUMENT, "bad box");
-        std::vector<mcacg::BoxRunStats> s;
         std::string err;
-        int rc = batch->impl->stats(&s, &err);
+        int alive = 0;
+        int rc = batch->impl->box(box).n_alive(&alive, &err);
         if (rc != 0) return finish(rc, err);
         if (n_spheres) *n_spheres = batch->impl->box(box).ns();
-        if (n_aggregates) *n_aggregates = s[size_t(box)].n_alive;
+        if (n_aggregates) *n_aggregates = alive;
         return 0;
     });
 }
@@ -616,38 +616,51 @@ int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state)
 int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_boxes) {
     return guarded([&] {
         if (!batch || !states || n_boxes != batch->impl->size()) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
-        std::vector<int> rcs(static_cast<size_t>(n_boxes), 0);
-        std::vector<std::string> errs(static_cast<size_t>(n_boxes));
         std::vector<double> times;
         std::string err;
         int rc = batch->impl->times(&times, &err);
         if (rc != 0) return finish(rc, err);
-        // one copy stream per worker thread, so boxes come back concurrently
+        // boxes without growth: packed on the device and copied straight
+        // into the caller's arrays, all boxes at once
+        std::vector<int> direct, grown;
+        for (int i = 0; i < n_boxes; ++i) (batch->impl->grows(i) ? grown : direct).push_back(i);
+        std::vector<mcacg::DeviceBox *> boxes;
+        std::vector<mcacg_state *> outs;
+        for (int i : direct) {
+            boxes.push_back(&batch->impl->box(i));
+            outs.push_back(&states[i]);
+        }
+        std::vector<int> rcs;
+        std::vector<std::string> errs;
+        rc = mcacg::DeviceBox::store_many(boxes, outs, batch->impl->stream(), &rcs, &errs, &err);
+        if (rc != 0) return finish(rc, err);
+        for (size_t k = 0; k < direct.size(); ++k) {
+            if (rcs[k] != 0) return fail(rcs[k], "box " + std::to_string(direct[k]) + ": " + errs[k]);
+            states[direct[k]].time = times[size_t(direct[k])];
+        }
+        // growing boxes: overlap and coordination refreshed on the host, one
+        // copy stream per worker thread
         struct CopyStream {
             cudaStream_t s = nullptr;
             ~CopyStream() {
                 if (s) cudaStreamDestroy(s);
             }
         };
-        mcacg::parallel_for(n_boxes, [&](int i) {
+        rcs.assign(grown.size(), 0);
+        errs.assign(grown.size(), std::string());
+        mcacg::parallel_for(int(grown.size()), [&](int k) {
             thread_local CopyStream cs;
             if (!cs.s) cudaStreamCreateWithFlags(&cs.s, cudaStreamNonBlocking);
-            if (!batch->impl->grows(i)) {
-                // packed on the device and copied straight into the caller's arrays
-                rcs[size_t(i)] = batch->impl->box(i).store(&states[i], &errs[size_t(i)], cs.s);
-                states[i].time = times[size_t(i)];
-                return;
-            }
-            // growing boxes: overlap and coordination refreshed on the host
+            const int i = grown[size_t(k)];
             mcacg::HostState st;
-            rcs[size_t(i)] = batch->impl->box(i).download(&st, &errs[size_t(i)], cs.s);
-            if (rcs[size_t(i)] != 0) return;
+            rcs[size_t(k)] = batch->impl->box(i).download(&st, &errs[size_t(k)], cs.s);
+            if (rcs[size_t(k)] != 0) return;
             mcacg::host_refresh_overlap(&st);
             st.time = times[size_t(i)];
-            rcs[size_t(i)] = store_host_state(st, &states[i], &errs[size_t(i)]);
+            rcs[size_t(k)] = store_host_state(st, &states[i], &errs[size_t(k)]);
         });
-        for (int i = 0; i < n_boxes; ++i)
-            if (rcs[size_t(i)] != 0) return fail(rcs[size_t(i)], "box " + std::to_string(i) + ": " + errs[size_t(i)]);
+        for (size_t k = 0; k < grown.size(); ++k)
+            if (rcs[k] != 0) return fail(rcs[k], "box " + std::to_string(grown[k]) + ": " + errs[k]);
         return 0;
     });
 }

@@ -2,6 +2,7 @@
 // download, launches of the single-box kernels).
 #pragma once
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -118,6 +119,12 @@ class DeviceBox {
     // The host arrays must stay valid until this returns.
     static int create(const HostState &st, void *stream, DeviceBox **out, std::string *err);
     static int create(const StateView &v, void *stream, DeviceBox **out, std::string *err);
+    // Many boxes on one stream: one device allocation holds them all (freed
+    // with the last of them), the copies go in one stream and the load and
+    // grid kernels run over all boxes at once. States of one call have the
+    // same integer width. On error, *err names the failing box.
+    static int create_many(const std::vector<StateView> &views, void *stream,
+                           std::vector<std::unique_ptr<DeviceBox>> *out, std::string *err);
     ~DeviceBox();
     DeviceBox(const DeviceBox &) = delete;
     DeviceBox &operator=(const DeviceBox &) = delete;
@@ -148,11 +155,19 @@ class DeviceBox {
     // Capacities are out->n_spheres and out->n_aggregates; the scalars are
     // set on return.
     int store(mcacg_state *out, std::string *err, void *copy_stream = nullptr);
+    // store() for many boxes at once on 'stream': their scalars in one copy,
+    // the packing kernels over all boxes, the pieces copied in one stream.
+    // (*rcs)[i] and (*errs)[i] report box i; the return value reports the
+    // call itself.
+    static int store_many(const std::vector<DeviceBox *> &boxes, const std::vector<mcacg_state *> &outs,
+                          void *stream, std::vector<int> *rcs, std::vector<std::string> *errs, std::string *err);
     // Rebuilds the Verlet grid from the aggregate positions with 'cap' rooms per cell.
     int rebuild_grid(int cap, std::string *err);
     int sync(std::string *err);
     void set_profiling(bool on);
     Profile take_profile();
+    // Live aggregates (after the work queued on the box's stream).
+    int n_alive(int *n, std::string *err);
     int ns() const { return ns_; }
     int nslots() const { return nslots_; }
     void *devbox_ptr() { return devbox_; }  // DevBox* (opaque to host code)
@@ -166,6 +181,7 @@ class DeviceBox {
     bool own_stream_ = false;
     int ns_ = 0, nslots_ = 0;
     std::vector<void *> allocations_;
+    std::shared_ptr<void> arena_;  // the allocation shared by boxes made together
     void *host_out_ = nullptr;  // mapped pinned result buffer
     void *dev_out_ = nullptr;
     bool profiling_ = false;

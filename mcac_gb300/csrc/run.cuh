@@ -319,6 +319,35 @@ __device__ inline double thread_update_aggregate(const BoxRun &R, int a, bool fu
     return rmax;
 }
 
+// The pick tree from the time steps: leaves 1/time_step of the live slots
+// (0 elsewhere), then each level from the one below, children summed in
+// order, and the total of the top level into the loop state.
+__device__ inline void block_tree_build(const BoxRun &R) {
+    const DevBox &b = R.box;
+    const int tid = threadIdx.x, NT = blockDim.x;
+    for (int a = tid; a < R.tree_len[0]; a += NT)
+        R.tree[R.tree_off[0] + a] = (a < b.nslots && b.agg_n[a] > 0) ? 1.0 / A(b, AGG_TIME_STEP, a) : 0.0;
+    __syncthreads();
+    for (int lev = 1; lev < R.tree_levels; ++lev) {
+        for (int g = tid; g < R.tree_len[lev]; g += NT) {
+            double sum = 0.0;
+            for (int k = 0; k < kTreeFan; ++k) {
+                const int c = g * kTreeFan + k;
+                if (c < R.tree_len[lev - 1]) sum += R.tree[R.tree_off[lev - 1] + c];
+            }
+            R.tree[R.tree_off[lev] + g] = sum;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const int top = R.tree_levels - 1;
+        double total = 0.0;
+        for (int k = 0; k < R.tree_len[top]; ++k) total += R.tree[R.tree_off[top] + k];
+        R.st->weight_total = total;
+    }
+    __syncthreads();
+}
+
 // The per-step update of every aggregate after growth (calcul.cpp:180-206):
 // fields, Verlet and fine cells (centres move as spheres grow unevenly),
 // maxradius, and the pick tree rebuilt from the new time steps.
@@ -362,28 +391,8 @@ __device__ inline void block_update_all(const BoxRun &R, RS &sm, bool full) {
                 if (b.agg_n[a] > 0) regrid(b, a, agg_pos(b, a));
         }
     }
-    // pick tree: leaves 1/time_step, then each level from the one below
-    for (int a = tid; a < R.tree_len[0]; a += NT)
-        R.tree[R.tree_off[0] + a] = (a < b.nslots && b.agg_n[a] > 0) ? 1.0 / A(b, AGG_TIME_STEP, a) : 0.0;
     __syncthreads();
-    for (int lev = 1; lev < R.tree_levels; ++lev) {
-        for (int g = tid; g < R.tree_len[lev]; g += NT) {
-            double sum = 0.0;
-            for (int k = 0; k < kTreeFan; ++k) {
-                const int c = g * kTreeFan + k;
-                if (c < R.tree_len[lev - 1]) sum += R.tree[R.tree_off[lev - 1] + c];
-            }
-            R.tree[R.tree_off[lev] + g] = sum;
-        }
-        __syncthreads();
-    }
-    if (tid == 0) {
-        const int top = R.tree_levels - 1;
-        double total = 0.0;
-        for (int k = 0; k < R.tree_len[top]; ++k) total += R.tree[R.tree_off[top] + k];
-        R.st->weight_total = total;
-    }
-    __syncthreads();
+    block_tree_build(R);
     tree_cache_load(R, sm.tree);
 }
 

@@ -90,6 +90,12 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
     }
 }
 
+// The scalars of n boxes in one array.
+__global__ void k_gather_run_scalars(const BoxRun *runs, int n, DevScalars *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = *runs[i].box.sc;
+}
+
 // The pick trees of n boxes from their time steps, one block per box
 // (block_tree_build); the total weight goes to each box's loop state.
 __global__ void __launch_bounds__(256) k_tree_build(const BoxRun *runs, int n) {
@@ -202,6 +208,7 @@ BatchRunner::~BatchRunner() {
     for (void *p : trees_) cudaFree(p);
     if (runs_dev_) cudaFree(runs_dev_);
     if (states_dev_) cudaFree(states_dev_);
+    if (sc_dev_) cudaFree(sc_dev_);
     owned_.clear();
     if (own_stream_ && stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
 }
@@ -294,6 +301,7 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
     std::vector<RunState> states(static_cast<size_t>(n));
     if (!ok_cuda(cudaMalloc(&runs_dev_, sizeof(BoxRun) * size_t(n)), err, "cudaMalloc")) return ST_CUDA;
     if (!ok_cuda(cudaMalloc(&states_dev_, sizeof(RunState) * size_t(n)), err, "cudaMalloc")) return ST_CUDA;
+    if (!ok_cuda(cudaMalloc(&sc_dev_, sizeof(DevScalars) * size_t(n)), err, "cudaMalloc")) return ST_CUDA;
     RunState *states_dev = static_cast<RunState *>(states_dev_);
     // the pick trees of all boxes in one allocation, built on the device
     std::vector<size_t> tree_off(static_cast<size_t>(n) + 1, 0);
@@ -517,14 +525,15 @@ int BatchRunner::stats(std::vector<BoxRunStats> *out, std::string *err) {
     if (!ok_cuda(cudaMemcpyAsync(st.data(), states_dev_, sizeof(RunState) * size_t(n), cudaMemcpyDeviceToHost, s),
                  err, "download"))
         return ST_CUDA;
+    // the boxes' scalars gathered on the device, then one copy
     std::vector<DevScalars> sc(static_cast<size_t>(n));
-    for (int i = 0; i < n; ++i) {
-        const DevBox &b = *static_cast<DevBox *>(boxes_[size_t(i)]->devbox_ptr());
-        if (!ok_cuda(cudaMemcpyAsync(&sc[size_t(i)], b.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s), err,
-                     "download"))
-            return ST_CUDA;
-    }
-    if (!ok_cuda(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
+    k_gather_run_scalars<<<(n + 255) / 256, 256, 0, s>>>(static_cast<const BoxRun *>(runs_dev_), n,
+                                                          static_cast<DevScalars *>(sc_dev_));
+    if (!ok_cuda(cudaGetLastError(), err, "k_gather_run_scalars") ||
+        !ok_cuda(cudaMemcpyAsync(sc.data(), sc_dev_, sizeof(DevScalars) * size_t(n), cudaMemcpyDeviceToHost, s), err,
+                 "download") ||
+        !ok_cuda(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
     out->resize(size_t(n));
     for (int i = 0; i < n; ++i) {
         BoxRunStats &o = (*out)[size_t(i)];

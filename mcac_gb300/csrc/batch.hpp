@@ -74,6 +74,7 @@ class BatchRunner {
     bool own_stream_ = false;
     void *runs_dev_ = nullptr;    // BoxRun[n]
     void *states_dev_ = nullptr;  // RunState[n]
+    void *sc_dev_ = nullptr;      // DevScalars[n], gathered by stats()
     std::vector<void *> trees_;
     double last_ms_ = 0;
     int launches_ = 0;

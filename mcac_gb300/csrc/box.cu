@@ -478,6 +478,13 @@ DevBox plan_box(const StateView &st) {
     const double nf = std::floor(st.box_length / h);
     b.fine_div = (nf > double(st.n_div) && nf <= double(kFineMaxDiv)) ? int(nf) : 0;
     b.fine_step = b.fine_div > 0 ? double(b.fine_div) / st.box_length : 0.0;
+    b.inv_L = 1.0 / st.box_length;
+    b.Lf = float(st.box_length);
+    b.inv_Lf = 1.0f / b.Lf;
+    b.margin_f = float(b.margin);
+    b.fine_step_f = float(b.fine_step);
+    b.inv_fine_cells = b.fine_div > 0 ? 1.0f / float(double(b.fine_div) * b.fine_div * b.fine_div) : 0.0f;
+    b.inv_cells = 1.0f / float(b.n_cells);
     // capacities
     const int avg = (st.nslots + b.n_cells - 1) / b.n_cells;
     b.cell_cap = std::max({64, 2 * maxc, 8 * avg});

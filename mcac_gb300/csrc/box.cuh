@@ -53,6 +53,10 @@ struct DevBox {
     double L;        // box_length
     double step;     // double(n_div) / box_length
     double margin;   // FP32 screening margin (absolute, metres)
+    double inv_L;    // 1 / box_length
+    // FP32 copies for the screens and the fine grid
+    float Lf, inv_Lf, margin_f, fine_step_f;
+    float inv_fine_cells, inv_cells;  // 1 / fine_div^3, 1 / n_cells
     int n_div;
     int n_cells;
     int ns;          // spheres
@@ -310,36 +314,53 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
 
     const Vec3 sp = agg_pos(b, src);
     const double rmax_src = A(b, AGG_RMAX, src);
-    if (tid == 0) {
-        double mindist = rmax_src + sc->maxradius;
-        Vec3 vec{dist * dir.x, dist * dir.y, dist * dir.z};
-        sm.range = neighborhood_range(sp, vec, mindist, b.n_div, b.L);
-        // The fine grid finds the same neighbours when every aggregate that
-        // can pass the bounding-sphere filter lies in the fine cells visited:
-        // its centre is within rmax_src + rmax <= mindist of the path. The
-        // range is widened by 1e-6 of a fine cell, far above the rounding of
-        // these bounds and of the periodic images (~1e-13 of a cell). Used
-        // when it visits fewer cells and aggregates.
-        sm.use_fine = 0;
-        if (b.fine_div > 0) {
-            const double pos[3] = {sp.x, sp.y, sp.z}, v[3] = {vec.x, vec.y, vec.z};
-            const double hf = 1e-6 / b.fine_step;
-            double n_fine = 1.0, n_coarse = 1.0;
-            for (int l = 0; l < 3; ++l) {
-                const double lo = floor((pos[l] - mindist + dmin(v[l], 0.) - hf) * b.fine_step);
-                const double hi = floor((pos[l] + mindist + dmax(v[l], 0.) + hf) * b.fine_step);
-                const bool part = (hi - lo + 1.0 < double(b.fine_div)) && lo > -1e9 && hi < 1e9;
-                sm.fine_lo[l] = part ? int(lo) : 0;
-                sm.fine_n[l] = part ? int(hi - lo + 1.0) : b.fine_div;
-                n_fine *= double(sm.fine_n[l]);
-                n_coarse *= double(sm.range.hi[l] - sm.range.lo[l] + 1);
+    const float4 src_f = b.agg_f4[src];  // FP32 centre and r_max of the source
+    // Lanes 0-2 of warp 0 take one axis each (FP64 work costs the same for
+    // one lane as for the warp): the reference's Verlet cell range, and the
+    // fine range. The fine grid finds the same neighbours when every
+    // aggregate that can pass the bounding-sphere filter lies in the fine
+    // cells visited: its centre is within rmax_src + rmax <= mindist of the
+    // path. The fine range is computed in FP32 and widened by 2e-3 of a fine
+    // cell: its rounding (and that of the aggregates' FP32 fine cells) stays
+    // below 1e-4 of a cell while it spans less than the box, and a range of
+    // the box or more is the whole axis.
+    if (tid < 32) {
+        int lo = 0, hi = 0, flo = 0, fn = 0;
+        if (tid < 3) {
+            const double mindist = rmax_src + sc->maxradius;
+            const double sl = tid == 0 ? sp.x : (tid == 1 ? sp.y : sp.z);
+            const double vl = dist * (tid == 0 ? dir.x : (tid == 1 ? dir.y : dir.z));
+            neighborhood_axis(sl, vl, mindist, b.n_div, b.L, b.inv_L, &lo, &hi);
+            sm.range.lo[tid] = lo;
+            sm.range.hi[tid] = hi;
+            if (b.fine_div > 0) {
+                const float pf = tid == 0 ? src_f.x : (tid == 1 ? src_f.y : src_f.z);
+                const float mf = float(mindist), vf = float(vl);
+                const float flof = floorf((pf - mf + fminf(vf, 0.f)) * b.fine_step_f - 2e-3f);
+                const float fhif = floorf((pf + mf + fmaxf(vf, 0.f)) * b.fine_step_f + 2e-3f);
+                const bool part = (fhif - flof + 1.f < float(b.fine_div)) && flof > -1e6f && fhif < 1e6f;
+                flo = part ? int(flof) : 0;
+                fn = part ? int(fhif - flof + 1.f) : b.fine_div;
+                sm.fine_lo[tid] = flo;
+                sm.fine_n[tid] = fn;
             }
-            const double alive = double(sc->n_alive);
-            const double nf3 = double(b.fine_div) * double(b.fine_div) * double(b.fine_div);
-            const double cost_fine = n_fine * (1.0 + alive / nf3);
-            const double cost_coarse = n_coarse * (1.0 + alive / double(b.n_cells));
-            sm.use_fine = (n_fine <= double(kFineMaxCells)) && (cost_fine < cost_coarse);
         }
+        const int nc = hi - lo + 1;
+        const int nc1 = __shfl_sync(0xffffffffu, nc, 1), nc2 = __shfl_sync(0xffffffffu, nc, 2);
+        const int fn1 = __shfl_sync(0xffffffffu, fn, 1), fn2 = __shfl_sync(0xffffffffu, fn, 2);
+        if (tid == 0) {
+            sm.use_fine = 0;
+            if (b.fine_div > 0) {
+                // visit the grid that reads fewer cells and list entries
+                const int n_fine = fn * fn1 * fn2;
+                const float alive = float(sc->n_alive);
+                const float cost_fine = float(n_fine) * (1.f + alive * b.inv_fine_cells);
+                const float cost_coarse = float(nc) * float(nc1) * float(nc2) * (1.f + alive * b.inv_cells);
+                sm.use_fine = (n_fine <= kFineMaxCells) && (cost_fine < cost_coarse);
+            }
+        }
+    }
+    if (tid == 0) {
         sm.n_cand = 0;
         sm.n_surv = 0;
         sm.found_source = 0;
@@ -371,9 +392,9 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
 
     // FP32 sweep of the bounding sphere of the source.
     Sweep32 w;
-    w.px = float(sp.x);
-    w.py = float(sp.y);
-    w.pz = float(sp.z);
+    w.px = src_f.x;
+    w.py = src_f.y;
+    w.pz = src_f.z;
     w.ux = float(dir.x);
     w.uy = float(dir.y);
     w.uz = float(dir.z);
@@ -381,9 +402,11 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     w.cx = 0.5f * w.dist * w.ux;
     w.cy = 0.5f * w.dist * w.uy;
     w.cz = 0.5f * w.dist * w.uz;
-    w.L = float(b.L);
-    w.invL = 1.0f / w.L;
-    const float margin = float(b.margin + 1e-6 * dist);
+    w.L = b.Lf;
+    w.invL = b.inv_Lf;
+    // b.margin and 1e-6 dist, each rounded to FP32 (the screen keeps them
+    // conservative: both bound errors far smaller than themselves)
+    const float margin = b.margin_f + 1e-6f * w.dist;
     w.zmax = fmaxf(fabsf(w.dist * w.ux), fmaxf(fabsf(w.dist * w.uy), fabsf(w.dist * w.uz)));
     w.margin = margin;
 
@@ -394,7 +417,7 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     // bounding-sphere filter of one neighbour; 'key' is its position in the
     // reference's neighbour list order (Verlet cell rank in the scan, then slot)
     auto consider = [&](int slot, long long key, float4 of) {
-        if (!capsule_hit(w, of.x, of.y, of.z, float(rmax_src) + of.w + margin)) return;
+        if (!capsule_hit(w, of.x, of.y, of.z, src_f.w + of.w + margin)) return;
         const double ox = A(b, AGG_X, slot), oy = A(b, AGG_Y, slot), oz = A(b, AGG_Z, slot);
         const double orm = A(b, AGG_RMAX, slot);
         double db = sweep_contact_distance(sp, rmax_src, Vec3{ox, oy, oz}, orm, dir, dist, b.L);
@@ -877,20 +900,23 @@ __device__ __forceinline__ void cell_insert(const DevBox &b, int cell, int slot)
     b.cell_pos[slot] = n;
     b.cell_n[cell] = n + 1;
 }
-// Fine grid cell of a position (clamped into the grid).
-// Periodic fine cell index of one coordinate (a position of exactly L falls
-// in cell 0, its periodic image).
-__device__ __forceinline__ int fine_index(double x, double step, int n) {
-    double f = floor(x * step);
-    if (!(f > -1e9 && f < 1e9)) f = 0.0;
+// Fine grid cells, in FP32: the fine grid is this library's own search
+// structure (the neighbours that count are the Verlet grid's), so a cell only
+// has to agree with the query's fine range, which is widened by far more
+// than the FP32 rounding. Periodic index of one coordinate (a position that
+// rounds to L falls in cell 0, its periodic image).
+__device__ __forceinline__ int fine_index(float x, float step, int n) {
+    float f = floorf(x * step);
+    if (!(f > -1e6f && f < 1e6f)) f = 0.f;
     return periodic_cell(static_cast<int>(f), n);
 }
-__device__ __forceinline__ int fine_cell_of(const DevBox &b, Vec3 p) {
+__device__ __forceinline__ int fine_cell_of(const DevBox &b, float x, float y, float z) {
     const int n = b.fine_div;
-    const int ix = fine_index(p.x, b.fine_step, n);
-    const int iy = fine_index(p.y, b.fine_step, n);
-    const int iz = fine_index(p.z, b.fine_step, n);
-    return (ix * n + iy) * n + iz;
+    return (fine_index(x, b.fine_step_f, n) * n + fine_index(y, b.fine_step_f, n)) * n +
+           fine_index(z, b.fine_step_f, n);
+}
+__device__ __forceinline__ int fine_cell_of(const DevBox &b, Vec3 p) {
+    return fine_cell_of(b, float(p.x), float(p.y), float(p.z));
 }
 // Take a slot out of its fine cell's list / put it at the head of one (one thread).
 __device__ __forceinline__ void fine_unlink(const DevBox &b, int slot) {
@@ -913,10 +939,8 @@ __device__ __forceinline__ void fine_link(const DevBox &b, int slot, int c) {
 // the same move in the fine grid (one thread). The loads that do not depend
 // on one another are issued first: a move costs three rounds of memory
 // latency instead of one per list operation.
-__device__ __forceinline__ void regrid(const DevBox &b, int slot, Vec3 p) {
-    const int c = cell_of(b, p);
+__device__ __forceinline__ void regrid_to(const DevBox &b, int slot, int c, int fc) {
     const bool fine = b.fine_div > 0;
-    const int fc = fine ? fine_cell_of(b, p) : -1;
     // round 1: everything indexed by the slot or by the new cells
     const int old = b.agg_cell[slot];
     const int k = b.cell_pos[slot];
@@ -966,22 +990,38 @@ __device__ __forceinline__ void regrid(const DevBox &b, int slot, Vec3 p) {
     }
 }
 
+__device__ __forceinline__ void regrid(const DevBox &b, int slot, Vec3 p) {
+    regrid_to(b, slot, cell_of(b, p), b.fine_div > 0 ? fine_cell_of(b, p) : -1);
+}
+
 // --------------------------------------------------------------- translate
-// Aggregate::translate (aggregats/aggregat.cpp:148-161).
+// Aggregate::translate (aggregats/aggregat.cpp:148-161). Lanes 0-2 of warp 0
+// take one axis each (the FP64 work of one lane costs as much as that of the
+// warp), lane 0 then moves the slot in the grids.
 __device__ inline void block_translate(const DevBox &b, int slot, Vec3 v, double *refpos_sm) {
     const int tid = threadIdx.x;
-    if (tid == 0) {
-        double x = periodic_position(A(b, AGG_X, slot) + v.x, b.L);
-        double y = periodic_position(A(b, AGG_Y, slot) + v.y, b.L);
-        double z = periodic_position(A(b, AGG_Z, slot) + v.z, b.L);
-        A(b, AGG_X, slot) = x;
-        A(b, AGG_Y, slot) = y;
-        A(b, AGG_Z, slot) = z;
-        b.agg_f4[slot] = make_float4(float(x), float(y), float(z), float(A(b, AGG_RMAX, slot)));
-        refpos_sm[0] = x - A(b, AGG_RX, slot);
-        refpos_sm[1] = y - A(b, AGG_RY, slot);
-        refpos_sm[2] = z - A(b, AGG_RZ, slot);
-        regrid(b, slot, Vec3{x, y, z});
+    if (tid < 32) {
+        double x = 0.0;
+        float xf = 0.f;
+        int vc = 0, fc = 0;
+        if (tid < 3) {
+            const double vl = tid == 0 ? v.x : (tid == 1 ? v.y : v.z);
+            x = periodic_position(A(b, AGG_X + tid, slot) + vl, b.L);
+            A(b, AGG_X + tid, slot) = x;
+            refpos_sm[tid] = x - A(b, AGG_RX + tid, slot);
+            xf = float(x);
+            vc = min(max(verlet_coord(x, b.step), 0), b.n_div - 1);
+            if (b.fine_div > 0) fc = fine_index(xf, b.fine_step_f, b.fine_div);
+        }
+        const float yf = __shfl_sync(0xffffffffu, xf, 1), zf = __shfl_sync(0xffffffffu, xf, 2);
+        const int vy = __shfl_sync(0xffffffffu, vc, 1), vz = __shfl_sync(0xffffffffu, vc, 2);
+        const int fy = __shfl_sync(0xffffffffu, fc, 1), fz = __shfl_sync(0xffffffffu, fc, 2);
+        if (tid == 0) {
+            const float rm = b.agg_f4[slot].w;  // r_max is unchanged by a move
+            b.agg_f4[slot] = make_float4(xf, yf, zf, rm);
+            const int n = b.fine_div;
+            regrid_to(b, slot, (vc * b.n_div + vy) * b.n_div + vz, n > 0 ? (fc * n + fy) * n + fz : -1);
+        }
     }
     __syncthreads();
     const double rx = refpos_sm[0], ry = refpos_sm[1], rz = refpos_sm[2];

@@ -157,29 +157,41 @@ MCACG_HD int verlet_coord(double x, double step) { return static_cast<int>(floor
 struct CellRange {
     int lo[3], hi[3];
 };
+// floor(a / w) as the reference computes it (the correctly rounded quotient,
+// then floor) from the product a * inv_w, inv_w = 1 / w rounded: the product
+// is within 2 ulp of the quotient, so the two floors agree unless an integer
+// lies within 4 ulp of the product; then the division decides.
+MCACG_HD double floor_div(double a, double w, double inv_w) {
+    const double q = a * inv_w;
+    const double f = floor(q);
+    const double tol = fabs(q) * 0x1p-50 + 0x1p-50;
+    const double g = q - f;  // exact
+    if (g > tol && g < 1.0 - tol) return f;
+    return floor(a / w);
+}
+// One axis of Verlet::get_neighborhood (verlet/verlet.cpp:52-78): the
+// inclusive cell range [lo, hi] before periodic wrapping, the whole axis
+// when it spans n_div cells or more (or is not finite).
+MCACG_HD void neighborhood_axis(double s, double v, double distance, int n_div, double width, double inv_width,
+                                int *lo_out, int *hi_out) {
+    const double p = s + distance + dmax(v, 0.);
+    const double m = s - distance + dmin(v, 0.);
+    const double lo = floor_div(static_cast<double>(n_div) * m, width, inv_width);
+    const double hi = floor_div(static_cast<double>(n_div) * p, width, inv_width) + 1;
+    if (!(hi - lo < n_div) || !(lo > -1e9) || !(hi < 1e9) || int(hi) - int(lo) >= n_div) {
+        *lo_out = 0;
+        *hi_out = n_div - 1;
+        return;
+    }
+    *lo_out = static_cast<int>(lo);
+    *hi_out = static_cast<int>(hi);
+}
 MCACG_HD CellRange neighborhood_range(Vec3 src, Vec3 vec, double distance, int n_div, double width) {
     const double s[3] = {src.x, src.y, src.z};
     const double v[3] = {vec.x, vec.y, vec.z};
     CellRange r;
 MCACG_UNROLL
-    for (int l = 0; l < 3; ++l) {
-        double p = s[l] + distance + dmax(v[l], 0.);
-        double m = s[l] - distance + dmin(v[l], 0.);
-        double lo = floor(static_cast<double>(n_div) * m / width);
-        double hi = floor(static_cast<double>(n_div) * p / width) + 1;
-        // a range of n_div cells or more (or a non-finite one) is the whole axis
-        if (!(hi - lo < n_div) || !(lo > -1e9) || !(hi < 1e9)) {
-            r.lo[l] = 0;
-            r.hi[l] = n_div - 1;
-            continue;
-        }
-        r.lo[l] = static_cast<int>(lo);
-        r.hi[l] = static_cast<int>(hi);
-        if (r.hi[l] - r.lo[l] >= n_div) {
-            r.lo[l] = 0;
-            r.hi[l] = n_div - 1;
-        }
-    }
+    for (int l = 0; l < 3; ++l) neighborhood_axis(s[l], v[l], distance, n_div, width, 1.0 / width, &r.lo[l], &r.hi[l]);
     return r;
 }
 

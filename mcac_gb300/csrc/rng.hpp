@@ -55,6 +55,11 @@ struct RandStream {
         double v = next_int();
         return v / 2147483647.0;
     }
+    // The device loop's draws: the same rand() values scaled by a product
+    // (last bit aside) or drawn in FP32. Its pick and directions follow the
+    // reference statistically, and FP64 instructions are scarce on the GPU.
+    MCACG_HD double uniform_mul() { return double(next_int()) * (1.0 / 2147483647.0); }
+    MCACG_HD float uniform_f() { return float(next_int()) * (1.0f / 2147483647.0f); }
 };
 
 }  // namespace mcacg

@@ -175,7 +175,7 @@ TreeLayout tree_layout(int nslots) {
 // total doubles of device memory) receives the sum tree, built by
 // k_tree_build from the box's time steps once the records are on the device.
 int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *state_dev, BoxRun *run,
-                 RunState *state, double *tree) {
+                 RunState *state, unsigned long long *tree) {
     const TreeLayout tl = tree_layout(b.nslots);
     std::memset(state, 0, sizeof(*state));
     state->rng.seed(uint32_t(p.random_seed < 0 ? 0 : p.random_seed));
@@ -183,8 +183,15 @@ int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *
     state->weight_total = 0.0;  // set by k_tree_build
     std::memset(run, 0, sizeof(*run));
     run->box = b;
-    run->phys = PhysParams{p.viscosity, p.gaz_mean_free_path, p.fractal_dimension, p.density, p.temperature,
-                           p.with_surface_reactions ? p.u_sg : 0.0, p.with_surface_reactions ? 1 : 0,
+    run->phys = PhysParams{p.viscosity,
+                           p.gaz_mean_free_path,
+                           p.fractal_dimension,
+                           p.density,
+                           p.temperature,
+                           p.with_surface_reactions ? p.u_sg : 0.0,
+                           1.0 / p.gaz_mean_free_path,
+                           1.0 / p.fractal_dimension,
+                           p.with_surface_reactions ? 1 : 0,
                            int(std::max<int64_t>(1, p.full_aggregate_update_frequency))};
     run->lim.number_of_aggregates_limit = p.number_of_aggregates_limit;
     run->lim.n_iter_without_event_limit = p.n_iter_without_event_limit;
@@ -310,12 +317,13 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
         tree_off[size_t(i) + 1] = tree_off[size_t(i)] + size_t(tree_layout(b.nslots).total);
     }
     void *trees = nullptr;
-    if (!ok_cuda(cudaMalloc(&trees, sizeof(double) * tree_off[size_t(n)]), err, "cudaMalloc")) return ST_CUDA;
+    if (!ok_cuda(cudaMalloc(&trees, sizeof(unsigned long long) * tree_off[size_t(n)]), err, "cudaMalloc"))
+        return ST_CUDA;
     trees_.push_back(trees);
     for (int i = 0; i < n; ++i) {
         const DevBox &b = *static_cast<DevBox *>(boxes_[size_t(i)]->devbox_ptr());
         int rc = make_box_run(b, params[size_t(i)], times[size_t(i)], states_dev + i, &runs[size_t(i)],
-                              &states[size_t(i)], static_cast<double *>(trees) + tree_off[size_t(i)]);
+                              &states[size_t(i)], static_cast<unsigned long long *>(trees) + tree_off[size_t(i)]);
         if (rc != ST_OK) return rc;
     }
     if (!ok_cuda(cudaMemcpyAsync(runs_dev_, runs.data(), sizeof(BoxRun) * size_t(n), cudaMemcpyHostToDevice, s), err,
@@ -716,9 +724,11 @@ int Server::admit(std::string *err) {
         BoxRun run;
         RunState st;
         const DevBox &db = *static_cast<DevBox *>(d->devbox_ptr());
-        if (!ok_cuda(cudaMalloc(&sl.tree, sizeof(double) * size_t(tree_layout(db.nslots).total)), err, "cudaMalloc"))
+        if (!ok_cuda(cudaMalloc(&sl.tree, sizeof(unsigned long long) * size_t(tree_layout(db.nslots).total)), err,
+                     "cudaMalloc"))
             return ST_CUDA;
-        rc = make_box_run(db, take[i].p, states[i].time, states_dev + slot, &run, &st, static_cast<double *>(sl.tree));
+        rc = make_box_run(db, take[i].p, states[i].time, states_dev + slot, &run, &st,
+                          static_cast<unsigned long long *>(sl.tree));
         if (rc != ST_OK) return rc;
         if (!ok_cuda(cudaMemcpyAsync(states_dev + slot, &st, sizeof(st), cudaMemcpyHostToDevice, s), err, "upload") ||
             !ok_cuda(cudaMemcpyAsync(runs_dev + slot, &run, sizeof(run), cudaMemcpyHostToDevice, s), err, "upload"))

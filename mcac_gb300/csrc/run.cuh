@@ -27,6 +27,7 @@ constexpr int kMaxTreeLevels = 8;
 struct PhysParams {
     double viscosity, lambda, fractal_dimension, density, temperature;
     double u_sg;        // surface growth velocity dr/dt (m/s)
+    double inv_lambda, inv_fractal_dimension;
     int growth;         // with_surface_reactions
     int full_update_every;  // full_aggregate_update_frequency
 };
@@ -44,6 +45,9 @@ struct RunState {
     double time;
     double weight_total;     // sum over live slots of 1/time_step
     double inv_weight;       // 1 / weight_total (the step's time increment)
+    double tree_scale;       // pick tree weights are round(scale / time_step), scale a power of 2
+    double inv_tree_scale;
+    unsigned long long tree_total;  // the pick tree's integer total
     long long steps, events, n_iter_without_event;
     int finished;
     int status;
@@ -62,7 +66,7 @@ struct BoxRun {
     PhysParams phys;
     RunLimits lim;
     RunState *st;
-    double *tree;            // all levels, leaves first
+    unsigned long long *tree;  // all levels, leaves first (fixed-point weights)
     int tree_levels;
     int tree_off[kMaxTreeLevels];
     int tree_len[kMaxTreeLevels];
@@ -76,9 +80,16 @@ constexpr int kMovedCap = 64;  // grid moves listed per update of all aggregates
 // level is not kept.
 constexpr int kTreeCache = 128;
 struct TreeCache {
-    double v[kTreeCache];
+    unsigned long long v[kTreeCache];
     int coff[kMaxTreeLevels];
 };
+// The tree's weights are integers: the live slots' 1/time_step times a power
+// of 2 chosen at each rebuild so that the total stays below 2^62, rounded,
+// and at least 1 (relative rounding below 1e-13 at 1e5 slots). Sums are then
+// exact in any order and the descent runs on the integer pipes: FP64 is
+// scarce on this GPU. The pick follows the weights as the FP64 sums did, up
+// to that rounding (the device loop follows the reference statistically).
+constexpr unsigned long long kTreeHeadroom = 1ULL << 62;
 
 
 template <class QS, class MS>
@@ -90,8 +101,9 @@ struct RunSmemT {
     MergeOut mout;
     double refpos[3];
     double dir[3];
-    double t_pick, dt, full, move;
-    int slot, contact, stop, merged;
+    unsigned long long t_pick;  // pick target in the tree's fixed point
+    double dt, full, move;
+    int slot, contact, stop, merged, rescale;
     int keep, removed;
     int ms, os, oslot;  // contact of this step: spheres and the other slot
     unsigned long long tree_tmp;  // block reduction scratch
@@ -123,36 +135,43 @@ __device__ inline void tree_cache_load(const BoxRun &R, TreeCache &c) {
     __syncthreads();
 }
 
-// Warp 0: descend from the top level to a leaf holding the target 't'.
-__device__ inline int tree_sample(const BoxRun &R, const TreeCache &c, double t) {
+// Warp 0: descend from the top level to a leaf holding the target 't'
+// (0 <= t < total).
+__device__ inline int tree_sample(const BoxRun &R, const TreeCache &c, unsigned long long t) {
     const int lane = threadIdx.x & 31;
     int node = 0;  // index within the current level
     for (int lev = R.tree_levels - 1; lev >= 0; --lev) {
         const int base = node * kTreeFan;
         const int len = R.tree_len[lev];
         const int co = c.coff[lev];
-        double v = (base + lane < len) ? (co >= 0 ? c.v[co + base + lane] : R.tree[R.tree_off[lev] + base + lane])
-                                       : 0.0;
+        const unsigned long long v =
+            (base + lane < len) ? (co >= 0 ? c.v[co + base + lane] : R.tree[R.tree_off[lev] + base + lane]) : 0ULL;
         // inclusive scan over the 32 children (fixed order)
-        double incl = v;
+        unsigned long long incl = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            double y = __shfl_up_sync(0xffffffffu, incl, o);
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += y;
         }
-        unsigned over = __ballot_sync(0xffffffffu, incl > t && v > 0.0);
-        unsigned nonzero = __ballot_sync(0xffffffffu, v > 0.0);
-        int pick = over ? __ffs(over) - 1 : (nonzero ? 31 - __clz(nonzero) : 0);
-        double before = __shfl_sync(0xffffffffu, incl - v, pick);
-        t -= before;
+        const unsigned over = __ballot_sync(0xffffffffu, incl > t && v > 0ULL);
+        const unsigned nonzero = __ballot_sync(0xffffffffu, v > 0ULL);
+        const int pick = over ? __ffs(over) - 1 : (nonzero ? 31 - __clz(nonzero) : 0);
+        t -= __shfl_sync(0xffffffffu, incl - v, pick);
         node = base + pick;
     }
     return node;
 }
 
+// The fixed-point weight of a slot with this time step (live slots only).
+__device__ __forceinline__ unsigned long long tree_weight(const RunState &st, double time_step) {
+    const double w = fmin((1.0 / time_step) * st.tree_scale, double(kTreeHeadroom));
+    const unsigned long long q = __double2ull_rn(w);
+    return q > 0ULL ? q : 1ULL;
+}
+
 // Warp 0: set leaf 'slot' to 'w' and refresh its ancestors (in global
 // memory and in the kept copy); returns the new total.
-__device__ inline double tree_set(const BoxRun &R, TreeCache &c, int slot, double w) {
+__device__ inline unsigned long long tree_set(const BoxRun &R, TreeCache &c, int slot, unsigned long long w) {
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
         R.tree[R.tree_off[0] + slot] = w;
@@ -160,13 +179,13 @@ __device__ inline double tree_set(const BoxRun &R, TreeCache &c, int slot, doubl
     }
     __syncwarp();
     int idx = slot;
-    double total = 0.0;
+    unsigned long long total = 0ULL;
     for (int lev = 0; lev < R.tree_levels; ++lev) {
         const int g = idx / kTreeFan;
         const int len = R.tree_len[lev];
         const int co = c.coff[lev];
         const int k = g * kTreeFan + lane;
-        double v = (k < len) ? (co >= 0 ? c.v[co + k] : R.tree[R.tree_off[lev] + k]) : 0.0;
+        unsigned long long v = (k < len) ? (co >= 0 ? c.v[co + k] : R.tree[R.tree_off[lev] + k]) : 0ULL;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lev + 1 < R.tree_levels) {
@@ -183,26 +202,41 @@ __device__ inline double tree_set(const BoxRun &R, TreeCache &c, int slot, doubl
     return total;
 }
 
+// The loop state's FP64 total weight and its inverse (the time increment of
+// a step) from the tree's integer total.
+__device__ __forceinline__ void tree_total_to_state(RunState &st, unsigned long long total) {
+    st.tree_total = total;
+    st.weight_total = double(total) * st.inv_tree_scale;
+    st.inv_weight = 1.0 / st.weight_total;
+}
+
 // ------------------------------------------------------------ physics
 // update_partial's physics (aggregat.cpp:264-276, physical_model.cpp:550-617)
 // with CUDA's erf / exp / pow.
 __device__ inline void device_physics(const PhysParams &p, double V, double vol_pp, double dp, double rg, double *f_agg,
                                double *d_m, double *time_step, double *lpm, double *dg_over_dp) {
+    // The same formulas with the common factors taken once: one pow (its
+    // square root form squared), reciprocals of the gas mean free path and
+    // of the fractal dimension from the host, and six divisions (FP64 is
+    // scarce on this GPU; the device loop follows the reference
+    // statistically, and these values agree with it to the last bits).
     const double r = 0.5 * dp;
     const double a = 1.142, b = 0.558, c = 0.999;
-    const double fe = 0.689 * (1. + erf(((p.lambda / r) + 4.454) / 10.628));
-    const double cc = 1.0 + a * p.lambda / r + b * p.lambda / r * exp(-c * r / p.lambda);
+    const double lr = p.lambda / r;
+    const double fe = 0.689 * (1. + erf((lr + 4.454) * (1.0 / 10.628)));
+    const double cc = 1.0 + lr * (a + b * exp(-c * r * p.inv_lambda));
     const double ratio = V / vol_pp;
-    const double f = (6. * pi_value() * p.viscosity * r / cc) * pow(ratio, fe / p.fractal_dimension);
-    const double ar = r * pow(ratio, fe / p.fractal_dimension / 2.0);
-    const double cc_a = 1.0 + a * p.lambda / ar + b * p.lambda / ar * exp(-c * ar / p.lambda);
+    const double pw2 = pow(ratio, 0.5 * fe * p.inv_fractal_dimension);
+    const double pw = pw2 * pw2;
+    const double f = (6. * pi_value() * p.viscosity * r / cc) * pw;
+    const double ar = r * pw2;
+    const double cc_a = 1.0 + (p.lambda / ar) * (a + b * exp(-c * ar * p.inv_lambda));
     *f_agg = f;
-    *d_m = (cc_a / cc) * 2.0 * r * pow(ratio, fe / p.fractal_dimension);
-    const double masse = p.density * V;
-    *time_step = 3. * (masse / f);
-    const double diffusivity = kBoltzmann * p.temperature / f;
-    *lpm = sqrt(6. * diffusivity * *time_step);
-    *dg_over_dp = 2 * rg / dp;
+    *d_m = (cc_a / cc) * 2.0 * r * pw;
+    const double inv_f = 1.0 / f;
+    *time_step = 3. * (p.density * V) * inv_f;
+    *lpm = sqrt(6. * kBoltzmann * p.temperature * inv_f * *time_step);
+    *dg_over_dp = rg / r;
 }
 
 __device__ __forceinline__ bool run_finished(const BoxRun &R, const RunState &st, int n_alive) {
@@ -320,18 +354,58 @@ __device__ inline double thread_update_aggregate(const BoxRun &R, int a, bool fu
     return rmax;
 }
 
-// The pick tree from the time steps: leaves 1/time_step of the live slots
-// (0 elsewhere), then each level from the one below, children summed in
-// order, and the total of the top level into the loop state.
+// The pick tree from the time steps: the scale from the largest weight and
+// the live count, leaves of the live slots (0 elsewhere), then each level
+// from the one below, and the total into the loop state. The FP64 weights
+// sit in the leaves (as bits) between the two passes.
 __device__ inline void block_tree_build(const BoxRun &R) {
     const DevBox &b = R.box;
     const int tid = threadIdx.x, NT = blockDim.x;
-    for (int a = tid; a < R.tree_len[0]; a += NT)
-        R.tree[R.tree_off[0] + a] = (a < b.nslots && b.agg_n[a] > 0) ? 1.0 / A(b, AGG_TIME_STEP, a) : 0.0;
+    __shared__ unsigned long long max_bits;
+    __shared__ int n_live;
+    if (tid == 0) {
+        max_bits = 0ULL;
+        n_live = 0;
+    }
+    __syncthreads();
+    unsigned long long mb = 0ULL;  // non-negative doubles order like their bits
+    int live = 0;
+    for (int a = tid; a < R.tree_len[0]; a += NT) {
+        double w = 0.0;
+        if (a < b.nslots && b.agg_n[a] > 0) {
+            w = 1.0 / A(b, AGG_TIME_STEP, a);
+            ++live;
+        }
+        const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(w));
+        R.tree[R.tree_off[0] + a] = bits;
+        mb = bits > mb ? bits : mb;
+    }
+    atomicMax(&max_bits, mb);
+    atomicAdd(&n_live, live);
+    __syncthreads();
+    if (tid == 0) {
+        // n_live * max weight * scale < 2^62
+        int e = 0;
+        frexp(double(n_live > 0 ? n_live : 1) * __longlong_as_double(static_cast<long long>(max_bits)), &e);
+        const int k = max(-1000, min(1000, 62 - e));
+        R.st->tree_scale = ldexp(1.0, k);
+        R.st->inv_tree_scale = ldexp(1.0, -k);
+    }
+    __syncthreads();
+    const double scale = R.st->tree_scale;
+    for (int a = tid; a < R.tree_len[0]; a += NT) {
+        const double w = __longlong_as_double(static_cast<long long>(R.tree[R.tree_off[0] + a]));
+        unsigned long long q = 0ULL;
+        if (w > 0.0) {
+            q = __double2ull_rn(fmin(w * scale, double(kTreeHeadroom)));
+            q = q > 0ULL ? q : 1ULL;
+        }
+        R.tree[R.tree_off[0] + a] = q;
+    }
     __syncthreads();
     for (int lev = 1; lev < R.tree_levels; ++lev) {
         for (int g = tid; g < R.tree_len[lev]; g += NT) {
-            double sum = 0.0;
+            unsigned long long sum = 0ULL;
             for (int k = 0; k < kTreeFan; ++k) {
                 const int c = g * kTreeFan + k;
                 if (c < R.tree_len[lev - 1]) sum += R.tree[R.tree_off[lev - 1] + c];
@@ -342,10 +416,9 @@ __device__ inline void block_tree_build(const BoxRun &R) {
     }
     if (tid == 0) {
         const int top = R.tree_levels - 1;
-        double total = 0.0;
+        unsigned long long total = 0ULL;
         for (int k = 0; k < R.tree_len[top]; ++k) total += R.tree[R.tree_off[top] + k];
-        R.st->weight_total = total;
-        R.st->inv_weight = 1.0 / total;
+        tree_total_to_state(*R.st, total);
     }
     __syncthreads();
 }
@@ -411,7 +484,12 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
             st.finished = 1;
             sm.stop = 1;
         }
-        if (!sm.stop) sm.t_pick = st.rng.uniform_mul() * st.weight_total;
+        if (!sm.stop) {
+            // the target: floor(total * rand() / 2^31), below the total
+            const unsigned long long total = st.tree_total;
+            const unsigned long long r = static_cast<unsigned long long>(st.rng.next_int());
+            sm.t_pick = (__umul64hi(r, total) << 33) | ((r * total) >> 31);
+        }
     }
     __syncthreads();
     if (sm.stop) return false;
@@ -533,12 +611,18 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
         __syncthreads();
         if (sm.stop) return false;
         if (sm.merged && tid < 32 && !R.phys.growth) {
-            tree_set(R, sm.tree, sm.removed, 0.0);
-            double total = tree_set(R, sm.tree, sm.keep, 1.0 / A(b, AGG_TIME_STEP, sm.keep));
+            tree_set(R, sm.tree, sm.removed, 0ULL);
+            const unsigned long long total =
+                tree_set(R, sm.tree, sm.keep, tree_weight(st, A(b, AGG_TIME_STEP, sm.keep)));
             if (tid == 0) {
-                st.weight_total = total;
-                st.inv_weight = 1.0 / total;
+                tree_total_to_state(st, total);
+                sm.rescale = total > kTreeHeadroom;  // a new scale keeps the total clear of 2^64
             }
+        }
+        __syncthreads();
+        if (sm.merged && !R.phys.growth && sm.rescale) {
+            block_tree_build(R);
+            tree_cache_load(R, sm.tree);
         }
     }
     if (R.phys.growth) {

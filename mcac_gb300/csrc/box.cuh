@@ -275,6 +275,7 @@ struct QuerySmemT {
     float warp_f[32];
     float warp_f2[32];
     int n_cand;
+    int n_screen;  // neighbours passing the FP32 screen, before the FP64 filter
     int n_surv;
     int found_source;
     int flat_base;
@@ -362,6 +363,7 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     }
     if (tid == 0) {
         sm.n_cand = 0;
+        sm.n_screen = 0;
         sm.n_surv = 0;
         sm.found_source = 0;
         sm.flat_base = 0;
@@ -414,19 +416,17 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     const CellRange rg = sm.range;
     const int nx = rg.hi[0] - rg.lo[0] + 1, ny = rg.hi[1] - rg.lo[1] + 1, nz = rg.hi[2] - rg.lo[2] + 1;
     const int n_scan = nx * ny * nz;
-    // bounding-sphere filter of one neighbour; 'key' is its position in the
-    // reference's neighbour list order (Verlet cell rank in the scan, then slot)
+    // bounding-sphere filter of one neighbour, first part: the FP32 screen;
+    // 'key' is its position in the reference's neighbour list order (Verlet
+    // cell rank in the scan, then slot). Those passing wait (in the
+    // candidates' prefix and key scratch, free until the pair search) for
+    // the FP64 test after the scan: one copy of that code, run densely.
+    long long *screen_key = reinterpret_cast<long long *>(sm.best_ij);
     auto consider = [&](int slot, long long key, float4 of) {
         if (!capsule_hit(w, of.x, of.y, of.z, src_f.w + of.w + margin)) return;
-        const double ox = A(b, AGG_X, slot), oy = A(b, AGG_Y, slot), oz = A(b, AGG_Z, slot);
-        const double orm = A(b, AGG_RMAX, slot);
-        double db = sweep_contact_distance(sp, rmax_src, Vec3{ox, oy, oz}, orm, dir, dist, b.L);
-        if (db < dist) {
-            int k = atomicAdd(&sm.n_cand, 1);  // < nslots: one entry per aggregate
-            sm.cand_db[k] = db;
-            sm.cand_key[k] = key;
-            sm.cand_slot[k] = slot;
-        }
+        const int k = atomicAdd(&sm.n_screen, 1);  // < nslots: one entry per aggregate
+        sm.cand_prefix[k] = slot;
+        screen_key[k] = key;
     };
     int n_cells_visited = n_scan;
     if (sm.use_fine) {
@@ -452,9 +452,9 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
                     heads[u] = b.fine_head[(size_t(fi) * nf + fj) * nf + fk];
                 }
             }
-#pragma unroll
+#pragma unroll 1
             for (int u = 0; u < kHeads; ++u) {
-                int slot = heads[u];
+                int slot = u == 0 ? heads[0] : (u == 1 ? heads[1] : (u == 2 ? heads[2] : heads[3]));
                 for (int guard = 0; slot >= 0 && guard < b.nslots; ++guard) {
                     // the three loads of a list entry are independent
                     const int nxt = b.fine_next[slot];
@@ -532,14 +532,34 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     }
     if (tid == 0) {
         sm.out.n_scanned = sm.flat_base;
-        sm.out.cyc_scan = clock64() - sm.t_q0;
         sm.out.n_cells = n_cells_visited;
-        sm.out.n_candidates = sm.n_cand;
     }
     if (!sm.found_source) {
         if (tid == 0) sm.out.status = ST_VERLET;  // "Aggregate not on the verlet list"
         __syncthreads();
         return;
+    }
+    // bounding-sphere filter, second part: the exact FP64 sweep
+    {
+        const int n_screen = sm.n_screen;
+        for (int k = tid; k < n_screen; k += NT) {
+            const int slot = sm.cand_prefix[k];
+            const long long key = screen_key[k];
+            const double ox = A(b, AGG_X, slot), oy = A(b, AGG_Y, slot), oz = A(b, AGG_Z, slot);
+            const double orm = A(b, AGG_RMAX, slot);
+            const double db = sweep_contact_distance(sp, rmax_src, Vec3{ox, oy, oz}, orm, dir, dist, b.L);
+            if (db < dist) {
+                const int j = atomicAdd(&sm.n_cand, 1);
+                sm.cand_db[j] = db;
+                sm.cand_key[j] = key;
+                sm.cand_slot[j] = slot;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            sm.out.n_candidates = sm.n_cand;
+            sm.out.cyc_scan = clock64() - sm.t_q0;
+        }
     }
     const int nc = sm.n_cand;
     if (nc == 0) {

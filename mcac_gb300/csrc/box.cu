@@ -111,8 +111,9 @@ __device__ void grid_clear_range(const DevBox &b, int t, int stride) {
 __device__ void grid_fill_range(const DevBox &b, int t, int stride) {
     for (int a = t; a < b.nslots; a += stride) {
         if (b.agg_n[a] == 0) continue;
-        const int c = cell_of(b, agg_pos(b, a));
-        b.agg_cell[a] = c;
+        const int key = cell_of(b, agg_pos(b, a));
+        const int c = cell_index(b, key);
+        b.agg_cell[a] = key;
         b.agg_f4[a] = make_float4(float(A(b, AGG_X, a)), float(A(b, AGG_Y, a)), float(A(b, AGG_Z, a)),
                                   float(A(b, AGG_RMAX, a)));
         const int k = atomicAdd(&b.cell_n[c], 1);

@@ -70,7 +70,7 @@ struct DevBox {
     double *agg;     // [21][nslots]
     int *agg_n;      // members (0: dead slot)
     int *agg_off;    // segment offset in the live pool
-    int *agg_cell;   // linear Verlet cell
+    int *agg_cell;   // Verlet cell (cell_key)
     float4 *agg_f4;  // FP32 (x, y, z, rmax) of each slot, for the neighbour screen
     int *pool_id[2];
     float4 *pool_pos[2];
@@ -163,12 +163,27 @@ __device__ __forceinline__ Vec3 agg_pos(const DevBox &b, int slot) {
 __device__ __forceinline__ Vec3 sph_pos(const DevBox &b, int s) {
     return Vec3{S(b, SPH_X, s), S(b, SPH_Y, s), S(b, SPH_Z, s)};
 }
+// A Verlet cell is kept as its coordinates packed in one int (10 bits each,
+// n_div <= 1024), so the neighbourhood test needs no division; the cell
+// lists are indexed by the linear cell.
+__device__ __forceinline__ int cell_key(int ix, int iy, int iz) { return ix | (iy << 10) | (iz << 20); }
+__device__ __forceinline__ int cell_index(const DevBox &b, int key) {
+    return ((key & 1023) * b.n_div + ((key >> 10) & 1023)) * b.n_div + (key >> 20);
+}
 __device__ __forceinline__ int cell_of(const DevBox &b, Vec3 p) {
     int ix = verlet_coord(p.x, b.step), iy = verlet_coord(p.y, b.step), iz = verlet_coord(p.z, b.step);
     ix = min(max(ix, 0), b.n_div - 1);
     iy = min(max(iy, 0), b.n_div - 1);
     iz = min(max(iz, 0), b.n_div - 1);
-    return (ix * b.n_div + iy) * b.n_div + iz;
+    return cell_key(ix, iy, iz);
+}
+// i mod n for i in [-2n, 3n)
+__device__ __forceinline__ int wrap_cell(int i, int n) {
+    i += i < 0 ? n : 0;
+    i += i < 0 ? n : 0;
+    i -= i >= n ? n : 0;
+    i -= i >= n ? n : 0;
+    return i;
 }
 
 // Order-preserving map of a double to an unsigned 64-bit key.
@@ -435,6 +450,13 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
         const int fny = sm.fine_n[1], fnz = sm.fine_n[2];
         const int n_f = sm.fine_n[0] * fny * fnz;
         const int nf = b.fine_div, nd = b.n_div;
+        // g -> (a, bb, c) by FP32 reciprocals: g < 2^21 and divisors <= 128^2
+        // keep (g + 1/2) / d at least 1/(2 d) from an integer, far above the
+        // FP32 error, so the floors are exact
+        const int fyz = fny * fnz;
+        const float inv_yz = 1.f / float(fyz), inv_z = 1.f / float(fnz);
+        const int flo0 = sm.fine_lo[0], flo1 = sm.fine_lo[1], flo2 = sm.fine_lo[2];
+        const int rlo0 = rg.lo[0], rlo1 = rg.lo[1], rlo2 = rg.lo[2];
         n_cells_visited = n_f;
         int visited = 0;
         constexpr int kHeads = 4;  // list heads fetched together per thread
@@ -445,10 +467,11 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
                 const int g = g0 + u * NT + tid;
                 heads[u] = -1;
                 if (g < n_f) {
-                    const int a = g / (fny * fnz), r = g % (fny * fnz), bb = r / fnz, c = r % fnz;
-                    const int fi = periodic_cell(sm.fine_lo[0] + a, nf);
-                    const int fj = periodic_cell(sm.fine_lo[1] + bb, nf);
-                    const int fk = periodic_cell(sm.fine_lo[2] + c, nf);
+                    const int a = int((float(g) + 0.5f) * inv_yz), r = g - a * fyz;
+                    const int bb = int((float(r) + 0.5f) * inv_z), c = r - bb * fnz;
+                    const int fi = wrap_cell(flo0 + a, nf);
+                    const int fj = wrap_cell(flo1 + bb, nf);
+                    const int fk = wrap_cell(flo2 + c, nf);
                     heads[u] = b.fine_head[(size_t(fi) * nf + fj) * nf + fk];
                 }
             }
@@ -458,15 +481,15 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
                 for (int guard = 0; slot >= 0 && guard < b.nslots; ++guard) {
                     // the three loads of a list entry are independent
                     const int nxt = b.fine_next[slot];
-                    const int lin = b.agg_cell[slot];
+                    const int key = b.agg_cell[slot];
                     const float4 of = b.agg_f4[slot];
                     ++visited;
                     if (slot == src) {
                         sm.found_source = 1;
                     } else {
-                        const int oa = periodic_cell(lin / (nd * nd) - rg.lo[0], nd);
-                        const int ob = periodic_cell((lin / nd) % nd - rg.lo[1], nd);
-                        const int oc = periodic_cell(lin % nd - rg.lo[2], nd);
+                        const int oa = wrap_cell((key & 1023) - rlo0, nd);
+                        const int ob = wrap_cell(((key >> 10) & 1023) - rlo1, nd);
+                        const int oc = wrap_cell((key >> 20) - rlo2, nd);
                         if (oa < nx && ob < ny && oc < nz)
                             consider(slot, (long long)((oa * ny + ob) * nz + oc) * b.nslots + slot, of);
                     }
@@ -959,17 +982,19 @@ __device__ __forceinline__ void fine_link(const DevBox &b, int slot, int c) {
 // the same move in the fine grid (one thread). The loads that do not depend
 // on one another are issued first: a move costs three rounds of memory
 // latency instead of one per list operation.
-__device__ __forceinline__ void regrid_to(const DevBox &b, int slot, int c, int fc) {
+__device__ __forceinline__ void regrid_to(const DevBox &b, int slot, int key, int fc) {
     const bool fine = b.fine_div > 0;
+    const int c = cell_index(b, key);
     // round 1: everything indexed by the slot or by the new cells
-    const int old = b.agg_cell[slot];
+    const int old_key = b.agg_cell[slot];
+    const int old = cell_index(b, old_key);
     const int k = b.cell_pos[slot];
     const int n_new = b.cell_n[c];
     const int fold = fine ? b.fine_cell[slot] : -1;
     const int fprev = fine ? b.fine_prev[slot] : -1;
     const int fnext = fine ? b.fine_next[slot] : -1;
     const int fhead = fine ? b.fine_head[fc] : -1;
-    if (c != old) {
+    if (key != old_key) {
         // round 2 and 3: the old cell's length, then its last item
         const int n_old = b.cell_n[old];
         int *items = b.cell_items + size_t(old) * b.cell_cap;
@@ -993,7 +1018,7 @@ __device__ __forceinline__ void regrid_to(const DevBox &b, int slot, int c, int 
             b.cell_pos[slot] = n_new;
             b.cell_n[c] = n_new + 1;
         }
-        b.agg_cell[slot] = c;
+        b.agg_cell[slot] = key;
     }
     if (fine && fc != fold) {
         // unlink from the old fine cell, link at the head of the new one (the
@@ -1040,7 +1065,7 @@ __device__ inline void block_translate(const DevBox &b, int slot, Vec3 v, double
             const float rm = b.agg_f4[slot].w;  // r_max is unchanged by a move
             b.agg_f4[slot] = make_float4(xf, yf, zf, rm);
             const int n = b.fine_div;
-            regrid_to(b, slot, (vc * b.n_div + vy) * b.n_div + vz, n > 0 ? (fc * n + fy) * n + fz : -1);
+            regrid_to(b, slot, cell_key(vc, vy, vz), n > 0 ? (fc * n + fy) * n + fz : -1);
         }
     }
     __syncthreads();

@@ -424,7 +424,7 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
         A(b, AGG_COORDINATION_NUMBER, keep) = coordination;
         b.agg_f4[keep] = make_float4(float(x), float(y), float(z), float(rmax));
         regrid(b, keep, Vec3{x, y, z});
-        cell_remove(b, b.agg_cell[removed], removed);
+        cell_remove(b, cell_index(b, b.agg_cell[removed]), removed);
         if (b.fine_div > 0) fine_unlink(b, removed);
         if (rmax > sc->maxradius) sc->maxradius = rmax;
         out->merged = 1;

@@ -6,4 +6,5 @@ with ctypes and mirrors the reference's C++ interface (see ``api``).
 """
 from .api import (CONTACT_DTYPE, AggregateContactInfo, AggregatList, Batch, PhysicalModel, Server,  # noqa: F401
                   calcul, device_count, init_state, resident_boxes, run_device, synthetic_state)
+from ._lib import StateBuffers  # noqa: F401
 from .snapshot import Snapshot  # noqa: F401

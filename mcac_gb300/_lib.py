@@ -229,16 +229,21 @@ class StateBuffers:
     pinned=True they sit in one page-locked block, so loading and storing
     the state moves them by DMA."""
 
-    def __init__(self, n_spheres: int, n_aggregates: int, pinned: bool = False):
+    @staticmethod
+    def _layout(ns: int, na: int):
+        return [("spheres", np.float64, (9, ns)), ("sphere_label", np.int64, (ns,)),
+                ("aggregates", np.float64, (21, na)), ("n_spheres", np.int64, (na,)), ("members", np.int64, (ns,))]
+
+    @staticmethod
+    def _bytes(ns: int, na: int) -> int:
+        return 8 * (11 * ns + 22 * na)
+
+    def __init__(self, n_spheres: int, n_aggregates: int, pinned: bool = False, _buf=None, _offset: int = 0):
         ns, na = int(n_spheres), int(n_aggregates)
-        if pinned:
-            layout = [("spheres", np.float64, (9, ns)), ("sphere_label", np.int64, (ns,)),
-                      ("aggregates", np.float64, (21, na)), ("n_spheres", np.int64, (na,)),
-                      ("members", np.int64, (ns,))]
-            total = sum(8 * int(np.prod(shape)) for _, _, shape in layout)
-            buf = _PinnedBlock(max(total, 8)).buffer()
-            off = 0
-            for name, dt, shape in layout:
+        if pinned or _buf is not None:
+            buf = _buf if _buf is not None else _PinnedBlock(max(self._bytes(ns, na), 8)).buffer()
+            off = _offset
+            for name, dt, shape in self._layout(ns, na):
                 count = int(np.prod(shape))
                 setattr(self, name, np.frombuffer(buf, dtype=dt, count=count, offset=off).reshape(shape))
                 off += 8 * count
@@ -251,6 +256,22 @@ class StateBuffers:
         self.state = State(ns, na, 0, 0.0, 0.0, 0.0,
                            ptr(self.spheres, f64), ptr(self.sphere_label, i64), ptr(self.aggregates, f64),
                            ptr(self.n_spheres, i64), ptr(self.members, i64))
+
+    @classmethod
+    def many(cls, sizes, pinned: bool = True) -> list:
+        """StateBuffers for many boxes ((n_spheres, n_aggregates) each); with
+        pinned=True all of them in one page-locked block, allocated at once
+        (large page-locked blocks made before the host memory fragments copy
+        fastest)."""
+        sizes = [(int(a), int(b)) for a, b in sizes]
+        if not pinned:
+            return [cls(ns, na) for ns, na in sizes]
+        buf = _PinnedBlock(max(8, sum(cls._bytes(ns, na) for ns, na in sizes))).buffer()
+        out, off = [], 0
+        for ns, na in sizes:
+            out.append(cls(ns, na, _buf=buf, _offset=off))
+            off += cls._bytes(ns, na)
+        return out
 
     @classmethod
     def from_snapshot(cls, snap, pinned: bool = False) -> "StateBuffers":

@@ -412,7 +412,7 @@ class Batch:
             for b in bufs:
                 b.state.n_spheres, b.state.n_aggregates = b.spheres.shape[1], b.aggregates.shape[1]
         else:
-            bufs = [StateBuffers(*self.box_sizes(box), pinned=pinned) for box in range(len(self.models))]
+            bufs = StateBuffers.many([self.box_sizes(box) for box in range(len(self.models))], pinned=pinned)
         arr = (_lib.State * len(bufs))(*[b.state for b in bufs])
         check(lib().mcacg_batch_store_states(self._b, arr, len(bufs)))
         for k, b in enumerate(bufs):

@@ -96,6 +96,11 @@ typedef struct mcacg_params {
     double mean_massic_radius;
     double friction_exponnant;
     double u_sg;
+    /* [output] (physical_model.cpp:185-187): when calcul appends a line to
+     * advancement.dat (PhysicalModel::time_to_write, physical_model.cpp:338-356) */
+    int64_t write_events_frequency;        /* default 1 */
+    int64_t write_between_event_frequency; /* default 100 */
+    double write_delta_t;                  /* seconds; <= 0: none (default -1) */
 } mcacg_params;
 
 /* Result of a contact search: AggregateContactInfo
@@ -135,6 +140,10 @@ typedef struct mcacg_run_opts {
     int64_t max_steps;          /* stop after this many MC steps; <= 0: only the stop criteria */
     mcacg_step_record *trace;   /* optional per-step records (host memory) */
     int64_t trace_capacity;
+    /* optional: the file the reference's calcul appends its time-resolved
+     * lines to (advancement.dat, calcul.cpp:29-43), written at the same steps
+     * with the same values and formatting */
+    const char *advancement_path;
 } mcacg_run_opts;
 
 typedef struct mcacg_run_stats {

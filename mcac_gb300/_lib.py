@@ -34,6 +34,7 @@ class Params(C.Structure):
         ("with_electric_charges", i32),
         ("box_length", f64), ("box_volume", f64), ("viscosity", f64), ("gaz_mean_free_path", f64),
         ("mean_massic_radius", f64), ("friction_exponnant", f64), ("u_sg", f64),
+        ("write_events_frequency", i64), ("write_between_event_frequency", i64), ("write_delta_t", f64),
     ]
 
 
@@ -57,7 +58,8 @@ class StepRecord(C.Structure):
 
 
 class RunOpts(C.Structure):
-    _fields_ = [("max_steps", i64), ("trace", C.POINTER(StepRecord)), ("trace_capacity", i64)]
+    _fields_ = [("max_steps", i64), ("trace", C.POINTER(StepRecord)), ("trace_capacity", i64),
+                ("advancement_path", C.c_char_p)]
 
 
 class RunStats(C.Structure):

@@ -9,6 +9,7 @@ physics itself.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import math
 from dataclasses import dataclass
 from pathlib import Path
@@ -266,10 +267,13 @@ class AggregatList:
         return {name: getattr(p, name) for name, _ in _lib.Profile._fields_}
 
     # -- whole runs and state
-    def calcul(self, max_steps: int = 0, trace: bool = False, trace_capacity: int = 0):
-        """The reference MC loop; returns (stats, records or None)."""
+    def calcul(self, max_steps: int = 0, trace: bool = False, trace_capacity: int = 0,
+               advancement: str | os.PathLike | None = None):
+        """The reference MC loop; returns (stats, records or None). With
+        'advancement', the reference's time-resolved lines are appended to
+        that file (advancement.dat of the reference's output directory)."""
         recs = None
-        opts = RunOpts(int(max_steps), None, 0)
+        opts = RunOpts(int(max_steps), None, 0, os.fsencode(advancement) if advancement is not None else None)
         if trace:
             cap = int(trace_capacity or max_steps or 1_000_000)
             recs = (StepRecord * cap)()
@@ -500,9 +504,9 @@ def run_device(aggregates: AggregatList, max_steps: int = 0) -> RunStats:
     return s
 
 
-def calcul(model: PhysicalModel, aggregates: AggregatList, max_steps: int = 0):
+def calcul(model: PhysicalModel, aggregates: AggregatList, max_steps: int = 0, advancement=None):
     """mcac::calcul (src/calcul.cpp:55-290) for the collision-only configuration."""
-    return aggregates.calcul(max_steps=max_steps)
+    return aggregates.calcul(max_steps=max_steps, advancement=advancement)
 
 
 __all__ = ["PhysicalModel", "AggregatList", "AggregateContactInfo", "init_state", "calcul", "device_count",

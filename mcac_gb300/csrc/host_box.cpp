@@ -2,6 +2,7 @@
 #include "host_box.hpp"
 
 #include <algorithm>
+#include <fstream>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -316,7 +317,50 @@ int HostBox::upload(const HostState &st, void *stream, std::string *err) {
     if (rc != ST_OK) return rc;
     dev_.reset(d);
     refresh();
+    init_model_values();
     return ST_OK;
+}
+
+// PhysicalModel's concentrations before the first update
+// (physical_model.cpp:266-267) and its input volume fraction.
+void HostBox::init_model_values() {
+    aggregate_concentration_ = static_cast<double>(p_.n_monomeres) / p_.box_volume;
+    monomer_concentration_ = aggregate_concentration_;
+    volume_fraction_ = p_.volume_fraction;
+}
+
+// PhysicalModel::time_to_write (physical_model.cpp:338-356).
+bool HostBox::time_to_write() {
+    if (p_.write_delta_t > 0) {
+        const uint64_t timestep = static_cast<uint64_t>(std::floor(time_ / p_.write_delta_t));
+        if (timestep > last_timestep_written_) {
+            last_timestep_written_ = timestep;
+            return true;
+        }
+    }
+    const uint64_t every_event = static_cast<uint64_t>(p_.write_events_frequency);
+    const uint64_t every_step = static_cast<uint64_t>(p_.write_between_event_frequency);
+    if (n_iter_without_event_ == 0 && static_cast<uint64_t>(total_events_) % every_event == 0) return true;
+    if (n_iter_without_event_ > 0 && static_cast<uint64_t>(n_iter_without_event_) % every_step == 0) return true;
+    return false;
+}
+
+// save_advancement (calcul.cpp:29-43): one line appended, default stream
+// formatting (6 significant digits), the values of the physical model.
+void HostBox::save_advancement(const char *path) const {
+    std::ofstream outfile;
+    outfile.open(path, std::ios_base::app);
+    outfile << time_;
+    outfile << " " << aggregate_concentration_;
+    outfile << " " << volume_fraction_;
+    outfile << " " << avg_npp_;
+    outfile << " " << p_.temperature;
+    outfile << " " << p_.box_volume;
+    outfile << " " << monomer_concentration_;
+    outfile << " " << p_.u_sg;
+    outfile << " " << 0.0;  // flux_nucleation: nucleation is outside this library's path
+    outfile << std::endl;
+    outfile.close();
 }
 
 int HostBox::create_random(const mcacg_params &p, void *stream, std::unique_ptr<HostBox> *out, std::string *err) {
@@ -681,9 +725,14 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
                         "(no surface reactions, no domain duplication/reduction, pick_method=random)";
         return ST_INPUT;
     }
+    if (opts.advancement_path && (p_.write_events_frequency <= 0 || p_.write_between_event_frequency <= 0)) {
+        if (err) *err = "write_events_frequency and write_between_event_frequency must be positive";
+        return ST_INPUT;
+    }
     int64_t steps = 0, events = 0;
     while (!finished()) {
         if (opts.max_steps > 0 && steps >= opts.max_steps) break;
+        if (time_to_write() && opts.advancement_path) save_advancement(opts.advancement_path);
         double max = max_time_step_;
         if (event_) sort_time_steps(max);
         const int64_t label = pick_random();
@@ -717,7 +766,12 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
         if (event_) {
             n_iter_without_event_ = 0;
             ++events;
+            ++total_events_;
             refresh();
+            // PhysicalModel::update after an event (calcul.cpp:274-279)
+            aggregate_concentration_ = static_cast<double>(alive_.size()) / p_.box_volume;
+            monomer_concentration_ = static_cast<double>(ns_) / p_.box_volume;
+            volume_fraction_ = total_volume() / p_.box_volume;
         } else {
             n_iter_without_event_++;
         }
@@ -743,6 +797,11 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
             r.reserved = 0;
         }
         ++steps;
+    }
+    // the final line, once, when the run has met its stop criteria (calcul.cpp:282)
+    if (opts.advancement_path && finished() && !advancement_closed_) {
+        save_advancement(opts.advancement_path);
+        advancement_closed_ = true;
     }
     if (stats) {
         stats->steps = steps;

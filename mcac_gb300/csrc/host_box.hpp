@@ -106,6 +106,16 @@ class HostBox {
     void dt_order_erase(int slot, double dt);
     void dt_order_insert(int slot, double dt);
     std::unique_ptr<DeviceBox> dev_;
+    // The PhysicalModel values that the reference's advancement.dat lines
+    // print (physical_model.cpp:266-267, 489-498) and its write bookkeeping
+    // (physical_model.cpp:338-356, calcul.cpp:60-68).
+    int64_t total_events_ = 0;
+    uint64_t last_timestep_written_ = 0;
+    double aggregate_concentration_ = 0, monomer_concentration_ = 0, volume_fraction_ = 0;
+    bool advancement_closed_ = false;  // the final line is written
+    void init_model_values();
+    bool time_to_write();
+    void save_advancement(const char *path) const;
 };
 
 // Random placement of the reference's AggregatList constructor into 'st'

@@ -101,6 +101,9 @@ void params_defaults(mcacg_params *p) {
     p->n_verlet_divisions = 10;
     p->gaz_mean_free_path = kFluidMeanFreePathRef;
     p->viscosity = kViscosityRef;
+    p->write_events_frequency = 1;
+    p->write_between_event_frequency = 100;
+    p->write_delta_t = -1;
 }
 
 int params_from_ini(const IniData &ini, mcacg_params *p, std::string *error) {
@@ -170,6 +173,9 @@ int params_from_ini(const IniData &ini, mcacg_params *p, std::string *error) {
     extract_bool(value_of(ini, "inter_potential", "with_potentials"), p->with_potentials);
     extract_bool(value_of(ini, "inter_potential", "with_electric_charges"), p->with_electric_charges);
     extract_bool(value_of(ini, "flame_coupling", "with_flame_coupling"), p->with_flame_coupling);
+    extract(value_of(ini, "output", "write_between_event_frequency"), p->write_between_event_frequency);
+    extract(value_of(ini, "output", "write_events_frequency"), p->write_events_frequency);
+    extract(value_of(ini, "output", "write_Delta_t"), p->write_delta_t);
     params_derive(p);
     return ST_OK;
 }

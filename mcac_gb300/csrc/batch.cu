@@ -300,7 +300,16 @@ int BatchRunner::init_stream(void *stream, std::string *err) {
 int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector<double> &times, std::string *err) {
     const int n = int(boxes_.size());
     growth_.assign(static_cast<size_t>(n), 0);
-    for (int i = 0; i < n; ++i) growth_[size_t(i)] = params[size_t(i)].with_surface_reactions ? 1 : 0;
+    volsurf_.assign(static_cast<size_t>(n), VS_NONE);
+    for (int i = 0; i < n; ++i) {
+        growth_[size_t(i)] = params[size_t(i)].with_surface_reactions ? 1 : 0;
+        volsurf_[size_t(i)] = params[size_t(i)].volsurf_method;
+        const int rc = boxes_[size_t(i)]->set_volsurf(params[size_t(i)].volsurf_method);
+        if (rc != ST_OK) {
+            if (err) *err = "box " + std::to_string(i) + ": volsurf_method not available";
+            return rc;
+        }
+    }
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
     for (DeviceBox *d : boxes_)
         if (d->sync(err) != ST_OK) return ST_CUDA;
@@ -575,7 +584,7 @@ int BatchRunner::download(int box, HostState *st, std::string *err) {
     if (box < 0 || box >= size()) return ST_BAD_ARGUMENT;
     int rc = boxes_[size_t(box)]->download(st, err);
     if (rc != ST_OK) return rc;
-    if (grows(box)) host_refresh_overlap(st);
+    if (refresh_overlap(box)) host_refresh_overlap(st);
     RunState r;
     if (!ok_cuda(cudaMemcpy(&r, static_cast<RunState *>(states_dev_) + box, sizeof(r), cudaMemcpyDeviceToHost), err,
                  "download"))
@@ -721,6 +730,13 @@ int Server::admit(std::string *err) {
         int rc = DeviceBox::create(states[i], stream_, &d, err);
         if (rc != ST_OK) return rc;
         sl.box.reset(d);
+        rc = d->set_volsurf(take[i].p.volsurf_method);
+        if (rc != ST_OK) {
+            const double t_fail = now();
+            done_.push_back(Completion{take[i].id, 0, 0, 0, 0.0, rc, 0, take[i].submit_s, t_fail, t_fail});
+            sl.box.reset();
+            continue;
+        }
         BoxRun run;
         RunState st;
         const DevBox &db = *static_cast<DevBox *>(d->devbox_ptr());
@@ -738,6 +754,7 @@ int Server::admit(std::string *err) {
             return ST_CUDA;
         sl.id = take[i].id;
         sl.growth = take[i].p.with_surface_reactions != 0;
+        sl.volsurf = take[i].p.volsurf_method;
         sl.bytes = footprint(take[i].p);
         sl.submit_s = take[i].submit_s;
         sl.admit_s = t_admit;
@@ -763,7 +780,7 @@ int Server::retire(std::string *err) {
         HostState final_state;
         if (keep_) {
             int rc = sl.box->download(&final_state, err);
-            if (rc == ST_OK && sl.growth) host_refresh_overlap(&final_state);
+            if (rc == ST_OK && sl.growth && sl.volsurf == VS_NONE) host_refresh_overlap(&final_state);
             if (rc != ST_OK) return rc;
             final_state.time = r.time;
         }

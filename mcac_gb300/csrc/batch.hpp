@@ -58,6 +58,11 @@ class BatchRunner {
     int times(std::vector<double> *out, std::string *err);
     // Box i grows by surface reactions (its overlap fields are refreshed on read-back).
     bool grows(int i) const { return growth_.size() > size_t(i) && growth_[size_t(i)]; }
+    // Box i's overlap and coordination fields are stale on the device (growth
+    // with volsurf "none") and are recomputed on read-back.
+    bool refresh_overlap(int i) const {
+        return grows(i) && volsurf_.size() > size_t(i) && volsurf_[size_t(i)] == MCACG_VOLSURF_NONE;
+    }
     DeviceBox &box(int i) { return *boxes_[size_t(i)]; }
     void *stream() const { return stream_; }
     // Kernel time of the last run() (CUDA events on the stream).
@@ -81,6 +86,7 @@ class BatchRunner {
     int threads_ = 0;
     bool auto_threads_ = true;
     std::vector<char> growth_;  // per box: surface reactions on
+    std::vector<int> volsurf_;  // per box: VolSurfMethods
     int tuned_active_ = 0;  // unfinished boxes at the last tuning
     int tune(int64_t budget, int64_t *done, float *ms_total, std::string *err);
 };
@@ -133,6 +139,7 @@ class Server {
         int64_t bytes = 0;
         double submit_s = 0, admit_s = 0;
         bool growth = false;
+        int volsurf = MCACG_VOLSURF_NONE;
     };
     int admit(std::string *err);
     int retire(std::string *err);

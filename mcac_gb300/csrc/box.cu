@@ -233,6 +233,7 @@ __device__ void load_spheres_range(const DevBox &b, const LoadStage &in, int t, 
             l = 0;
         }
         b.sph_slot[s] = int(l);
+        b.sph_volw[s] = S(b, SPH_VOLUME, s);
         long long m = load_int(in.members, in.wide, s);
         if (m < 0 || m >= b.ns) {
             load_fail(b, LOAD_MEMBER);
@@ -443,6 +444,7 @@ bool view_ok(const StateView &st) {
 // r_max, and the Verlet cell counts. No pointer is set.
 DevBox plan_box(const StateView &st) {
     DevBox b{};
+    b.volsurf = VS_NONE;
     b.L = st.box_length;
     b.n_div = st.n_div;
     b.step = double(st.n_div) / st.box_length;
@@ -510,6 +512,7 @@ size_t carve_box(DevBox &b, char *arena) {
     const size_t ns = size_t(b.ns), nslots = size_t(b.nslots);
     take((void **)&b.sph, sizeof(double) * 9 * ns);
     take((void **)&b.sph_slot, sizeof(int) * ns);
+    take((void **)&b.sph_volw, sizeof(double) * ns);
     take((void **)&b.agg, sizeof(double) * 21 * nslots);
     take((void **)&b.agg_n, sizeof(int) * nslots);
     take((void **)&b.agg_off, sizeof(int) * nslots);
@@ -787,6 +790,17 @@ DeviceBox::~DeviceBox() {
     if (host_out_) cudaFreeHost(host_out_);
     if (own_stream_ && stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
     delete static_cast<DevBox *>(devbox_);
+}
+
+int DeviceBox::set_volsurf(int method) {
+    // the exact SBL and ARVO back-ends are optional libraries of the
+    // reference, which stops with their error codes when they are absent
+    // (aggregat.cpp:329-346)
+    if (method == VS_SBL) return ST_SBL;
+    if (method == VS_ARVO) return ST_ARVO;
+    if (method != VS_NONE && method != VS_CAPS && method != VS_ALPHAS) return ST_INPUT;
+    static_cast<DevBox *>(devbox_)->volsurf = method;
+    return ST_OK;
 }
 
 int DeviceBox::set_stream(void *stream) {

@@ -67,6 +67,12 @@ struct DevBox {
     int pair_cap;    // intra-aggregate contact pairs in global scratch
     double *sph;     // [9][ns]
     int *sph_slot;   // owning slot
+    // each sphere's entry of its aggregate's per-sphere volumes at the last
+    // compute_volume_surface (Aggregate::volumes, aggregat.cpp:321-430): the
+    // sphere's volume, less its spherical caps for "caps"; update_partial
+    // weighs the centre of mass and Rg with it (aggregat.cpp:431-483)
+    double *sph_volw;
+    int volsurf;     // VolSurfMethods of the box (VS_NONE, VS_CAPS, VS_ALPHAS)
     double *agg;     // [21][nslots]
     int *agg_n;      // members (0: dead slot)
     int *agg_off;    // segment offset in the live pool

@@ -599,7 +599,7 @@ int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state)
         if (!batch || !state || box < 0 || box >= batch->impl->size())
             return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
         std::string err;
-        if (!batch->impl->grows(box)) {
+        if (!batch->impl->refresh_overlap(box)) {
             std::vector<double> times;
             int rc = batch->impl->times(&times, &err);
             if (rc == 0) rc = batch->impl->box(box).store(state, &err);
@@ -620,10 +620,11 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
         std::string err;
         int rc = batch->impl->times(&times, &err);
         if (rc != 0) return finish(rc, err);
-        // boxes without growth: packed on the device and copied straight
-        // into the caller's arrays, all boxes at once
+        // boxes whose device fields are current (all but growth with volsurf
+        // "none"): packed on the device and copied straight into the
+        // caller's arrays, all boxes at once
         std::vector<int> direct, grown;
-        for (int i = 0; i < n_boxes; ++i) (batch->impl->grows(i) ? grown : direct).push_back(i);
+        for (int i = 0; i < n_boxes; ++i) (batch->impl->refresh_overlap(i) ? grown : direct).push_back(i);
         std::vector<mcacg::DeviceBox *> boxes;
         std::vector<mcacg_state *> outs;
         for (int i : direct) {
@@ -638,8 +639,8 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
             if (rcs[k] != 0) return fail(rcs[k], "box " + std::to_string(direct[k]) + ": " + errs[k]);
             states[direct[k]].time = times[size_t(direct[k])];
         }
-        // growing boxes: overlap and coordination refreshed on the host, one
-        // copy stream per worker thread
+        // growing boxes with volsurf "none": overlap and coordination
+        // refreshed on the host, one copy stream per worker thread
         struct CopyStream {
             cudaStream_t s = nullptr;
             ~CopyStream() {

@@ -157,6 +157,86 @@ MCACG_HD int verlet_coord(double x, double step) { return static_cast<int>(floor
 struct CellRange {
     int lo[3], hi[3];
 };
+// Intersection (spheres/sphere_intersection.cpp:29-66): the volume and
+// surface of the cap that sphere 1 loses to sphere 2 at centre distance
+// 'dist' (v1, s1) and the other way round (v2, s2); a sphere inside the
+// other loses all of itself (its stored volume and surface).
+struct SphereCaps {
+    double v1, v2, s1, s2;
+};
+MCACG_HD SphereCaps sphere_caps(double r1, double vol1, double sur1, double r2, double vol2, double sur2,
+                                double dist) {
+    SphereCaps c{0., 0., 0., 0.};
+    if (dist <= 0) return c;
+    if (dist < r1 + r2) {
+        const double fd = r1 > r2 ? r1 - r2 : 0.0;  // std::fdim
+        if (dist >= fd) {
+            const double pi = pi_value();
+            const double a = r1 - dist, bb = r2 - dist;
+            const double h1 = (r2 * r2 - a * a) / (2. * dist);
+            const double h2 = (r1 * r1 - bb * bb) / (2. * dist);
+            c.v1 = pi * (h1 * h1) * (3 * r1 - h1) / 3.;
+            c.v2 = pi * (h2 * h2) * (3 * r2 - h2) / 3.;
+            c.s1 = 2 * pi * r1 * h1;
+            c.s2 = 2 * pi * r2 * h2;
+        } else if (r1 < r2) {
+            c.v1 = vol1;
+            c.s1 = sur1;
+        } else {
+            c.v2 = vol2;
+            c.s2 = sur2;
+        }
+    }
+    return c;
+}
+// volume_alpha_correction / surface_alpha_correction (aggregat.cpp:289-319)
+MCACG_HD double volume_alpha(double cn, double c20, double c30, double min_cn, double extreme) {
+    const double d = fabs(cn - min_cn);
+    double corr = 0.25 * (3.0 * c20 - c30) * cn - c30 * d * 0.62741833 - pow(d, 1.5) * 0.00332425;
+    if (corr < 0.0) corr = 1.0;
+    corr = dmin(corr, 1.0);
+    return dmax(1.0 - corr, extreme);
+}
+MCACG_HD double surface_alpha(double cn, double c10, double min_cn, double extreme) {
+    const double d = fabs(cn - min_cn);
+    double corr = 0.5 * c10 * cn - (c10 * c10) * d * 0.70132500 - (d * d) * 0.00450000;
+    if (corr < 0.0) corr = 1.0;
+    corr = dmin(corr, 1.0);
+    return dmax(1.0 - corr, extreme);
+}
+// The sums of the "alphas" method over one contact of sphere i (radius r1)
+// with sphere j (radius r2) at distance d (aggregat.cpp:394-413).
+struct AlphaSums {
+    double overlapping, c_s10, c_v20, c_v30, vp_sum, sp_sum;
+};
+MCACG_HD void alpha_add(AlphaSums &a, double r1, double r2, double d) {
+    const double c = (r1 + r2 - d) / (r1 + r2);
+    const double vp1 = pow(r1, 3), vp2 = pow(r2, 3);
+    const double sp1 = r1 * r1, sp2 = r2 * r2;
+    a.vp_sum += (vp1 + vp2);
+    a.sp_sum += (sp1 + sp2);
+    a.overlapping += c;
+    a.c_s10 += c * (sp1 + sp2);
+    a.c_v20 += (c * c) * (vp1 + vp2);
+    a.c_v30 += pow(c, 3) * (vp1 + vp2);
+}
+// The end of the "alphas" method: averages, coordination, and the corrected
+// volume and surface (aggregat.cpp:414-425); n spheres, 'entries' map
+// entries (each contact counted from both spheres).
+MCACG_HD void alpha_finish(const AlphaSums &a0, int n, int entries, double *volume, double *surface,
+                           double *overlapping, double *coordination) {
+    *overlapping = a0.overlapping;
+    if (entries > 0) {
+        const double c_s10 = a0.c_s10 / a0.sp_sum, c_v20 = a0.c_v20 / a0.vp_sum, c_v30 = a0.c_v30 / a0.vp_sum;
+        const double min_cn = 2 * (1.0 - 1.0 / static_cast<double>(n));
+        *overlapping = a0.overlapping / static_cast<double>(entries);
+        *coordination = static_cast<double>(entries) / static_cast<double>(n);
+        const double extreme = 1.0 / static_cast<double>(n);
+        *volume *= volume_alpha(*coordination, c_v20, c_v30, min_cn, extreme);
+        *surface *= surface_alpha(*coordination, c_s10, min_cn, extreme);
+    }
+}
+
 // floor(a / w) as the reference computes it (the correctly rounded quotient,
 // then floor) from the product a * inv_w, inv_w = 1 / w rounded: the product
 // is within 2 ulp of the quotient, so the two floors agree unless an integer

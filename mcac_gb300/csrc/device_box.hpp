@@ -130,6 +130,9 @@ class DeviceBox {
     DeviceBox &operator=(const DeviceBox &) = delete;
 
     int set_stream(void *stream);
+    // VolSurfMethods used by the merges and updates of this box
+    // (MCACG_VOLSURF_NONE, _CAPS or _ALPHAS); set before the box runs.
+    int set_volsurf(int method);
     void *stream() const { return stream_; }
     int query(int src_slot, const double dir[3], double dist, QueryResult *out, std::string *err);
     // n independent queries on the current state (nothing is moved): slots[k],

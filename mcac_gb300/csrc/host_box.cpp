@@ -108,21 +108,92 @@ void host_refresh_overlap(HostState *st) {
 int host_update_aggregate(const mcacg_params &p, const HostState &st, MemberLists::View members, double fields[21],
                           double *maxradius) {
     const int n = members.size();
+    // update_distances_and_overlapping (aggregat.cpp:719-764): the contact
+    // pairs i < j in (i, j) order, and each sphere's contacts in key order
+    struct Contact {
+        int j;
+        double d;
+    };
+    std::vector<std::vector<Contact>> adj(static_cast<size_t>(n));
     double overlapping = 0.0, coordination = 0.0;
-    overlap_fields(st, members, &overlapping, &coordination);
-    if (p.volsurf_method != VS_NONE) return ST_INPUT;  // other methods are device-only
-    // compute_volume_surface (aggregat.cpp:321-430), method "none"
+    int intersections = 0;
+    for (int i = 0; i < n; i++) {
+        const int si = members[size_t(i)];
+        for (int j = i + 1; j < n; j++) {
+            const int sj = members[size_t(j)];
+            const double dx = SF(st, SPH_RX, si) - SF(st, SPH_RX, sj);
+            const double dy = SF(st, SPH_RY, si) - SF(st, SPH_RY, sj);
+            const double dz = SF(st, SPH_RZ, si) - SF(st, SPH_RZ, sj);
+            const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+            const double rsum = SF(st, SPH_R, si) + SF(st, SPH_R, sj);
+            if (dist <= (1. + kCoordinationEpsilon) * rsum) {
+                adj[size_t(i)].push_back(Contact{j, dist});
+                adj[size_t(j)].push_back(Contact{i, dist});
+                const double c = (rsum - dist) / rsum;
+                overlapping += 2.0 * c;
+                intersections += 2;
+            }
+        }
+    }
+    if (intersections > 0) {
+        overlapping /= static_cast<double>(intersections);
+        coordination = static_cast<double>(intersections) / static_cast<double>(n);
+    }
+    // the exact SBL and ARVO back-ends are optional libraries of the
+    // reference, which stops with their error codes when they are absent
+    // (aggregat.cpp:329-346)
+    if (p.volsurf_method == VS_SBL) return ST_SBL;
+    if (p.volsurf_method == VS_ARVO) return ST_ARVO;
+    if (p.volsurf_method != VS_NONE && p.volsurf_method != VS_CAPS && p.volsurf_method != VS_ALPHAS)
+        return ST_INPUT;
+    // compute_volume_surface (aggregat.cpp:321-430): per-sphere volumes and
+    // surfaces, cut by the spherical caps of each contact for "caps" (the
+    // contacts of a sphere with later ones in key order), then summed; the
+    // "alphas" corrections act on the sums
+    std::vector<double> vols(static_cast<size_t>(n)), surfs(static_cast<size_t>(n));
+    for (int i = 0; i < n; i++) {
+        vols[size_t(i)] = SF(st, SPH_VOLUME, members[size_t(i)]);
+        surfs[size_t(i)] = SF(st, SPH_SURFACE, members[size_t(i)]);
+    }
+    if (p.volsurf_method == VS_CAPS) {
+        for (int i = 0; i < n; i++) {
+            const int si = members[size_t(i)];
+            for (const Contact &c : adj[size_t(i)]) {
+                if (c.j <= i) continue;
+                const int sj = members[size_t(c.j)];
+                const SphereCaps k = sphere_caps(SF(st, SPH_R, si), SF(st, SPH_VOLUME, si), SF(st, SPH_SURFACE, si),
+                                                 SF(st, SPH_R, sj), SF(st, SPH_VOLUME, sj), SF(st, SPH_SURFACE, sj), c.d);
+                vols[size_t(i)] = vols[size_t(i)] - k.v1;
+                surfs[size_t(i)] = surfs[size_t(i)] - k.s1;
+                vols[size_t(c.j)] = vols[size_t(c.j)] - k.v2;
+                surfs[size_t(c.j)] = surfs[size_t(c.j)] - k.s2;
+            }
+            vols[size_t(i)] = std::max(vols[size_t(i)], 0.0);
+            surfs[size_t(i)] = std::max(surfs[size_t(i)], 0.0);
+        }
+    }
     double volume = 0.0, surface = 0.0;
     for (int i = 0; i < n; i++) {
-        volume = volume + SF(st, SPH_VOLUME, members[size_t(i)]);
-        surface = surface + SF(st, SPH_SURFACE, members[size_t(i)]);
+        volume = volume + vols[size_t(i)];
+        surface = surface + surfs[size_t(i)];
+    }
+    if (p.volsurf_method == VS_ALPHAS) {
+        AlphaSums a{0., 0., 0., 0., 0., 0.};
+        int entries = 0;
+        for (int i = 0; i < n; i++) {
+            const double r1 = SF(st, SPH_R, members[size_t(i)]);
+            for (const Contact &c : adj[size_t(i)]) alpha_add(a, r1, SF(st, SPH_R, members[size_t(c.j)]), c.d);
+            entries += int(adj[size_t(i)].size());
+        }
+        alpha_finish(a, n, entries, &volume, &surface, &overlapping, &coordination);
     }
     if (volume <= 0 || surface <= 0) return ST_VOL_SURF;
-    // compute_mass_center (aggregat.cpp:431-452)
+    // compute_mass_center (aggregat.cpp:431-452), with the per-sphere volumes
+    // of compute_volume_surface
     double r[3] = {0., 0., 0.};
     for (int i = 0; i < n; i++) {
         int s = members[size_t(i)];
-        double vol = SF(st, SPH_VOLUME, s);
+        double vol = vols[size_t(i)];
         r[0] += SF(st, SPH_RX, s) * vol;
         r[1] += SF(st, SPH_RY, s) * vol;
         r[2] += SF(st, SPH_RZ, s) * vol;
@@ -151,7 +222,7 @@ int host_update_aggregate(const mcacg_params &p, const HostState &st, MemberList
     }
     for (int i = 0; i < n; i++) {
         int s = members[size_t(i)];
-        double vol = SF(st, SPH_VOLUME, s);
+        double vol = vols[size_t(i)];
         double rs = SF(st, SPH_R, s);
         arg = arg + vol * (dcen[size_t(i)] * dcen[size_t(i)]);
         brg = brg + vol * (rs * rs);
@@ -316,6 +387,11 @@ int HostBox::upload(const HostState &st, void *stream, std::string *err) {
     int rc = DeviceBox::create(st, stream, &d, err);
     if (rc != ST_OK) return rc;
     dev_.reset(d);
+    rc = dev_->set_volsurf(p_.volsurf_method);
+    if (rc != ST_OK) {
+        if (err) *err = "volsurf_method not available";
+        return rc;
+    }
     refresh();
     init_model_values();
     return ST_OK;

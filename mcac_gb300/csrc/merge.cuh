@@ -24,6 +24,7 @@ struct MergeSmemT {
     double diffpos[3];
     double r_cm[3];
     double sums[kSumSeries];
+    double vol_raw, overlap, coord;
     double rmax_warp[32];
     float tile_f[kPairTile * 4];
     int warp_tmp[32];
@@ -330,15 +331,44 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
     const size_t W = size_t(b.ns);
     for (int k = tid; k < n; k += NT) {
         int s = mem[k];
-        double vol = S(b, SPH_VOLUME, s);
-        double r = S(b, SPH_R, s);
-        wv[0 * W + k] = vol;
+        wv[0 * W + k] = S(b, SPH_VOLUME, s);
         wv[1 * W + k] = S(b, SPH_SURFACE, s);
+        wv[6 * W + k] = S(b, SPH_R, s);
+    }
+    __syncthreads();
+    if (b.volsurf == VS_CAPS && tid == 0) {
+        // compute_volume_surface, "caps" (aggregat.cpp:358-388): each
+        // sphere's contacts with later ones, in (i, j) order, take their caps
+        // off both spheres; a sphere is clamped at 0 once its own contacts
+        // are done. The reference visits a sphere's contacts in its hash
+        // map's order; here they go by index.
+        for (int p = 0; p < P; ++p) {
+            const int i = b.pair_i[p], j = b.pair_j[p];
+            const int si = mem[i], sj = mem[j];
+            const SphereCaps k = sphere_caps(S(b, SPH_R, si), S(b, SPH_VOLUME, si), S(b, SPH_SURFACE, si),
+                                             S(b, SPH_R, sj), S(b, SPH_VOLUME, sj), S(b, SPH_SURFACE, sj), b.pair_d[p]);
+            wv[0 * W + i] = wv[0 * W + i] - k.v1;
+            wv[1 * W + i] = wv[1 * W + i] - k.s1;
+            wv[0 * W + j] = wv[0 * W + j] - k.v2;
+            wv[1 * W + j] = wv[1 * W + j] - k.s2;
+        }
+        // the clamps: a sphere's value is final once its row is done, and
+        // later rows never touch it
+        for (int i = 0; i < n; ++i) {
+            wv[0 * W + i] = dmax(wv[0 * W + i], 0.0);
+            wv[1 * W + i] = dmax(wv[1 * W + i], 0.0);
+        }
+    }
+    __syncthreads();
+    for (int k = tid; k < n; k += NT) {
+        const int s = mem[k];
+        const double vol = wv[0 * W + k];
+        const double r = wv[6 * W + k];
         wv[2 * W + k] = S(b, SPH_RX, s) * vol;
         wv[3 * W + k] = S(b, SPH_RY, s) * vol;
         wv[4 * W + k] = S(b, SPH_RZ, s) * vol;
         wv[5 * W + k] = vol * (r * r);
-        wv[6 * W + k] = r;
+        b.sph_volw[s] = vol;
     }
     __syncthreads();
     {
@@ -355,6 +385,34 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
             }
             sm.sums[7] = ov;
             sm.n_pairs = P;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // the plain sum of the sphere volumes (update_partial's vol_pp)
+        sm.vol_raw = sm.sums[0];
+        if (b.volsurf == VS_CAPS) {
+            double v = 0.0;
+            for (int k = 0; k < n; ++k) v = v + S(b, SPH_VOLUME, mem[k]);
+            sm.vol_raw = v;
+        }
+        sm.overlap = 0.0;
+        sm.coord = 0.0;
+        if (P > 0) {
+            sm.overlap = sm.sums[7] / static_cast<double>(2 * P);
+            sm.coord = static_cast<double>(2 * P) / static_cast<double>(n);
+        }
+        if (b.volsurf == VS_ALPHAS) {
+            // compute_volume_surface, "alphas" (aggregat.cpp:391-426): the
+            // sums over every contact seen from both spheres (here each pair
+            // twice in a row, in (i, j) order), then the corrections
+            AlphaSums a{0., 0., 0., 0., 0., 0.};
+            for (int p = 0; p < P; ++p) {
+                const double ri = S(b, SPH_R, mem[b.pair_i[p]]), rj = S(b, SPH_R, mem[b.pair_j[p]]);
+                alpha_add(a, ri, rj, b.pair_d[p]);
+                alpha_add(a, rj, ri, b.pair_d[p]);
+            }
+            alpha_finish(a, n, 2 * P, &sm.sums[0], &sm.sums[1], &sm.overlap, &sm.coord);
         }
     }
     __syncthreads();
@@ -398,13 +456,8 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
         double brg = sm.sums[5];
         double rg = sqrt(fabs((arg + (3. / 5.) * brg) / V));
         double dp = 2 * sm.sums[6] / static_cast<double>(n);
-        double vol_pp = V / static_cast<double>(n);
-        double overlapping = 0.0, coordination = 0.0;
-        if (P > 0) {
-            int inter = 2 * P;
-            overlapping = sm.sums[7] / static_cast<double>(inter);
-            coordination = static_cast<double>(inter) / static_cast<double>(n);
-        }
+        double vol_pp = sm.vol_raw / static_cast<double>(n);
+        const double overlapping = sm.overlap, coordination = sm.coord;
         const int s0 = mem[0];
         double x = periodic_position(S(b, SPH_X, s0) + sm.r_cm[0], b.L);
         double y = periodic_position(S(b, SPH_Y, s0) + sm.r_cm[1], b.L);

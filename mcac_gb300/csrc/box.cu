@@ -442,7 +442,9 @@ bool view_ok(const StateView &st) {
 // Sizes, grids and capacities of a box from its state, by host arithmetic
 // over the live slots: one pass gives the largest r_max, the means of lpm and
 // r_max, and the Verlet cell counts. No pointer is set.
-DevBox plan_box(const StateView &st) {
+// What a box's sizes and fixed parameters need: the state's counts and box
+// alone (no pass over its arrays).
+DevBox plan_fixed(const StateView &st) {
     DevBox b{};
     b.volsurf = VS_NONE;
     b.L = st.box_length;
@@ -451,6 +453,22 @@ DevBox plan_box(const StateView &st) {
     b.n_cells = st.n_div * st.n_div * st.n_div;
     b.ns = st.ns;
     b.nslots = st.nslots;
+    b.inv_L = 1.0 / st.box_length;
+    b.Lf = float(st.box_length);
+    b.inv_Lf = 1.0f / b.Lf;
+    b.inv_cells = 1.0f / float(b.n_cells);
+    b.pool_cap = 2 * st.ns + 1024;
+    b.surv_cap = 1 << 16;
+    // contact pairs inside one aggregate: equal spheres touch at most 12
+    // others (the kissing number), so at most 6 pairs per sphere; the
+    // merge reports a capacity error beyond 8 per sphere
+    b.pair_cap = 8 * st.ns + 1024;
+    return b;
+}
+
+// The grids from one pass over the live slots: largest r_max, the means of
+// lpm and r_max, and the Verlet cell counts (host arithmetic).
+void plan_grids(const StateView &st, DevBox &b) {
     const double *agg = st.agg;
     auto AF = [&](int f, int a) { return agg[size_t(f) * size_t(st.nslots) + size_t(a)]; };
     double rmax_all = st.maxradius, lpm_sum = 0.0, rmax_sum = 0.0;
@@ -481,34 +499,31 @@ DevBox plan_box(const StateView &st) {
     const double nf = std::floor(st.box_length / h);
     b.fine_div = (nf > double(st.n_div) && nf <= double(kFineMaxDiv)) ? int(nf) : 0;
     b.fine_step = b.fine_div > 0 ? double(b.fine_div) / st.box_length : 0.0;
-    b.inv_L = 1.0 / st.box_length;
-    b.Lf = float(st.box_length);
-    b.inv_Lf = 1.0f / b.Lf;
     b.margin_f = float(b.margin);
     b.fine_step_f = float(b.fine_step);
     b.inv_fine_cells = b.fine_div > 0 ? 1.0f / float(double(b.fine_div) * b.fine_div * b.fine_div) : 0.0f;
-    b.inv_cells = 1.0f / float(b.n_cells);
-    // capacities
     const int avg = (st.nslots + b.n_cells - 1) / b.n_cells;
     b.cell_cap = std::max({64, 2 * maxc, 8 * avg});
-    b.pool_cap = 2 * st.ns + 1024;
-    b.surv_cap = 1 << 16;
-    // contact pairs inside one aggregate: equal spheres touch at most 12
-    // others (the kissing number), so at most 6 pairs per sphere; the
-    // merge reports a capacity error beyond 8 per sphere
-    b.pair_cap = 8 * st.ns + 1024;
+}
+
+DevBox plan_box(const StateView &st) {
+    DevBox b = plan_fixed(st);
+    plan_grids(st, b);
     return b;
 }
 
-// Places the box's arrays in 'arena' (nullptr: sizes them only, leaving the
-// pointers null) and returns the bytes used; every array starts on a
-// 256-byte boundary.
-size_t carve_box(DevBox &b, char *arena) {
+// Places the box's arrays (nullptr: sizes them only, leaving the pointers
+// null) and returns the bytes used; every array starts on a 256-byte
+// boundary. The fixed part depends on the counts alone; the grid part
+// (fine lists, Verlet cell lists) on plan_grids.
+size_t carve_take(char *arena, size_t *used, void **p, size_t bytes) {
+    *p = arena ? arena + *used : nullptr;
+    *used += (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
+    return *used;
+}
+size_t carve_fixed(DevBox &b, char *arena) {
     size_t used = 0;
-    auto take = [&](void **p, size_t bytes) {
-        *p = arena ? arena + used : nullptr;
-        used += (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
-    };
+    auto take = [&](void **p, size_t bytes) { carve_take(arena, &used, p, bytes); };
     const size_t ns = size_t(b.ns), nslots = size_t(b.nslots);
     take((void **)&b.sph, sizeof(double) * 9 * ns);
     take((void **)&b.sph_slot, sizeof(int) * ns);
@@ -524,14 +539,6 @@ size_t carve_box(DevBox &b, char *arena) {
     }
     take((void **)&b.cell_n, sizeof(int) * size_t(b.n_cells));
     take((void **)&b.cell_pos, sizeof(int) * nslots);
-    if (b.fine_div > 0) {
-        const size_t nf3 = size_t(b.fine_div) * size_t(b.fine_div) * size_t(b.fine_div);
-        take((void **)&b.fine_head, sizeof(int) * nf3);
-        take((void **)&b.fine_next, sizeof(int) * nslots);
-        take((void **)&b.fine_prev, sizeof(int) * nslots);
-        take((void **)&b.fine_cell, sizeof(int) * nslots);
-    }
-    take((void **)&b.cell_items, sizeof(int) * size_t(b.n_cells) * size_t(b.cell_cap));
     take((void **)&b.sc, sizeof(DevScalars));
     take((void **)&b.surv, sizeof(int4) * size_t(b.surv_cap));
     take((void **)&b.surv_res, sizeof(double) * size_t(b.surv_cap));
@@ -560,6 +567,25 @@ size_t carve_box(DevBox &b, char *arena) {
     take((void **)&b.best_res, sizeof(unsigned long long) * nc1);
     take((void **)&b.best_ij, sizeof(unsigned long long) * nc1);
     return used;
+}
+size_t carve_grids(DevBox &b, char *arena) {
+    size_t used = 0;
+    auto take = [&](void **p, size_t bytes) { carve_take(arena, &used, p, bytes); };
+    const size_t nslots = size_t(b.nslots);
+    b.fine_head = b.fine_next = b.fine_prev = b.fine_cell = nullptr;
+    if (b.fine_div > 0) {
+        const size_t nf3 = size_t(b.fine_div) * size_t(b.fine_div) * size_t(b.fine_div);
+        take((void **)&b.fine_head, sizeof(int) * nf3);
+        take((void **)&b.fine_next, sizeof(int) * nslots);
+        take((void **)&b.fine_prev, sizeof(int) * nslots);
+        take((void **)&b.fine_cell, sizeof(int) * nslots);
+    }
+    take((void **)&b.cell_items, sizeof(int) * size_t(b.n_cells) * size_t(b.cell_cap));
+    return used;
+}
+size_t carve_box(DevBox &b, char *arena) {
+    const size_t fixed = carve_fixed(b, arena);
+    return fixed + carve_grids(b, arena ? arena + fixed : nullptr);
 }
 
 // The copies of a state into a carved box on stream s: the tables to their
@@ -678,13 +704,17 @@ int DeviceBox::create_many(const std::vector<StateView> &views, void *stream,
         if (err) *err = "states of one batch must have the same integer width";
         return ST_BAD_ARGUMENT;
     }
-    // plans in parallel, then one allocation for every box
+    // The fixed part of every box in one allocation, sized from the counts
+    // alone, so the copies start at once; the grids are planned on the host
+    // threads (one pass over each state's live slots) while they run, then
+    // get a second allocation.
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     std::vector<DevBox> plans(static_cast<size_t>(n));
-    parallel_for(n, [&](int i) { plans[size_t(i)] = plan_box(views[size_t(i)]); });
     std::vector<size_t> off(static_cast<size_t>(n) + 1, 0);
     int max_items = 0;
     for (int i = 0; i < n; ++i) {
-        off[size_t(i) + 1] = off[size_t(i)] + carve_box(plans[size_t(i)], nullptr);
+        plans[size_t(i)] = plan_fixed(views[size_t(i)]);
+        off[size_t(i) + 1] = off[size_t(i)] + carve_fixed(plans[size_t(i)], nullptr);
         max_items = std::max({max_items, plans[size_t(i)].ns, plans[size_t(i)].nslots});
     }
     char *arena = nullptr;
@@ -693,28 +723,39 @@ int DeviceBox::create_many(const std::vector<StateView> &views, void *stream,
         return ST_CUDA;
     }
     std::shared_ptr<void> shared(arena, [](void *p) { cudaFree(p); });
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (int i = 0; i < n; ++i) carve_fixed(plans[size_t(i)], arena + off[size_t(i)]);
+    // the copies in one stream (the link is the limit)
+    for (int i = 0; i < n; ++i)
+        if (!upload_state(plans[size_t(i)], views[size_t(i)], s, err)) {
+            if (err) *err = "box " + std::to_string(i) + ": " + *err;
+            cudaStreamSynchronize(s);  // the copies read the caller's arrays
+            return ST_CUDA;
+        }
+    parallel_for(n, [&](int i) { plan_grids(views[size_t(i)], plans[size_t(i)]); });
+    std::vector<size_t> goff(static_cast<size_t>(n) + 1, 0);
+    for (int i = 0; i < n; ++i) goff[size_t(i) + 1] = goff[size_t(i)] + carve_grids(plans[size_t(i)], nullptr);
+    char *grid_arena = nullptr;
+    if (!cuda_ok(cudaMalloc((void **)&grid_arena, goff[size_t(n)]), err, "cudaMalloc")) {
+        cudaStreamSynchronize(s);
+        return ST_CUDA;
+    }
+    std::shared_ptr<void> shared_grids(grid_arena, [](void *p) { cudaFree(p); });
     std::vector<std::unique_ptr<DeviceBox>> boxes(static_cast<size_t>(n));
     for (int i = 0; i < n; ++i) {
         DevBox &b = plans[size_t(i)];
-        carve_box(b, arena + off[size_t(i)]);
+        carve_grids(b, grid_arena + goff[size_t(i)]);
         std::unique_ptr<DeviceBox> d(new DeviceBox());
         d->ns_ = b.ns;
         d->nslots_ = b.nslots;
         d->arena_ = shared;
+        d->arena_grids_ = shared_grids;
         d->stage_ = b.pair_i;
         d->stage_bytes_ = 32 * size_t(b.pair_cap);
         d->stream_ = s;
         d->devbox_ = new DevBox(b);
         boxes[size_t(i)] = std::move(d);
     }
-    // the copies in one stream (the link is the limit), then the load and
-    // grid kernels over all boxes at once
-    for (int i = 0; i < n; ++i)
-        if (!upload_state(plans[size_t(i)], views[size_t(i)], s, err)) {
-            if (err) *err = "box " + std::to_string(i) + ": " + *err;
-            return ST_CUDA;
-        }
+    // the load and grid kernels over all boxes at once
     const size_t tb = (sizeof(DevBox) * size_t(n) + 255) & ~size_t(255);
     const size_t ta = (sizeof(BoxArg) * size_t(n) + 255) & ~size_t(255);
     char *tmp = nullptr;

@@ -184,7 +184,8 @@ class DeviceBox {
     bool own_stream_ = false;
     int ns_ = 0, nslots_ = 0;
     std::vector<void *> allocations_;
-    std::shared_ptr<void> arena_;  // the allocation shared by boxes made together
+    std::shared_ptr<void> arena_;        // the allocations shared by boxes made together:
+    std::shared_ptr<void> arena_grids_;  // fixed parts, and grids
     void *host_out_ = nullptr;  // mapped pinned result buffer
     void *dev_out_ = nullptr;
     bool profiling_ = false;

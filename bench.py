@@ -187,13 +187,14 @@ def replica_seeds(n: int, first: int) -> list[int]:
     return seeds
 
 
-def replica_models(n: int, rank: int = 0):
+def replica_models(n: int, rank: int = 0, monomers: int = 100000):
     from mcac_gb300 import PhysicalModel
     # disjoint seed ranges per rank
     seeds = replica_seeds(n * (rank + 1), 1)[n * rank:]
+    text = C2_INI.replace("number = 100000", f"number = {int(monomers)}")
     models = []
     for seed in seeds:
-        pm = PhysicalModel(text=C2_INI)
+        pm = PhysicalModel(text=text)
         pm.set(random_seed=seed)
         models.append(pm)
     return models
@@ -232,7 +233,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
     R = args.replicas or resident_boxes(32)  # the most boxes one wave holds
-    models = replica_models(R, rank)
+    models = replica_models(R, rank, args.monomers)
     # page-locked host arrays for the end-to-end leg, in one block made
     # before the host memory fragments (such blocks copy fastest)
     from mcac_gb300 import StateBuffers
@@ -323,8 +324,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "metric": METRIC, "value": steps_all / wall, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": wall * 1000.0 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "100k-monomer box: LogNormal(30 nm, 1.25), 1000 ppm, 1700 K, seed 1, "
-                               "stop at 100 aggregates", "n_monomers": 100000, "replicas_per_gpu": R,
+        "config": {"workload": f"{args.monomers // 1000}k-monomer box: LogNormal(30 nm, 1.25), 1000 ppm, 1700 K, "
+                               "seed 1, stop at 100 aggregates", "n_monomers": args.monomers, "replicas_per_gpu": R,
                    "replica_seeds": f"{models[0].random_seed}..{models[-1].random_seed} on rank 0, skipping "
                                     f"{sorted(DEGENERATE_SEEDS)} (degenerate initial state)",
                    "mc_steps_per_box_per_bench_step": M,
@@ -757,6 +758,8 @@ def main() -> int:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mc-steps", type=int, default=2000, help="MC steps per box per bench step")
     ap.add_argument("--replicas", type=int, default=0, help="boxes per GPU (0: as many as stay resident)")
+    ap.add_argument("--monomers", type=int, default=100000,
+                    help="monomers per box (the benchmark's box has 100000; smaller boxes for profiling)")
     ap.add_argument("--threads", type=int, default=0, help="threads per box (64/128/256; 0: timed at the first run)")
     ap.add_argument("--e2e-steps", type=int, default=5, help="bench steps between upload and download (e2e)")
     ap.add_argument("--plain-steps", type=int, default=500)

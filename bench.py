@@ -149,13 +149,13 @@ def query_bytes(prof: dict) -> float:
 
 
 # DRAM bytes per MC step of the batched loop on this machine, from one ncu
-# capture of k_run (8 replicas x 200 steps, 64 threads per box): 10.69 MB
-# read + 1.8 KB written over 1,600 steps. The full-size launch (1216 boxes)
-# is too large to capture; its traffic grows with the steps done.
-K_RUN_DRAM_BYTES_PER_STEP = 6.68e3
+# capture of k_run (8 replicas x 200 steps, 32 threads per box): 10.76 MB
+# read + 768 B written over 1,600 steps. The full-size launch (2432 boxes,
+# ~185 GB) is too large to capture; its traffic grows with the steps done.
+K_RUN_DRAM_BYTES_PER_STEP = 6.72e3
 # DRAM bytes of one k_query_batch launch of the contact-search workload
 # (10,000 queries on the 1,000,000-sphere snapshot), from one ncu capture.
-K_QUERY_BATCH_DRAM_BYTES = 10.61e6
+K_QUERY_BATCH_DRAM_BYTES = 11.34e6
 
 
 # Seeds whose reference initial state is degenerate: one monomer is drawn so
@@ -337,7 +337,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": K_RUN_DRAM_BYTES_PER_STEP * steps_all / max(1, launches),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_run launch on "
-                                       "8 replicas x 200 steps (64 threads per box), 6.7 kB per MC step, scaled "
+                                       "8 replicas x 200 steps (32 threads per box), 6.7 kB per MC step, scaled "
                                        "by the MC steps of one launch",
                      "kernel": "k_run (batched MC loop)",
                      "bytes_per_launch": qbytes / max(1, launches), "us_per_launch": 1000.0 * total_ms / max(1, launches),

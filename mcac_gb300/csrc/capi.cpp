@@ -465,9 +465,8 @@ int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_s
         std::vector<mcacg_params> ps(params, params + n_boxes);
         for (const auto &p : ps)
             if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges ||
-                (p.with_surface_reactions && (p.u_sg < 0.0 || p.individual_surf_reactions)))
-                return fail(mcacg::ST_INPUT,
-                            "batched boxes cover collisions with optional surface growth (u_sg >= 0, not individual)");
+                (p.with_surface_reactions && p.u_sg < 0.0))
+                return fail(mcacg::ST_INPUT, "batched boxes cover collisions with optional surface growth (u_sg >= 0)");
         // placements in parallel: each box draws from its own copy of the C
         // library stream, so the result equals a sequential placement
         std::vector<mcacg::HostState> states(static_cast<size_t>(n_boxes));

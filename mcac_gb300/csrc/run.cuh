@@ -29,6 +29,7 @@ struct PhysParams {
     double u_sg;        // surface growth velocity dr/dt (m/s)
     double inv_lambda, inv_fractal_dimension;
     int growth;         // with_surface_reactions
+    int individual;     // individual_surf_reactions: only the moved aggregate grows and is updated
     int full_update_every;  // full_aggregate_update_frequency
 };
 
@@ -108,6 +109,7 @@ struct RunSmemT {
     int ms, os, oslot;  // contact of this step: spheres and the other slot
     unsigned long long tree_tmp;  // block reduction scratch
     double step_dt;               // this step's time increment
+    double dt_indiv, step_dt_indiv;  // the moved aggregate's own time step, and its increment
     int n_moved;                  // slots whose grid cell changed in the update of all aggregates
     int moved[kMovedCap];
     TreeCache tree;               // top levels of the pick tree
@@ -278,6 +280,27 @@ __device__ inline void block_grow_spheres(const BoxRun &R, double dt) {
         S(b, SPH_VOLUME, s) = vf * r3;
         S(b, SPH_SURFACE, s) = sf * r2;
         pool_pos[k].w = float(r);
+    }
+}
+
+// SphereList::croissance_surface (sphere_list.cpp:81-87) of one slot's
+// spheres: the individual mode grows only the moved aggregate, by its own
+// time step (calcul.cpp:108, 148, 159-160).
+__device__ inline void block_grow_slot(const BoxRun &R, int slot, double dt) {
+    const DevBox &b = R.box;
+    const double pi = pi_value();
+    const double vf = 4. * pi / 3., sf = 4. * pi;
+    const int *pool_id = b.pool_id[b.sc->pool_sel];
+    float4 *pool_pos = b.pool_pos[b.sc->pool_sel];
+    const int off = b.agg_off[slot], n = b.agg_n[slot];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int s = pool_id[off + k];
+        const double r = S(b, SPH_R, s) + R.phys.u_sg * dt;  // PhysicalModel::grow
+        const double r2 = r * r, r3 = r2 * r;
+        S(b, SPH_R, s) = r;
+        S(b, SPH_VOLUME, s) = vf * r3;
+        S(b, SPH_SURFACE, s) = sf * r2;
+        pool_pos[off + k].w = float(r);
     }
 }
 
@@ -538,6 +561,36 @@ __device__ inline void block_update_all(const BoxRun &R, RS &sm, bool full) {
     tree_cache_load(R, sm.tree);
 }
 
+// The update after growth: every aggregate (slot < 0) or one slot (the
+// individual mode): its fields, grid cells, maxradius and pick-tree leaf.
+template <class RS>
+__device__ inline void block_update_one_or_all(const BoxRun &R, RS &sm, int slot, bool full) {
+    if (slot < 0) {
+        block_update_all(R, sm, full);
+        return;
+    }
+    const DevBox &b = R.box;
+    if (threadIdx.x == 0) {
+        const double rm = thread_update_aggregate(R, slot, full);
+        if (rm > b.sc->maxradius) b.sc->maxradius = rm;
+        regrid(b, slot, agg_pos(b, slot));
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const unsigned long long total =
+            tree_set(R, sm.tree, slot, tree_weight(*R.st, A(b, AGG_TIME_STEP, slot)));
+        if (threadIdx.x == 0) {
+            tree_total_to_state(*R.st, total);
+            sm.rescale = total > kTreeHeadroom;
+        }
+    }
+    __syncthreads();
+    if (sm.rescale) {
+        block_tree_build(R);
+        tree_cache_load(R, sm.tree);
+    }
+}
+
 template <class RS>
 __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
     const int tid = threadIdx.x;
@@ -571,6 +624,7 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
             sm.slot = slot;
             sm.dt = st.inv_weight;
             sm.full = A(b, AGG_LPM, slot);
+            sm.dt_indiv = A(b, AGG_TIME_STEP, slot);
             // random_direction (tools.cpp:82-89): theta = 2 pi u1, phi =
             // acos(1 - 2 u2). cos(phi) is 1 - 2 u2 itself and sin(phi) =
             // 2 sqrt(u2 (1 - u2)). The angles are drawn in FP32 (the device
@@ -646,10 +700,16 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
         st.time = st.time + dt;
         sm.merged = 0;
         sm.step_dt = dt;
+        sm.step_dt_indiv = sm.contact ? sm.dt_indiv * (sm.move / sm.full + 0.0) : sm.dt_indiv;
     }
     __syncthreads();
     // surface reactions before the merge (calcul.cpp:157-172)
-    if (R.phys.growth) block_grow_spheres(R, sm.step_dt);
+    if (R.phys.growth) {
+        if (R.phys.individual)
+            block_grow_slot(R, slot, sm.step_dt_indiv);
+        else
+            block_grow_spheres(R, sm.step_dt);
+    }
     __syncthreads();
     if (sm.contact) {
         block_merge(b, ms, os, slot, oslot, sm.u.m, &sm.mout);
@@ -695,10 +755,15 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
     if (R.phys.growth) {
         // every aggregate after growth (and merge): update() on every
         // full_aggregate_update_frequency-th step without event, else
-        // update_partial() (calcul.cpp:180-206)
+        // update_partial() (calcul.cpp:180-206); in the individual mode only
+        // the moved aggregate, unless there was a merge
         __syncthreads();
         const long long every = R.phys.full_update_every > 0 ? R.phys.full_update_every : 1;
-        block_update_all(R, sm, st.n_iter_without_event % every == 0);
+        const bool full = st.n_iter_without_event % every == 0;
+        if (!R.phys.individual || sm.merged)
+            block_update_one_or_all(R, sm, -1, full);
+        else
+            block_update_one_or_all(R, sm, slot, full);
     }
     if (tid == 0) {
         st.cyc_merge += clock64() - t_phase;

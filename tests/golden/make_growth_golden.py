@@ -1,4 +1,4 @@
-"""Generates tests/golden/growth_ensemble.npz from the reference itself.
+"""Generates tests/golden/growth_{ensemble,individual}.npz from the reference itself.
 
 Surface growth (``[surface_growth] with_surface_reactions``) runs in the
 reference's own ``mcac::calcul`` (src/calcul.cpp:157-206: every sphere grows
@@ -13,7 +13,7 @@ with these distributions (tests/test_growth_gpu.py).
 
 Needs the reference sources and a C++ compiler; run from the repository root:
 
-    python tests/golden/make_growth_golden.py
+    python tests/golden/make_growth_golden.py [growth_ensemble.npz] [growth_individual.npz]
 """
 from __future__ import annotations
 
@@ -34,22 +34,23 @@ HARNESS = ROOT / "oracle" / "_ref" / "mcac_ref_harness"
 N_BOXES = 32
 
 
-def growth_ini(seed: int) -> str:
+def growth_ini(seed: int, individual: bool = False) -> str:
     return (f"[monomers]\nnumber = 300\nmean_diameter = 30\ndispersion_diameter = 1.25\n"
             f"initialisation_mode = lognormal\n[environment]\nvolume_fraction = 5e-3\ntemperature = 1700\n"
             f"[surface_growth]\nwith_surface_reactions = true\nflux_surfgrowth = 0.5\n"
             f"[limits]\nnumber_of_aggregates = 15\n"
-            f"[numerics]\nrandom_seed = {seed}\nwith_domain_duplication = false\n[output]\noutput_dir = out\n")
+            f"[numerics]\nrandom_seed = {seed}\nwith_domain_duplication = false\n"
+            + ("individual_surf_reactions = true\n" if individual else "")
+            + "[output]\noutput_dir = out\n")
 
 
-def main() -> int:
-    build.build_reference()
+def run_set(individual: bool, name: str) -> None:
     times, mean_r, npp, dgdp, box_of = [], [], [], [], []
     with tempfile.TemporaryDirectory(dir=ROOT) as tmp:
         work = Path(tmp)
         for b in range(N_BOXES):
             ini = work / f"g{b}.ini"
-            ini.write_text(growth_ini(600 + b))
+            ini.write_text(growth_ini(600 + b, individual))
             subprocess.run([str(HARNESS), "calcul", ini.name, f"g{b}"], cwd=work, check=True,
                            stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
             snap = Snapshot.load(work / f"g{b}_final.snap")
@@ -58,10 +59,19 @@ def main() -> int:
             npp.extend(snap.n_spheres.tolist())
             dgdp.extend(snap.aggregates[A["dg_over_dp"]].tolist())
             box_of.extend([b] * snap.na)
-    np.savez_compressed(OUT / "growth_ensemble.npz", ini=np.array(growth_ini(0)), seeds=np.arange(600, 600 + N_BOXES),
+    np.savez_compressed(OUT / name, ini=np.array(growth_ini(0, individual)), seeds=np.arange(600, 600 + N_BOXES),
                         time=np.array(times), mean_r=np.array(mean_r), npp=np.array(npp, dtype=np.int64),
                         dg_over_dp=np.array(dgdp), box=np.array(box_of, dtype=np.int64))
-    print(f"{N_BOXES} boxes: mean time {np.mean(times):.4g} s, mean radius {np.mean(mean_r):.4g} m")
+    print(f"{name}: {N_BOXES} boxes: mean time {np.mean(times):.4g} s, mean radius {np.mean(mean_r):.4g} m")
+
+
+def main() -> int:
+    build.build_reference()
+    sets = {"growth_ensemble.npz": False, "growth_individual.npz": True}
+    for name, individual in sets.items():
+        if len(sys.argv) > 1 and name not in sys.argv[1:]:
+            continue
+        run_set(individual, name)
     return 0
 
 

@@ -84,3 +84,44 @@ def test_growth_ensemble_matches_reference():
     assert abs(dg - dr) < 0.15, (dg, dr)
     assert abs(np.log(kg / kr)) < 0.3, (kg, kr)
     assert abs(npp_gpu.mean() / g["npp"].mean() - 1) < 0.1
+
+
+@pytest.mark.gpu
+def test_individual_growth_matches_reference():
+    """individual_surf_reactions: only the moved aggregate grows, by its own
+    time step, and only it is updated unless a merge happened
+    (calcul.cpp:108, 148, 159-166, 185-201); 32 boxes against the
+    reference binary's runs (tests/golden/growth_individual.npz)."""
+    g = load_golden("growth_individual.npz")
+    ini = str(g["ini"])
+    models = [PhysicalModel(text=ini.replace("random_seed = 0", f"random_seed = {int(s)}")) for s in g["seeds"]]
+    with Batch(models) as b:
+        before = b.store_all()
+        b.run(max_steps=0, steps_per_launch=10000)
+        st = b.stats()
+        assert np.all(st["finished"] == 1) and np.all(st["status"] == 0)
+        snaps = b.store_all()
+    # the spheres of different aggregates grew by different amounts (each by
+    # its aggregates' own time steps, about the box's time on average)
+    u = models[0].params.u_sg
+    ratio = []
+    for s0, s1 in zip(before, snaps):
+        grown = s1.spheres[S["r"]] - s0.spheres[S["r"]]
+        assert np.all(grown >= 0) and grown.std() > 0
+        ratio.append(grown.mean() / (u * (s1.time - s0.time)))
+    assert 0.5 < np.mean(ratio) < 2.0, np.mean(ratio)
+    t_gpu = np.array([s.time for s in snaps])
+    r_gpu = np.array([s.spheres[S["r"]].mean() for s in snaps])
+    npp_gpu = np.concatenate([s.n_spheres for s in snaps])
+    dg_gpu = np.concatenate([s.aggregates[A["dg_over_dp"]] for s in snaps])
+
+    def close(a, b_, k=4.0):
+        se = np.sqrt(a.var(ddof=1) / len(a) + b_.var(ddof=1) / len(b_))
+        return abs(a.mean() - b_.mean()) <= k * se
+
+    assert close(np.log(t_gpu), np.log(g["time"])), (t_gpu.mean(), g["time"].mean())
+    assert close(r_gpu, g["mean_r"]), (r_gpu.mean(), g["mean_r"].mean())
+    dg, kg = fractal_fit(npp_gpu, dg_gpu)
+    dr, kr = fractal_fit(g["npp"], g["dg_over_dp"])
+    assert abs(dg - dr) < 0.15, (dg, dr)
+    assert abs(npp_gpu.mean() / g["npp"].mean() - 1) < 0.1

@@ -42,10 +42,13 @@ struct BatchScratch {
     int4 *surv;
     double *surv_res;
 };
-constexpr int kBatchThreads = 256;  // two blocks per SM at 128 registers a thread
+// Threads per query block: 64, 128 or 256 (8, 4 or 2 blocks per SM at 128
+// registers a thread); the first large batch of a box times each and keeps
+// the fastest (results do not depend on it).
+constexpr int kBatchThreadChoices[] = {64, 128, 256};
 template <int NT>
-__global__ void __launch_bounds__(NT) k_query_batch(DevBox b, BatchScratch s, int n, const QueryIn *in,
-                                                    QueryOut *out) {
+__global__ void __launch_bounds__(NT, 512 / NT) k_query_batch(DevBox b, BatchScratch s, int n, const QueryIn *in,
+                                                              QueryOut *out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     QuerySmem &sm = *reinterpret_cast<QuerySmem *>(smem_raw);
     __shared__ int q_cur;
@@ -981,15 +984,42 @@ int DeviceBox::query_batch(int n, const int *slots, const double *dirs, const do
         }
     DevBox &b = *static_cast<DevBox *>(devbox_);
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
-    int dev = 0, n_sm = 0, per_sm = 0;
+    int dev = 0, n_sm = 0;
     if (!cuda_ok(cudaGetDevice(&dev), err, "cudaGetDevice")) return ST_CUDA;
     if (!cuda_ok(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), err, "device attribute"))
         return ST_CUDA;
-    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_query_batch<kBatchThreads>, kBatchThreads,
-                                                               sizeof(QuerySmem)),
-                 err, "occupancy"))
-        return ST_CUDA;
-    const int blocks = std::max(1, std::min(n, std::max(1, per_sm) * std::max(1, n_sm)));
+    static bool attrs = false;
+    if (!attrs) {
+        auto set = [&](const void *k) {
+            return cuda_ok(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(QuerySmem))),
+                           err, "cudaFuncSetAttribute") &&
+                   cuda_ok(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100), err,
+                           "cudaFuncSetAttribute");
+        };
+        if (!set((const void *)k_query_batch<64>) || !set((const void *)k_query_batch<128>) ||
+            !set((const void *)k_query_batch<256>))
+            return ST_CUDA;
+        attrs = true;
+    }
+    // blocks of each size the GPU holds at once; the scratch is sized for
+    // the most of them
+    auto resident = [&](int nt, int *blocks) {
+        int per_sm = 0;
+        cudaError_t e = nt == 64    ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_query_batch<64>, 64,
+                                                                                    sizeof(QuerySmem))
+                        : nt == 128 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_query_batch<128>, 128,
+                                                                                    sizeof(QuerySmem))
+                                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_query_batch<256>, 256,
+                                                                                    sizeof(QuerySmem));
+        *blocks = std::max(1, std::min(n, std::max(1, per_sm) * std::max(1, n_sm)));
+        return cuda_ok(e, err, "occupancy");
+    };
+    int blocks = 1;
+    for (int nt : kBatchThreadChoices) {
+        int nb = 1;
+        if (!resident(nt, &nb)) return ST_CUDA;
+        blocks = std::max(blocks, nb);
+    }
 
     // scratch layout: counter, inputs, outputs, then per-block candidate and
     // survivor slices
@@ -1045,17 +1075,44 @@ int DeviceBox::query_batch(int n, const int *slots, const double *dirs, const do
     bool ok = cuda_ok(cudaMemcpyAsync(d_in, hin.data(), sizeof(QueryIn) * size_t(n), cudaMemcpyHostToDevice, s), err,
                       "query upload") &&
               cuda_ok(cudaMemsetAsync(sc.next, 0, sizeof(int), s), err, "query counter");
-    if (ok) {
+    auto launch = [&](int nt, float *ms) {
+        int nb = 1;
+        if (!resident(nt, &nb)) return false;
+        if (!cuda_ok(cudaMemsetAsync(sc.next, 0, sizeof(int), s), err, "query counter")) return false;
         cudaEventRecord(e0, s);
-        k_query_batch<kBatchThreads><<<blocks, kBatchThreads, sizeof(QuerySmem), s>>>(b, sc, n, d_in, d_out);
+        if (nt == 64)
+            k_query_batch<64><<<nb, 64, sizeof(QuerySmem), s>>>(b, sc, n, d_in, d_out);
+        else if (nt == 128)
+            k_query_batch<128><<<nb, 128, sizeof(QuerySmem), s>>>(b, sc, n, d_in, d_out);
+        else
+            k_query_batch<256><<<nb, 256, sizeof(QuerySmem), s>>>(b, sc, n, d_in, d_out);
         cudaEventRecord(e1, s);
-        ok = cuda_ok(cudaGetLastError(), err, "k_query_batch") &&
-             cuda_ok(cudaMemcpyAsync(hout.data(), d_out, sizeof(QueryOut) * size_t(n), cudaMemcpyDeviceToHost, s),
-                     err, "query download") &&
-             cuda_ok(cudaStreamSynchronize(s), err, "k_query_batch");
-    }
+        if (!cuda_ok(cudaGetLastError(), err, "k_query_batch") || !cuda_ok(cudaEventSynchronize(e1), err, "k_query_batch"))
+            return false;
+        cudaEventElapsedTime(ms, e0, e1);
+        return true;
+    };
     float ms = 0.f;
-    if (ok) cudaEventElapsedTime(&ms, e0, e1);
+    if (ok && batch_threads_ == 0 && n >= 1024) {
+        // the first large batch: each block size on the same queries (they
+        // only read the box), the fastest kept
+        float best = 0.f;
+        for (int nt : kBatchThreadChoices) {
+            float t = 0.f;
+            ok = ok && launch(nt, &t);
+            if (ok && (best == 0.f || t < best)) {
+                best = t;
+                batch_threads_ = nt;
+            }
+        }
+        ms = best;
+    } else if (ok) {
+        ok = launch(batch_threads_ ? batch_threads_ : 256, &ms);
+    }
+    ok = ok &&
+         cuda_ok(cudaMemcpyAsync(hout.data(), d_out, sizeof(QueryOut) * size_t(n), cudaMemcpyDeviceToHost, s), err,
+                 "query download") &&
+         cuda_ok(cudaStreamSynchronize(s), err, "k_query_batch");
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (!ok) return ST_CUDA;

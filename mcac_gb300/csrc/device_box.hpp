@@ -192,6 +192,7 @@ class DeviceBox {
     void *ev_[2] = {nullptr, nullptr};
     void *batch_mem_ = nullptr;  // query_batch scratch, grown on demand
     size_t batch_bytes_ = 0;
+    int batch_threads_ = 0;      // query_batch block size (0: timed at the first large batch)
     void *stage_ = nullptr;      // the merge's pair scratch, also the store staging area
     size_t stage_bytes_ = 0;
     Profile prof_;

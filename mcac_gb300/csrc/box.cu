@@ -628,6 +628,58 @@ int blocks_per_box(int n_boxes, int max_items) {
     return std::max(1, std::min({want, 256, (max_items + 255) / 256}));
 }
 
+// A few streams that share the copies of many boxes (several copy engines
+// at work, their per-copy latencies overlapped), forked from and joined back
+// into a main stream.
+class CopyStreams {
+  public:
+    explicit CopyStreams(int n) {
+        for (int i = 0; i < n; ++i) {
+            cudaStream_t st = nullptr;
+            if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) break;
+            streams_.push_back(st);
+        }
+    }
+    ~CopyStreams() {
+        for (cudaStream_t st : streams_) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+        if (ev_) cudaEventDestroy(ev_);
+    }
+    CopyStreams(const CopyStreams &) = delete;
+    CopyStreams &operator=(const CopyStreams &) = delete;
+    // stream k of the set (the main stream when none could be made)
+    cudaStream_t at(size_t k, cudaStream_t main) const {
+        return streams_.empty() ? main : streams_[k % streams_.size()];
+    }
+    // the set's streams start after the work queued on 'main' so far
+    bool fork(cudaStream_t main) {
+        if (streams_.empty()) return true;
+        if (!ev_ && cudaEventCreateWithFlags(&ev_, cudaEventDisableTiming) != cudaSuccess) return false;
+        if (cudaEventRecord(ev_, main) != cudaSuccess) return false;
+        for (cudaStream_t st : streams_)
+            if (cudaStreamWaitEvent(st, ev_, 0) != cudaSuccess) return false;
+        return true;
+    }
+    // 'main' continues after the work queued on the set so far
+    bool join(cudaStream_t main) {
+        for (cudaStream_t st : streams_) {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+            const bool ok = cudaEventRecord(e, st) == cudaSuccess && cudaStreamWaitEvent(main, e, 0) == cudaSuccess;
+            cudaEventDestroy(e);
+            if (!ok) return false;
+        }
+        return true;
+    }
+
+  private:
+    std::vector<cudaStream_t> streams_;
+    cudaEvent_t ev_ = nullptr;
+};
+constexpr int kCopyStreams = 4;
+
 }  // namespace
 
 int DeviceBox::create(const StateView &st, void *stream, DeviceBox **out, std::string *err) {
@@ -727,13 +779,21 @@ int DeviceBox::create_many(const std::vector<StateView> &views, void *stream,
     }
     std::shared_ptr<void> shared(arena, [](void *p) { cudaFree(p); });
     for (int i = 0; i < n; ++i) carve_fixed(plans[size_t(i)], arena + off[size_t(i)]);
-    // the copies in one stream (the link is the limit)
+    // the copies, spread over a few streams, then joined into the main one
+    CopyStreams copies(kCopyStreams);
+    if (!copies.fork(s)) {
+        if (err) *err = "copy streams";
+        return ST_CUDA;
+    }
     for (int i = 0; i < n; ++i)
-        if (!upload_state(plans[size_t(i)], views[size_t(i)], s, err)) {
+        if (!upload_state(plans[size_t(i)], views[size_t(i)], copies.at(size_t(i), s), err)) {
             if (err) *err = "box " + std::to_string(i) + ": " + *err;
-            cudaStreamSynchronize(s);  // the copies read the caller's arrays
-            return ST_CUDA;
+            return ST_CUDA;  // the copy streams are synchronised on the way out
         }
+    if (!copies.join(s)) {
+        if (err) *err = "copy streams";
+        return ST_CUDA;
+    }
     parallel_for(n, [&](int i) { plan_grids(views[size_t(i)], plans[size_t(i)]); });
     std::vector<size_t> goff(static_cast<size_t>(n) + 1, 0);
     for (int i = 0; i < n; ++i) goff[size_t(i) + 1] = goff[size_t(i)] + carve_grids(plans[size_t(i)], nullptr);
@@ -1384,8 +1444,15 @@ int DeviceBox::store_many(const std::vector<DeviceBox *> &boxes, const std::vect
     k_boxes<OP_PACK_RANKS><<<n, kScanThreads, 0, s>>>(dboxes, dargs, n, 1);
     k_boxes<OP_PACK><<<n * per, 256, 0, s>>>(dboxes, dargs, n, per);
     if (!cuda_ok(cudaGetLastError(), err, "store")) return ST_CUDA;
+    // the copies, spread over a few streams after the packing
+    CopyStreams copies(kCopyStreams);
+    if (!copies.fork(s)) {
+        if (err) *err = "copy streams";
+        return ST_CUDA;
+    }
+    cudaStream_t cs = s;
     auto get = [&](void *dst, const void *src, size_t bytes) {
-        return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s), err, "store");
+        return cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, cs), err, "store");
     };
     for (int i = 0; i < n; ++i) {
         const int na = args[size_t(i)].a;
@@ -1393,13 +1460,14 @@ int DeviceBox::store_many(const std::vector<DeviceBox *> &boxes, const std::vect
         const DevBox &b = host_boxes[size_t(i)];
         const PackStage ps = pack_stage(b, na, args[size_t(i)].b);
         mcacg_state *o = outs[size_t(i)];
+        cs = copies.at(size_t(i), s);
         if (!(get(o->spheres, b.sph, sizeof(double) * 9 * size_t(b.ns)) &&
               get(o->sphere_label, ps.label, 8 * size_t(b.ns)) && get(o->aggregates, ps.agg, 168 * size_t(na)) &&
               get(o->n_spheres_per_aggregate, ps.count, 8 * size_t(na)) &&
               get(o->members, ps.members, 8 * size_t(b.ns))))
             return ST_CUDA;
     }
-    if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
+    if (!copies.join(s) || !cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
     for (int i = 0; i < n; ++i) {
         if (args[size_t(i)].a < 0) continue;
         const DevBox &b = host_boxes[size_t(i)];

@@ -184,15 +184,18 @@ VerletError = _exc("VerletError", 3)
 InputError = _exc("InputError", 4)
 AbandonError = _exc("AbandonError", 5)
 TooDenseError = _exc("TooDenseError", 6)
+SBLError = _exc("SBLError", 7)
 VolSurfError = _exc("VolSurfError", 8)
 MergeError = _exc("MergeError", 9)
+ARVOError = _exc("ARVOError", 10)
 CudaError = _exc("CudaError", 100)
 CapacityError = _exc("CapacityError", 101)
 DeviceTimeout = _exc("DeviceTimeout", 102)
 BadArgument = _exc("BadArgument", 103)
 NoDevice = _exc("NoDevice", 104)
-_BY_CODE = {c.code: c for c in (IOError_, VerletError, InputError, AbandonError, TooDenseError, VolSurfError,
-                                MergeError, CudaError, CapacityError, DeviceTimeout, BadArgument, NoDevice)}
+_BY_CODE = {c.code: c for c in (IOError_, VerletError, InputError, AbandonError, TooDenseError, SBLError,
+                                VolSurfError, MergeError, ARVOError, CudaError, CapacityError, DeviceTimeout,
+                                BadArgument, NoDevice)}
 
 
 def check(rc: int) -> None:

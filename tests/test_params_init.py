@@ -80,3 +80,38 @@ def test_too_dense_is_reported():
                             "[numerics]\nrandom_seed = 1\n")
     with pytest.raises(TooDenseError):
         init_state(pm)
+
+
+def test_output_write_rule_parameters():
+    # [output] write_* keys (physical_model.cpp:76-78, 185-187): defaults,
+    # values, and the reference's extract semantics (an invalid value leaves
+    # the default)
+    p = PhysicalModel(text="[monomers]\nnumber = 10\n").params
+    assert (p.write_events_frequency, p.write_between_event_frequency, p.write_delta_t) == (1, 100, -1.0)
+    p = PhysicalModel(text="[output]\nwrite_events_frequency = 3\nwrite_between_event_frequency = 37\n"
+                           "write_Delta_t = 2e-6\n").params
+    assert (p.write_events_frequency, p.write_between_event_frequency, p.write_delta_t) == (3, 37, 2e-6)
+    p = PhysicalModel(text="[output]\nwrite_between_event_frequency = often\n").params
+    assert p.write_between_event_frequency == 100
+
+
+@pytest.mark.parametrize("method", ["caps", "alphas"])
+def test_placement_with_corrected_volume_methods(method):
+    # a monomer has no contact: "caps" and "alphas" leave its volume and
+    # surface as "none" does, so the placement is the same bit for bit
+    base = "[monomers]\nnumber = 300\ndispersion_diameter = 1.3\n[numerics]\nrandom_seed = 5\n"
+    ref = init_state(PhysicalModel(text=base)).to_snapshot()
+    got = init_state(PhysicalModel(text=base + f"[surface_growth]\nvolsurf_method = {method}\n")).to_snapshot()
+    np.testing.assert_array_equal(got.spheres, ref.spheres)
+    np.testing.assert_array_equal(got.aggregates, ref.aggregates)
+
+
+def test_exact_volume_back_ends_are_reported():
+    # the SBL and ARVO back-ends are optional libraries of the reference,
+    # which stops with their error codes when they are absent
+    from mcac_gb300._lib import ARVOError, SBLError
+    base = "[monomers]\nnumber = 20\n[numerics]\nrandom_seed = 5\n[surface_growth]\nvolsurf_method = "
+    with pytest.raises(SBLError):
+        init_state(PhysicalModel(text=base + "sbl\n"))
+    with pytest.raises(ARVOError):
+        init_state(PhysicalModel(text=base + "arvo\n"))

@@ -155,7 +155,7 @@ def query_bytes(prof: dict) -> float:
 K_RUN_DRAM_BYTES_PER_STEP = 6.72e3
 # DRAM bytes of one k_query_batch launch of the contact-search workload
 # (10,000 queries on the 1,000,000-sphere snapshot), from one ncu capture.
-K_QUERY_BATCH_DRAM_BYTES = 11.34e6
+K_QUERY_BATCH_DRAM_BYTES = 12.12e6
 
 
 # Seeds whose reference initial state is degenerate: one monomer is drawn so

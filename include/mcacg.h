@@ -326,6 +326,11 @@ int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state
 /* Page-locked host memory (freed by mcacg_host_free), for state arrays that
  * are loaded and stored by DMA. */
 int mcacg_host_alloc(int64_t bytes, void **ptr);
+/* Merged aggregates of at least n_spheres spheres find their intra-aggregate
+ * contact pairs on a hashed cell grid (O(n)), smaller ones by testing all
+ * pairs (O(n^2)); both give the same pairs. Process-wide, read by boxes
+ * created afterwards; default 2048. *previous (may be NULL) gets the old value. */
+int mcacg_set_merge_grid_min(int32_t n_spheres, int32_t *previous);
 int mcacg_host_free(void *ptr);
 int mcacg_batch_destroy(mcacg_batch *batch);
 /* Boxes the device-resident loop runs at once on the current device with

@@ -295,6 +295,16 @@ class AggregatList:
         return sb.to_snapshot(volsurf_method=int(self.model.params.volsurf_method))
 
 
+def set_merge_grid_min(n_spheres: int) -> int:
+    """Merged aggregates of at least n_spheres spheres find their contact
+    pairs on a hashed cell grid, smaller ones by testing all pairs (the same
+    pairs either way). Read by boxes created afterwards; returns the previous
+    value (default 2048)."""
+    prev = C.c_int32(0)
+    check(lib().mcacg_set_merge_grid_min(int(n_spheres), C.byref(prev)))
+    return prev.value
+
+
 def device_count() -> int:
     n = C.c_int()
     check(lib().mcacg_device_count(C.byref(n)))

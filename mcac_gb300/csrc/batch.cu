@@ -33,11 +33,6 @@ using RunSmemFor = typename std::conditional<(NT <= 32), RunSmemSmall, RunSmem>:
 // wall time of one launch when boxes run to their stop criteria
 constexpr long long kRunLaunchBudgetNs = 200LL * 1000 * 1000;
 
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 // Each block advances its box by at most max_steps steps; with budget_ns > 0
 // it also stops after that much wall time, so that boxes of very different
@@ -63,24 +58,16 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
         int *sdst = reinterpret_cast<int *>(&st);
         for (int k = threadIdx.x; k < swords; k += NT) sdst[k] = ssrc[k];
     }
-    __shared__ unsigned long long t_start;
-    __shared__ int out_of_time;
     __syncthreads();
     if (threadIdx.x == 0) {
         R.st = &st;
-        t_start = global_ns();
-        out_of_time = 0;
+        // every step starts only before the deadline (a step is never cut)
+        sm.deadline = budget_ns > 0 ? global_ns() + (unsigned long long)budget_ns : 0ULL;
     }
     __syncthreads();
     tree_cache_load(R, sm.tree);
-    for (long long s = 0; s < max_steps; ++s) {
-        if (budget_ns > 0 && (s & 15) == 0) {
-            if (threadIdx.x == 0) out_of_time = global_ns() - t_start >= (unsigned long long)budget_ns;
-            __syncthreads();
-            if (out_of_time) break;
-        }
+    for (long long s = 0; s < max_steps; ++s)
         if (!block_mc_step(R, sm)) break;
-    }
     __syncthreads();
     {
         const int swords = int(sizeof(RunState) / sizeof(int));

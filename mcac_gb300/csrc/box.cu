@@ -12,7 +12,17 @@
 #include "host_parallel.hpp"
 #include "merge.cuh"
 
+#include <atomic>
+
 namespace mcacg {
+
+namespace {
+std::atomic<int> g_merge_grid_min{2048};
+}
+
+int merge_grid_min() { return g_merge_grid_min.load(std::memory_order_relaxed); }
+int set_merge_grid_min(int n) { return g_merge_grid_min.exchange(n); }
+
 
 // ------------------------------------------------------------------ kernels
 __global__ void __launch_bounds__(kQueryThreads) k_query(DevBox b, int src, double dx, double dy, double dz,
@@ -466,6 +476,7 @@ DevBox plan_fixed(const StateView &st) {
     // others (the kissing number), so at most 6 pairs per sphere; the
     // merge reports a capacity error beyond 8 per sphere
     b.pair_cap = 8 * st.ns + 1024;
+    b.grid_pairs_min = merge_grid_min();
     return b;
 }
 

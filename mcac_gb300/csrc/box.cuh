@@ -65,6 +65,7 @@ struct DevBox {
     int pool_cap;    // entries per pool buffer
     int surv_cap;    // survivors in global scratch
     int pair_cap;    // intra-aggregate contact pairs in global scratch
+    int grid_pairs_min;  // merged aggregates from this size find their pairs on a cell grid
     double *sph;     // [9][ns]
     int *sph_slot;   // owning slot
     // each sphere's entry of its aggregate's per-sphere volumes at the last

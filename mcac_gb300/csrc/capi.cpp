@@ -665,6 +665,15 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
     });
 }
 
+int mcacg_set_merge_grid_min(int32_t n_spheres, int32_t *previous) {
+    return guarded([&] {
+        if (n_spheres < 1) return fail(MCACG_ERR_BAD_ARGUMENT, "n_spheres must be positive");
+        int old = mcacg::set_merge_grid_min(n_spheres);
+        if (previous) *previous = old;
+        return 0;
+    });
+}
+
 int mcacg_host_alloc(int64_t bytes, void **ptr) {
     return guarded([&] {
         if (!ptr || bytes <= 0) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");

@@ -112,6 +112,12 @@ struct MergeResult {
     double maxradius;
 };
 
+// Merged aggregates of at least this many spheres find their contact pairs
+// on a hashed cell grid, smaller ones by testing all pairs (the same pairs
+// either way). Process-wide; read when a box is created. Default 2048.
+int merge_grid_min();
+int set_merge_grid_min(int n);  // returns the previous value
+
 class DeviceBox {
   public:
     // Uploads a state to the current device. Returns a status code; an

@@ -75,6 +75,12 @@ struct BoxRun {
 
 constexpr int kMovedCap = 64;  // grid moves listed per update of all aggregates
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // The top levels of a box's pick tree (up to kTreeCache entries) are kept in
 // shared memory for a launch: the descent then reads global memory only for
 // the lower levels. coff[lev] is the level's offset in the copy, -1 if the
@@ -103,6 +109,7 @@ struct RunSmemT {
     double refpos[3];
     double dir[3];
     unsigned long long t_pick;  // pick target in the tree's fixed point
+    unsigned long long deadline;  // %globaltimer time after which no step starts (0: none)
     double dt, full, move;
     int slot, contact, stop, merged, rescale;
     int keep, removed;
@@ -604,6 +611,10 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
             st.finished = 1;
             sm.stop = 1;
         }
+        // a time-capped launch: checked before every step, so that a box of
+        // expensive steps does not hold the launch (and the other boxes,
+        // which wait for it) past the cap
+        if (!sm.stop && sm.deadline != 0ULL && global_ns() >= sm.deadline) sm.stop = 1;
         if (!sm.stop) {
             // the target: floor(total * rand() / 2^31), below the total
             const unsigned long long total = st.tree_total;

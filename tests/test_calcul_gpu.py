@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from conftest import load_golden
-from mcac_gb300 import AggregatList, PhysicalModel
+from mcac_gb300 import AggregatList, PhysicalModel, set_merge_grid_min
 from oracle import oracle_py as O
 
 FIELDS = ["picked", "contact", "merged", "moving_sphere", "other_sphere", "moving_agg", "other_agg", "n_agg_after"]
@@ -58,6 +58,20 @@ def test_lognormal_run_matches_oracle_step_by_step():
     g = load_golden("ln_late.npz")
     st = compare_runs(str(g["ini"]))
     assert st.events == int(g["run_events"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fixture", ["c1_trace.npz", "ln_late.npz"])
+def test_run_with_cell_grid_pair_search_matches_oracle(fixture):
+    """Every merge finds its intra-aggregate contact pairs on the hashed cell
+    grid (used from 2048 merged spheres by default, here from 2): same steps,
+    same merges, same final state byte for byte."""
+    g = load_golden(fixture)
+    prev = set_merge_grid_min(2)
+    try:
+        compare_runs(str(g["ini"]))
+    finally:
+        set_merge_grid_min(prev)
 
 
 @pytest.mark.gpu

@@ -2,6 +2,8 @@
 import ctypes
 import re
 
+import pytest
+
 from conftest import ROOT
 
 
@@ -31,3 +33,18 @@ def test_abi_version_and_errors():
     # a null argument is rejected with a status, not a crash
     assert lib.mcacg_params_default(None) == 103
     assert b"null" in lib.mcacg_last_error()
+
+
+def test_merge_grid_threshold_setting():
+    """The all-pairs / cell-grid switch of the merge is a process-wide
+    setting: positive sizes only, the previous value returned."""
+    from mcac_gb300 import set_merge_grid_min
+    from mcac_gb300._lib import MCACError
+    with pytest.raises(MCACError):
+        set_merge_grid_min(0)
+    prev = set_merge_grid_min(64)
+    try:
+        assert prev == 2048
+        assert set_merge_grid_min(128) == 64
+    finally:
+        set_merge_grid_min(prev)

@@ -992,7 +992,7 @@ __device__ __forceinline__ void fine_link(const DevBox &b, int slot, int c) {
 __device__ __forceinline__ void regrid_to(const DevBox &b, int slot, int key, int fc) {
     const bool fine = b.fine_div > 0;
     const int c = cell_index(b, key);
-    // round 1: everything indexed by the slot or by the new cells
+    // pass 1: everything indexed by the slot or by the new cells
     const int old_key = b.agg_cell[slot];
     const int old = cell_index(b, old_key);
     const int k = b.cell_pos[slot];
@@ -1002,7 +1002,7 @@ __device__ __forceinline__ void regrid_to(const DevBox &b, int slot, int key, in
     const int fnext = fine ? b.fine_next[slot] : -1;
     const int fhead = fine ? b.fine_head[fc] : -1;
     if (key != old_key) {
-        // round 2 and 3: the old cell's length, then its last item
+        // passes 2 and 3: the old cell's length, then its last item
         const int n_old = b.cell_n[old];
         int *items = b.cell_items + size_t(old) * b.cell_cap;
         int kk = k;

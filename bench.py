@@ -156,6 +156,10 @@ K_RUN_DRAM_BYTES_PER_STEP = 6.72e3
 # DRAM bytes of one k_query_batch launch of the contact-search workload
 # (10,000 queries on the 1,000,000-sphere snapshot), from one ncu capture.
 K_QUERY_BATCH_DRAM_BYTES = 12.12e6
+# DRAM bytes per MC step of k_run on the ensemble benchmark's windows, from
+# one ncu capture of a small case of the same workload (None until measured).
+K_RUN_ENS_DRAM_BYTES_PER_STEP = None
+K_RUN_ENS_TRAFFIC_SOURCE = ""
 
 
 # Seeds whose reference initial state is degenerate: one monomer is drawn so
@@ -493,6 +497,19 @@ def cpu_baseline_sample(args) -> dict | None:
 ENS_WORKLOAD = ("batched ensemble: 512 independent boxes, seed 1000+b, N ~ round(exp(U[ln 256, ln 16384])), "
                 "50/50 monodisperse 30 nm or LogNormal(30 nm, 1.25), volume fraction ~ U[100, 5000] ppm, "
                 "T ~ U[1500, 1900] K, stop at 1 aggregate or 10000 steps without an event")
+# The two step windows of the ensemble benchmark. Window a runs every box
+# from its initial placement until at most ENS_A_AGGREGATES aggregates are
+# left (or ENS_A_STEPS steps, or a stop criterion); window b continues each
+# box for ENS_B_STEPS more steps under its own criteria. A box's first
+# ~10^5 steps are cheap on a CPU core; below ~100 aggregates one step costs
+# the reference 1-100 ms, so a whole run to one aggregate takes a core hours
+# for the largest boxes: window b samples that stage at a fixed step count.
+ENS_A_AGGREGATES = 100
+ENS_A_STEPS = 100_000
+ENS_B_STEPS = 500
+ENS_WINDOWS = (f"every box from its reference initial placement through window a (until at most "
+               f"{ENS_A_AGGREGATES} aggregates are left, {ENS_A_STEPS} MC steps are done or a stop criterion "
+               f"is met), then window b (the next {ENS_B_STEPS} MC steps under the box's own stop criteria)")
 
 
 def ensemble_inis(n_boxes: int = 512, first_seed: int = 1000) -> list[str]:
@@ -513,128 +530,345 @@ def ensemble_inis(n_boxes: int = 512, first_seed: int = 1000) -> list[str]:
     return inis
 
 
-def run_ensemble(args, rank: int, world: int) -> dict | None:
-    """The 512-box ensemble to completion (or --cap-seconds): boxes/hour."""
+def ini_monomers(ini: str) -> int:
+    for line in ini.splitlines():
+        k, _, v = line.partition("=")
+        if k.strip() == "number":
+            return int(v)
+    raise ValueError("no [monomers] number")
+
+
+def assign_boxes(sizes: list[int], world: int) -> list[list[int]]:
+    """Box indices per rank: largest box first to the rank holding the
+    fewest monomers so far (device-memory footprint grows with the monomer
+    count), so that ranks hold near-equal memory and work. Deterministic;
+    every box goes to exactly one rank; each rank's list is in box order."""
+    loads = [0] * world
+    out: list[list[int]] = [[] for _ in range(world)]
+    for b in sorted(range(len(sizes)), key=lambda k: (-sizes[k], k)):
+        r = min(range(world), key=lambda q: (loads[q], q))
+        out[r].append(b)
+        loads[r] += sizes[b]
+    return [sorted(x) for x in out]
+
+
+def ens_config(n_boxes: int) -> dict:
+    """The workload description both arms print (identical by construction)."""
+    return {"workload": ENS_WORKLOAD + "; " + ENS_WINDOWS, "boxes": n_boxes,
+            "window_a": {"until_aggregates": ENS_A_AGGREGATES, "max_steps": ENS_A_STEPS},
+            "window_b": {"steps": ENS_B_STEPS}, "seeds": f"1000..{999 + n_boxes}"}
+
+
+def merge_bytes(prof: dict) -> float:
+    """Algorithmic bytes of the merges counted in 'prof': the merged
+    aggregate's FP64 sphere rows (72 B each), its 168-byte record and its
+    intra-aggregate contact pairs (16 B each). The removed spheres' 32-byte
+    rewrite is not counted (no per-merge count of removed spheres is kept;
+    it is at most 32 B x merged spheres)."""
+    return 72.0 * prof["merged_spheres"] + 168.0 * prof["merges"] + 16.0 * prof["merge_pairs"]
+
+
+def _ens_models(inis, boxes, limit_a):
+    from mcac_gb300 import PhysicalModel
+    models = []
+    for b in boxes:
+        pm = PhysicalModel(text=inis[b])
+        pm.set(number_of_aggregates_limit=limit_a)
+        models.append(pm)
+    return models
+
+
+def _windows_once(models, states, outs, stream, flush, threads=0):
+    """One bench step: upload the initial states, run window a then window b
+    on the GPU, download the final states. Returns (kernel ms, wall s,
+    steps, k_run launches, work counters, per-box stats, threads used)."""
+    import torch
+
+    from mcac_gb300 import Batch
+    flush.zero_()  # L2 flushed between timed iterations
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = Batch(models, stream=stream.cuda_stream, states=states)  # host -> device
+    b.threads = threads
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.run(max_steps=ENS_A_STEPS, steps_per_launch=ENS_A_STEPS)
+    la = b.last_run()[1]
+    threads_a = b.threads
+    b.set_aggregate_limit(1)
+    b.threads = threads  # chosen again for the later stage
+    b.run(max_steps=ENS_B_STEPS, steps_per_launch=ENS_B_STEPS)
+    lb = b.last_run()[1]
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = b.stats()
+    if outs is not None:
+        b.store_all(raw=True, out=outs)  # device -> host
+    wall = time.perf_counter() - t0
+    work = b.work()
+    threads_b = b.threads
+    b.close()
+    return ms, wall, int(st["steps"].sum()), la + lb, work, st, (threads_a, threads_b)
+
+
+def plain_single_box_windows(models, states, stream, flush, picks) -> dict:
+    """The plain single-box GPU path: the same device loop with one box per
+    launch (what mcacg_run_device runs), the same two windows, box by box."""
+    tot_ms, tot_steps = 0.0, 0
+    for k in picks:
+        ms, _, steps, _, _, _, _ = _windows_once([models[k]], [states[k]], None, stream, flush)
+        tot_ms += ms
+        tot_steps += steps
+    return {"value": tot_steps / (tot_ms / 1000.0), "unit": UNIT, "boxes": len(picks), "steps": tot_steps,
+            "note": "one box per launch through the device-resident loop (mcacg_run_device's path), same windows, "
+                    "boxes run one after another; a sample of the ensemble's boxes (every "
+                    f"{max(1, len(models) // max(1, len(picks)))}th of this rank's)"}
+
+
+def run_ensemble_windows(args, rank: int, world: int) -> dict | None:
+    """The ensemble benchmark (default): MC steps/s over windows a and b."""
     import numpy as np
     import torch
 
-    from mcac_gb300 import Batch, PhysicalModel
+    from mcac_gb300 import Batch, StateBuffers
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
-    inis = ensemble_inis(args.boxes)[rank::world]  # boxes are sharded across ranks
-    models = [PhysicalModel(text=t) for t in inis]
+    inis = ensemble_inis(args.boxes)
+    sizes = [ini_monomers(t) for t in inis]
+    mine = assign_boxes(sizes, world)[rank]
+    cpu_pool = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle_py  # the CPU sample's processes start before any GPU work
+        cpu_pool = oracle_py.window_pool(os.cpu_count() or 1)
     t0 = time.perf_counter()
-    batch = Batch(models, stream=stream.cuda_stream)
-    batch.threads = args.threads
+    models = _ens_models(inis, mine, ENS_A_AGGREGATES)
+    # the reference placements (host, bit-identical with the reference),
+    # kept in page-locked arrays; a second set receives the final states
+    n = [int(m.params.n_monomeres) for m in models]
+    states = StateBuffers.many([(k, k) for k in n], pinned=True)
+    outs = StateBuffers.many([(k, k) for k in n], pinned=True)
+    with Batch(models, stream=stream.cuda_stream) as b0:
+        b0.store_all(raw=True, out=states)
     setup_s = time.perf_counter() - t0
-    done_at = np.full(len(models), np.nan)
+    state_bytes = sum(int(s.spheres.nbytes + s.sphere_label.nbytes + s.aggregates.nbytes + s.n_spheres.nbytes
+                          + s.members.nbytes) for s in states)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    for _ in range(args.warmup):
+        _windows_once(models, states, outs, stream, flush, args.threads)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
     sampler = ClockSampler(dev)
     sampler.start()
+    tot_ms = tot_wall = 0.0
+    tot_steps = launches = 0
+    work_sum: dict = {}
+    threads_seen = set()
+    out_bytes = 0
+    for _ in range(args.steps):
+        ms, wall, steps, nl, work, st, th = _windows_once(models, states, outs, stream, flush, args.threads)
+        tot_ms += ms
+        tot_wall += wall
+        tot_steps += steps
+        launches += nl + 1  # k_run launches + the window switch
+        threads_seen.add(th)
+        for k, v in work.items():
+            work_sum[k] = work_sum.get(k, 0) + v
+        out_bytes = sum(int(o.spheres.nbytes + o.sphere_label.nbytes + o.aggregates.nbytes + o.n_spheres.nbytes
+                            + o.members.nbytes) for o in outs) + int(st.nbytes)
+    if world > 1:
+        torch.distributed.barrier()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    kernel_ms, launches = 0.0, 0
-    while True:
-        # each box as fast as it goes; finish times read every second
-        batch.run_timed(1000.0)
-        ms, nl = batch.last_run()
-        kernel_ms += ms
-        launches += nl
-        st = batch.stats()
-        now = time.perf_counter() - t0
-        fin = (st["finished"] == 1) | (st["status"] != 0)
-        done_at[fin & np.isnan(done_at)] = now
-        if fin.all() or now > args.cap_seconds:
-            break
-    wall = time.perf_counter() - t0
     clocks = sampler.stop()
-    st = batch.stats()
-    steps = int(st["steps"].sum())
-    n_done = int(np.isfinite(done_at).sum())
-    failed = int((st["status"] != 0).sum())
-    work = batch.work()
-    threads_used = batch.threads
-    # where the boxes with the most device time spend it
-    box_work = [batch.box_work(k) for k in range(len(models))]
-    box_cycles = np.array([sum(bw[c] for c in ("cycles_pick", "cycles_query", "cycles_move", "cycles_merge"))
-                           for bw in box_work], dtype=np.float64)
-    order = np.argsort(box_cycles)[::-1][:8]
-    slowest = []
-    for k in order:
-        bw = box_work[int(k)]
-        q = max(1, bw["queries"])
-        cyc = sum(bw[c] for c in ("cycles_pick", "cycles_query", "cycles_move", "cycles_merge"))
-        slowest.append({"box": int(k), "n_monomers": int(models[k].params.n_monomeres),
-                        "aggregates_left": int(st["n_aggregates"][k]), "steps": int(st["steps"][k]),
-                        "done_s": None if not np.isfinite(done_at[k]) else float(done_at[k]),
-                        "cycles_per_step": cyc / q, "device_s": cyc / 2.07e9, "phase_share": phase_share(bw),
-                        "per_query": {f: bw[f] / q for f in ("mov_spheres", "scanned", "cells", "candidates",
-                                                             "cand_spheres", "refined")},
-                        "per_merge": {f: bw[f] / max(1, bw["merges"]) for f in ("merged_spheres", "merge_pairs")}})
-    batch.close()
-    vals = torch.tensor([wall, float(steps), float(n_done), kernel_ms / 1000.0], device="cuda",
-                        dtype=torch.float64)
+    last_stats = st
+    times = torch.tensor([tot_ms / 1000.0, float(tot_steps), tot_wall], device="cuda", dtype=torch.float64)
+    if world > 1:
+        import torch.distributed as dist
+        tmax, tsum = times.clone(), times.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        kern_s, steps_all, wall_s = float(tmax[0]), float(tsum[1]), float(tmax[2])
+    else:
+        kern_s, steps_all, wall_s = float(times[0]), float(times[1]), float(times[2])
+    completion = None
+    if not args.no_completion:
+        completion = ensemble_to_completion(args, inis, mine, states, stream, world)
+    if rank != 0:
+        return None
+    peak, peak_kind = peaks()
+    qb, mb = query_bytes(work_sum), merge_bytes(work_sum)
+    achieved = (qb + mb) / kern_s / 1e9 if kern_s > 0 else 0.0
+    out = {
+        "metric": METRIC, "value": steps_all / kern_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": kern_s * 1000.0 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": ens_config(args.boxes),
+        "run": {"path": "device-resident MC loop, one thread block per box, all boxes of a window in one launch",
+                "parallelism": f"{len(mine)} boxes on rank 0 of {world} (assigned by monomer count)",
+                "l2": "flushed (256 MB write) before each bench step; states > L2",
+                "setup_s": round(setup_s, 2), "threads_per_box": sorted(threads_seen),
+                "steps_per_bench_step": tot_steps // max(1, args.steps),
+                "aggregates_after": {"min": int(last_stats["n_aggregates"].min()),
+                                     "median": float(np.median(last_stats["n_aggregates"])),
+                                     "max": int(last_stats["n_aggregates"].max())},
+                "boxes_finished": int((last_stats["finished"] == 1).sum()),
+                "boxes_failed": int((last_stats["status"] != 0).sum())},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "kernel": "k_run (batched MC loop)",
+                     "bytes_per_launch": (qb + mb) / max(1, launches - args.steps),
+                     "us_per_launch": 1e6 * kern_s / max(1, launches - args.steps),
+                     "bytes_model": "per contact query: 16 B x moving spheres + 36 B x aggregates scanned + 8 B x "
+                                    "cells + 16 B x candidate spheres + 64 B x FP64-refined pairs; per merge: 72 B x "
+                                    "merged spheres + 168 B + 16 B x contact pairs"},
+        "e2e": {"value": steps_all / wall_s, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": out_bytes,
+                "note": "per bench step: the initial states uploaded from page-locked host arrays, windows a and b "
+                        "run, the final states and per-box statistics downloaded (wall clock)"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "work": work_sum,
+        "phase_share": phase_share(work_sum),
+    }
+    k_traffic = K_RUN_ENS_DRAM_BYTES_PER_STEP
+    if k_traffic:
+        out["roofline"]["traffic"] = k_traffic * (steps_all / max(1, launches - args.steps))
+        out["roofline"]["traffic_source"] = K_RUN_ENS_TRAFFIC_SOURCE
+    if completion is not None:
+        out["to_completion"] = completion
+    if not args.no_plain:
+        picks = list(range(0, len(models), max(1, len(models) // args.plain_boxes)))[:args.plain_boxes]
+        out["plain_single_box"] = plain_single_box_windows(models, states, stream, flush, picks)
+    if cpu_pool is not None:
+        out["cpu_baseline"] = ens_cpu_sample(inis, cpu_pool, args.cpu_boxes)
+        cpu_pool.close()
+    else:
+        out["cpu_baseline"] = None
+    return out
+
+
+def ensemble_to_completion(args, inis, mine, states, stream, world) -> dict:
+    """Every box from its initial placement to its own stop criteria
+    (1 aggregate or 10000 steps without an event): boxes/hour, with each
+    box's finish time. Launches of at most 200 ms in which each box does as
+    many steps as fit."""
+    import numpy as np
+    import torch
+
+    from mcac_gb300 import Batch
+    models = _ens_models(inis, mine, 1)
+    with Batch(models, stream=stream.cuda_stream, states=states) as batch:
+        done_at = np.full(len(models), np.nan)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        kernel_ms, launches = 0.0, 0
+        while True:
+            batch.run_timed(1000.0)
+            ms, nl = batch.last_run()
+            kernel_ms += ms
+            launches += nl
+            st = batch.stats()
+            now = time.perf_counter() - t0
+            fin = (st["finished"] == 1) | (st["status"] != 0)
+            done_at[fin & np.isnan(done_at)] = now
+            if fin.all() or now > args.cap_seconds:
+                break
+        wall = time.perf_counter() - t0
+        st = batch.stats()
+        steps = int(st["steps"].sum())
+        n_done = int(np.isfinite(done_at).sum())
+        failed = int((st["status"] != 0).sum())
+        box_work = [batch.box_work(k) for k in range(len(models))]
+    vals = torch.tensor([wall, float(steps), float(n_done)], device="cuda", dtype=torch.float64)
     if world > 1:
         import torch.distributed as dist
         tmax, tsum = vals.clone(), vals.clone()
         dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
         dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
         wall, steps, n_done = float(tmax[0]), int(tsum[1]), int(tsum[2])
-    if rank != 0:
-        return None
+    cyc = np.array([sum(bw[c] for c in ("cycles_pick", "cycles_query", "cycles_move", "cycles_merge"))
+                    for bw in box_work], dtype=np.float64)
+    slow = int(np.argmax(cyc))
     fin_times = np.sort(done_at[np.isfinite(done_at)])
-    res = {
-        "metric": "boxes/hour", "value": n_done / wall * 3600.0, "unit": "boxes/h", "n_gpus": world,
-        "steps": launches, "warmup": 0, "ms_per_step": 1000.0 * wall / max(1, launches),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": ENS_WORKLOAD, "boxes": args.boxes, "finished": n_done, "failed": failed,
-                   "wall_s": wall, "cap_s": args.cap_seconds, "setup_s": round(setup_s, 2),
-                   "launches": "at most 200 ms each, every box doing as many steps as fit",
-                   "threads_per_box": threads_used,
-                   "time_to_finish_s": {q: float(np.quantile(fin_times, p)) for q, p in
-                                        (("p50", 0.5), ("p90", 0.9), ("max", 1.0))} if len(fin_times) else None},
-        "mc_steps_per_s": steps / wall,
-        "kernel_s": kernel_ms / 1000.0,
-        "clocks": clocks,
-        "gpu_launches": launches,
-        "work": work,
-        "phase_share": phase_share(work),
-        "slowest_boxes": slowest,
-    }
-    if not args.no_cpu_baseline:
-        res["cpu_baseline"] = ensemble_cpu_sample(inis, args.cpu_seconds)
-    return res
+    return {"boxes_per_hour": n_done / wall * 3600.0, "wall_s": wall, "finished": n_done, "failed": failed,
+            "cap_s": args.cap_seconds, "mc_steps": steps, "mc_steps_per_s": steps / wall,
+            "kernel_s": kernel_ms / 1000.0, "launches": launches,
+            "time_to_finish_s": {q: float(np.quantile(fin_times, p)) for q, p in
+                                 (("p50", 0.5), ("p90", 0.9), ("max", 1.0))} if len(fin_times) else None,
+            "slowest_box": {"box": int(mine[slow]), "n_monomers": int(models[slow].params.n_monomeres),
+                            "steps": int(st["steps"][slow]), "device_s": float(cyc[slow] / 2.07e9),
+                            "done_s": float(done_at[slow]) if np.isfinite(done_at[slow]) else None,
+                            "phase_share": phase_share(box_work[slow])},
+            "note": "every box to its own stop criteria; launches of at most 200 ms, each box doing as many steps "
+                    "as fit; the CPU reference is not run this far (one large box takes it hours)"}
 
 
-def _ens_worker(job):
-    ini, seconds = job
-    from oracle import oracle_py
-    box = oracle_py.OracleBox(ini)
-    steps, t0 = 0, time.perf_counter()
-    finished = False
-    while time.perf_counter() - t0 < seconds:
-        st, _ = box.calcul(max_steps=500)
-        steps += int(st.steps)
-        if st.finished:
-            finished = True
-            break
-    dt = time.perf_counter() - t0
-    box.close()
-    return steps, dt, finished
+def _ens_jobs(inis, boxes):
+    sizes = [ini_monomers(inis[b]) for b in boxes]
+    order = sorted(range(len(boxes)), key=lambda k: (-sizes[k], boxes[k]))  # largest first
+    return [(boxes[k], inis[boxes[k]], ENS_A_AGGREGATES, ENS_A_STEPS, ENS_B_STEPS, 1) for k in order]
 
 
-def ensemble_cpu_sample(inis, seconds: float) -> dict:
-    """The oracle on all host cores: one box per core from the start of the
-    ensemble, each advanced for at most 'seconds'; MC steps/s summed."""
-    import multiprocessing as mp
+def _farm_summary(res, wall, procs) -> dict:
+    steps = sum(r["steps_a"] + r["steps_b"] for _, r in res)
+    return {"steps": steps, "wall_s": wall, "value": steps / wall,
+            "steps_a": sum(r["steps_a"] for _, r in res), "steps_b": sum(r["steps_b"] for _, r in res),
+            "cpu_s_a": sum(r["s_a"] for _, r in res), "cpu_s_b": sum(r["s_b"] for _, r in res),
+            "procs": procs}
+
+
+def ens_cpu_sample(inis, pool, n_boxes: int) -> dict:
+    """The oracle on all host cores over a sample of the ensemble's boxes
+    (every k-th box), the same two windows."""
     procs = os.cpu_count() or 1
-    jobs = [(ini, seconds) for ini in inis[:procs]]
-    with mp.get_context("spawn").Pool(procs) as pool:
-        res = pool.map(_ens_worker, jobs)
-    return {"value": sum(r[0] / r[1] for r in res), "unit": "MC steps/s", "cores": procs, "kind": "port",
-            "sample": f"the first {len(jobs)} boxes of the ensemble, one per core, up to {seconds:.0f} s each "
-                      f"({sum(r[2] for r in res)} finished in that time)"}
+    from oracle import oracle_py
+    boxes = list(range(0, len(inis), max(1, len(inis) // n_boxes)))[:n_boxes]
+    t = time.perf_counter()
+    res = oracle_py.farm_windows(_ens_jobs(inis, boxes), procs, pool=pool)
+    s = _farm_summary(res, time.perf_counter() - t, procs)
+    return {"value": s["value"], "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{len(boxes)} of the {len(inis)} boxes (every {len(inis) // len(boxes)}th), both windows, "
+                      f"farmed over {procs} processes, largest first ({s['steps']} MC steps in {s['wall_s']:.1f} s)"}
+
+
+def run_ensemble_reference(args) -> dict:
+    """The reference arm of the ensemble benchmark: the oracle (the C
+    restatement of the reference, pinned to it) on every host core, over all
+    boxes and both windows. The K timed bench steps each take 1/K of the
+    boxes (box b in step b mod K); all are farmed at once, largest box first,
+    so the cores stay busy, and the value is steps / wall time."""
+    from oracle import oracle_py
+    procs = os.cpu_count() or 1
+    inis = ensemble_inis(args.boxes)
+    pool = oracle_py.window_pool(procs)
+    small = min(range(len(inis)), key=lambda b: ini_monomers(inis[b]))
+    for _ in range(args.warmup):  # untimed: every worker once on a short run
+        oracle_py.farm_windows([(small, inis[small], ENS_A_AGGREGATES, 2000, 0, 1)] * procs, procs, pool=pool)
+    t = time.perf_counter()
+    res = oracle_py.farm_windows(_ens_jobs(inis, list(range(len(inis)))), procs, pool=pool)
+    wall = time.perf_counter() - t
+    pool.close()
+    s = _farm_summary(res, wall, procs)
+    sample = (f"all {len(inis)} boxes, both windows, farmed over {procs} processes largest first "
+              f"({s['steps']} MC steps: {s['steps_a']} in window a, {s['steps_b']} in window b; "
+              f"{s['cpu_s_a']:.0f} + {s['cpu_s_b']:.0f} core-seconds); each box placed by the oracle's own "
+              f"restatement of the reference placement")
+    return {
+        "impl": "reference", "metric": METRIC, "value": s["value"], "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": ens_config(args.boxes),
+        "cpu_baseline": {"value": s["value"], "unit": UNIT, "cores": procs, "kind": "port", "sample": sample,
+                         "host_cpus": os.cpu_count()},
+        "e2e": {"value": s["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "windows": {"a_steps_per_s": s["steps_a"] / wall if wall else None,
+                    "core_seconds": {"a": s["cpu_s_a"], "b": s["cpu_s_b"]}},
+    }
 
 
 SERVE_WORKLOAD = ("serving stream: seeded Poisson arrivals at --rate runs/s for --serve-seconds, "
@@ -766,9 +1000,13 @@ def main() -> int:
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "contact-search", "ensemble", "serve"],
-                    help="c2: replicas of the 100k-monomer box (headline); contact-search: batched queries; "
-                         "ensemble: the 512-box ensemble to completion (boxes/hour)")
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "c2", "contact-search", "serve"],
+                    help="ensemble (default): the 512-box ensemble through two step windows, MC steps/s, plus "
+                         "its run to completion (boxes/hour); c2: replicas of the 100k-monomer box; "
+                         "contact-search: batched queries; serve: the serving stream (p50/p99)")
+    ap.add_argument("--no-completion", action="store_true", help="ensemble: skip the run to completion")
+    ap.add_argument("--plain-boxes", type=int, default=8, help="ensemble: boxes of the plain single-box sample")
+    ap.add_argument("--cpu-boxes", type=int, default=16, help="ensemble: boxes of the rank-0 CPU sample")
     ap.add_argument("--boxes", type=int, default=512, help="ensemble boxes")
     ap.add_argument("--cap-seconds", type=float, default=240.0, help="ensemble / serving wall-time cap")
     ap.add_argument("--rate", type=float, default=50.0, help="serving arrivals per second")
@@ -782,7 +1020,11 @@ def main() -> int:
     if args.impl == "reference":
         if rank != 0:
             return 0
-        ref = run_contact_search_reference if args.workload == "contact-search" else run_reference
+        ref = {"ensemble": run_ensemble_reference, "contact-search": run_contact_search_reference,
+               "c2": run_reference}.get(args.workload)
+        if ref is None:
+            print(json.dumps({"impl": "reference", "unavailable": f"no CPU reference for --workload {args.workload}"}))
+            return 0
         print(json.dumps(ref(args)))
         return 0
     if world > 1:
@@ -790,7 +1032,7 @@ def main() -> int:
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    runner = {"c2": run_ours, "contact-search": run_contact_search, "ensemble": run_ensemble,
+    runner = {"c2": run_ours, "contact-search": run_contact_search, "ensemble": run_ensemble_windows,
               "serve": run_serve}[args.workload]
     out = runner(args, rank, world)
     if out is not None:

@@ -351,6 +351,14 @@ int mcacg_batch_run(mcacg_batch *batch, int64_t max_steps, int64_t steps_per_lau
  * very different cost never wait for one another. Returns early once every
  * box has met its stop criteria. */
 int mcacg_batch_run_timed(mcacg_batch *batch, double wall_ms);
+/* Sets every box's number_of_aggregates stop criterion
+ * (PhysicalModel::finished, physical_model.cpp:288-337) to 'limit'. Boxes
+ * that stopped without an error are re-armed: each re-checks all of its
+ * criteria before its next step, so a box that has already met the new
+ * limit or another criterion does no further step. Lets one batch run a
+ * stage of its runs (say, down to 100 aggregates) and then the rest. No
+ * counterpart in the reference. */
+int mcacg_batch_set_aggregate_limit(mcacg_batch *batch, int64_t limit);
 /* Per-box counters since creation (arrays of n_boxes). */
 int mcacg_batch_stats(mcacg_batch *batch, mcacg_run_stats *stats);
 int mcacg_batch_size(const mcacg_batch *batch, int32_t *n_boxes);

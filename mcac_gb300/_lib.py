@@ -124,6 +124,7 @@ SIGNATURES = {
     "mcacg_resident_boxes": [i32, C.POINTER(i32)],
     "mcacg_batch_set_threads": [vp, i32],
     "mcacg_batch_threads": [vp, C.POINTER(i32)],
+    "mcacg_batch_set_aggregate_limit": [vp, i64],
     "mcacg_batch_run": [vp, i64, i64],
     "mcacg_batch_run_timed": [vp, f64],
     "mcacg_batch_stats": [vp, C.POINTER(RunStats)],

@@ -383,6 +383,12 @@ class Batch:
     def run(self, max_steps: int = 0, steps_per_launch: int = 20000) -> None:
         check(lib().mcacg_batch_run(self._b, int(max_steps), int(steps_per_launch)))
 
+    def set_aggregate_limit(self, limit: int) -> None:
+        """Every box's number_of_aggregates stop criterion becomes 'limit';
+        boxes that stopped without an error continue at the next run (each
+        re-checks all of its criteria first)."""
+        check(lib().mcacg_batch_set_aggregate_limit(self._b, int(limit)))
+
     def stats(self) -> np.ndarray:
         n = len(self.models)
         arr = (RunStats * n)()

@@ -83,6 +83,17 @@ __global__ void k_gather_run_scalars(const BoxRun *runs, int n, DevScalars *out)
     if (i < n) out[i] = *runs[i].box.sc;
 }
 
+// A new aggregate-count stop criterion for n boxes: boxes that stopped
+// without an error run again and re-check every criterion before their next
+// step.
+__global__ void k_set_aggregate_limit(BoxRun *runs, int n, long long limit) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    runs[i].lim.number_of_aggregates_limit = limit;
+    RunState *st = runs[i].st;
+    if (st != nullptr && st->status == ST_OK) st->finished = 0;
+}
+
 // The pick trees of n boxes from their time steps, one block per box
 // (block_tree_build); the total weight goes to each box's loop state.
 __global__ void __launch_bounds__(256) k_tree_build(const BoxRun *runs, int n) {
@@ -346,7 +357,12 @@ int BatchRunner::set_threads(int threads) {
 
 // Times each block size on a short slice of the run (results do not depend
 // on the block size) and keeps the fastest. Returns the MC steps done.
-int BatchRunner::tune(int64_t budget, int64_t *done, float *ms_total, std::string *err) {
+// With one_wave, only block sizes at which every unfinished box is resident
+// at once are tried: time-capped launches give each block its wall-time
+// budget from its own start, so a second wave of blocks would start only
+// when the first has used its budget, doubling the launch and halving every
+// box's share of it.
+int BatchRunner::tune(int64_t budget, int64_t *done, float *ms_total, std::string *err, bool one_wave) {
     cudaStream_t s = static_cast<cudaStream_t>(stream_);
     const int n = int(boxes_.size());
     const BoxRun *runs = static_cast<const BoxRun *>(runs_dev_);
@@ -359,6 +375,10 @@ int BatchRunner::tune(int64_t budget, int64_t *done, float *ms_total, std::strin
     int rc = ST_OK;
     for (int nt : kRunThreadChoices) {
         if (budget > 0 && *done + probe > budget) break;
+        if (one_wave && nt != kRunThreadChoices[0]) {
+            int resident = 0;
+            if (resident_boxes(nt, &resident, err) == ST_OK && resident < tuned_active_) continue;
+        }
         cudaEventRecord(e0, s);
         if (!ok_cuda(launch_k_run(nt, n, s, runs, n, (long long)probe), err, "k_run")) {
             rc = ST_CUDA;
@@ -405,7 +425,7 @@ int BatchRunner::run(int64_t max_steps, int64_t chunk, std::string *err) {
     };
     if (auto_threads_ && threads_ == 0) {
         rc = count_active(&tuned_active_);
-        if (rc == ST_OK) rc = tune(max_steps, &done, &ms_total, err);
+        if (rc == ST_OK) rc = tune(max_steps, &done, &ms_total, err, max_steps <= 0);
         if (rc != ST_OK) return rc;
     }
     const float ms_tune = ms_total;
@@ -447,7 +467,7 @@ int BatchRunner::run(int64_t max_steps, int64_t chunk, std::string *err) {
             if (auto_threads_ && active * 2 <= tuned_active_) {
                 tuned_active_ = active;
                 float mt = 0.f;
-                rc = tune(0, &done, &mt, err);
+                rc = tune(0, &done, &mt, err, true);
                 ms_total += mt;
                 if (rc != ST_OK) break;
             }
@@ -482,9 +502,11 @@ int BatchRunner::run_timed(double wall_ms, std::string *err) {
     int active = 0;
     int rc = count_active(&active);
     if (rc != ST_OK) return rc;
-    if (auto_threads_ && (threads_ == 0 || active * 2 <= tuned_active_) && active > 0) {
+    int resident_now = 0;
+    if (threads_ != 0 && resident_boxes(threads_, &resident_now, err) != ST_OK) return ST_CUDA;
+    if (auto_threads_ && (threads_ == 0 || active * 2 <= tuned_active_ || resident_now < active) && active > 0) {
         tuned_active_ = active;
-        rc = tune(0, &done, &ms_total, err);
+        rc = tune(0, &done, &ms_total, err, true);
         if (rc != ST_OK) return rc;
     }
     cudaEvent_t e0, e1;
@@ -513,7 +535,7 @@ int BatchRunner::run_timed(double wall_ms, std::string *err) {
         if (rc != ST_OK) break;
         if (auto_threads_ && active > 0 && active * 2 <= tuned_active_) {
             tuned_active_ = active;
-            rc = tune(0, &done, &ms_total, err);
+            rc = tune(0, &done, &ms_total, err, true);
             if (rc != ST_OK) break;
         }
     }
@@ -521,6 +543,15 @@ int BatchRunner::run_timed(double wall_ms, std::string *err) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
+}
+
+int BatchRunner::set_aggregate_limit(int64_t limit, std::string *err) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    const int n = int(boxes_.size());
+    if (n == 0) return ST_OK;
+    k_set_aggregate_limit<<<(n + 255) / 256, 256, 0, s>>>(static_cast<BoxRun *>(runs_dev_), n, (long long)limit);
+    if (!ok_cuda(cudaGetLastError(), err, "k_set_aggregate_limit")) return ST_CUDA;
+    return ST_OK;
 }
 
 int BatchRunner::stats(std::vector<BoxRunStats> *out, std::string *err) {

@@ -53,6 +53,10 @@ class BatchRunner {
     // fit), returning early when all have met their stop criteria.
     int run_timed(double wall_ms, std::string *err);
     int stats(std::vector<BoxRunStats> *out, std::string *err);
+    // Replaces every box's number_of_aggregates stop criterion; boxes that
+    // stopped without an error are re-armed and re-check all their criteria
+    // before their next step.
+    int set_aggregate_limit(int64_t limit, std::string *err);
     int download(int box, HostState *st, std::string *err);
     // Physical time of every box.
     int times(std::vector<double> *out, std::string *err);
@@ -88,7 +92,7 @@ class BatchRunner {
     std::vector<char> growth_;  // per box: surface reactions on
     std::vector<int> volsurf_;  // per box: VolSurfMethods
     int tuned_active_ = 0;  // unfinished boxes at the last tuning
-    int tune(int64_t budget, int64_t *done, float *ms_total, std::string *err);
+    int tune(int64_t budget, int64_t *done, float *ms_total, std::string *err, bool one_wave);
 };
 
 // Continuous-batching request loop: 'capacity' block slots; between kernel

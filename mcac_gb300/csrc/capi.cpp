@@ -715,6 +715,16 @@ int mcacg_batch_set_threads(mcacg_batch *batch, int32_t threads) {
     });
 }
 
+int mcacg_batch_set_aggregate_limit(mcacg_batch *batch, int64_t limit) {
+    return guarded([&] {
+        if (!batch) return fail(MCACG_ERR_BAD_ARGUMENT, "null batch");
+        std::string err;
+        const int rc = batch->impl->set_aggregate_limit(limit, &err);
+        if (rc != 0) return fail(rc, err);
+        return 0;
+    });
+}
+
 int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads) {
     return guarded([&] {
         if (!batch || !threads) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");

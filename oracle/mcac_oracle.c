@@ -418,6 +418,7 @@ int64_t mo_size(const mo_box *b) { return b->na; }
 int64_t mo_n_spheres(const mo_box *b) { return b->ns; }
 double mo_time(const mo_box *b) { return b->time; }
 void mo_set_time(mo_box *b, double t) { b->time = t; }
+void mo_set_aggregate_limit(mo_box *b, int64_t limit) { b->p.number_of_aggregates_limit = limit; }
 
 /* Derived box length and gas properties (physical_model.cpp:228-262,
  * 536-546). */

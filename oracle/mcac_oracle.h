@@ -78,6 +78,9 @@ double mo_get_time_step(const mo_box *b, double max);
 void mo_refresh(mo_box *b);
 double mo_time(const mo_box *b);
 void mo_set_time(mo_box *b, double t);
+/* Replaces the number_of_aggregates stop criterion (a benchmark runs a box in
+ * stages: down to some aggregate count, then on). */
+void mo_set_aggregate_limit(mo_box *b, int64_t limit);
 
 /* The MC loop of src/calcul.cpp:66-281 (collision-only). Stops at the
  * parameters' criteria or after max_steps (> 0). */

@@ -41,6 +41,15 @@ class MoStats(C.Structure):
                 ("reserved", i32)]
 
 
+# one traced MC step: mo_step_record of mcac_oracle.h
+STEP_DTYPE = np.dtype([
+    ("step", "<i8"), ("picked", "<i8"), ("contact", "<i8"), ("merged", "<i8"),
+    ("moving_sphere", "<i8"), ("other_sphere", "<i8"), ("moving_agg", "<i8"), ("other_agg", "<i8"),
+    ("n_agg_after", "<i8"), ("deltatemps", "<f8"), ("full_distance", "<f8"), ("dir", "<f8", 3),
+    ("contact_distance", "<f8"), ("move_distance", "<f8"), ("time_after", "<f8"), ("reserved", "<f8"),
+])
+
+
 _lib = None
 
 
@@ -67,6 +76,7 @@ def lib():
             "mo_sort_indices": (None, [P(f64), P(i64), i64]),
             "mo_time": (f64, [C.c_void_p]),
             "mo_set_time": (None, [C.c_void_p, f64]),
+            "mo_set_aggregate_limit": (None, [C.c_void_p, i64]),
             "mo_calcul": (C.c_int, [C.c_void_p, i64, C.c_void_p, i64, P(MoStats)]),
         }
         for name, (res, args) in sig.items():
@@ -185,8 +195,10 @@ class OracleBox:
             raise RuntimeError(f"oracle error {rc}")
         return bool(m.value)
 
+    def set_aggregate_limit(self, limit: int) -> None:
+        lib().mo_set_aggregate_limit(self.h, int(limit))
+
     def calcul(self, max_steps=0, trace=False, trace_capacity=0):
-        from mcac_gb300.snapshot import STEP_DTYPE
         st = MoStats()
         buf = None
         cap = 0
@@ -224,11 +236,13 @@ def sort_indices(keys: np.ndarray) -> np.ndarray:
 
 
 # ---------------------------------------------------------------- bench
+# The CPU legs of bench.py. They use nothing of the product: each box is
+# placed by this restatement's own copy of the reference placement
+# (mo_box_new_random, bit-identical with the reference's).
+
 def _worker(args):
-    ini_text, snap_bytes, seconds, chunk = args
-    from mcac_gb300.snapshot import Snapshot
-    snap = Snapshot.from_bytes(snap_bytes)
-    box = OracleBox(ini_text, snap)
+    ini_text, seconds, chunk = args
+    box = OracleBox(ini_text)
     steps = 0
     t0 = time.perf_counter()
     while time.perf_counter() - t0 < seconds:
@@ -245,17 +259,11 @@ def bench_sample(ini_text: str, seconds: float = 15.0, processes: int = 1, steps
                  chunk: int = 200) -> dict:
     """MC steps/s of the restatement on a bounded sample of the workload.
 
-    The initial state is the reference placement (identical in the product
-    and here); each process advances its own copy of the box from that
-    state for 'seconds' of wall time. With several processes the value is
-    the sum of their rates (independent boxes, one per core).
+    Each process places its own copy of the box (the reference placement)
+    and advances it for 'seconds' of wall time; with several processes the
+    value is the sum of their rates (independent boxes, one per core).
     """
-    from mcac_gb300 import PhysicalModel, init_state
-    pm = PhysicalModel(text=ini_text)
-    snap = init_state(pm).to_snapshot()
-    blob = snap.to_bytes()
-    per = seconds
-    jobs = [(ini_text, blob, per, chunk)] * processes
+    jobs = [(ini_text, seconds, chunk)] * processes
     if processes == 1:
         res = [_worker(jobs[0])]
     else:
@@ -265,6 +273,56 @@ def bench_sample(ini_text: str, seconds: float = 15.0, processes: int = 1, steps
     total_steps = sum(r[0] for r in res)
     value = sum(r[0] / r[1] for r in res)
     return {"value": value, "unit": "MC steps/s", "cores": processes, "kind": "port",
-            "sample": f"{processes} independent copies of the 100k-monomer box from the reference initial state, "
-                      f"~{per:.0f} s of MC steps each ({total_steps} steps in total)",
+            "sample": f"{processes} independent copies of the box from the reference initial state, "
+                      f"~{seconds:.0f} s of MC steps each ({total_steps} steps in total)",
             "host_cpus": os.cpu_count()}
+
+
+def run_windows(ini_text: str, agg_limit_a: int, steps_a: int, steps_b: int, final_limit: int) -> dict:
+    """One box through the two benchmark windows (calcul.cpp:66-281 each).
+
+    Window a: from the initial placement until at most agg_limit_a
+    aggregates are left, steps_a steps are done or a stop criterion of the
+    parameters is met. Window b: from there, the next steps_b steps under the
+    box's own aggregate criterion final_limit (or fewer, if the box stops).
+    Placement is not timed; the steps are (process CPU wall time).
+    """
+    box = OracleBox(ini_text)
+    n0 = box.size()
+    box.set_aggregate_limit(agg_limit_a)
+    t0 = time.perf_counter()
+    sa, _ = box.calcul(max_steps=steps_a)
+    t1 = time.perf_counter()
+    na = int(sa.n_aggregates)
+    box.set_aggregate_limit(final_limit)
+    sb, _ = box.calcul(max_steps=steps_b)
+    t2 = time.perf_counter()
+    out = {"n_aggregates_0": n0, "steps_a": int(sa.steps), "events_a": int(sa.events), "s_a": t1 - t0,
+           "n_aggregates_a": na, "steps_b": int(sb.steps), "events_b": int(sb.events), "s_b": t2 - t1,
+           "n_aggregates_b": int(sb.n_aggregates), "finished": int(sb.finished)}
+    box.close()
+    return out
+
+
+def _window_job(job):
+    k, ini_text, agg_limit_a, steps_a, steps_b, final_limit = job
+    return k, run_windows(ini_text, agg_limit_a, steps_a, steps_b, final_limit)
+
+
+def farm_windows(jobs: list, processes: int, pool=None) -> list:
+    """run_windows over many boxes on 'processes' host processes (a spawn
+    pool: the workers load only this restatement). jobs: (key, ini_text,
+    agg_limit_a, steps_a, steps_b, final_limit), submitted in the given order
+    (largest first keeps the cores busy to the end); returns (key, result)
+    in completion order."""
+    if processes <= 1 and pool is None:
+        return [_window_job(j) for j in jobs]
+    if pool is not None:
+        return list(pool.imap_unordered(_window_job, jobs))
+    with mp.get_context("spawn").Pool(processes) as p:
+        return list(p.imap_unordered(_window_job, jobs))
+
+
+def window_pool(processes: int):
+    """A spawn pool for farm_windows, started before any GPU work."""
+    return mp.get_context("spawn").Pool(processes)

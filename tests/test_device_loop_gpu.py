@@ -281,3 +281,36 @@ def test_batch_loads_host_states_in_place():
     for edit, what in cases:
         with pytest.raises(MCACError, match=what):
             Batch(models[:1], states=[broken(edit)])
+
+
+@pytest.mark.gpu
+def test_split_by_aggregate_count_keeps_trajectories():
+    """A run stopped at an intermediate aggregate count and resumed under the
+    final criterion (mcacg_batch_set_aggregate_limit, the two windows of the
+    ensemble benchmark) is the uninterrupted run, bit for bit."""
+    models = [PhysicalModel(text=small_ini(n, 120 + k, mode="lognormal", disp=1.25, fv=4e-3, nagg=8))
+              for k, n in enumerate([260, 540, 390, 700])]
+    with Batch(models) as b:
+        b.run(max_steps=0, steps_per_launch=5000)
+        ref = b.store_all()
+        ref_st = b.stats()
+    staged = [PhysicalModel(text=small_ini(n, 120 + k, mode="lognormal", disp=1.25, fv=4e-3, nagg=40))
+              for k, n in enumerate([260, 540, 390, 700])]
+    with Batch(staged) as b:
+        b.run(max_steps=0, steps_per_launch=5000)
+        st = b.stats()
+        assert np.all(st["finished"] == 1) and np.all(st["n_aggregates"] <= 40)
+        assert np.all(st["steps"] < ref_st["steps"])
+        b.set_aggregate_limit(8)
+        b.run(max_steps=0, steps_per_launch=5000)
+        st = b.stats()
+        assert np.all(st["finished"] == 1) and np.all(st["status"] == 0)
+        assert np.array_equal(st["steps"], ref_st["steps"])
+        for s1, s2 in zip(b.store_all(), ref):
+            assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64))
+            assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64))
+            assert np.array_equal(s1.members, s2.members)
+        # a limit the boxes already meet leaves them where they are
+        b.set_aggregate_limit(100)
+        b.run(max_steps=0, steps_per_launch=5000)
+        assert np.array_equal(b.stats()["steps"], ref_st["steps"])

@@ -93,9 +93,21 @@ def build_oracle(verbose: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def build_reference(verbose: bool = False) -> Path | None:
-    """The reference's own sources, where present (never on the GPU host)."""
-    ref = Path(os.environ.get("MCAC_REFERENCE", "/root/reference"))
+def reference_dir() -> Path:
+    """The reference's source directory, from the MCAC_REFERENCE environment
+    variable (the golden-vector generators need it; there is no default)."""
+    ref = os.environ.get("MCAC_REFERENCE")
+    if not ref or not (Path(ref) / "src" / "calcul.cpp").exists():
+        raise RuntimeError("set MCAC_REFERENCE to the reference's source directory (the one holding src/calcul.cpp)")
+    return Path(ref)
+
+
+def build_reference(reference: str | Path | None, verbose: bool = False) -> Path | None:
+    """The reference's own sources, from the directory 'reference' when it
+    holds them (the oracle's reference build; skipped when None or absent)."""
+    if reference is None:
+        return None
+    ref = Path(reference)
     if not (ref / "src" / "calcul.cpp").exists() or shutil.which("make") is None:
         return None
     _run(["make", "-s", "-C", str(ROOT), "-f", "oracle/ref.mk", f"REF={ref}", f"-j{os.cpu_count() or 2}"])
@@ -104,10 +116,12 @@ def build_reference(verbose: bool = False) -> Path | None:
     return ORACLE / "_ref"
 
 
-def build_all(verbose: bool = False) -> None:
+def build_all(reference: str | Path | None = None, verbose: bool = False) -> None:
+    """The library, the oracle and, given the reference's source directory,
+    the reference build (default: the MCAC_REFERENCE environment variable)."""
     build_library(verbose)
     build_oracle(verbose)
-    build_reference(verbose)
+    build_reference(reference if reference is not None else os.environ.get("MCAC_REFERENCE"), verbose)
 
 
 if __name__ == "__main__":

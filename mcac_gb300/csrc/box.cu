@@ -570,6 +570,8 @@ size_t carve_fixed(DevBox &b, char *arena) {
         b.pair_tmp_d = pairs ? b.pair_d + pc : nullptr;
     }
     take((void **)&b.row_cnt, sizeof(int) * (std::max(ns, nslots) + 2));
+    // 64 B per sphere: the merge sums' per-sphere terms, and the merge's
+    // cell-grid pair search (at most 52 B per merged sphere + 4, merge.cuh)
     take((void **)&b.work, sizeof(double) * 8 * ns);
     take((void **)&b.counters, sizeof(int) * 8);
     const size_t nc1 = nslots + 1;

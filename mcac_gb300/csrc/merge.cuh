@@ -291,6 +291,9 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
         // 8000-sphere aggregates needs 10^8 pair tests otherwise).
         // Scratch after the n float4 of relf: cell coordinates (int4, n),
         // bucket counts/starts (2^k + 1 >= 2n + 1), sorted sphere indices (n).
+        // With nb < 4n that is 16n + 16n + 4(nb + 1) + 4n <= 52n + 4 bytes,
+        // inside the work area of 8 doubles (64 B) per sphere of the box
+        // (n <= ns); a larger carve needs a larger work area.
         int4 *cellc = reinterpret_cast<int4 *>(relf + n);
         int nb = 1;
         while (nb < 2 * n) nb <<= 1;

@@ -12,7 +12,9 @@
 # DEBUG_MCAC is not defined (it would force seed 0).
 #
 # Usage: make -f oracle/ref.mk REF=/path/to/reference   (run from the repo root)
-REF ?= /root/reference
+ifndef REF
+$(error REF must name the reference's source directory)
+endif
 OUT := oracle/_ref
 CXX ?= g++
 CXXFLAGS := -std=gnu++17 -O2 -frounding-math -ffp-contract=off -fopenmp -w \

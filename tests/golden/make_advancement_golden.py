@@ -12,7 +12,8 @@ the parameter files that made them (advancement_<case>.ini).
 tests/test_advancement_gpu.py compares the host-driven loop's file with them
 byte for byte.
 
-Needs the reference sources and a C++ compiler; run from the repository root:
+Needs the reference sources (MCAC_REFERENCE names their directory) and a C++
+compiler; run from the repository root:
 
     python tests/golden/make_advancement_golden.py
 """
@@ -71,7 +72,7 @@ def ini_text(name: str) -> str:
 
 
 def main() -> int:
-    build.build_reference()
+    build.build_reference(build.reference_dir())
     with tempfile.TemporaryDirectory(dir=ROOT) as tmp:
         for name in CASES:
             work = Path(tmp) / name

@@ -20,7 +20,7 @@ compressed .npz files:
                     properties) for the reference's validation parameter
                     files and for the configurations above.
 
-Needs the reference sources (default /root/reference, or MCAC_REFERENCE) and
+Needs the reference sources (MCAC_REFERENCE names their directory) and
 a C++ compiler; run from the repository root:
 
     python tests/golden/make_golden.py
@@ -156,7 +156,7 @@ def parse_meta(text: str) -> dict:
 
 
 def main() -> int:
-    ref = build.build_reference(verbose=True)
+    ref = build.build_reference(build.reference_dir(), verbose=True)
     if ref is None or not HARNESS.exists():
         print("reference sources not found; nothing generated", file=sys.stderr)
         return 1
@@ -211,7 +211,7 @@ def main() -> int:
 
         # ---- PhysicalModel-derived values
         meta = {}
-        refdir = Path(os.environ.get("MCAC_REFERENCE", "/root/reference"))
+        refdir = build.reference_dir()
         inis = {p.stem: p.read_text() for p in sorted((refdir / "validation").glob("params_*.ini"))}
         # examples/classic.ini is left out: it enables interaction potentials
         # with an external table, a path this library does not cover.

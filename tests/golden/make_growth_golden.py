@@ -11,7 +11,8 @@ stores, per box, the final physical time, the mean sphere radius and the
 (monomers, Rg/dp) pairs of the final aggregates. The device loop is compared
 with these distributions (tests/test_growth_gpu.py).
 
-Needs the reference sources and a C++ compiler; run from the repository root:
+Needs the reference sources (MCAC_REFERENCE names their directory) and a C++
+compiler; run from the repository root:
 
     python tests/golden/make_growth_golden.py [growth_ensemble.npz] [growth_individual.npz]
 """
@@ -66,7 +67,7 @@ def run_set(individual: bool, name: str) -> None:
 
 
 def main() -> int:
-    build.build_reference()
+    build.build_reference(build.reference_dir())
     sets = {"growth_ensemble.npz": False, "growth_individual.npz": True}
     for name, individual in sets.items():
         if len(sys.argv) > 1 and name not in sys.argv[1:]:

@@ -14,7 +14,8 @@ final aggregate its monomer count, Rg/dp, and its volume and surface over
 the plain sums of its spheres' (the corrections' effect). The device loop is
 compared with these distributions (tests/test_volsurf_gpu.py).
 
-Needs the reference sources and a C++ compiler; run from the repository root:
+Needs the reference sources (MCAC_REFERENCE names their directory) and a C++
+compiler; run from the repository root:
 
     python tests/golden/make_volsurf_golden.py
 """
@@ -61,7 +62,7 @@ def box_stats(snap: Snapshot):
 
 
 def main() -> int:
-    build.build_reference()
+    build.build_reference(build.reference_dir())
     for method in ("alphas", "caps"):
         with tempfile.TemporaryDirectory(dir=ROOT) as tmp:
             work = Path(tmp)

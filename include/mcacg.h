@@ -256,15 +256,19 @@ int mcacg_distance_to_next_contacts(mcacg_box *box, int32_t n, const int64_t *so
  * gave the device to its own memory pool, one that must not take the
  * device-wide synchronisation of cudaMalloc/cudaFree, one under a fixed
  * memory budget). All device scratch is one 32 MiB __device__ array of the
- * library. At most 65536 queries per call (MCACG_ERR_CAPACITY beyond); a box
- * whose per-block candidate lists (44 bytes per aggregate slot) do not fit
- * it is refused with MCACG_ERR_CAPACITY. The first call on each device, with
- * that device current, looks the array up (cudaGetSymbolAddress); make it
- * before any stream capture begins. Each call zeroes its query counter and
- * status word, copies the queries in, runs on the box's stream and waits for
- * it. The array is shared by all boxes on a device: overlapping calls would
- * race on it, so the library serialises them with a lock. No counterpart in
- * the reference. */
+ * library. At most 65536 queries per call (MCACG_ERR_CAPACITY beyond); each
+ * thread block keeps up to 16384 refined sphere pairs, as the allocating
+ * entry point does (a query refining more fails with MCACG_ERR_CAPACITY on
+ * both); a box whose per-block lists (44 bytes per aggregate slot plus
+ * 384 KiB of refined pairs) do not fit the array is refused with
+ * MCACG_ERR_CAPACITY. Every call looks the array up on the current device
+ * (cudaGetSymbolAddress, which allocates nothing); the first call on a
+ * device also loads the library's module there, so make it before any
+ * stream capture begins. Each call zeroes its query counter and status
+ * word, copies the queries in, runs on the box's stream and waits for it.
+ * The array is shared by all boxes on a device: overlapping calls would race
+ * on it, so the library serialises them with a lock. No counterpart in the
+ * reference. */
 int mcacg_distance_to_next_contacts_static(mcacg_box *box, int32_t n, const int64_t *sources,
                                            const double *directions, const double *distances, mcacg_contact *out);
 /* Aggregate::translate (aggregat.hpp:108, aggregat.cpp:148-161). */

@@ -321,10 +321,27 @@ int mcacg_distance_to_next_contacts_static(mcacg_box *box, int32_t n, const int6
     return guarded([&] {
         if (!box || n < 0 || (n > 0 && (!sources || !directions || !distances || !out)))
             return fail(MCACG_ERR_BAD_ARGUMENT, "null argument or negative count");
+        // labels to slots here, on the host, from the box's live-slot list
+        const mcacg::HostBox &hb = *box->impl;
+        std::vector<int> slots(static_cast<size_t>(n));
+        for (int k = 0; k < n; ++k) {
+            if (sources[k] < 0 || sources[k] >= int64_t(hb.size()))
+                return fail(MCACG_ERR_BAD_ARGUMENT, "label out of range in query " + std::to_string(k));
+            slots[size_t(k)] = hb.slot_of(sources[k]);
+        }
         std::string err;
-        return finish(mcacg::query_batch_static(box->impl->device(), box->impl->size(), n, sources, directions,
-                                                distances, out, &err),
-                      err);
+        const int rc = mcacg::query_batch_static(box->impl->device(), n, slots.data(), directions, distances, out, &err);
+        for (int k = 0; k < n && rc == 0; ++k) {
+            mcacg_contact &c = out[k];
+            if (c.moving_sphere >= 0) {
+                c.moving_aggregate = sources[k];
+                c.other_aggregate = hb.label_of(int(c.other_aggregate));  // the kernel wrote the slot
+            } else {
+                c.moving_aggregate = -1;
+                c.other_aggregate = -1;
+            }
+        }
+        return finish(rc, err);
     });
 }
 

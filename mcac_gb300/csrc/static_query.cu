@@ -11,15 +11,21 @@
 // the module. The library calls no cudaMalloc, cudaFree or other allocating
 // routine on this path.
 //
-// Limits: at most kStaticMaxQueries queries per call; a box whose candidate
-// lists (44 bytes per aggregate slot per block) do not fit the array even
-// for one block is refused; fewer blocks run concurrently than on the
-// allocating path when the box is large.
+// Limits: at most kStaticMaxQueries queries per call; each thread block
+// keeps kStaticSurvivors refined sphere pairs in the array, as many as the
+// allocating path keeps, so a query fails with MCACG_ERR_CAPACITY here
+// exactly when it does there; a box whose candidate lists (44 bytes per
+// aggregate slot) and survivor lists (384 KiB) do not fit the array for one
+// block is refused; fewer blocks run concurrently than on the allocating
+// path (about 32 MiB / (384 KiB + 44 B x slots)).
 //
-// Set-up: the first call on each device looks up the array's address with
-// cudaGetSymbolAddress, with that device current, and keeps it; make that
-// first call before any stream capture begins. Every call then clears the
-// two words that must start at zero (the query counter and the status) with
+// Set-up: every call looks up the array's address on the current device
+// with cudaGetSymbolAddress (it allocates nothing, and a context made again
+// after a device reset gets the new address); the first call on a device
+// also loads the module, so make it before any stream capture begins. The
+// labels are turned into slots on the host before the call and the hit
+// slot back into a label after it. Every call then clears the two words
+// that must start at zero (the query counter and the status) with
 // cudaMemsetAsync, copies the queries in, runs the kernel, copies the
 // results out and waits for its stream.
 //
@@ -41,8 +47,7 @@ namespace mcacg {
 
 constexpr size_t kStaticScratchBytes = size_t(32) << 20;  // 32 MiB
 constexpr int kStaticMaxQueries = 1 << 16;
-constexpr int kStaticSurvivors = 1 << 12;  // HBM survivors per block
-constexpr int kStaticMaxDevices = 64;
+constexpr int kStaticSurvivors = 1 << 14;  // HBM survivors per block, as on the allocating path
 
 namespace {
 
@@ -50,7 +55,7 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 
 struct StaticScratch {
     int *header;  // [0] next query, [1] first failing status: zero at launch
-    const long long *sources;
+    const int *slots;
     const double *dirs;
     const double *dists;
     mcacg_contact *out;
@@ -60,49 +65,10 @@ struct StaticScratch {
     size_t o_key, o_slot, o_order, o_prefix, o_res, o_ij, o_surv, o_sres;
 };
 
-// Slot of the live aggregate with the given label: labels are the ranks of
-// the live slots in slot order. Block-wide; every thread gets the answer.
-__device__ int block_slot_of_label(const DevBox &b, long long label, int *warp_tmp, int *found) {
-    const int NT = blockDim.x, tid = threadIdx.x;
-    const int chunk = (b.nslots + NT - 1) / NT;
-    const int lo = min(b.nslots, tid * chunk), hi = min(b.nslots, lo + chunk);
-    int c = 0;
-    for (int i = lo; i < hi; ++i) c += b.agg_n[i] > 0;
-    if (tid == 0) *found = -1;
-    int total = 0;
-    const int before = block_exclusive_scan(c, warp_tmp, total);
-    if (label >= before && label < before + c) {
-        long long r = before;
-        for (int i = lo; i < hi; ++i) {
-            if (b.agg_n[i] > 0) {
-                if (r == label) {
-                    *found = i;
-                    break;
-                }
-                ++r;
-            }
-        }
-    }
-    __syncthreads();
-    const int slot = *found;
-    __syncthreads();
-    return slot;
-}
-
-// Number of live slots below 'slot' (the label of a live slot).
-__device__ int block_live_before(const DevBox &b, int slot, int *warp_tmp) {
-    int c = 0;
-    for (int i = threadIdx.x; i < slot; i += blockDim.x) c += b.agg_n[i] > 0;
-    int total = 0;
-    block_exclusive_scan(c, warp_tmp, total);
-    return total;
-}
-
 __global__ void __launch_bounds__(kQueryThreads) k_query_static(DevBox b, StaticScratch s, int n) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     QuerySmem &sm = *reinterpret_cast<QuerySmem *>(smem_raw);
-    __shared__ int q_cur, found;
-    __shared__ int warp_tmp[32];
+    __shared__ int q_cur;
     char *mine = s.blocks + size_t(blockIdx.x) * s.block_bytes;
     b.cand_db = reinterpret_cast<double *>(mine);
     b.cand_key = reinterpret_cast<long long *>(mine + s.o_key);
@@ -119,24 +85,19 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_static(DevBox b, Static
         __syncthreads();
         const int q = q_cur;
         if (q >= n) break;  // block-uniform
-        const long long label = s.sources[q];
-        const int slot = block_slot_of_label(b, label, warp_tmp, &found);
+        const int slot = s.slots[q];
+        // the host fills in the labels: moving_aggregate from the query,
+        // other_aggregate from the hit slot written here
         mcacg_contact c{CUDART_INF, -1, -1, -1, -1};
-        if (slot < 0) {
-            if (threadIdx.x == 0) atomicCAS(&s.header[1], 0, int(ST_BAD_ARGUMENT));
-        } else {
-            block_query(b, slot, Vec3{s.dirs[3 * q], s.dirs[3 * q + 1], s.dirs[3 * q + 2]}, s.dists[q], sm);
-            __syncthreads();
-            const QueryOut o = sm.out;
-            c.distance = o.distance;
-            if (o.status != ST_OK && threadIdx.x == 0) atomicCAS(&s.header[1], 0, o.status);
-            if (o.moving_sphere >= 0) {
-                const int other = block_live_before(b, o.other_slot, warp_tmp);
-                c.moving_sphere = o.moving_sphere;
-                c.other_sphere = o.other_sphere;
-                c.moving_aggregate = label;
-                c.other_aggregate = other;
-            }
+        block_query(b, slot, Vec3{s.dirs[3 * q], s.dirs[3 * q + 1], s.dirs[3 * q + 2]}, s.dists[q], sm);
+        __syncthreads();
+        const QueryOut o = sm.out;
+        c.distance = o.distance;
+        if (o.status != ST_OK && threadIdx.x == 0) atomicCAS(&s.header[1], 0, o.status);
+        if (o.moving_sphere >= 0) {
+            c.moving_sphere = o.moving_sphere;
+            c.other_sphere = o.other_sphere;
+            c.other_aggregate = o.other_slot;
         }
         if (threadIdx.x == 0) s.out[q] = c;
         __syncthreads();
@@ -152,12 +113,11 @@ bool ok_or(cudaError_t e, std::string *err, const char *what) {
 size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
 std::mutex g_static_lock;
-void *g_static_ptr[kStaticMaxDevices] = {};
 
 }  // namespace
 
-int query_batch_static(DeviceBox &dev, int n_alive, int n, const int64_t *sources, const double *dirs,
-                       const double *dists, mcacg_contact *out, std::string *err) {
+int query_batch_static(DeviceBox &dev, int n, const int *slots, const double *dirs, const double *dists,
+                       mcacg_contact *out, std::string *err) {
     if (n < 0) {
         if (err) *err = "negative query count";
         return ST_BAD_ARGUMENT;
@@ -167,24 +127,18 @@ int query_batch_static(DeviceBox &dev, int n_alive, int n, const int64_t *source
         return ST_CAPACITY;
     }
     for (int k = 0; k < n; ++k)
-        if (sources[k] < 0 || sources[k] >= n_alive) {
-            if (err) *err = "label out of range in query " + std::to_string(k);
+        if (slots[k] < 0 || slots[k] >= dev.nslots()) {
+            if (err) *err = "slot out of range in query " + std::to_string(k);
             return ST_BAD_ARGUMENT;
         }
     if (n == 0) return ST_OK;
     std::lock_guard<std::mutex> hold(g_static_lock);
     int device = 0;
     if (!ok_or(cudaGetDevice(&device), err, "cudaGetDevice")) return ST_CUDA;
-    if (device < 0 || device >= kStaticMaxDevices) {
-        if (err) *err = "device index beyond the static-scratch table";
-        return ST_CAPACITY;
-    }
-    if (!g_static_ptr[device]) {
-        void *p = nullptr;
-        if (!ok_or(cudaGetSymbolAddress(&p, g_static_scratch), err, "cudaGetSymbolAddress")) return ST_CUDA;
-        g_static_ptr[device] = p;
-    }
-    char *base = static_cast<char *>(g_static_ptr[device]);
+    // the array's address in the current context (no allocation)
+    void *addr = nullptr;
+    if (!ok_or(cudaGetSymbolAddress(&addr, g_static_scratch), err, "cudaGetSymbolAddress")) return ST_CUDA;
+    char *base = static_cast<char *>(addr);
     const DevBox &b = *static_cast<const DevBox *>(dev.devbox_ptr());
     cudaStream_t stream = static_cast<cudaStream_t>(dev.stream());
 
@@ -194,7 +148,7 @@ int query_batch_static(DeviceBox &dev, int n_alive, int n, const int64_t *source
     const size_t o_header = off;
     off += 256;
     const size_t o_src = off;
-    off += round256(sizeof(int64_t) * size_t(n));
+    off += round256(sizeof(int) * size_t(n));
     const size_t o_dirs = off;
     off += round256(3 * sizeof(double) * size_t(n));
     const size_t o_dists = off;
@@ -238,7 +192,7 @@ int query_batch_static(DeviceBox &dev, int n_alive, int n, const int64_t *source
     size_t blocks = size_t(std::max(1, per_sm)) * size_t(std::max(1, n_sm));
     blocks = std::min(blocks, std::min(fit, size_t(n)));
     s.header = reinterpret_cast<int *>(base + o_header);
-    s.sources = reinterpret_cast<const long long *>(base + o_src);
+    s.slots = reinterpret_cast<const int *>(base + o_src);
     s.dirs = reinterpret_cast<const double *>(base + o_dirs);
     s.dists = reinterpret_cast<const double *>(base + o_dists);
     s.out = reinterpret_cast<mcacg_contact *>(base + o_out);
@@ -246,9 +200,8 @@ int query_batch_static(DeviceBox &dev, int n_alive, int n, const int64_t *source
 
     int status = 0;
     bool ok = ok_or(cudaMemsetAsync(base + o_header, 0, 2 * sizeof(int), stream), err, "clear counter") &&
-              ok_or(cudaMemcpyAsync(base + o_src, sources, sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice,
-                                    stream),
-                    err, "upload sources") &&
+              ok_or(cudaMemcpyAsync(base + o_src, slots, sizeof(int) * size_t(n), cudaMemcpyHostToDevice, stream),
+                    err, "upload slots") &&
               ok_or(cudaMemcpyAsync(base + o_dirs, dirs, 3 * sizeof(double) * size_t(n), cudaMemcpyHostToDevice,
                                     stream),
                     err, "upload directions") &&

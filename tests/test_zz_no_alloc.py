@@ -1,10 +1,13 @@
 """The batched contact query that allocates no device memory.
 
 mcacg_distance_to_next_contacts_static keeps every device buffer in a
-file-scope array. Called through the C-ABI twice in a row, it must give the
-same answers, byte for byte, as mcacg_distance_to_next_contacts on the same
-box; requests beyond its fixed limits must fail with a clear error. The file
-is named to be collected last, and it passes alone in a fresh process too.
+file-scope array, for callers that cannot allocate device memory while they
+run. Called through the C-ABI twice in a row, it must give the same answers,
+byte for byte, as mcacg_distance_to_next_contacts on the same box; it must
+leave the device's free memory unchanged, also on boxes that the allocating
+entry point never touched; requests beyond its fixed limits must fail with a
+clear error. The file is named to be collected last, and it passes alone in
+a fresh process too.
 """
 import ctypes as C
 
@@ -40,6 +43,33 @@ def test_static_scratch_queries_equal_allocating_queries():
 
 
 @pytest.mark.gpu
+def test_static_scratch_allocates_nothing():
+    """After the first call on the device (which loads the module holding
+    the array), calls on fresh boxes and on used ones leave the device's free
+    memory as it was; the allocating entry point runs only afterwards, as
+    the check of the answers."""
+    import torch
+    case = contact_search_case(n_spheres=20_000, n_aggregates=400, n_queries=2000, seed=23)
+    with AggregatList(case.model, case.state) as a, AggregatList(case.model, case.state) as b:
+        first = static_queries(a, case.sources, case.directions, case.distances)  # set-up call on this device
+        torch.cuda.synchronize()
+        torch.cuda.mem_get_info()
+        free0, _ = torch.cuda.mem_get_info()
+        outs = [static_queries(b, case.sources, case.directions, case.distances) for _ in range(3)]
+        outs += [static_queries(a, case.sources, case.directions, 3.0 * case.distances) for _ in range(2)]
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0, (free0, free1)
+        for o in outs[:3]:
+            assert np.array_equal(o.view(np.uint8), first.view(np.uint8))
+        assert np.array_equal(outs[3].view(np.uint8), outs[4].view(np.uint8))
+        ref, _ = b.distance_to_next_contacts(case.sources, case.directions, case.distances)
+        assert np.array_equal(first.view(np.uint8), ref.view(np.uint8))
+        ref3, _ = a.distance_to_next_contacts(case.sources, case.directions, 3.0 * case.distances)
+        assert np.array_equal(outs[3].view(np.uint8), ref3.view(np.uint8))
+
+
+@pytest.mark.gpu
 def test_static_scratch_limits():
     case = contact_search_case(n_spheres=5_000, n_aggregates=100, n_queries=4, seed=22)
     with AggregatList(case.model, case.state) as box:
@@ -57,7 +87,8 @@ def test_static_scratch_limits():
 
 @pytest.mark.gpu
 def test_static_scratch_refuses_a_box_too_large_for_it():
-    # 1,000,000 aggregate slots need 44 MB of candidate lists per block
+    # 1,000,000 aggregate slots need 44 MB of candidate lists per block, more
+    # than the whole 32 MiB array
     from mcac_gb300 import PhysicalModel, synthetic_state
     from mcac_gb300.workloads import contact_search_ini
     pm = PhysicalModel(text=contact_search_ini(1_000_000, seed=3, sigma_geo=1.25, volume_fraction=1e-3))

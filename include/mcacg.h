@@ -363,6 +363,19 @@ int mcacg_batch_run_timed(mcacg_batch *batch, double wall_ms);
  * stage of its runs (say, down to 100 aggregates) and then the rest. No
  * counterpart in the reference. */
 int mcacg_batch_set_aggregate_limit(mcacg_batch *batch, int64_t limit);
+/* Diagnostics of the device loop's random draws (no counterpart in the
+ * reference; they check the loop's statistics against the reference's
+ * AggregatList::pick_random, aggregat_list.cpp:59-66, 124-141, and
+ * random_direction, tools.cpp:82-89).
+ * mcacg_batch_pick_histogram: at least n_picks picks (*picks_done gets the
+ * number) from box 'box''s current pick tree by the loop's own descent,
+ * nothing moved, drawn from rand() streams seeded seed, seed + 1, ...;
+ * counts[label] for the live aggregates (*n_labels of them, at most
+ * 'capacity'). mcacg_draw_directions: n unit vectors by the loop's direction
+ * draw, out[3k..3k+2] (stream of thread t seeded seed + t). */
+int mcacg_batch_pick_histogram(mcacg_batch *batch, int32_t box, int64_t n_picks, uint32_t seed, int64_t *counts,
+                               int64_t capacity, int64_t *n_labels, int64_t *picks_done);
+int mcacg_draw_directions(int64_t n, uint32_t seed, double *out);
 /* Per-box counters since creation (arrays of n_boxes). */
 int mcacg_batch_stats(mcacg_batch *batch, mcacg_run_stats *stats);
 int mcacg_batch_size(const mcacg_batch *batch, int32_t *n_boxes);

@@ -305,6 +305,13 @@ def set_merge_grid_min(n_spheres: int) -> int:
     return prev.value
 
 
+def draw_directions(n: int, seed: int = 1) -> np.ndarray:
+    """n unit vectors from the device loop's direction draw (n x 3)."""
+    out = np.zeros((int(n), 3), dtype=np.float64)
+    check(lib().mcacg_draw_directions(int(n), int(seed) & 0xffffffff, ptr(out, C.c_double)))
+    return out
+
+
 def device_count() -> int:
     n = C.c_int()
     check(lib().mcacg_device_count(C.byref(n)))
@@ -388,6 +395,17 @@ class Batch:
         boxes that stopped without an error continue at the next run (each
         re-checks all of its criteria first)."""
         check(lib().mcacg_batch_set_aggregate_limit(self._b, int(limit)))
+
+    def pick_histogram(self, box: int, n_picks: int, seed: int = 1) -> tuple[np.ndarray, int]:
+        """Counts per label of n_picks (at least) picks from box 'box''s
+        current pick tree by the device loop's own descent (nothing moves),
+        and the number of picks made."""
+        na = self.box_sizes(box)[1]
+        counts = np.zeros(max(na, 1), dtype=np.int64)
+        n_lab, done = C.c_int64(), C.c_int64()
+        check(lib().mcacg_batch_pick_histogram(self._b, int(box), int(n_picks), int(seed) & 0xffffffff,
+                                               ptr(counts, C.c_int64), len(counts), C.byref(n_lab), C.byref(done)))
+        return counts[:n_lab.value], done.value
 
     def stats(self) -> np.ndarray:
         n = len(self.models)

@@ -94,6 +94,50 @@ __global__ void k_set_aggregate_limit(BoxRun *runs, int n, long long limit) {
     if (st != nullptr && st->status == ST_OK) st->finished = 0;
 }
 
+// Diagnostics of the device loop's random draws (one warp per block): the
+// pick's descent of box 'box''s sum tree for per_warp targets per warp, each
+// warp with its own rand() stream (seed + block), counted per slot.
+__global__ void __launch_bounds__(32) k_pick_histogram(const BoxRun *runs, int box, long long per_warp,
+                                                       unsigned seed, unsigned long long *counts) {
+    __shared__ TreeCache cache;
+    const BoxRun &R = runs[box];
+    tree_cache_load(R, cache);
+    RandStream rng;
+    if (threadIdx.x == 0) rng.seed(seed + blockIdx.x);
+    const unsigned long long total = R.st->tree_total;
+    for (long long k = 0; k < per_warp; ++k) {
+        unsigned long long t = 0;
+        if (threadIdx.x == 0) t = pick_target(rng, total);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        const int slot = tree_sample(R, cache, t);
+        if (threadIdx.x == 0 && slot >= 0 && slot < R.box.nslots) atomicAdd(&counts[slot], 1ULL);
+    }
+}
+// The counts of the live slots in slot order, i.e. by label (one thread).
+__global__ void k_counts_by_label(const int *agg_n, int nslots, const unsigned long long *by_slot,
+                                  long long *by_label, int *n_live) {
+    int r = 0;
+    for (int s = 0; s < nslots; ++s)
+        if (agg_n[s] > 0) by_label[r++] = (long long)by_slot[s];
+    *n_live = r;
+}
+// The device loop's directions: thread t draws directions t, t + T, t + 2T,
+// ... (T threads in all) from its own rand() stream (seed + t).
+__global__ void k_directions(long long n, unsigned seed, double *out) {
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    RandStream rng;
+    rng.seed(seed + unsigned(t));
+    for (long long i = t; i < n; i += T) {
+        double d[3];
+        draw_direction(rng, d);
+        out[3 * i] = d[0];
+        out[3 * i + 1] = d[1];
+        out[3 * i + 2] = d[2];
+    }
+}
+
 // The pick trees of n boxes from their time steps, one block per box
 // (block_tree_build); the total weight goes to each box's loop state.
 __global__ void __launch_bounds__(256) k_tree_build(const BoxRun *runs, int n) {
@@ -543,6 +587,56 @@ int BatchRunner::run_timed(double wall_ms, std::string *err) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
+}
+
+int BatchRunner::pick_histogram(int box, int64_t n_picks, uint32_t seed, std::vector<int64_t> *by_label,
+                                int64_t *picks_done, std::string *err) {
+    if (box < 0 || box >= size() || n_picks <= 0) {
+        if (err) *err = "box out of range or no picks asked";
+        return ST_BAD_ARGUMENT;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    const DevBox &b = *static_cast<const DevBox *>(boxes_[size_t(box)]->devbox_ptr());
+    const int nslots = b.nslots;
+    constexpr int kWarps = 256;
+    const long long per_warp = (n_picks + kWarps - 1) / kWarps;
+    void *mem = nullptr;
+    const size_t bytes = sizeof(unsigned long long) * size_t(nslots) * 2 + 256;
+    if (!ok_cuda(cudaMalloc(&mem, bytes), err, "cudaMalloc")) return ST_CUDA;
+    auto *by_slot = static_cast<unsigned long long *>(mem);
+    auto *lab = reinterpret_cast<long long *>(by_slot + nslots);
+    int *n_live_dev = reinterpret_cast<int *>(lab + nslots);
+    int n_live = 0;
+    by_label->assign(size_t(nslots), 0);
+    bool ok = ok_cuda(cudaMemsetAsync(by_slot, 0, sizeof(unsigned long long) * size_t(nslots), s), err, "memset");
+    if (ok) {
+        k_pick_histogram<<<kWarps, 32, 0, s>>>(static_cast<const BoxRun *>(runs_dev_), box, per_warp, seed, by_slot);
+        k_counts_by_label<<<1, 1, 0, s>>>(b.agg_n, nslots, by_slot, lab, n_live_dev);
+        ok = ok_cuda(cudaGetLastError(), err, "k_pick_histogram") &&
+             ok_cuda(cudaMemcpyAsync(by_label->data(), lab, sizeof(long long) * size_t(nslots), cudaMemcpyDeviceToHost,
+                                     s),
+                     err, "download") &&
+             ok_cuda(cudaMemcpyAsync(&n_live, n_live_dev, sizeof(int), cudaMemcpyDeviceToHost, s), err, "download") &&
+             ok_cuda(cudaStreamSynchronize(s), err, "k_pick_histogram");
+    }
+    cudaFree(mem);
+    if (!ok) return ST_CUDA;
+    by_label->resize(size_t(n_live));
+    *picks_done = per_warp * kWarps;
+    return ST_OK;
+}
+
+int BatchRunner::draw_directions(int64_t n, uint32_t seed, double *out, std::string *err) {
+    if (n <= 0) return ST_OK;
+    void *mem = nullptr;
+    if (!ok_cuda(cudaMalloc(&mem, sizeof(double) * 3 * size_t(n)), err, "cudaMalloc")) return ST_CUDA;
+    const long long threads = std::min<long long>(n, 1 << 16);
+    k_directions<<<unsigned((threads + 255) / 256), 256>>>(n, seed, static_cast<double *>(mem));
+    const bool ok = ok_cuda(cudaGetLastError(), err, "k_directions") &&
+                    ok_cuda(cudaMemcpy(out, mem, sizeof(double) * 3 * size_t(n), cudaMemcpyDeviceToHost), err,
+                            "download");
+    cudaFree(mem);
+    return ok ? ST_OK : ST_CUDA;
 }
 
 int BatchRunner::set_aggregate_limit(int64_t limit, std::string *err) {

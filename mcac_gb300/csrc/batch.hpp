@@ -57,6 +57,15 @@ class BatchRunner {
     // stopped without an error are re-armed and re-check all their criteria
     // before their next step.
     int set_aggregate_limit(int64_t limit, std::string *err);
+    // Diagnostics of the loop's random draws. pick_histogram: at least n_picks
+    // picks of box 'box''s current pick tree (nothing moves; 256 warps with
+    // rand() streams seeded seed, seed + 1, ...), counted per label;
+    // *picks_done gets the picks made. draw_directions: n directions of the
+    // loop's direction draw (thread t's stream seeded seed + t) into host
+    // memory, 3 doubles each.
+    int pick_histogram(int box, int64_t n_picks, uint32_t seed, std::vector<int64_t> *by_label,
+                       int64_t *picks_done, std::string *err);
+    static int draw_directions(int64_t n, uint32_t seed, double *out, std::string *err);
     int download(int box, HostState *st, std::string *err);
     // Physical time of every box.
     int times(std::vector<double> *out, std::string *err);

@@ -742,6 +742,36 @@ int mcacg_batch_set_aggregate_limit(mcacg_batch *batch, int64_t limit) {
     });
 }
 
+int mcacg_batch_pick_histogram(mcacg_batch *batch, int32_t box, int64_t n_picks, uint32_t seed, int64_t *counts,
+                               int64_t capacity, int64_t *n_labels, int64_t *picks_done) {
+    return guarded([&] {
+        if (!batch || !counts || !n_labels || !picks_done) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        std::vector<int64_t> by_label;
+        std::string err;
+        int64_t done = 0;
+        const int rc = batch->impl->pick_histogram(box, n_picks, seed, &by_label, &done, &err);
+        if (rc != 0) return finish(rc, err);
+        if (int64_t(by_label.size()) > capacity) return fail(MCACG_ERR_BAD_ARGUMENT, "counts array too small");
+        std::copy(by_label.begin(), by_label.end(), counts);
+        *n_labels = int64_t(by_label.size());
+        *picks_done = done;
+        return 0;
+    });
+}
+
+int mcacg_draw_directions(int64_t n, uint32_t seed, double *out) {
+    return guarded([&] {
+        if (n < 0 || (n > 0 && !out)) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument or negative count");
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count < 1) {
+            cudaGetLastError();
+            return fail(MCACG_ERR_NO_DEVICE, "no CUDA device");
+        }
+        std::string err;
+        return finish(mcacg::BatchRunner::draw_directions(n, seed, out, &err), err);
+    });
+}
+
 int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads) {
     return guarded([&] {
         if (!batch || !threads) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");

@@ -171,6 +171,34 @@ __device__ inline int tree_sample(const BoxRun &R, const TreeCache &c, unsigned 
     return node;
 }
 
+// The pick's target in the tree's fixed point from one rand() value r:
+// floor(total * r / 2^31), below the total.
+__device__ __forceinline__ unsigned long long pick_target(RandStream &rng, unsigned long long total) {
+    const unsigned long long r = static_cast<unsigned long long>(rng.next_int());
+    return (__umul64hi(r, total) << 33) | ((r * total) >> 31);
+}
+
+// random_direction (tools.cpp:82-89): theta = 2 pi u1, phi = acos(1 - 2 u2),
+// from two rand() values. cos(phi) is 1 - 2 u2 itself and sin(phi) =
+// 2 sqrt(u2 (1 - u2)). The angles are drawn in FP32 (the device loop follows
+// the reference statistically; FP64 is scarce on this GPU) and the vector is
+// brought to unit length in FP64 by one Newton step on its norm: with
+// |d|^2 = 1 + e, e ~ 1e-7, the factor 1.5 - 0.5 |d|^2 leaves
+// |d| - 1 ~ 3e^2/8 < 1e-13, far inside the 1e-10 contact tolerance of the
+// merge.
+__device__ __forceinline__ void draw_direction(RandStream &rng, double d[3]) {
+    const float u1 = rng.uniform_f(), u2 = rng.uniform_f();
+    const float cpf = 1.f - 2.f * u2;
+    const float spf = 2.f * sqrtf(u2 * (1.f - u2));
+    float sth, cth;
+    sincospif(2.f * u1, &sth, &cth);
+    const double dx = double(spf * cth), dy = double(spf * sth), dz = double(cpf);
+    const double k = 1.5 - 0.5 * (dx * dx + dy * dy + dz * dz);
+    d[0] = dx * k;
+    d[1] = dy * k;
+    d[2] = dz * k;
+}
+
 // The fixed-point weight of a slot with this time step (live slots only).
 __device__ __forceinline__ unsigned long long tree_weight(const RunState &st, double time_step) {
     const double w = fmin((1.0 / time_step) * st.tree_scale, double(kTreeHeadroom));
@@ -615,12 +643,7 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
         // expensive steps does not hold the launch (and the other boxes,
         // which wait for it) past the cap
         if (!sm.stop && sm.deadline != 0ULL && global_ns() >= sm.deadline) sm.stop = 1;
-        if (!sm.stop) {
-            // the target: floor(total * rand() / 2^31), below the total
-            const unsigned long long total = st.tree_total;
-            const unsigned long long r = static_cast<unsigned long long>(st.rng.next_int());
-            sm.t_pick = (__umul64hi(r, total) << 33) | ((r * total) >> 31);
-        }
+        if (!sm.stop) sm.t_pick = pick_target(st.rng, st.tree_total);
     }
     __syncthreads();
     if (sm.stop) return false;
@@ -636,24 +659,7 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
             sm.dt = st.inv_weight;
             sm.full = A(b, AGG_LPM, slot);
             sm.dt_indiv = A(b, AGG_TIME_STEP, slot);
-            // random_direction (tools.cpp:82-89): theta = 2 pi u1, phi =
-            // acos(1 - 2 u2). cos(phi) is 1 - 2 u2 itself and sin(phi) =
-            // 2 sqrt(u2 (1 - u2)). The angles are drawn in FP32 (the device
-            // loop follows the reference statistically; FP64 is scarce on
-            // this GPU) and the vector is brought to unit length in FP64 by
-            // one Newton step on its norm: with |d|^2 = 1 + e, e ~ 1e-7, the
-            // factor 1.5 - 0.5 |d|^2 leaves |d| - 1 ~ 3e^2/8 < 1e-13, far
-            // inside the 1e-10 contact tolerance of the merge.
-            const float u1 = st.rng.uniform_f(), u2 = st.rng.uniform_f();
-            const float cpf = 1.f - 2.f * u2;
-            const float spf = 2.f * sqrtf(u2 * (1.f - u2));
-            float sth, cth;
-            sincospif(2.f * u1, &sth, &cth);
-            const double dx = double(spf * cth), dy = double(spf * sth), dz = double(cpf);
-            const double k = 1.5 - 0.5 * (dx * dx + dy * dy + dz * dz);
-            sm.dir[0] = dx * k;
-            sm.dir[1] = dy * k;
-            sm.dir[2] = dz * k;
+            draw_direction(st.rng, sm.dir);
         }
     }
     __syncthreads();

@@ -347,6 +347,22 @@ int mcacg_resident_boxes(int32_t threads, int32_t *boxes);
  * finished (runs to the stop criteria). Results do not depend on it. */
 int mcacg_batch_set_threads(mcacg_batch *batch, int32_t threads);
 int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads);
+/* Speculative rounds of the batch's loop: a cluster of ctas_per_box thread
+ * blocks per box (1: none, 2, 4 or 8; 0, the default: chosen by timing
+ * together with the threads per box). Between two merges the pick tree is
+ * fixed, so the picks and directions of the next steps depend on the box's
+ * rand() stream alone: each block of the cluster answers one of the next
+ * steps' contact queries at once, and the steps are committed in order up
+ * to the first one whose answer a committed move could change (same
+ * aggregate, or swept bounding capsules within reach) or the first merge;
+ * the rest is drawn again. Results do not depend on it: every run is the
+ * one-block loop's, bit for bit. The helper blocks' query scratch is
+ * allocated once per batch (about 44 bytes per aggregate slot and 384 KiB
+ * per helper and box), only when it fits half of the free device memory;
+ * boxes with surface reactions always run one step at a time. No
+ * counterpart in the reference, whose loop is sequential. */
+int mcacg_batch_set_speculation(mcacg_batch *batch, int32_t ctas_per_box);
+int mcacg_batch_speculation(const mcacg_batch *batch, int32_t *ctas_per_box);
 /* Advances every unfinished box by at most max_steps steps (<= 0: until all
  * meet their stop criteria) in kernel launches of steps_per_launch steps. */
 int mcacg_batch_run(mcacg_batch *batch, int64_t max_steps, int64_t steps_per_launch);

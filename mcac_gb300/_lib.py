@@ -125,6 +125,8 @@ SIGNATURES = {
     "mcacg_batch_set_threads": [vp, i32],
     "mcacg_batch_threads": [vp, C.POINTER(i32)],
     "mcacg_batch_set_aggregate_limit": [vp, i64],
+    "mcacg_batch_set_speculation": [vp, i32],
+    "mcacg_batch_speculation": [vp, C.POINTER(i32)],
     "mcacg_batch_pick_histogram": [vp, i32, i64, C.c_uint32, C.POINTER(i64), i64, C.POINTER(i64), C.POINTER(i64)],
     "mcacg_draw_directions": [i64, C.c_uint32, C.POINTER(f64)],
     "mcacg_batch_run": [vp, i64, i64],

@@ -382,6 +382,18 @@ class Batch:
     def threads(self, value: int) -> None:
         check(lib().mcacg_batch_set_threads(self._b, int(value)))
 
+    @property
+    def speculation(self) -> int:
+        """Thread blocks per box of the loop's speculative rounds (1: none)."""
+        n = C.c_int32(0)
+        check(lib().mcacg_batch_speculation(self._b, C.byref(n)))
+        return n.value
+
+    @speculation.setter
+    def speculation(self, value: int) -> None:
+        """0: chosen by timing (default); 1: none; 2, 4 or 8 blocks per box."""
+        check(lib().mcacg_batch_set_speculation(self._b, int(value)))
+
     def run_timed(self, wall_ms: float) -> None:
         """Runs every unfinished box for about wall_ms of wall time, each as
         fast as it goes (returns early when all are done)."""

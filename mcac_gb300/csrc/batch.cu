@@ -12,6 +12,7 @@
 #include "host_parallel.hpp"
 #include "host_box.hpp"
 #include "run.cuh"
+#include "spec.cuh"
 
 namespace mcacg {
 
@@ -70,6 +71,93 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
         if (!block_mc_step(R, sm)) break;
     __syncthreads();
     {
+        const int swords = int(sizeof(RunState) / sizeof(int));
+        const int *ssrc = reinterpret_cast<const int *>(&st);
+        int *sdst = reinterpret_cast<int *>(st_global);
+        for (int k = threadIdx.x; k < swords; k += NT) sdst[k] = ssrc[k];
+    }
+}
+
+// The same loop with speculative rounds (spec.cuh): a cluster of K CTAs per
+// box (grid n * K, clusters of K consecutive blocks), K steps per round,
+// committed in order by the leader CTA (rank 0). helpers[box * (kSpecMax -
+// 1) + rank - 1] is the query scratch of helper rank 'rank'.
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_run_spec(const BoxRun *runs, const SpecScratch *helpers, int n,
+                                                           long long max_steps, long long budget_ns) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int K = int(cluster.num_blocks());
+    const int rank = int(cluster.block_rank());
+    const int box = int(blockIdx.x) / K;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    RunSmemFor<NT> &sm = *reinterpret_cast<RunSmemFor<NT> *>(smem_raw);
+    __shared__ __align__(16) BoxRun R;
+    __shared__ __align__(16) RunState st;
+    __shared__ __align__(16) SpecShared sh;
+    // the same for every CTA of a cluster (one box per cluster)
+    if (box >= n || runs[box].st == nullptr) return;
+    RunState *st_global = runs[box].st;
+    {
+        const int words = int(sizeof(BoxRun) / sizeof(int));
+        const int *src = reinterpret_cast<const int *>(&runs[box]);
+        int *dst = reinterpret_cast<int *>(&R);
+        for (int k = threadIdx.x; k < words; k += NT) dst[k] = src[k];
+        if (rank == 0) {
+            const int swords = int(sizeof(RunState) / sizeof(int));
+            const int *ssrc = reinterpret_cast<const int *>(st_global);
+            int *sdst = reinterpret_cast<int *>(&st);
+            for (int k = threadIdx.x; k < swords; k += NT) sdst[k] = ssrc[k];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (rank == 0) {
+            R.st = &st;
+            sm.deadline = budget_ns > 0 ? global_ns() + (unsigned long long)budget_ns : 0ULL;
+            sh.tree_gen = 0;
+        } else {
+            const SpecScratch &h = helpers[size_t(box) * (kSpecMax - 1) + size_t(rank - 1)];
+            R.box.cand_db = h.cand_db;
+            R.box.cand_key = h.cand_key;
+            R.box.cand_slot = h.cand_slot;
+            R.box.cand_order = h.cand_order;
+            R.box.cand_prefix = h.cand_prefix;
+            R.box.best_res = h.best_res;
+            R.box.best_ij = h.best_ij;
+            R.box.surv = h.surv;
+            R.box.surv_res = h.surv_res;
+            R.box.surv_cap = h.surv_cap;
+        }
+    }
+    __syncthreads();
+    tree_cache_load(R, sm.tree);
+    SpecShared *lead = cluster.map_shared_rank(&sh, 0);
+    int gen = 0;
+    long long done = 0, t0 = 0;
+    for (;;) {
+        if (rank == 0) {
+            if (threadIdx.x == 0) t0 = clock64();
+            spec_prepare(R, sm, sh, K, max_steps - done);
+        }
+        cluster.sync();
+        const int stop = lead->stop, njobs = lead->n_jobs, tgen = lead->tree_gen;
+        if (stop) break;
+        if (rank < njobs) {
+            if (rank != 0 && tgen != gen) {
+                tree_cache_load(R, sm.tree);  // the leader's merges changed the tree
+                gen = tgen;
+            }
+            spec_query(R, sm, &lead->job[rank], &lead->res[rank]);
+        }
+        cluster.sync();
+        if (rank == 0) {
+            if (threadIdx.x == 0) st.cyc_query += clock64() - t0;
+            done += spec_commit(R, sm, sh, njobs);
+        }
+    }
+    cluster.sync();  // no CTA leaves while another may still read its shared memory
+    if (rank == 0) {
         const int swords = int(sizeof(RunState) / sizeof(int));
         const int *ssrc = reinterpret_cast<const int *>(&st);
         int *sdst = reinterpret_cast<int *>(st_global);
@@ -179,6 +267,64 @@ cudaError_t launch_k_run(int nt, int grid, cudaStream_t s, const BoxRun *runs, i
     }
     return cudaGetLastError();
 }
+template <int NT>
+cudaLaunchConfig_t spec_config(int k, int n, cudaStream_t s, cudaLaunchAttribute *attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(n) * unsigned(k));
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = sizeof(RunSmemFor<NT>);
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = unsigned(k);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+template <int NT>
+cudaError_t launch_spec_t(int k, int n, cudaStream_t s, const BoxRun *runs, const SpecScratch *h, long long steps,
+                          long long budget_ns) {
+    static bool prepared = false;
+    if (!prepared) {
+        cudaError_t e = cudaFuncSetAttribute(k_run_spec<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(sizeof(RunSmemFor<NT>)));
+        if (e != cudaSuccess) return e;
+        prepared = true;
+    }
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = spec_config<NT>(k, n, s, attr);
+    return cudaLaunchKernelEx(&cfg, k_run_spec<NT>, runs, h, n, steps, budget_ns);
+}
+cudaError_t launch_spec(int nt, int k, int n, cudaStream_t s, const BoxRun *runs, const SpecScratch *h,
+                        long long steps, long long budget_ns) {
+    switch (nt) {
+        case 32: return launch_spec_t<32>(k, n, s, runs, h, steps, budget_ns);
+        case 64: return launch_spec_t<64>(k, n, s, runs, h, steps, budget_ns);
+        case 128: return launch_spec_t<128>(k, n, s, runs, h, steps, budget_ns);
+        case 512: return launch_spec_t<512>(k, n, s, runs, h, steps, budget_ns);
+        default: return launch_spec_t<256>(k, n, s, runs, h, steps, budget_ns);
+    }
+}
+// Clusters of k CTAs of nt threads the device keeps resident at once.
+template <int NT>
+cudaError_t spec_clusters_t(int k, int *clusters) {
+    cudaError_t e = cudaFuncSetAttribute(k_run_spec<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(sizeof(RunSmemFor<NT>)));
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = spec_config<NT>(k, 1, nullptr, attr);
+    return cudaOccupancyMaxActiveClusters(clusters, k_run_spec<NT>, &cfg);
+}
+cudaError_t spec_clusters(int nt, int k, int *clusters) {
+    switch (nt) {
+        case 32: return spec_clusters_t<32>(k, clusters);
+        case 64: return spec_clusters_t<64>(k, clusters);
+        case 128: return spec_clusters_t<128>(k, clusters);
+        case 512: return spec_clusters_t<512>(k, clusters);
+        default: return spec_clusters_t<256>(k, clusters);
+    }
+}
 int occupancy_k_run(int nt, int *per_sm) {
     cudaError_t e;
     switch (nt) {
@@ -256,6 +402,8 @@ int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *
 BatchRunner::~BatchRunner() {
     if (stream_) cudaStreamSynchronize(static_cast<cudaStream_t>(stream_));
     for (void *p : trees_) cudaFree(p);
+    if (spec_mem_) cudaFree(spec_mem_);
+    if (spec_tab_) cudaFree(spec_tab_);
     if (runs_dev_) cudaFree(runs_dev_);
     if (states_dev_) cudaFree(states_dev_);
     if (sc_dev_) cudaFree(sc_dev_);
@@ -346,6 +494,7 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
     volsurf_.assign(static_cast<size_t>(n), VS_NONE);
     for (int i = 0; i < n; ++i) {
         growth_[size_t(i)] = params[size_t(i)].with_surface_reactions ? 1 : 0;
+        any_growth_ = any_growth_ || growth_[size_t(i)] != 0;
         volsurf_[size_t(i)] = params[size_t(i)].volsurf_method;
         const int rc = boxes_[size_t(i)]->set_volsurf(params[size_t(i)].volsurf_method);
         if (rc != ST_OK) {
@@ -391,6 +540,87 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
     return ST_OK;
 }
 
+int BatchRunner::set_speculation(int k) {
+    if (k != 0 && k != 1 && k != 2 && k != 4 && k != 8) return ST_BAD_ARGUMENT;
+    auto_spec_ = k == 0;
+    spec_k_ = k == 0 ? 1 : k;
+    return ST_OK;
+}
+
+// Helper-CTA scratch for speculative rounds, once: for each box, the query
+// lists of up to kSpecMax - 1 helpers (fewer when the device lacks room).
+// Returns the most CTAs per box it allows (1: none).
+int BatchRunner::spec_room(std::string *err) {
+    if (spec_max_ > 0) return spec_max_;
+    spec_max_ = 1;
+    const int n = int(boxes_.size());
+    auto r256 = [](size_t x) { return (x + 255) & ~size_t(255); };
+    std::vector<size_t> set_bytes(static_cast<size_t>(n));
+    size_t per_helper = 0;
+    for (int i = 0; i < n; ++i) {
+        const size_t nc1 = size_t(boxes_[size_t(i)]->nslots()) + 1;
+        set_bytes[size_t(i)] = 4 * r256(8 * nc1) + 3 * r256(4 * nc1) + r256(sizeof(int4) * kSpecSurvivors) +
+                               r256(sizeof(double) * kSpecSurvivors);
+        per_helper += set_bytes[size_t(i)];
+    }
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return spec_max_;
+    }
+    int kmax = kSpecMax;
+    while (kmax > 1 && per_helper * size_t(kmax - 1) > free_b / 2) kmax /= 2;
+    if (kmax < 2) return spec_max_;
+    std::vector<SpecScratch> tab(size_t(n) * (kSpecMax - 1));
+    if (!ok_cuda(cudaMalloc(&spec_mem_, per_helper * size_t(kmax - 1)), err, "cudaMalloc") ||
+        !ok_cuda(cudaMalloc(&spec_tab_, sizeof(SpecScratch) * tab.size()), err, "cudaMalloc")) {
+        if (spec_mem_) cudaFree(spec_mem_);
+        spec_mem_ = nullptr;
+        cudaGetLastError();
+        return spec_max_;
+    }
+    char *p = static_cast<char *>(spec_mem_);
+    for (int i = 0; i < n; ++i) {
+        const size_t nc1 = size_t(boxes_[size_t(i)]->nslots()) + 1;
+        for (int h = 0; h < kmax - 1; ++h) {
+            SpecScratch &t = tab[size_t(i) * (kSpecMax - 1) + size_t(h)];
+            char *q = p;
+            auto take = [&](size_t bytes) {
+                char *r = q;
+                q += r256(bytes);
+                return r;
+            };
+            t.cand_db = reinterpret_cast<double *>(take(8 * nc1));
+            t.cand_key = reinterpret_cast<long long *>(take(8 * nc1));
+            t.best_res = reinterpret_cast<unsigned long long *>(take(8 * nc1));
+            t.best_ij = reinterpret_cast<unsigned long long *>(take(8 * nc1));
+            t.cand_slot = reinterpret_cast<int *>(take(4 * nc1));
+            t.cand_order = reinterpret_cast<int *>(take(4 * nc1));
+            t.cand_prefix = reinterpret_cast<int *>(take(4 * nc1));
+            t.surv = reinterpret_cast<int4 *>(take(sizeof(int4) * kSpecSurvivors));
+            t.surv_res = reinterpret_cast<double *>(take(sizeof(double) * kSpecSurvivors));
+            t.surv_cap = kSpecSurvivors;
+            t.pad = 0;
+            p += set_bytes[size_t(i)];
+        }
+    }
+    if (!ok_cuda(cudaMemcpy(spec_tab_, tab.data(), sizeof(SpecScratch) * tab.size(), cudaMemcpyHostToDevice), err,
+                 "upload"))
+        return spec_max_;
+    spec_max_ = kmax;
+    return spec_max_;
+}
+
+// One launch of the loop at nt threads per CTA and k CTAs per box.
+cudaError_t BatchRunner::launch_run(int nt, int k, long long steps, long long budget_ns) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    const int n = int(boxes_.size());
+    const BoxRun *runs = static_cast<const BoxRun *>(runs_dev_);
+    if (k > 1) k = std::min(k, spec_room(nullptr));  // helper scratch set up at the first such launch
+    if (k <= 1 || !spec_tab_) return launch_k_run(nt, n, s, runs, n, steps, budget_ns);
+    return launch_spec(nt, k, n, s, runs, static_cast<const SpecScratch *>(spec_tab_), steps, budget_ns);
+}
+
 int BatchRunner::set_threads(int threads) {
     if (threads != 0 && threads != 32 && threads != 64 && threads != 128 && threads != 256 && threads != 512)
         return ST_BAD_ARGUMENT;
@@ -407,45 +637,74 @@ int BatchRunner::set_threads(int threads) {
 // when the first has used its budget, doubling the launch and halving every
 // box's share of it.
 int BatchRunner::tune(int64_t budget, int64_t *done, float *ms_total, std::string *err, bool one_wave) {
-    cudaStream_t s = static_cast<cudaStream_t>(stream_);
-    const int n = int(boxes_.size());
-    const BoxRun *runs = static_cast<const BoxRun *>(runs_dev_);
     const int64_t probe = 32;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    float best_ms = 0.f;
-    int best = threads_ ? threads_ : 256;
     int rc = ST_OK;
-    for (int nt : kRunThreadChoices) {
-        if (budget > 0 && *done + probe > budget) break;
-        if (one_wave && nt != kRunThreadChoices[0]) {
-            int resident = 0;
-            if (resident_boxes(nt, &resident, err) == ST_OK && resident < tuned_active_) continue;
-        }
-        cudaEventRecord(e0, s);
-        if (!ok_cuda(launch_k_run(nt, n, s, runs, n, (long long)probe), err, "k_run")) {
+    // one probe launch of 'probe' steps per unfinished box; its time, or a
+    // negative value when it was skipped (budget) or failed
+    auto time_probe = [&](int nt, int k) -> float {
+        if (budget > 0 && *done + probe > budget) return -1.f;
+        cudaEventRecord(e0, static_cast<cudaStream_t>(stream_));
+        if (!ok_cuda(launch_run(nt, k, (long long)probe, 0), err, "k_run")) {
             rc = ST_CUDA;
-            break;
+            return -1.f;
         }
-        cudaEventRecord(e1, s);
+        cudaEventRecord(e1, static_cast<cudaStream_t>(stream_));
         if (!ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {
             rc = ST_CUDA;
-            break;
+            return -1.f;
         }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         *ms_total += ms;
         ++launches_;
         *done += probe;
-        if (best_ms == 0.f || ms < best_ms) {
-            best_ms = ms;
-            best = nt;
+        return ms;
+    };
+    // first the block size (at the fixed speculation, or none when it is
+    // chosen too), then the CTAs per box at that block size
+    const int k1 = auto_spec_ ? 1 : spec_k_;
+    float best_ms = 0.f;
+    int best = threads_ ? threads_ : 256;
+    if (auto_threads_ || threads_ == 0) {
+        for (int nt : kRunThreadChoices) {
+            if (one_wave && nt != kRunThreadChoices[0]) {
+                int resident = 0;
+                if (resident_boxes(nt, &resident, err) == ST_OK && resident < tuned_active_) continue;
+            }
+            const float ms = time_probe(nt, k1);
+            if (rc != ST_OK || ms < 0.f) break;
+            if (best_ms == 0.f || ms < best_ms) {
+                best_ms = ms;
+                best = nt;
+            }
         }
+        if (rc == ST_OK && best_ms > 0.f) threads_ = best;
+    }
+    if (rc == ST_OK && auto_spec_ && !any_growth_) {
+        const int kmax = spec_room(err);
+        if (best_ms == 0.f) best_ms = time_probe(threads_ ? threads_ : 256, 1);
+        int best_k = 1;
+        for (int k = 2; k <= kmax && rc == ST_OK && best_ms > 0.f; k *= 2) {
+            int clusters = 0;
+            if (spec_clusters(threads_ ? threads_ : 256, k, &clusters) != cudaSuccess) {
+                cudaGetLastError();
+                break;
+            }
+            if (clusters < 1 || (one_wave && clusters < tuned_active_)) break;
+            const float ms = time_probe(threads_ ? threads_ : 256, k);
+            if (rc != ST_OK || ms < 0.f) break;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_k = k;
+            }
+        }
+        if (rc == ST_OK) spec_k_ = best_k;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (rc == ST_OK && best_ms > 0.f) threads_ = best;
     return rc;
 }
 
@@ -485,7 +744,7 @@ int BatchRunner::run(int64_t max_steps, int64_t chunk, std::string *err) {
         // doing as many steps as it can in it
         const long long budget = max_steps <= 0 ? kRunLaunchBudgetNs : 0;
         cudaEventRecord(e0, s);
-        if (!ok_cuda(launch_k_run(nt, n, s, runs, n, (long long)steps, budget), err, "k_run")) {
+        if (!ok_cuda(launch_run(nt, spec_k_, (long long)steps, budget), err, "k_run")) {
             rc = ST_CUDA;
             break;
         }
@@ -562,7 +821,7 @@ int BatchRunner::run_timed(double wall_ms, std::string *err) {
         const long long budget = std::max(1LL, std::min(kRunLaunchBudgetNs, (long long)(left * 1e6)));
         const int nt = threads_ ? threads_ : 256;
         cudaEventRecord(e0, s);
-        if (!ok_cuda(launch_k_run(nt, n, s, runs, n, 1LL << 50, budget), err, "k_run")) {
+        if (!ok_cuda(launch_run(nt, spec_k_, 1LL << 50, budget), err, "k_run")) {
             rc = ST_CUDA;
             break;
         }

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../../include/mcacg.h"
 #include "device_box.hpp"
 
@@ -43,6 +45,11 @@ class BatchRunner {
     // run, and again when half of the running boxes have finished).
     int set_threads(int threads);
     int threads() const { return threads_; }
+    // CTAs per box of the loop's speculative rounds (spec.cuh): 1 (none), 2,
+    // 4 or 8, or 0 (the default) to choose by timing with the block size.
+    // Results do not depend on it.
+    int set_speculation(int k);
+    int speculation() const { return spec_max_ > 0 && spec_max_ < spec_k_ ? spec_max_ : spec_k_; }
 
     int size() const { return int(boxes_.size()); }
     // Advances every unfinished box by at most max_steps MC steps (<= 0: until
@@ -102,6 +109,14 @@ class BatchRunner {
     std::vector<int> volsurf_;  // per box: VolSurfMethods
     int tuned_active_ = 0;  // unfinished boxes at the last tuning
     int tune(int64_t budget, int64_t *done, float *ms_total, std::string *err, bool one_wave);
+    int spec_room(std::string *err);
+    cudaError_t launch_run(int nt, int k, long long steps, long long budget_ns);
+    int spec_k_ = 1;          // CTAs per box in use
+    bool auto_spec_ = true;   // chosen by tune()
+    int spec_max_ = 0;        // CTAs per box the helper scratch allows (0: not set up yet)
+    bool any_growth_ = false; // a box grows (every step changes every radius: no speculation)
+    void *spec_mem_ = nullptr;  // helper query scratch
+    void *spec_tab_ = nullptr;  // SpecScratch[n * (kSpecMax - 1)]
 };
 
 // Continuous-batching request loop: 'capacity' block slots; between kernel

@@ -772,6 +772,23 @@ int mcacg_draw_directions(int64_t n, uint32_t seed, double *out) {
     });
 }
 
+int mcacg_batch_set_speculation(mcacg_batch *batch, int32_t ctas_per_box) {
+    return guarded([&] {
+        if (!batch) return fail(MCACG_ERR_BAD_ARGUMENT, "null batch");
+        if (batch->impl->set_speculation(ctas_per_box) != 0)
+            return fail(MCACG_ERR_BAD_ARGUMENT, "CTAs per box must be 0, 1, 2, 4 or 8");
+        return 0;
+    });
+}
+
+int mcacg_batch_speculation(const mcacg_batch *batch, int32_t *ctas_per_box) {
+    return guarded([&] {
+        if (!batch || !ctas_per_box) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");
+        *ctas_per_box = batch->impl->speculation();
+        return 0;
+    });
+}
+
 int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads) {
     return guarded([&] {
         if (!batch || !threads) return fail(MCACG_ERR_BAD_ARGUMENT, "null argument");

@@ -186,8 +186,8 @@ __device__ __forceinline__ unsigned long long pick_target(RandStream &rng, unsig
 // |d|^2 = 1 + e, e ~ 1e-7, the factor 1.5 - 0.5 |d|^2 leaves
 // |d| - 1 ~ 3e^2/8 < 1e-13, far inside the 1e-10 contact tolerance of the
 // merge.
-__device__ __forceinline__ void draw_direction(RandStream &rng, double d[3]) {
-    const float u1 = rng.uniform_f(), u2 = rng.uniform_f();
+__device__ __forceinline__ void direction_from(int r1, int r2, double d[3]) {
+    const float u1 = float(r1) * (1.0f / 2147483647.0f), u2 = float(r2) * (1.0f / 2147483647.0f);
     const float cpf = 1.f - 2.f * u2;
     const float spf = 2.f * sqrtf(u2 * (1.f - u2));
     float sth, cth;
@@ -197,6 +197,12 @@ __device__ __forceinline__ void draw_direction(RandStream &rng, double d[3]) {
     d[0] = dx * k;
     d[1] = dy * k;
     d[2] = dz * k;
+}
+// The same from the stream's next two values (u1 first).
+__device__ __forceinline__ void draw_direction(RandStream &rng, double d[3]) {
+    const int r1 = rng.next_int();
+    const int r2 = rng.next_int();
+    direction_from(r1, r2, d);
 }
 
 // The fixed-point weight of a slot with this time step (live slots only).
@@ -626,85 +632,42 @@ __device__ inline void block_update_one_or_all(const BoxRun &R, RS &sm, int slot
     }
 }
 
+// The query's answer into the step's shared state and the box's counters
+// (thread 0).
 template <class RS>
-__device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
+__device__ inline void apply_query(RunState &st, RS &sm, const QueryOut &q) {
+    if (q.status != ST_OK) {
+        st.status = q.status;
+        sm.stop = 1;
+    }
+    sm.contact = q.distance <= sm.full;
+    sm.move = sm.contact ? q.distance : sm.full;
+    sm.ms = q.moving_sphere;
+    sm.os = q.other_sphere;
+    sm.oslot = q.other_slot;
+    st.c_queries += 1;
+    st.c_mov += q.n_mov;
+    st.c_scanned += q.n_scanned;
+    st.c_cells += q.n_cells;
+    st.c_candidates += q.n_candidates;
+    st.c_cand_spheres += q.n_cand_spheres;
+    st.c_refined += q.n_pairs_refined;
+    st.cyc_qscan += q.cyc_scan;
+    st.cyc_qpairs += q.cyc_pairs;
+}
+
+// The rest of a step once its pick (sm.slot, sm.dir, sm.dt, sm.full,
+// sm.dt_indiv) and its query's answer (sm.contact, sm.move, sm.ms, sm.os,
+// sm.oslot) are known: translation, time, surface reactions, merge, pick
+// tree, counters and the stop criteria (all threads). Returns false when
+// the box stopped on an error.
+template <class RS>
+__device__ inline bool step_commit(const BoxRun &R, RS &sm, long long &t_phase) {
     const int tid = threadIdx.x;
     const DevBox &b = R.box;
     RunState &st = *R.st;
-    long long t_phase = 0;
-    if (tid == 0) {
-        t_phase = clock64();
-        sm.stop = st.finished || st.status != ST_OK;
-        if (!sm.stop && run_finished(R, st, b.sc->n_alive)) {
-            st.finished = 1;
-            sm.stop = 1;
-        }
-        // a time-capped launch: checked before every step, so that a box of
-        // expensive steps does not hold the launch (and the other boxes,
-        // which wait for it) past the cap
-        if (!sm.stop && sm.deadline != 0ULL && global_ns() >= sm.deadline) sm.stop = 1;
-        if (!sm.stop) sm.t_pick = pick_target(st.rng, st.tree_total);
-    }
-    __syncthreads();
-    if (sm.stop) return false;
-    if (tid < 32) {
-        int slot = tree_sample(R, sm.tree, sm.t_pick);
-        if (tid == 0) {
-            if (slot < 0 || slot >= b.nslots || b.agg_n[slot] == 0) {
-                st.status = ST_UNKNOWN;  // the tree lost a live slot: stop this box
-                sm.stop = 1;
-                slot = 0;
-            }
-            sm.slot = slot;
-            sm.dt = st.inv_weight;
-            sm.full = A(b, AGG_LPM, slot);
-            sm.dt_indiv = A(b, AGG_TIME_STEP, slot);
-            draw_direction(st.rng, sm.dir);
-        }
-    }
-    __syncthreads();
-    if (sm.stop) return false;
-    if (tid == 0) {
-        const long long t = clock64();
-        st.cyc_pick += t - t_phase;
-        t_phase = t;
-    }
     const int slot = sm.slot;
     const Vec3 dir{sm.dir[0], sm.dir[1], sm.dir[2]};
-    if (R.lim.with_collisions) {
-        block_query(b, slot, dir, sm.full, sm.u.q);
-        if (tid == 0) {
-            const QueryOut &q = sm.u.q.out;
-            if (q.status != ST_OK) {
-                st.status = q.status;
-                sm.stop = 1;
-            }
-            sm.contact = q.distance <= sm.full;
-            sm.move = sm.contact ? q.distance : sm.full;
-            sm.ms = q.moving_sphere;
-            sm.os = q.other_sphere;
-            sm.oslot = q.other_slot;
-            st.c_queries += 1;
-            st.c_mov += q.n_mov;
-            st.c_scanned += q.n_scanned;
-            st.c_cells += q.n_cells;
-            st.c_candidates += q.n_candidates;
-            st.c_cand_spheres += q.n_cand_spheres;
-            st.c_refined += q.n_pairs_refined;
-            st.cyc_qscan += q.cyc_scan;
-            st.cyc_qpairs += q.cyc_pairs;
-        }
-    } else if (tid == 0) {
-        sm.contact = 0;
-        sm.move = sm.full;
-    }
-    __syncthreads();
-    if (sm.stop) return false;
-    if (tid == 0) {
-        const long long t = clock64();
-        st.cyc_query += t - t_phase;
-        t_phase = t;
-    }
     const int ms = sm.ms, os = sm.os, oslot = sm.oslot;
     block_translate(b, slot, Vec3{dir.x * sm.move, dir.y * sm.move, dir.z * sm.move}, sm.refpos);
     if (tid == 0) {
@@ -795,6 +758,68 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
     }
     __syncthreads();
     return true;
+}
+
+// One MC step of one box by the whole block. Returns false when the box is
+// finished or in error (then nothing was done).
+template <class RS>
+__device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
+    const int tid = threadIdx.x;
+    const DevBox &b = R.box;
+    RunState &st = *R.st;
+    long long t_phase = 0;
+    if (tid == 0) {
+        t_phase = clock64();
+        sm.stop = st.finished || st.status != ST_OK;
+        if (!sm.stop && run_finished(R, st, b.sc->n_alive)) {
+            st.finished = 1;
+            sm.stop = 1;
+        }
+        // a time-capped launch: checked before every step, so that a box of
+        // expensive steps does not hold the launch (and the other boxes,
+        // which wait for it) past the cap
+        if (!sm.stop && sm.deadline != 0ULL && global_ns() >= sm.deadline) sm.stop = 1;
+        if (!sm.stop) sm.t_pick = pick_target(st.rng, st.tree_total);
+    }
+    __syncthreads();
+    if (sm.stop) return false;
+    if (tid < 32) {
+        int slot = tree_sample(R, sm.tree, sm.t_pick);
+        if (tid == 0) {
+            if (slot < 0 || slot >= b.nslots || b.agg_n[slot] == 0) {
+                st.status = ST_UNKNOWN;  // the tree lost a live slot: stop this box
+                sm.stop = 1;
+                slot = 0;
+            }
+            sm.slot = slot;
+            sm.dt = st.inv_weight;
+            sm.full = A(b, AGG_LPM, slot);
+            sm.dt_indiv = A(b, AGG_TIME_STEP, slot);
+            draw_direction(st.rng, sm.dir);
+        }
+    }
+    __syncthreads();
+    if (sm.stop) return false;
+    if (tid == 0) {
+        const long long t = clock64();
+        st.cyc_pick += t - t_phase;
+        t_phase = t;
+    }
+    if (R.lim.with_collisions) {
+        block_query(b, sm.slot, Vec3{sm.dir[0], sm.dir[1], sm.dir[2]}, sm.full, sm.u.q);
+        if (tid == 0) apply_query(st, sm, sm.u.q.out);
+    } else if (tid == 0) {
+        sm.contact = 0;
+        sm.move = sm.full;
+    }
+    __syncthreads();
+    if (sm.stop) return false;
+    if (tid == 0) {
+        const long long t = clock64();
+        st.cyc_query += t - t_phase;
+        t_phase = t;
+    }
+    return step_commit(R, sm, t_phase);
 }
 
 }  // namespace mcacg

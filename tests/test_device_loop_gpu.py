@@ -314,3 +314,48 @@ def test_split_by_aggregate_count_keeps_trajectories():
         b.set_aggregate_limit(100)
         b.run(max_steps=0, steps_per_launch=5000)
         assert np.array_equal(b.stats()["steps"], ref_st["steps"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("threads", [32, 128])
+def test_speculative_rounds_give_the_same_runs(threads):
+    """Boxes advanced by clusters of 2, 4 or 8 thread blocks (that many
+    steps' queries per round, committed in order up to the first conflict or
+    merge) end bit for bit where the one-block loop ends, with the same step
+    counts: sparse boxes (long runs without an event), dense ones (frequent
+    merges and conflicts) and a larger one, to a stop criterion, in launches
+    of a fixed step count and in time-capped launches."""
+    specs = [(300, 5e-3, 10), (900, 2e-4, 40), (600, 1e-3, 20), (2500, 2e-3, 150)]
+    models = [PhysicalModel(text=small_ini(n, 150 + k, mode=("lognormal" if k % 2 else "normal"), disp=1.3, fv=fv,
+                                           nagg=nagg))
+              for k, (n, fv, nagg) in enumerate(specs)]
+
+    def run(k, mode):
+        with Batch(models) as b:
+            b.threads = threads
+            b.speculation = k
+            if mode == "criterion":
+                b.run(max_steps=0, steps_per_launch=20000)
+            elif mode == "steps":
+                b.run(max_steps=3001, steps_per_launch=700)
+            else:
+                for _ in range(100000):
+                    b.run_timed(2.0)
+                    if np.all(b.stats()["finished"] == 1):
+                        break
+            assert b.speculation == k
+            st = b.stats()
+            assert np.all(st["status"] == 0)
+            return st, b.store_all()
+
+    for mode in ("criterion", "steps", "timed"):
+        ref_st, ref = run(1, mode)
+        for k in (2, 4, 8):
+            st, snaps = run(k, mode)
+            assert np.array_equal(st["steps"], ref_st["steps"]), (mode, k)
+            assert np.array_equal(st["events"], ref_st["events"]), (mode, k)
+            assert np.array_equal(st["time"].view(np.int64), ref_st["time"].view(np.int64)), (mode, k)
+            for s1, s2 in zip(snaps, ref):
+                assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64)), (mode, k)
+                assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64)), (mode, k)
+                assert np.array_equal(s1.members, s2.members), (mode, k)

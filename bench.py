@@ -590,26 +590,31 @@ def _windows_once(models, states, outs, stream, flush, threads=0):
     t0 = time.perf_counter()
     b = Batch(models, stream=stream.cuda_stream, states=states)  # host -> device
     b.threads = threads
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0, em, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     e0.record(stream)
     b.run(max_steps=ENS_A_STEPS, steps_per_launch=ENS_A_STEPS)
     la = b.last_run()[1]
-    threads_a = b.threads
+    threads_a = (b.threads, b.speculation)
+    steps_a = int(b.stats()["steps"].sum())
+    em.record(stream)
     b.set_aggregate_limit(1)
     b.threads = threads  # chosen again for the later stage
+    b.speculation = 0
     b.run(max_steps=ENS_B_STEPS, steps_per_launch=ENS_B_STEPS)
     lb = b.last_run()[1]
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
+    windows = {"a_ms": e0.elapsed_time(em), "b_ms": em.elapsed_time(e1), "a_steps": steps_a}
     st = b.stats()
     if outs is not None:
         b.store_all(raw=True, out=outs)  # device -> host
     wall = time.perf_counter() - t0
     work = b.work()
-    threads_b = b.threads
+    threads_b = (b.threads, b.speculation)
     b.close()
-    return ms, wall, int(st["steps"].sum()), la + lb, work, st, (threads_a, threads_b)
+    windows["b_steps"] = int(st["steps"].sum()) - steps_a
+    return ms, wall, int(st["steps"].sum()), la + lb, work, st, (threads_a, threads_b), windows
 
 
 def plain_single_box_windows(models, states, stream, flush, picks) -> dict:
@@ -617,7 +622,7 @@ def plain_single_box_windows(models, states, stream, flush, picks) -> dict:
     launch (what mcacg_run_device runs), the same two windows, box by box."""
     tot_ms, tot_steps = 0.0, 0
     for k in picks:
-        ms, _, steps, _, _, _, _ = _windows_once([models[k]], [states[k]], None, stream, flush)
+        ms, _, steps, _, _, _, _, _ = _windows_once([models[k]], [states[k]], None, stream, flush)
         tot_ms += ms
         tot_steps += steps
     return {"value": tot_steps / (tot_ms / 1000.0), "unit": UNIT, "boxes": len(picks), "steps": tot_steps,
@@ -657,7 +662,7 @@ def run_ensemble_windows(args, rank: int, world: int) -> dict | None:
                           + s.members.nbytes) for s in states)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     for _ in range(args.warmup):
-        _windows_once(models, states, outs, stream, flush, args.threads)
+        _windows_once(models, states, outs, stream, flush, args.threads)  # untimed
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -668,8 +673,11 @@ def run_ensemble_windows(args, rank: int, world: int) -> dict | None:
     work_sum: dict = {}
     threads_seen = set()
     out_bytes = 0
+    win = {"a_ms": 0.0, "b_ms": 0.0, "a_steps": 0, "b_steps": 0}
     for _ in range(args.steps):
-        ms, wall, steps, nl, work, st, th = _windows_once(models, states, outs, stream, flush, args.threads)
+        ms, wall, steps, nl, work, st, th, w = _windows_once(models, states, outs, stream, flush, args.threads)
+        for k in win:
+            win[k] += w[k]
         tot_ms += ms
         tot_wall += wall
         tot_steps += steps
@@ -709,7 +717,12 @@ def run_ensemble_windows(args, rank: int, world: int) -> dict | None:
         "run": {"path": "device-resident MC loop, one thread block per box, all boxes of a window in one launch",
                 "parallelism": f"{len(mine)} boxes on rank 0 of {world} (assigned by monomer count)",
                 "l2": "flushed (256 MB write) before each bench step; states > L2",
-                "setup_s": round(setup_s, 2), "threads_per_box": sorted(threads_seen),
+                "setup_s": round(setup_s, 2),
+                "threads_and_ctas_per_box": sorted(threads_seen),
+                "windows": {"a": {"mc_steps_per_s": win["a_steps"] / (win["a_ms"] / 1e3) if win["a_ms"] else None,
+                                  "ms_per_bench_step": win["a_ms"] / args.steps},
+                            "b": {"mc_steps_per_s": win["b_steps"] / (win["b_ms"] / 1e3) if win["b_ms"] else None,
+                                  "ms_per_bench_step": win["b_ms"] / args.steps}},
                 "steps_per_bench_step": tot_steps // max(1, args.steps),
                 "aggregates_after": {"min": int(last_stats["n_aggregates"].min()),
                                      "median": float(np.median(last_stats["n_aggregates"])),

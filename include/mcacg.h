@@ -342,14 +342,13 @@ int mcacg_batch_destroy(mcacg_batch *batch);
  * SMs. Batches up to this size take one wave. */
 int mcacg_resident_boxes(int32_t threads, int32_t *boxes);
 /* Threads per box of the batch's loop: 32, 64, 128, 256 or 512, or 0 (the
- * default) to let mcacg_batch_run time each on a short slice of the run and
- * keep the fastest, and choose again when half of the running boxes have
- * finished (runs to the stop criteria). Results do not depend on it. */
+ * default): the largest size at which every unfinished box is resident at
+ * once, chosen at the start of a run and again whenever half of the boxes
+ * running at the last choice have finished. Results do not depend on it. */
 int mcacg_batch_set_threads(mcacg_batch *batch, int32_t threads);
 int mcacg_batch_threads(const mcacg_batch *batch, int32_t *threads);
 /* Speculative rounds of the batch's loop: a cluster of ctas_per_box thread
- * blocks per box (1: none, 2, 4 or 8; 0, the default: chosen by timing
- * together with the threads per box). Between two merges the pick tree is
+ * blocks per box (1, the default, or 0: none; 2, 4 or 8). Between two merges the pick tree is
  * fixed, so the picks and directions of the next steps depend on the box's
  * rand() stream alone: each block of the cluster answers one of the next
  * steps' contact queries at once, and the steps are committed in order up

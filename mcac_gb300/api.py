@@ -373,7 +373,8 @@ class Batch:
 
     @property
     def threads(self) -> int:
-        """Threads per box of the loop (0 until chosen by the first run)."""
+        """Threads per box of the loop (0 until chosen at the first run: the
+        largest size at which every unfinished box is resident)."""
         n = C.c_int32(0)
         check(lib().mcacg_batch_threads(self._b, C.byref(n)))
         return n.value
@@ -391,7 +392,7 @@ class Batch:
 
     @speculation.setter
     def speculation(self, value: int) -> None:
-        """0: chosen by timing (default); 1: none; 2, 4 or 8 blocks per box."""
+        """1 (the default) or 0: none; 2, 4 or 8 blocks per box."""
         check(lib().mcacg_batch_set_speculation(self._b, int(value)))
 
     def run_timed(self, wall_ms: float) -> None:

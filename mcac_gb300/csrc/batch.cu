@@ -494,7 +494,6 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
     volsurf_.assign(static_cast<size_t>(n), VS_NONE);
     for (int i = 0; i < n; ++i) {
         growth_[size_t(i)] = params[size_t(i)].with_surface_reactions ? 1 : 0;
-        any_growth_ = any_growth_ || growth_[size_t(i)] != 0;
         volsurf_[size_t(i)] = params[size_t(i)].volsurf_method;
         const int rc = boxes_[size_t(i)]->set_volsurf(params[size_t(i)].volsurf_method);
         if (rc != ST_OK) {
@@ -542,8 +541,8 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
 
 int BatchRunner::set_speculation(int k) {
     if (k != 0 && k != 1 && k != 2 && k != 4 && k != 8) return ST_BAD_ARGUMENT;
-    auto_spec_ = k == 0;
     spec_k_ = k == 0 ? 1 : k;
+    if (auto_threads_) threads_ = 0;  // the block size is chosen again for the new cluster size
     return ST_OK;
 }
 
@@ -629,83 +628,38 @@ int BatchRunner::set_threads(int threads) {
     return ST_OK;
 }
 
-// Times each block size on a short slice of the run (results do not depend
-// on the block size) and keeps the fastest. Returns the MC steps done.
-// With one_wave, only block sizes at which every unfinished box is resident
-// at once are tried: time-capped launches give each block its wall-time
-// budget from its own start, so a second wave of blocks would start only
-// when the first has used its budget, doubling the launch and halving every
-// box's share of it.
-int BatchRunner::tune(int64_t budget, int64_t *done, float *ms_total, std::string *err, bool one_wave) {
-    const int64_t probe = 32;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    int rc = ST_OK;
-    // one probe launch of 'probe' steps per unfinished box; its time, or a
-    // negative value when it was skipped (budget) or failed
-    auto time_probe = [&](int nt, int k) -> float {
-        if (budget > 0 && *done + probe > budget) return -1.f;
-        cudaEventRecord(e0, static_cast<cudaStream_t>(stream_));
-        if (!ok_cuda(launch_run(nt, k, (long long)probe, 0), err, "k_run")) {
-            rc = ST_CUDA;
-            return -1.f;
-        }
-        cudaEventRecord(e1, static_cast<cudaStream_t>(stream_));
-        if (!ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {
-            rc = ST_CUDA;
-            return -1.f;
-        }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        *ms_total += ms;
-        ++launches_;
-        *done += probe;
-        return ms;
-    };
-    // first the block size (at the fixed speculation, or none when it is
-    // chosen too), then the CTAs per box at that block size
-    const int k1 = auto_spec_ ? 1 : spec_k_;
-    float best_ms = 0.f;
-    int best = threads_ ? threads_ : 256;
-    if (auto_threads_ || threads_ == 0) {
-        for (int nt : kRunThreadChoices) {
-            if (one_wave && nt != kRunThreadChoices[0]) {
-                int resident = 0;
-                if (resident_boxes(nt, &resident, err) == ST_OK && resident < tuned_active_) continue;
-            }
-            const float ms = time_probe(nt, k1);
-            if (rc != ST_OK || ms < 0.f) break;
-            if (best_ms == 0.f || ms < best_ms) {
-                best_ms = ms;
-                best = nt;
-            }
-        }
-        if (rc == ST_OK && best_ms > 0.f) threads_ = best;
-    }
-    if (rc == ST_OK && auto_spec_ && !any_growth_) {
-        const int kmax = spec_room(err);
-        if (best_ms == 0.f) best_ms = time_probe(threads_ ? threads_ : 256, 1);
-        int best_k = 1;
-        for (int k = 2; k <= kmax && rc == ST_OK && best_ms > 0.f; k *= 2) {
-            int clusters = 0;
-            if (spec_clusters(threads_ ? threads_ : 256, k, &clusters) != cudaSuccess) {
+// Chooses the threads per box for the unfinished boxes (tuned_active_ of
+// them): the largest block size at which every one of them is resident at
+// once. A run's wall time is the chain of steps of its slowest boxes, and a
+// box's step is a chain of dependent loads and block barriers whose parallel
+// parts (the neighbour scan, the sphere-pair search, the merge's pair
+// search) shorten with more threads; a second wave of blocks, though, would
+// wait for the first (and time-capped launches give each block its budget
+// from its own start, so a second wave also halves every box's share of a
+// launch). Timing a few steps of each size, as this once did, chose by the
+// boxes' cheap first steps and, late in a run, spent seconds on steps of the
+// large aggregates run with 32 threads. Speculative rounds (spec.cuh) stay
+// off unless set (set_speculation): clusters of several blocks per box
+// leave fewer boxes resident at a given block size, and measured on the
+// benchmark ensemble they gained at most 10% on its slowest chains. Returns
+// ST_OK (nothing is run).
+int BatchRunner::tune(int64_t, int64_t *, float *, std::string *err, bool) {
+    if (!auto_threads_ && threads_ != 0) return ST_OK;
+    int best = kRunThreadChoices[0];
+    for (int nt : kRunThreadChoices) {
+        int resident = 0;
+        if (spec_k_ > 1) {
+            if (spec_clusters(nt, spec_k_, &resident) != cudaSuccess) {
                 cudaGetLastError();
-                break;
+                resident = 0;
             }
-            if (clusters < 1 || (one_wave && clusters < tuned_active_)) break;
-            const float ms = time_probe(threads_ ? threads_ : 256, k);
-            if (rc != ST_OK || ms < 0.f) break;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best_k = k;
-            }
+        } else if (resident_boxes(nt, &resident, err) != ST_OK) {
+            return ST_CUDA;
         }
-        if (rc == ST_OK) spec_k_ = best_k;
+        if (resident >= tuned_active_) best = nt;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return rc;
+    threads_ = best;
+    return ST_OK;
 }
 
 int BatchRunner::run(int64_t max_steps, int64_t chunk, std::string *err) {
@@ -759,10 +713,10 @@ int BatchRunner::run(int64_t max_steps, int64_t chunk, std::string *err) {
         ++launches_;
         done += steps;
         if (max_steps > 0 && done >= max_steps) break;
-        if (max_steps <= 0) {
-            // until every box has met its stop criterion (or failed); when
-            // half of the boxes running at the last tuning have finished, the
-            // block size is chosen again
+        {
+            // until every box has met its stop criterion (or failed), or the
+            // step count; when half of the boxes running at the last choice
+            // have finished, the block size is chosen again
             int active = 0;
             rc = count_active(&active);
             if (rc != ST_OK) break;

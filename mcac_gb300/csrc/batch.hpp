@@ -41,13 +41,13 @@ class BatchRunner {
     // Boxes the device loop keeps resident at once on the current device
     // (thread blocks per SM at its register and shared-memory use x SMs).
     static int resident_boxes(int threads, int *boxes, std::string *err);
-    // Threads per box (64, 128, 256 or 512; 0: chosen by timing at the next
-    // run, and again when half of the running boxes have finished).
+    // Threads per box (32, 64, 128, 256 or 512; 0: the largest at which all
+    // unfinished boxes are resident, chosen at the next run and again when
+    // half of the running boxes have finished).
     int set_threads(int threads);
     int threads() const { return threads_; }
-    // CTAs per box of the loop's speculative rounds (spec.cuh): 1 (none), 2,
-    // 4 or 8, or 0 (the default) to choose by timing with the block size.
-    // Results do not depend on it.
+    // CTAs per box of the loop's speculative rounds (spec.cuh): 1 (none, the
+    // default; 0 means the same), 2, 4 or 8. Results do not depend on it.
     int set_speculation(int k);
     int speculation() const { return spec_max_ > 0 && spec_max_ < spec_k_ ? spec_max_ : spec_k_; }
 
@@ -112,9 +112,7 @@ class BatchRunner {
     int spec_room(std::string *err);
     cudaError_t launch_run(int nt, int k, long long steps, long long budget_ns);
     int spec_k_ = 1;          // CTAs per box in use
-    bool auto_spec_ = true;   // chosen by tune()
     int spec_max_ = 0;        // CTAs per box the helper scratch allows (0: not set up yet)
-    bool any_growth_ = false; // a box grows (every step changes every radius: no speculation)
     void *spec_mem_ = nullptr;  // helper query scratch
     void *spec_tab_ = nullptr;  // SpecScratch[n * (kSpecMax - 1)]
 };

@@ -578,7 +578,7 @@ def _ens_models(inis, boxes, limit_a):
     return models
 
 
-def _windows_once(models, states, outs, stream, flush, threads=0):
+def _windows_once(models, states, outs, stream, flush, threads=0, a_steps=ENS_A_STEPS):
     """One bench step: upload the initial states, run window a then window b
     on the GPU, download the final states. Returns (kernel ms, wall s,
     steps, k_run launches, work counters, per-box stats, threads used)."""
@@ -592,7 +592,7 @@ def _windows_once(models, states, outs, stream, flush, threads=0):
     b.threads = threads
     e0, em, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     e0.record(stream)
-    b.run(max_steps=ENS_A_STEPS, steps_per_launch=ENS_A_STEPS)
+    b.run(max_steps=a_steps, steps_per_launch=a_steps)
     la = b.last_run()[1]
     threads_a = (b.threads, b.speculation)
     steps_a = int(b.stats()["steps"].sum())
@@ -662,7 +662,7 @@ def run_ensemble_windows(args, rank: int, world: int) -> dict | None:
                           + s.members.nbytes) for s in states)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     for _ in range(args.warmup):
-        _windows_once(models, states, outs, stream, flush, args.threads)  # untimed
+        _windows_once(models, states, outs, stream, flush, args.threads, args.a_steps or ENS_A_STEPS)  # untimed
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -675,7 +675,8 @@ def run_ensemble_windows(args, rank: int, world: int) -> dict | None:
     out_bytes = 0
     win = {"a_ms": 0.0, "b_ms": 0.0, "a_steps": 0, "b_steps": 0}
     for _ in range(args.steps):
-        ms, wall, steps, nl, work, st, th, w = _windows_once(models, states, outs, stream, flush, args.threads)
+        ms, wall, steps, nl, work, st, th, w = _windows_once(models, states, outs, stream, flush, args.threads,
+                                                             args.a_steps or ENS_A_STEPS)
         for k in win:
             win[k] += w[k]
         tot_ms += ms
@@ -713,7 +714,8 @@ def run_ensemble_windows(args, rank: int, world: int) -> dict | None:
         "metric": METRIC, "value": steps_all / kern_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": kern_s * 1000.0 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": ens_config(args.boxes),
+        "config": ens_config(args.boxes) if not args.a_steps else dict(ens_config(args.boxes), profiling_case=
+                  f"window a capped at {args.a_steps} steps"),
         "run": {"path": "device-resident MC loop, one thread block per box, all boxes of a window in one launch",
                 "parallelism": f"{len(mine)} boxes on rank 0 of {world} (assigned by monomer count)",
                 "l2": "flushed (256 MB write) before each bench step; states > L2",
@@ -1020,6 +1022,9 @@ def main() -> int:
     ap.add_argument("--no-completion", action="store_true", help="ensemble: skip the run to completion")
     ap.add_argument("--plain-boxes", type=int, default=8, help="ensemble: boxes of the plain single-box sample")
     ap.add_argument("--cpu-boxes", type=int, default=16, help="ensemble: boxes of the rank-0 CPU sample")
+    ap.add_argument("--a-steps", type=int, default=0,
+                    help="ensemble: cap of window a's steps (0: the benchmark's 100000); a smaller cap makes a small "
+                         "profiling case of the same kernels")
     ap.add_argument("--boxes", type=int, default=512, help="ensemble boxes")
     ap.add_argument("--cap-seconds", type=float, default=240.0, help="ensemble / serving wall-time cap")
     ap.add_argument("--rate", type=float, default=50.0, help="serving arrivals per second")

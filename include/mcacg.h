@@ -335,6 +335,15 @@ int mcacg_host_alloc(int64_t bytes, void **ptr);
  * pairs (O(n^2)); both give the same pairs. Process-wide, read by boxes
  * created afterwards; default 2048. *previous (may be NULL) gets the old value. */
 int mcacg_set_merge_grid_min(int32_t n_spheres, int32_t *previous);
+/* Once at most n_aggregates aggregates of a box are left (0: never; at most
+ * 128; default 128), the device-resident loop keeps the list of its live
+ * aggregates in shared memory: the pick scans the list instead of descending
+ * the pick tree in device memory, and a contact query takes its neighbours
+ * from it instead of walking the Verlet cells around the moving aggregate
+ * (the same neighbours, the same order). Process-wide, read by batches and
+ * servers created afterwards; results do not depend on it. *previous (may be
+ * NULL) gets the old value. */
+int mcacg_set_live_list_max(int32_t n_aggregates, int32_t *previous);
 int mcacg_host_free(void *ptr);
 int mcacg_batch_destroy(mcacg_batch *batch);
 /* Boxes the device-resident loop runs at once on the current device with

@@ -120,6 +120,7 @@ SIGNATURES = {
     "mcacg_batch_destroy": [vp],
     "mcacg_host_alloc": [i64, C.POINTER(vp)],
     "mcacg_set_merge_grid_min": [C.c_int32, C.POINTER(C.c_int32)],
+    "mcacg_set_live_list_max": [C.c_int32, C.POINTER(C.c_int32)],
     "mcacg_host_free": [vp],
     "mcacg_resident_boxes": [i32, C.POINTER(i32)],
     "mcacg_batch_set_threads": [vp, i32],

@@ -312,6 +312,15 @@ def draw_directions(n: int, seed: int = 1) -> np.ndarray:
     return out
 
 
+def set_live_list_max(n_aggregates: int) -> int:
+    """Live aggregates from which the device loop lists them in shared memory
+    (0: never, at most 128); process-wide, for batches made afterwards.
+    Returns the previous value."""
+    prev = C.c_int32()
+    check(lib().mcacg_set_live_list_max(int(n_aggregates), C.byref(prev)))
+    return prev.value
+
+
 def device_count() -> int:
     n = C.c_int()
     check(lib().mcacg_device_count(C.byref(n)))

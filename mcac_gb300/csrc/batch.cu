@@ -65,8 +65,14 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
         // every step starts only before the deadline (a step is never cut)
         sm.deadline = budget_ns > 0 ? global_ns() + (unsigned long long)budget_ns : 0ULL;
     }
+    if (threadIdx.x == 0) {
+        sm.live.allow = 1;
+        sm.live.max = R.live_max;
+        sm.live.on = 0;
+    }
     __syncthreads();
     tree_cache_load(R, sm.tree);
+    live_load(R, sm.live, sm.u.q.warp_tmp);
     for (long long s = 0; s < max_steps; ++s)
         if (!block_mc_step(R, sm)) break;
     __syncthreads();
@@ -116,7 +122,11 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run_spec(const BoxRun *runs, c
             R.st = &st;
             sm.deadline = budget_ns > 0 ? global_ns() + (unsigned long long)budget_ns : 0ULL;
             sh.tree_gen = 0;
-        } else {
+        }
+        sm.live.allow = 0;  // the rounds pick from the tree (every CTA keeps a copy of its top)
+        sm.live.on = 0;
+        sm.live.max = 0;
+        if (rank != 0) {
             const SpecScratch &h = helpers[size_t(box) * (kSpecMax - 1) + size_t(rank - 1)];
             R.box.cand_db = h.cand_db;
             R.box.cand_key = h.cand_key;
@@ -232,6 +242,13 @@ __global__ void __launch_bounds__(256) k_tree_build(const BoxRun *runs, int n) {
     if (int(blockIdx.x) >= n) return;
     block_tree_build(runs[blockIdx.x]);
 }
+
+namespace {
+std::atomic<int> g_live_list_max{kLiveMax};
+}  // namespace
+
+int live_list_max() { return g_live_list_max.load(std::memory_order_relaxed); }
+int set_live_list_max(int n) { return g_live_list_max.exchange(n); }
 
 namespace {
 
@@ -390,6 +407,7 @@ int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *
     run->st = state_dev;
     run->tree = tree;
     run->tree_levels = tl.levels;
+    run->live_max = live_list_max();
     for (int k = 0; k < kMaxTreeLevels; ++k) {
         run->tree_off[k] = tl.off[k];
         run->tree_len[k] = tl.len[k];

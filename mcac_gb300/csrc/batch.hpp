@@ -13,6 +13,12 @@
 
 namespace mcacg {
 
+// Process-wide: the device loop keeps a list of the live slots in shared
+// memory once at most this many aggregates are left (0: never; at most 128),
+// read by boxes set up afterwards. Results do not depend on it.
+int live_list_max();
+int set_live_list_max(int n);  // returns the previous value
+
 struct BoxRunStats {
     int64_t steps, events, n_alive;
     double time;

@@ -312,6 +312,21 @@ struct QuerySmemT {
 using QuerySmem = QuerySmemT<1024, 512, 256>;
 using QuerySmemSmall = QuerySmemT<256, 256, 128>;
 
+// The live slots of a box with few aggregates left, in ascending slot order,
+// with their pick weights (kept in shared memory by the device loop). With
+// it a query reads its neighbours from the list instead of walking the
+// Verlet cells around it (late in a run most of those cells are empty), and
+// the pick scans the list instead of descending the tree from HBM.
+constexpr int kLiveMax = 128;
+struct LiveList {
+    int on;      // the list is in use
+    int n;       // live slots listed
+    int allow;   // the kernel may use a list (0: never)
+    int max;     // use a list from this many live aggregates down (<= kLiveMax)
+    int slot[kLiveMax];
+    unsigned long long w[kLiveMax];
+};
+
 // -------------------------------------------------------------- the query
 // AggregatList::distance_to_next_contact (aggregats/aggregat_list.cpp:447-532):
 //  1. neighbourhood = aggregates in the Verlet cells covering the swept
@@ -325,7 +340,8 @@ using QuerySmemSmall = QuerySmemT<256, 256, 128>;
 //     early exits.
 // Must be called by all threads of the block.
 template <class SM>
-__device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double dist, SM &sm) {
+__device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double dist, SM &sm,
+                                   const LiveList *live = nullptr) {
     constexpr int kCellChunk = SM::kCellChunk;
     constexpr int kMoveTile = SM::kMoveTile;
     constexpr int kMaxSurvivorsSmem = SM::kSurv;
@@ -451,7 +467,29 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
         screen_key[k] = key;
     };
     int n_cells_visited = n_scan;
-    if (sm.use_fine) {
+    if (live != nullptr && live->on) {
+        // few aggregates left: the live list in slot order, each aggregate
+        // kept when its Verlet cell is in the reference's neighbourhood, with
+        // the scan key of the fine walk below (the same set, the same keys)
+        const int nd = b.n_div;
+        const int rlo0 = rg.lo[0], rlo1 = rg.lo[1], rlo2 = rg.lo[2];
+        for (int k = tid; k < live->n; k += NT) {
+            const int slot = live->slot[k];
+            const int key = b.agg_cell[slot];
+            const int oa = wrap_cell((key & 1023) - rlo0, nd);
+            const int ob = wrap_cell(((key >> 10) & 1023) - rlo1, nd);
+            const int oc = wrap_cell((key >> 20) - rlo2, nd);
+            if (!(oa < nx && ob < ny && oc < nz)) continue;
+            if (slot == src) {
+                sm.found_source = 1;
+            } else {
+                consider(slot, (long long)((oa * ny + ob) * nz + oc) * b.nslots + slot, b.agg_f4[slot]);
+            }
+        }
+        if (tid == 0) sm.flat_base = live->n;
+        n_cells_visited = 0;
+        __syncthreads();
+    } else if (sm.use_fine) {
         // walk the fine cells; keep the aggregates whose Verlet cell is in
         // the reference's neighbourhood
         const int fny = sm.fine_n[1], fnz = sm.fine_n[2];

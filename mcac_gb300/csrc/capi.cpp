@@ -691,6 +691,15 @@ int mcacg_set_merge_grid_min(int32_t n_spheres, int32_t *previous) {
     });
 }
 
+int mcacg_set_live_list_max(int32_t n_aggregates, int32_t *previous) {
+    return guarded([&] {
+        if (n_aggregates < 0 || n_aggregates > 128) return fail(MCACG_ERR_BAD_ARGUMENT, "n_aggregates must be 0..128");
+        int old = mcacg::set_live_list_max(n_aggregates);
+        if (previous) *previous = old;
+        return 0;
+    });
+}
+
 int mcacg_host_alloc(int64_t bytes, void **ptr) {
     return guarded([&] {
         if (!ptr || bytes <= 0) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");

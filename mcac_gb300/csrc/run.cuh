@@ -69,6 +69,7 @@ struct BoxRun {
     RunState *st;
     unsigned long long *tree;  // all levels, leaves first (fixed-point weights)
     int tree_levels;
+    int live_max;  // the loop keeps a live list from this many live aggregates down (0: never)
     int tree_off[kMaxTreeLevels];
     int tree_len[kMaxTreeLevels];
 };
@@ -120,6 +121,7 @@ struct RunSmemT {
     int n_moved;                  // slots whose grid cell changed in the update of all aggregates
     int moved[kMovedCap];
     TreeCache tree;               // top levels of the pick tree
+    LiveList live;                // the live slots when few are left (box.cuh)
 };
 using RunSmem = RunSmemT<QuerySmem, MergeSmem>;
 using RunSmemSmall = RunSmemT<QuerySmemSmall, MergeSmemSmall>;
@@ -251,6 +253,92 @@ __device__ __forceinline__ void tree_total_to_state(RunState &st, unsigned long 
     st.tree_total = total;
     st.weight_total = double(total) * st.inv_tree_scale;
     st.inv_weight = 1.0 / st.weight_total;
+}
+
+// ------------------------------------------------------------ live list
+// (Re)builds the list of live slots in slot order with their tree leaf
+// weights when at most live.max aggregates are left (all threads); turns it
+// off otherwise. The pick and the query then read the list.
+__device__ inline void live_load(const BoxRun &R, LiveList &L, int *warp_tmp) {
+    const DevBox &b = R.box;
+    const int tid = threadIdx.x, NT = blockDim.x;
+    const int n_alive = b.sc->n_alive;
+    const bool want = L.allow && !R.phys.growth && n_alive <= L.max && L.max <= kLiveMax;
+    __syncthreads();
+    if (!want) {
+        if (tid == 0) L.on = 0;
+        __syncthreads();
+        return;
+    }
+    // ordered compaction: each thread a contiguous run of slots
+    const int per = (b.nslots + NT - 1) / NT;
+    const int lo = min(b.nslots, tid * per), hi = min(b.nslots, lo + per);
+    int c = 0;
+    for (int a = lo; a < hi; ++a) c += b.agg_n[a] > 0;
+    int total = 0;
+    int k = block_exclusive_scan(c, warp_tmp, total);
+    if (total <= kLiveMax) {
+        for (int a = lo; a < hi; ++a) {
+            if (b.agg_n[a] > 0) {
+                L.slot[k] = a;
+                L.w[k] = R.tree[R.tree_off[0] + a];
+                ++k;
+            }
+        }
+    }
+    if (tid == 0) {
+        L.n = total;
+        L.on = total <= kLiveMax ? 1 : 0;
+    }
+    __syncthreads();
+}
+
+// Warp 0: the first listed slot whose running weight (in slot order)
+// exceeds t -- the leaf the tree's descent reaches for the same target,
+// the weights being the tree's exact integers.
+__device__ inline int live_sample(const LiveList &L, unsigned long long t) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long v[4];
+    unsigned long long sum = 0ULL;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int i = 4 * lane + j;
+        v[j] = i < L.n ? L.w[i] : 0ULL;
+        sum += v[j];
+    }
+    unsigned long long incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const unsigned over = __ballot_sync(0xffffffffu, incl > t);
+    const int src = over ? __ffs(over) - 1 : 31;
+    int idx = -1;
+    if (lane == src) {
+        unsigned long long run = incl - sum;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            run += v[j];
+            if (idx < 0 && v[j] > 0ULL && run > t) idx = 4 * lane + j;
+        }
+    }
+    idx = __shfl_sync(0xffffffffu, idx, src);
+    return (idx >= 0 && idx < L.n) ? L.slot[idx] : -1;
+}
+
+// After a merge (thread 0): the removed slot leaves the list, the kept one
+// takes its new weight.
+__device__ inline void live_merge(LiveList &L, int keep, int removed, unsigned long long w_keep) {
+    int j = 0;
+    for (int i = 0; i < L.n; ++i) {
+        const int s = L.slot[i];
+        if (s == removed) continue;
+        L.slot[j] = s;
+        L.w[j] = s == keep ? w_keep : L.w[i];
+        ++j;
+    }
+    L.n = j;
 }
 
 // ------------------------------------------------------------ physics
@@ -719,17 +807,22 @@ __device__ inline bool step_commit(const BoxRun &R, RS &sm, long long &t_phase) 
         if (sm.stop) return false;
         if (sm.merged && tid < 32 && !R.phys.growth) {
             tree_set(R, sm.tree, sm.removed, 0ULL);
-            const unsigned long long total =
-                tree_set(R, sm.tree, sm.keep, tree_weight(st, A(b, AGG_TIME_STEP, sm.keep)));
+            const unsigned long long wk = tree_weight(st, A(b, AGG_TIME_STEP, sm.keep));
+            const unsigned long long total = tree_set(R, sm.tree, sm.keep, wk);
             if (tid == 0) {
                 tree_total_to_state(st, total);
                 sm.rescale = total > kTreeHeadroom;  // a new scale keeps the total clear of 2^64
+                if (sm.live.on) live_merge(sm.live, sm.keep, sm.removed, wk);
             }
         }
         __syncthreads();
         if (sm.merged && !R.phys.growth && sm.rescale) {
             block_tree_build(R);
             tree_cache_load(R, sm.tree);
+            live_load(R, sm.live, sm.u.q.warp_tmp);  // every weight changed
+        } else if (sm.merged && !R.phys.growth && !sm.live.on && sm.live.allow &&
+                   b.sc->n_alive <= sm.live.max) {
+            live_load(R, sm.live, sm.u.q.warp_tmp);  // few enough left now
         }
     }
     if (R.phys.growth) {
@@ -784,7 +877,7 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
     __syncthreads();
     if (sm.stop) return false;
     if (tid < 32) {
-        int slot = tree_sample(R, sm.tree, sm.t_pick);
+        int slot = sm.live.on ? live_sample(sm.live, sm.t_pick) : tree_sample(R, sm.tree, sm.t_pick);
         if (tid == 0) {
             if (slot < 0 || slot >= b.nslots || b.agg_n[slot] == 0) {
                 st.status = ST_UNKNOWN;  // the tree lost a live slot: stop this box
@@ -806,7 +899,7 @@ __device__ inline bool block_mc_step(const BoxRun &R, RS &sm) {
         t_phase = t;
     }
     if (R.lim.with_collisions) {
-        block_query(b, sm.slot, Vec3{sm.dir[0], sm.dir[1], sm.dir[2]}, sm.full, sm.u.q);
+        block_query(b, sm.slot, Vec3{sm.dir[0], sm.dir[1], sm.dir[2]}, sm.full, sm.u.q, &sm.live);
         if (tid == 0) apply_query(st, sm, sm.u.q.out);
     } else if (tid == 0) {
         sm.contact = 0;

@@ -359,3 +359,38 @@ def test_speculative_rounds_give_the_same_runs(threads):
                 assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64)), (mode, k)
                 assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64)), (mode, k)
                 assert np.array_equal(s1.members, s2.members), (mode, k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("threads", [32, 256])
+def test_live_list_gives_the_same_runs(threads):
+    """Once few aggregates are left the loop picks from, and finds
+    neighbours through, a list of the live aggregates in shared memory
+    (mcacg_set_live_list_max); the runs are those of the tree and the Verlet
+    cells, bit for bit, down to one aggregate."""
+    from mcac_gb300.api import set_live_list_max
+    specs = [(400, 5e-3), (700, 1e-3), (1500, 3e-3)]
+    models = [PhysicalModel(text=small_ini(n, 170 + k, mode=("lognormal" if k % 2 else "normal"), disp=1.3, fv=fv,
+                                           nagg=1, wait=20000))
+              for k, (n, fv) in enumerate(specs)]
+    runs = {}
+    for live in (0, 128, 40):
+        prev = set_live_list_max(live)
+        try:
+            with Batch(models) as b:
+                b.threads = threads
+                b.run(max_steps=0, steps_per_launch=20000)
+                st = b.stats()
+                assert np.all(st["status"] == 0) and np.all(st["finished"] == 1)
+                runs[live] = (st, b.store_all())
+        finally:
+            set_live_list_max(prev)
+    ref_st, ref = runs[0]
+    for live in (128, 40):
+        st, snaps = runs[live]
+        assert np.array_equal(st["steps"], ref_st["steps"]), live
+        assert np.array_equal(st["time"].view(np.int64), ref_st["time"].view(np.int64)), live
+        for s1, s2 in zip(snaps, ref):
+            assert np.array_equal(s1.spheres.view(np.int64), s2.spheres.view(np.int64)), live
+            assert np.array_equal(s1.aggregates.view(np.int64), s2.aggregates.view(np.int64)), live
+            assert np.array_equal(s1.members, s2.members), live

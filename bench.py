@@ -156,15 +156,15 @@ K_RUN_DRAM_BYTES_PER_STEP = 6.72e3
 # DRAM bytes of one k_query_batch launch of the contact-search workload
 # (10,000 queries on the 1,000,000-sphere snapshot), from one ncu capture.
 K_QUERY_BATCH_DRAM_BYTES = 12.12e6
-# DRAM bytes per MC step of k_run on the ensemble benchmark's windows, from
-# one ncu capture (--set full) of a small case of the same workload: the
-# first 128 boxes, window a capped at 2000 steps, 128 threads per box:
-# 257.0 MB read + 62.5 MB written over 249,941 steps.
-K_RUN_ENS_DRAM_BYTES_PER_STEP = 1.278e3
-K_RUN_ENS_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_run launch on a small case of "
-                            "this workload (first 128 boxes, window a capped at 2000 steps, 128 threads per box): "
-                            "1.28 kB per MC step, scaled by the MC steps of one launch; that case's state (150 MB) "
-                            "mostly stays in L2 (92% hit rate), so the full run's traffic may be higher")
+# DRAM bytes per MC step of k_run on the ensemble benchmark's window a, from
+# one ncu capture of the full-size benchmark (1-pass metrics
+# dram__bytes_read.sum + dram__bytes_write.sum, window a's launch: 72.1 GB
+# read + 13.1 GB written over 18.15 M steps in 2.94 s). A small case of the
+# same kernel that stays in L2 moves 1.28 kB per step.
+K_RUN_ENS_DRAM_BYTES_PER_STEP = 4.69e3
+K_RUN_ENS_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum (1 pass) of window a's k_run launch of "
+                            "this benchmark at full size: 85.2 GB over 18.15 M MC steps, 4.69 kB per step, scaled "
+                            "by the MC steps of one launch (window b's launch moves less per step)")
 
 
 # Seeds whose reference initial state is degenerate: one monomer is drawn so

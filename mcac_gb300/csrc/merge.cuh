@@ -450,18 +450,23 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
         b.sph_volw[s] = vol;
     }
     __syncthreads();
+    // overlapping's terms (rsum - d) / rsum of the (i, j)-ordered pairs, formed
+    // in parallel (each one rounding as in the reference); summed in pair
+    // order below. The pair sort's scratch is free by now.
+    double *ov_terms = b.pair_tmp_d;
+    for (int p = tid; p < P; p += NT) {
+        const double rsum = S(b, SPH_R, mem[b.pair_i[p]]) + S(b, SPH_R, mem[b.pair_j[p]]);
+        ov_terms[p] = (rsum - b.pair_d[p]) / rsum;
+    }
+    __syncthreads();
     {
         // seven independent ordered sums, one per lane of the first warp
         if (tid < 7) sm.sums[tid] = ordered_sum(wv + size_t(tid) * W, n);
-        if (tid == 0) {
-            // overlapping: sequential over (i, j)-ordered pairs
+        // the overlap sum, sequential over the pairs, on the second warp
+        // when there is one (beside the seven)
+        if (tid == (NT > 32 ? 32 : 0)) {
             double ov = 0.0;
-            for (int p = 0; p < P; ++p) {
-                int i = b.pair_i[p], j = b.pair_j[p];
-                double rsum = S(b, SPH_R, mem[i]) + S(b, SPH_R, mem[j]);
-                double c = (rsum - b.pair_d[p]) / rsum;
-                ov += 2.0 * c;
-            }
+            for (int p = 0; p < P; ++p) ov += 2.0 * ov_terms[p];
             sm.sums[7] = ov;
             sm.n_pairs = P;
         }

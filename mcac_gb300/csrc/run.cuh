@@ -342,32 +342,37 @@ __device__ inline void live_merge(LiveList &L, int keep, int removed, unsigned l
 }
 
 // ------------------------------------------------------------ physics
-// update_partial's physics (aggregat.cpp:264-276, physical_model.cpp:550-617)
-// with CUDA's erf / exp / pow.
+// update_partial's physics (aggregat.cpp:264-276, physical_model.cpp:550-617):
+// friction, mobility diameter, time step and mean free path, in FP32 with
+// CUDA's erff / expf / powf. FP64 runs at 1/64 of the FP32 rate on this
+// part, and one merge's physics took ~10 us of FP64 (four transcendental
+// functions, divisions and a square root on one thread); these values only
+// set the loop's rates, which it follows statistically. Relative error of
+// the results about 1e-6 (a few FP32 roundings and the functions' 1-2 ulp);
+// the values stay far inside FP32's range (f ~1e-12..1e-6 kg/s, time steps
+// ~1e-9..1e-2 s). The common factors are taken once: one pow (its square
+// root form squared) and the reciprocals of the gas mean free path and of
+// the fractal dimension from the host. dg/dp, a geometric ratio, stays FP64.
 __device__ inline void device_physics(const PhysParams &p, double V, double vol_pp, double dp, double rg, double *f_agg,
                                double *d_m, double *time_step, double *lpm, double *dg_over_dp) {
-    // The same formulas with the common factors taken once: one pow (its
-    // square root form squared), reciprocals of the gas mean free path and
-    // of the fractal dimension from the host, and six divisions (FP64 is
-    // scarce on this GPU; the device loop follows the reference
-    // statistically, and these values agree with it to the last bits).
-    const double r = 0.5 * dp;
-    const double a = 1.142, b = 0.558, c = 0.999;
-    const double lr = p.lambda / r;
-    const double fe = 0.689 * (1. + erf((lr + 4.454) * (1.0 / 10.628)));
-    const double cc = 1.0 + lr * (a + b * exp(-c * r * p.inv_lambda));
-    const double ratio = V / vol_pp;
-    const double pw2 = pow(ratio, 0.5 * fe * p.inv_fractal_dimension);
-    const double pw = pw2 * pw2;
-    const double f = (6. * pi_value() * p.viscosity * r / cc) * pw;
-    const double ar = r * pw2;
-    const double cc_a = 1.0 + (p.lambda / ar) * (a + b * exp(-c * ar * p.inv_lambda));
-    *f_agg = f;
-    *d_m = (cc_a / cc) * 2.0 * r * pw;
-    const double inv_f = 1.0 / f;
-    *time_step = 3. * (p.density * V) * inv_f;
-    *lpm = sqrt(6. * kBoltzmann * p.temperature * inv_f * *time_step);
-    *dg_over_dp = rg / r;
+    const float r = float(0.5 * dp);
+    const float a = 1.142f, b = 0.558f, c = 0.999f;
+    const float lambda = float(p.lambda), inv_lambda = float(p.inv_lambda);
+    const float lr = lambda / r;
+    const float fe = 0.689f * (1.f + erff((lr + 4.454f) * (1.f / 10.628f)));
+    const float cc = 1.f + lr * (a + b * expf(-c * r * inv_lambda));
+    const float ratio = float(V) / float(vol_pp);
+    const float pw2 = powf(ratio, 0.5f * fe * float(p.inv_fractal_dimension));
+    const float pw = pw2 * pw2;
+    const float f = (6.f * float(pi_value()) * float(p.viscosity) * r / cc) * pw;
+    const float ar = r * pw2;
+    const float cc_a = 1.f + (lambda / ar) * (a + b * expf(-c * ar * inv_lambda));
+    const float ts = 3.f * (float(p.density) * float(V)) / f;
+    *f_agg = double(f);
+    *d_m = double((cc_a / cc) * 2.f * r * pw);
+    *time_step = double(ts);
+    *lpm = double(sqrtf(6.f * float(kBoltzmann) * float(p.temperature) / f * ts));
+    *dg_over_dp = rg / (0.5 * dp);
 }
 
 __device__ __forceinline__ bool run_finished(const BoxRun &R, const RunState &st, int n_alive) {

@@ -647,8 +647,22 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
         sm.cand_order[rank] = k;
     }
     __syncthreads();
-    // per-candidate sphere prefix (in sorted order) and best keys
-    if (tid == 0) {
+    // per-candidate sphere prefix (in sorted order) and best keys; up to 32
+    // candidates the counts are read by the lanes of warp 0 at once and
+    // scanned there (the chain of dependent loads of one thread otherwise)
+    if (nc <= 32) {
+        if (tid < 32) {
+            const int cnt = tid < nc ? b.agg_n[sm.cand_slot[sm.cand_order[tid]]] : 0;
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (tid >= o) incl += y;
+            }
+            if (tid < nc) sm.cand_prefix[tid] = incl - cnt;
+            if (tid == nc - 1) sm.cand_prefix[nc] = incl;
+        }
+    } else if (tid == 0) {
         int run = 0;
         for (int r = 0; r < nc; ++r) {
             sm.cand_prefix[r] = run;
@@ -931,31 +945,52 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     }
     __syncthreads();
 
-    // ---- 4: the reference's ordered walk with early exits
-    if (tid == 0) {
+    // ---- 4: the reference's ordered walk with early exits (warp 0; up to
+    // 32 candidates their values are read by the lanes at once and the walk
+    // goes through them by shuffles)
+    if (tid < 32) {
         double best = CUDART_INF;
         int best_r = -1;
-        for (int r = 0; r < nc; ++r) {
-            if (best <= 0.) break;
-            if (best < sm.cand_db[sm.cand_order[r]]) break;
-            if (sm.best_res[r] == ~0ULL) continue;  // no finite pair: +inf never wins
-            double res = dkey_inv(sm.best_res[r]);
-            if (res < best) {
-                best = res;
-                best_r = r;
+        if (nc <= 32) {
+            const double db_l = tid < nc ? sm.cand_db[sm.cand_order[tid]] : 0.0;
+            const unsigned long long br_l = tid < nc ? sm.best_res[tid] : ~0ULL;
+            for (int r = 0; r < nc; ++r) {
+                const double db_r = __shfl_sync(0xffffffffu, db_l, r);
+                const unsigned long long br_r = __shfl_sync(0xffffffffu, br_l, r);
+                if (best <= 0.) break;
+                if (best < db_r) break;
+                if (br_r == ~0ULL) continue;  // no finite pair: +inf never wins
+                const double res = dkey_inv(br_r);
+                if (res < best) {
+                    best = res;
+                    best_r = r;
+                }
+            }
+        } else if (tid == 0) {
+            for (int r = 0; r < nc; ++r) {
+                if (best <= 0.) break;
+                if (best < sm.cand_db[sm.cand_order[r]]) break;
+                if (sm.best_res[r] == ~0ULL) continue;  // no finite pair: +inf never wins
+                double res = dkey_inv(sm.best_res[r]);
+                if (res < best) {
+                    best = res;
+                    best_r = r;
+                }
             }
         }
-        sm.out.distance = best;
-        if (best_r >= 0) {
-            unsigned long long ij = sm.best_ij[best_r];
-            int i = int(ij >> 32), j = int(ij & 0xffffffffu);
-            int cslot = sm.cand_slot[sm.cand_order[best_r]];
-            sm.out.moving_sphere = pool_id[off_m + i];
-            sm.out.other_sphere = pool_id[b.agg_off[cslot] + j];
-            sm.out.other_slot = cslot;
+        if (tid == 0) {
+            sm.out.distance = best;
+            if (best_r >= 0) {
+                unsigned long long ij = sm.best_ij[best_r];
+                int i = int(ij >> 32), j = int(ij & 0xffffffffu);
+                int cslot = sm.cand_slot[sm.cand_order[best_r]];
+                sm.out.moving_sphere = pool_id[off_m + i];
+                sm.out.other_sphere = pool_id[b.agg_off[cslot] + j];
+                sm.out.other_slot = cslot;
+            }
+            sm.out.n_pairs_refined = sm.n_refined;
+            sm.out.cyc_pairs = clock64() - sm.t_q0 - sm.out.cyc_scan;
         }
-        sm.out.n_pairs_refined = sm.n_refined;
-        sm.out.cyc_pairs = clock64() - sm.t_q0 - sm.out.cyc_scan;
     }
     __syncthreads();
 }

@@ -533,19 +533,27 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
     for (int o = 16; o > 0; o >>= 1) rmax_local = dmax(rmax_local, __shfl_xor_sync(0xffffffffu, rmax_local, o));
     if ((tid & 31) == 0) sm.rmax_warp[tid >> 5] = rmax_local;
     __syncthreads();
+    // the removed slot leaves the grids on the second warp, beside the sums
+    // below (the grid lists are unordered: the order of their updates sets
+    // no result); with one warp, thread 0 does it after them
+    const int grid_thread = NT > 32 ? 32 : 0;
+    if (grid_thread != 0 && tid == grid_thread) {
+        cell_remove(b, cell_index(b, b.agg_cell[removed]), removed);
+        if (b.fine_div > 0) fine_unlink(b, removed);
+    }
+    double x = 0.0, y = 0.0, z = 0.0, rmax = 0.0, vol_pp = 0.0;
     if (tid == 0) {
-        double rmax = 0.0;
         for (int k = 0; k < NT / 32; ++k) rmax = dmax(rmax, sm.rmax_warp[k]);
         double arg = ordered_sum(wv + 7 * W, n);
         double brg = sm.sums[5];
         double rg = sqrt(fabs((arg + (3. / 5.) * brg) / V));
         double dp = 2 * sm.sums[6] / static_cast<double>(n);
-        double vol_pp = sm.vol_raw / static_cast<double>(n);
+        vol_pp = sm.vol_raw / static_cast<double>(n);
         const double overlapping = sm.overlap, coordination = sm.coord;
         const int s0 = mem[0];
-        double x = periodic_position(S(b, SPH_X, s0) + sm.r_cm[0], b.L);
-        double y = periodic_position(S(b, SPH_Y, s0) + sm.r_cm[1], b.L);
-        double z = periodic_position(S(b, SPH_Z, s0) + sm.r_cm[2], b.L);
+        x = periodic_position(S(b, SPH_X, s0) + sm.r_cm[0], b.L);
+        y = periodic_position(S(b, SPH_Y, s0) + sm.r_cm[1], b.L);
+        z = periodic_position(S(b, SPH_Z, s0) + sm.r_cm[2], b.L);
         A(b, AGG_RG, keep) = rg;
         A(b, AGG_RMAX, keep) = rmax;
         A(b, AGG_VOLUME, keep) = V;
@@ -560,9 +568,14 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
         A(b, AGG_OVERLAPPING, keep) = overlapping;
         A(b, AGG_COORDINATION_NUMBER, keep) = coordination;
         b.agg_f4[keep] = make_float4(float(x), float(y), float(z), float(rmax));
+    }
+    __syncthreads();
+    if (tid == 0) {
+        if (grid_thread == 0) {
+            cell_remove(b, cell_index(b, b.agg_cell[removed]), removed);
+            if (b.fine_div > 0) fine_unlink(b, removed);
+        }
         regrid(b, keep, Vec3{x, y, z});
-        cell_remove(b, cell_index(b, b.agg_cell[removed]), removed);
-        if (b.fine_div > 0) fine_unlink(b, removed);
         if (rmax > sc->maxradius) sc->maxradius = rmax;
         out->merged = 1;
         out->status = ST_OK;

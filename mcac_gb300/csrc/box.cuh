@@ -284,6 +284,13 @@ struct QuerySmemT {
     unsigned long long *best_ij;
     float4 mov[kMoveTile];
     short mov_sel[kMoveTile];  // moving spheres of the tile that can reach a candidate
+    // up to 32 candidates (the usual case) their sorted sphere prefix, slots
+    // and pool offsets are kept here too, so the pair search reads them
+    // from shared memory instead of chasing cand_order -> cand_slot ->
+    // agg_off in device memory for every candidate sphere
+    int c_pre[33];
+    int c_slot[32];
+    int c_off[32];
     float4 cand_c[kCullCands];  // candidate centre (FP32)
     float cand_ext[kCullCands]; // candidate extent from that centre (max |q - c| + r_q)
     int n_sel;
@@ -652,15 +659,25 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     // scanned there (the chain of dependent loads of one thread otherwise)
     if (nc <= 32) {
         if (tid < 32) {
-            const int cnt = tid < nc ? b.agg_n[sm.cand_slot[sm.cand_order[tid]]] : 0;
+            const int cs = tid < nc ? sm.cand_slot[sm.cand_order[tid]] : 0;
+            const int cnt = tid < nc ? b.agg_n[cs] : 0;
+            const int coff = tid < nc ? b.agg_off[cs] : 0;
             int incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, incl, o);
                 if (tid >= o) incl += y;
             }
-            if (tid < nc) sm.cand_prefix[tid] = incl - cnt;
-            if (tid == nc - 1) sm.cand_prefix[nc] = incl;
+            if (tid < nc) {
+                sm.cand_prefix[tid] = incl - cnt;
+                sm.c_pre[tid] = incl - cnt;
+                sm.c_slot[tid] = cs;
+                sm.c_off[tid] = coff;
+            }
+            if (tid == nc - 1) {
+                sm.cand_prefix[nc] = incl;
+                sm.c_pre[nc] = incl;
+            }
         }
     } else if (tid == 0) {
         int run = 0;
@@ -679,7 +696,13 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     // ---- 3: pair search
     const int n_mov = b.agg_n[src];
     const int off_m = b.agg_off[src];
-    const int n_other = sm.cand_prefix[nc];
+    // the candidates' sorted prefix, slots and pool offsets: shared memory up
+    // to 32 candidates, device memory beyond
+    const bool small_nc = nc <= 32;
+    const int *cpre = small_nc ? sm.c_pre : sm.cand_prefix;
+    auto cand_slot_of = [&](int r) { return small_nc ? sm.c_slot[r] : sm.cand_slot[sm.cand_order[r]]; };
+    auto cand_off_of = [&](int r) { return small_nc ? sm.c_off[r] : b.agg_off[sm.cand_slot[sm.cand_order[r]]]; };
+    const int n_other = cpre[nc];
     if (tid == 0) sm.out.n_cand_spheres = n_other;
     // With few candidates and a large moving aggregate, the moving spheres
     // that cannot come within reach of any candidate's spheres are dropped
@@ -691,15 +714,14 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     const bool cull = nc <= kCullCands && n_mov >= 8;
     if (cull) {
         for (int r = tid; r < nc; r += NT) {
-            sm.cand_c[r] = b.agg_f4[sm.cand_slot[sm.cand_order[r]]];
+            sm.cand_c[r] = b.agg_f4[cand_slot_of(r)];
             sm.cand_ext[r] = 0.f;
         }
         __syncthreads();
         for (int f = tid; f < n_other; f += NT) {
             int r = 0;
-            while (r + 1 < nc && sm.cand_prefix[r + 1] <= f) ++r;
-            const int cslot = sm.cand_slot[sm.cand_order[r]];
-            const float4 q = pool_pos[b.agg_off[cslot] + (f - sm.cand_prefix[r])];
+            while (r + 1 < nc && cpre[r + 1] <= f) ++r;
+            const float4 q = pool_pos[cand_off_of(r) + (f - cpre[r])];
             const float4 c = sm.cand_c[r];
             float ex = q.x - c.x, ey = q.y - c.y, ez = q.z - c.z;
             ex -= w.L * rintf(ex * w.invL);
@@ -877,12 +899,11 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
             int lo = 0, hi = nc - 1;
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
-                if (sm.cand_prefix[mid] <= f) lo = mid; else hi = mid - 1;
+                if (cpre[mid] <= f) lo = mid; else hi = mid - 1;
             }
             const int r = lo;
-            const int cslot = sm.cand_slot[sm.cand_order[r]];
-            const int jl = f - sm.cand_prefix[r];
-            const int pj = b.agg_off[cslot] + jl;
+            const int jl = f - cpre[r];
+            const int pj = cand_off_of(r) + jl;
             const float4 q = pool_pos[pj];
             // can any moving sphere reach this one?
             if (!capsule_hit(w, q.x, q.y, q.z, mov_reach + q.w)) continue;
@@ -983,7 +1004,7 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
             if (best_r >= 0) {
                 unsigned long long ij = sm.best_ij[best_r];
                 int i = int(ij >> 32), j = int(ij & 0xffffffffu);
-                int cslot = sm.cand_slot[sm.cand_order[best_r]];
+                int cslot = cand_slot_of(best_r);
                 sm.out.moving_sphere = pool_id[off_m + i];
                 sm.out.other_sphere = pool_id[b.agg_off[cslot] + j];
                 sm.out.other_slot = cslot;

@@ -932,8 +932,8 @@ def run_serve(args, rank: int, world: int) -> dict | None:
     stream = torch.cuda.current_stream()
     reqs = serve_requests(args.serve_seconds, args.rate, args.serve_nmax, seed=5000 + rank)
     models = [PhysicalModel(text=ini) for _, ini, _ in reqs]
-    threads = args.threads or 32
-    capacity = resident_boxes(threads)
+    threads = args.threads  # 0: each epoch at the largest size keeping every active run resident
+    capacity = resident_boxes(threads or 32)
     budget = int(0.5 * torch.cuda.get_device_properties(dev).total_memory)
     lat, steps_done, finished = [], 0, 0
     sampler = ClockSampler(dev)
@@ -973,7 +973,8 @@ def run_serve(args, rank: int, world: int) -> dict | None:
         "latency_s": {"p50": q(0.5), "p90": q(0.9), "p99": q(0.99), "max": q(1.0)},
         "config": {"workload": SERVE_WORKLOAD, "rate_per_s": args.rate, "arrival_seconds": args.serve_seconds,
                    "n_max": args.serve_nmax, "requests": len(reqs), "completed": int(len(lat)),
-                   "finished_to_criterion": finished, "capacity_slots": capacity, "threads_per_box": threads,
+                   "finished_to_criterion": finished, "capacity_slots": capacity,
+                   "threads_per_box": threads or "largest keeping every active run resident, per epoch",
                    "memory_budget_bytes": budget, "epoch_steps": args.epoch_steps, "epoch_ms": args.epoch_ms,
                    "wall_s": wall,
                    "surface_growth_requests": int(sum(g for _, _, g in reqs)),

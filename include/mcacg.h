@@ -436,7 +436,9 @@ typedef struct mcacg_completion {
 int mcacg_server_create(int32_t capacity, int64_t memory_budget_bytes, void *cuda_stream, int32_t keep_final_states,
                         mcacg_server **server);
 int mcacg_server_destroy(mcacg_server *server);
-/* Threads per box of the server's epochs: 32, 64, 128, 256 (default) or 512.
+/* Threads per box of the server's epochs: 32, 64, 128, 256 (default) or 512,
+ * or 0: at each epoch the largest size at which every active run is resident
+ * at once.
  * With smaller blocks more slots fit on the GPU at once
  * (mcacg_resident_boxes); results do not depend on it. */
 int mcacg_server_set_threads(mcacg_server *server, int32_t threads);

@@ -517,7 +517,8 @@ class Server:
         self.close()
 
     def set_threads(self, threads: int) -> None:
-        """Threads per box of the epochs (32, 64, 128, 256 or 512)."""
+        """Threads per box of the epochs (32, 64, 128, 256 or 512; 0: at each
+        epoch the largest size at which every active run is resident)."""
         check(lib().mcacg_server_set_threads(self._s, int(threads)))
 
     def set_epoch_ms(self, ms: float) -> None:

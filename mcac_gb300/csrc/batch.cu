@@ -993,7 +993,8 @@ int Server::create(int capacity, int64_t memory_budget, void *stream, bool keep_
 }
 
 int Server::set_threads(int threads) {
-    if (threads != 32 && threads != 64 && threads != 128 && threads != 256 && threads != 512) return ST_BAD_ARGUMENT;
+    if (threads != 0 && threads != 32 && threads != 64 && threads != 128 && threads != 256 && threads != 512)
+        return ST_BAD_ARGUMENT;
     threads_ = threads;
     return ST_OK;
 }
@@ -1156,9 +1157,22 @@ int Server::step(int64_t epoch_steps, std::string *err) {
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
+        // threads per box: as set, or (0) the largest size at which every
+        // active box is resident at once (empty slots leave at once)
+        int nt = threads_;
+        if (nt == 0) {
+            const int active = n_active();
+            nt = kRunThreadChoices[0];
+            for (int c : kRunThreadChoices) {
+                int resident = 0;
+                if (BatchRunner::resident_boxes(c, &resident, err) != ST_OK) return ST_CUDA;
+                if (resident >= active) nt = c;
+            }
+        }
+        last_threads_ = nt;
         cudaEventRecord(e0, s);
-        const cudaError_t le = launch_k_run(threads_, capacity_, s, static_cast<const BoxRun *>(runs_dev_),
-                                            capacity_, (long long)epoch_steps, epoch_budget_ns_);
+        const cudaError_t le = launch_k_run(nt, capacity_, s, static_cast<const BoxRun *>(runs_dev_), capacity_,
+                                            (long long)epoch_steps, epoch_budget_ns_);
         ++launches_;
         cudaEventRecord(e1, s);
         if (!ok_cuda(le, err, "k_run") || !ok_cuda(cudaEventSynchronize(e1), err, "k_run")) {

@@ -143,8 +143,11 @@ class Server {
     int submit(const mcacg_params &p, int64_t *id, std::string *err);
     // admit, one kernel epoch of at most 'epoch_steps' steps per box, retire
     int step(int64_t epoch_steps, std::string *err);
-    // Threads per box of the epochs (64, 128, 256 or 512; default 256).
+    // Threads per box of the epochs (32, 64, 128, 256 or 512; default 256;
+    // 0: at each epoch the largest size at which every active box is
+    // resident at once).
     int set_threads(int threads);
+    int last_threads() const { return last_threads_; }
     // Wall-time cap of an epoch in milliseconds (0: epochs end by steps only).
     void set_epoch_ms(double ms) { epoch_budget_ns_ = ms > 0 ? (long long)(ms * 1e6) : 0; }
     int n_active() const;
@@ -177,6 +180,7 @@ class Server {
     int retire(std::string *err);
     int capacity_ = 0;
     int threads_ = 256;
+    int last_threads_ = 0;           // threads per box of the last epoch
     long long epoch_budget_ns_ = 0;  // wall-time cap of an epoch (0: steps only)
     int64_t budget_ = 0, mem_in_use_ = 0, next_id_ = 0;
     bool keep_ = false;

@@ -888,7 +888,7 @@ int mcacg_server_set_threads(mcacg_server *server, int32_t threads) {
     return guarded([&] {
         if (!server) return fail(MCACG_ERR_BAD_ARGUMENT, "null server");
         if (server->impl->set_threads(threads) != 0)
-            return fail(MCACG_ERR_BAD_ARGUMENT, "threads per box must be 32, 64, 128, 256 or 512");
+            return fail(MCACG_ERR_BAD_ARGUMENT, "threads per box must be 0, 32, 64, 128, 256 or 512");
         return 0;
     });
 }

@@ -72,14 +72,16 @@ def test_memory_budget_limits_concurrency():
 
 
 @pytest.mark.gpu
-def test_time_capped_epochs_give_the_same_runs():
+@pytest.mark.parametrize("threads", [64, 0])
+def test_time_capped_epochs_give_the_same_runs(threads):
     """Epochs cut by wall time (each box does as many steps as fit) change
-    how far a box gets per epoch, never its trajectory."""
+    how far a box gets per epoch, never its trajectory; nor does the block
+    size, fixed or chosen at each epoch by the number of active runs (0)."""
     models = [PhysicalModel(text=req_ini(n, 950 + k)) for k, n in enumerate([260, 520, 380])]
     done = {}
     with Server(capacity=2, keep_final_states=True) as srv:
         srv.set_epoch_ms(2.0)
-        srv.set_threads(64)
+        srv.set_threads(threads)
         ids = [srv.submit(m) for m in models]
         for _ in range(100_000):
             active, pending = srv.step(1_000_000)

@@ -336,8 +336,8 @@ int mcacg_host_alloc(int64_t bytes, void **ptr);
  * created afterwards; default 2048. *previous (may be NULL) gets the old value. */
 int mcacg_set_merge_grid_min(int32_t n_spheres, int32_t *previous);
 /* Once at most n_aggregates aggregates of a box are left (0: never; at most
- * 128; default 128), the device-resident loop keeps the list of its live
- * aggregates in shared memory: the pick scans the list instead of descending
+ * 128; default 128), the device-resident loop at 64 or more threads per box
+ * keeps the list of its live aggregates in shared memory: the pick scans the list instead of descending
  * the pick tree in device memory, and a contact query takes its neighbours
  * from it instead of walking the Verlet cells around the moving aggregate
  * (the same neighbours, the same order). Process-wide, read by batches and

@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
         sm.deadline = budget_ns > 0 ? global_ns() + (unsigned long long)budget_ns : 0ULL;
     }
     if (threadIdx.x == 0) {
-        sm.live.allow = 1;
+        sm.live.allow = decltype(sm.live)::kCap > 1 ? 1 : 0;
         sm.live.max = R.live_max;
         sm.live.on = 0;
     }

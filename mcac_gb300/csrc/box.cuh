@@ -325,14 +325,19 @@ using QuerySmemSmall = QuerySmemT<256, 256, 128>;
 // Verlet cells around it (late in a run most of those cells are empty), and
 // the pick scans the list instead of descending the tree from HBM.
 constexpr int kLiveMax = 128;
-struct LiveList {
+template <int N>
+struct LiveListT {
+    static constexpr int kCap = N;
     int on;      // the list is in use
     int n;       // live slots listed
     int allow;   // the kernel may use a list (0: never)
-    int max;     // use a list from this many live aggregates down (<= kLiveMax)
-    int slot[kLiveMax];
-    unsigned long long w[kLiveMax];
+    int max;     // use a list from this many live aggregates down (<= kCap)
+    int slot[N];
+    unsigned long long w[N];
 };
+using LiveList = LiveListT<kLiveMax>;
+// one warp per box keeps no list: its shared memory holds 16 boxes an SM
+using LiveListNone = LiveListT<1>;
 
 // -------------------------------------------------------------- the query
 // AggregatList::distance_to_next_contact (aggregats/aggregat_list.cpp:447-532):
@@ -346,9 +351,9 @@ struct LiveList {
 //  4. the candidates are walked in filter order with the reference's two
 //     early exits.
 // Must be called by all threads of the block.
-template <class SM>
+template <class SM, class LL = LiveList>
 __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double dist, SM &sm,
-                                   const LiveList *live = nullptr) {
+                                   const LL *live = nullptr) {
     constexpr int kCellChunk = SM::kCellChunk;
     constexpr int kMoveTile = SM::kMoveTile;
     constexpr int kMaxSurvivorsSmem = SM::kSurv;

@@ -86,11 +86,17 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // shared memory for a launch: the descent then reads global memory only for
 // the lower levels. coff[lev] is the level's offset in the copy, -1 if the
 // level is not kept.
-constexpr int kTreeCache = 128;
-struct TreeCache {
-    unsigned long long v[kTreeCache];
+template <int N>
+struct TreeCacheT {
+    static constexpr int kCap = N;
+    unsigned long long v[N];
     int coff[kMaxTreeLevels];
 };
+// one warp per box (16 boxes an SM): 128 entries; larger blocks: 640, so
+// that the two levels above the leaves of a box of up to ~20 000 slots stay
+// on chip and a pick reads one level of the tree from device memory
+using TreeCache = TreeCacheT<128>;
+using TreeCacheLarge = TreeCacheT<640>;
 // The tree's weights are integers: the live slots' 1/time_step times a power
 // of 2 chosen at each rebuild so that the total stays below 2^62, rounded,
 // and at least 1 (relative rounding below 1e-13 at 1e5 slots). Sums are then
@@ -100,7 +106,7 @@ struct TreeCache {
 constexpr unsigned long long kTreeHeadroom = 1ULL << 62;
 
 
-template <class QS, class MS>
+template <class QS, class MS, class TC, class LL>
 struct RunSmemT {
     union {
         QS q;
@@ -120,20 +126,21 @@ struct RunSmemT {
     double dt_indiv, step_dt_indiv;  // the moved aggregate's own time step, and its increment
     int n_moved;                  // slots whose grid cell changed in the update of all aggregates
     int moved[kMovedCap];
-    TreeCache tree;               // top levels of the pick tree
-    LiveList live;                // the live slots when few are left (box.cuh)
+    TC tree;                      // top levels of the pick tree
+    LL live;                      // the live slots when few are left (box.cuh)
 };
-using RunSmem = RunSmemT<QuerySmem, MergeSmem>;
-using RunSmemSmall = RunSmemT<QuerySmemSmall, MergeSmemSmall>;
+using RunSmem = RunSmemT<QuerySmem, MergeSmem, TreeCacheLarge, LiveList>;
+using RunSmemSmall = RunSmemT<QuerySmemSmall, MergeSmemSmall, TreeCache, LiveListNone>;
 
 // ------------------------------------------------------------ sum tree
 // Marks the kept levels and copies them (all threads).
-__device__ inline void tree_cache_load(const BoxRun &R, TreeCache &c) {
+template <class TC>
+__device__ inline void tree_cache_load(const BoxRun &R, TC &c) {
     if (threadIdx.x == 0) {
         int used = 0;
         for (int lev = kMaxTreeLevels - 1; lev >= 0; --lev) c.coff[lev] = -1;
         for (int lev = R.tree_levels - 1; lev >= 0; --lev) {
-            if (used + R.tree_len[lev] > kTreeCache) break;
+            if (used + R.tree_len[lev] > TC::kCap) break;
             c.coff[lev] = used;
             used += R.tree_len[lev];
         }
@@ -148,7 +155,8 @@ __device__ inline void tree_cache_load(const BoxRun &R, TreeCache &c) {
 
 // Warp 0: descend from the top level to a leaf holding the target 't'
 // (0 <= t < total).
-__device__ inline int tree_sample(const BoxRun &R, const TreeCache &c, unsigned long long t) {
+template <class TC>
+__device__ inline int tree_sample(const BoxRun &R, const TC &c, unsigned long long t) {
     const int lane = threadIdx.x & 31;
     int node = 0;  // index within the current level
     for (int lev = R.tree_levels - 1; lev >= 0; --lev) {
@@ -216,7 +224,8 @@ __device__ __forceinline__ unsigned long long tree_weight(const RunState &st, do
 
 // Warp 0: set leaf 'slot' to 'w' and refresh its ancestors (in global
 // memory and in the kept copy); returns the new total.
-__device__ inline unsigned long long tree_set(const BoxRun &R, TreeCache &c, int slot, unsigned long long w) {
+template <class TC>
+__device__ inline unsigned long long tree_set(const BoxRun &R, TC &c, int slot, unsigned long long w) {
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
         R.tree[R.tree_off[0] + slot] = w;
@@ -259,11 +268,12 @@ __device__ __forceinline__ void tree_total_to_state(RunState &st, unsigned long 
 // (Re)builds the list of live slots in slot order with their tree leaf
 // weights when at most live.max aggregates are left (all threads); turns it
 // off otherwise. The pick and the query then read the list.
-__device__ inline void live_load(const BoxRun &R, LiveList &L, int *warp_tmp) {
+template <class LL>
+__device__ inline void live_load(const BoxRun &R, LL &L, int *warp_tmp) {
     const DevBox &b = R.box;
     const int tid = threadIdx.x, NT = blockDim.x;
     const int n_alive = b.sc->n_alive;
-    const bool want = L.allow && !R.phys.growth && n_alive <= L.max && L.max <= kLiveMax;
+    const bool want = L.allow && !R.phys.growth && n_alive <= L.max && L.max <= LL::kCap;
     __syncthreads();
     if (!want) {
         if (tid == 0) L.on = 0;
@@ -277,7 +287,7 @@ __device__ inline void live_load(const BoxRun &R, LiveList &L, int *warp_tmp) {
     for (int a = lo; a < hi; ++a) c += b.agg_n[a] > 0;
     int total = 0;
     int k = block_exclusive_scan(c, warp_tmp, total);
-    if (total <= kLiveMax) {
+    if (total <= LL::kCap) {
         for (int a = lo; a < hi; ++a) {
             if (b.agg_n[a] > 0) {
                 L.slot[k] = a;
@@ -288,7 +298,7 @@ __device__ inline void live_load(const BoxRun &R, LiveList &L, int *warp_tmp) {
     }
     if (tid == 0) {
         L.n = total;
-        L.on = total <= kLiveMax ? 1 : 0;
+        L.on = total <= LL::kCap ? 1 : 0;
     }
     __syncthreads();
 }
@@ -296,7 +306,9 @@ __device__ inline void live_load(const BoxRun &R, LiveList &L, int *warp_tmp) {
 // Warp 0: the first listed slot whose running weight (in slot order)
 // exceeds t -- the leaf the tree's descent reaches for the same target,
 // the weights being the tree's exact integers.
-__device__ inline int live_sample(const LiveList &L, unsigned long long t) {
+template <class LL>
+__device__ inline int live_sample(const LL &L, unsigned long long t) {
+    static_assert(LL::kCap <= 128, "four entries a lane");
     const int lane = threadIdx.x & 31;
     unsigned long long v[4];
     unsigned long long sum = 0ULL;
@@ -329,7 +341,8 @@ __device__ inline int live_sample(const LiveList &L, unsigned long long t) {
 
 // After a merge (thread 0): the removed slot leaves the list, the kept one
 // takes its new weight.
-__device__ inline void live_merge(LiveList &L, int keep, int removed, unsigned long long w_keep) {
+template <class LL>
+__device__ inline void live_merge(LL &L, int keep, int removed, unsigned long long w_keep) {
     int j = 0;
     for (int i = 0; i < L.n; ++i) {
         const int s = L.slot[i];

@@ -265,11 +265,13 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tmp, int &t
 // room); MoveTile: moving spheres staged per pass; SurvSmem: refined pairs
 // kept in shared memory (the rest in HBM). The small plan lets 16 boxes
 // share an SM.
-template <int CellChunk, int MoveTile, int SurvSmem>
+template <int CellChunk, int MoveTile, int SurvSmem, int CandCache>
 struct QuerySmemT {
     static constexpr int kCellChunk = CellChunk;
     static constexpr int kMoveTile = MoveTile;
     static constexpr int kSurv = SurvSmem;
+    static constexpr int kCandCache = CandCache;
+    static_assert(CandCache <= 32, "the cache is filled by the lanes of one warp");
     static constexpr int kGridMax = CellChunk >= 1024 ? 32 : (CellChunk >= 256 ? 16 : 11);  // grid cells per axis
     static_assert(kGridMax * kGridMax <= CellChunk, "grid must fit the cell arrays");
     int cell_prefix[kCellChunk + 1];
@@ -284,13 +286,13 @@ struct QuerySmemT {
     unsigned long long *best_ij;
     float4 mov[kMoveTile];
     short mov_sel[kMoveTile];  // moving spheres of the tile that can reach a candidate
-    // up to 32 candidates (the usual case) their sorted sphere prefix, slots
-    // and pool offsets are kept here too, so the pair search reads them
-    // from shared memory instead of chasing cand_order -> cand_slot ->
-    // agg_off in device memory for every candidate sphere
-    int c_pre[33];
-    int c_slot[32];
-    int c_off[32];
+    // up to kCandCache candidates (the usual case) their sorted sphere
+    // prefix, slots and pool offsets are kept here too, so the pair search
+    // reads them from shared memory instead of chasing cand_order ->
+    // cand_slot -> agg_off in device memory for every candidate sphere
+    int c_pre[CandCache + 1];
+    int c_slot[CandCache];
+    int c_off[CandCache];
     float4 cand_c[kCullCands];  // candidate centre (FP32)
     float cand_ext[kCullCands]; // candidate extent from that centre (max |q - c| + r_q)
     int n_sel;
@@ -316,8 +318,9 @@ struct QuerySmemT {
     CellRange range;
     QueryOut out;
 };
-using QuerySmem = QuerySmemT<1024, 512, 256>;
-using QuerySmemSmall = QuerySmemT<256, 256, 128>;
+using QuerySmem = QuerySmemT<1024, 512, 256, 32>;
+// the one-warp plan: 16 boxes an SM leave 14.25 KB of shared memory a box
+using QuerySmemSmall = QuerySmemT<256, 256, 128, 4>;
 
 // The live slots of a box with few aggregates left, in ascending slot order,
 // with their pick weights (kept in shared memory by the device loop). With
@@ -675,13 +678,15 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
             }
             if (tid < nc) {
                 sm.cand_prefix[tid] = incl - cnt;
-                sm.c_pre[tid] = incl - cnt;
-                sm.c_slot[tid] = cs;
-                sm.c_off[tid] = coff;
+                if (tid < SM::kCandCache) {
+                    sm.c_pre[tid] = incl - cnt;
+                    sm.c_slot[tid] = cs;
+                    sm.c_off[tid] = coff;
+                }
             }
             if (tid == nc - 1) {
                 sm.cand_prefix[nc] = incl;
-                sm.c_pre[nc] = incl;
+                if (nc <= SM::kCandCache) sm.c_pre[nc] = incl;
             }
         }
     } else if (tid == 0) {
@@ -702,8 +707,8 @@ __device__ inline void block_query(const DevBox &b, int src, Vec3 dir, double di
     const int n_mov = b.agg_n[src];
     const int off_m = b.agg_off[src];
     // the candidates' sorted prefix, slots and pool offsets: shared memory up
-    // to 32 candidates, device memory beyond
-    const bool small_nc = nc <= 32;
+    // to kCandCache candidates, device memory beyond
+    const bool small_nc = nc <= SM::kCandCache;
     const int *cpre = small_nc ? sm.c_pre : sm.cand_prefix;
     auto cand_slot_of = [&](int r) { return small_nc ? sm.c_slot[r] : sm.cand_slot[sm.cand_order[r]]; };
     auto cand_off_of = [&](int r) { return small_nc ? sm.c_off[r] : b.agg_off[sm.cand_slot[sm.cand_order[r]]]; };

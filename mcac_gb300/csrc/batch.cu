@@ -40,13 +40,13 @@ constexpr long long kRunLaunchBudgetNs = 200LL * 1000 * 1000;
 // cost do not wait for one another between launches.
 template <int NT>
 __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n, long long max_steps,
-                                                      long long budget_ns) {
+                                                      long long budget_ns, const int *order) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RunSmemFor<NT> &sm = *reinterpret_cast<RunSmemFor<NT> *>(smem_raw);
     __shared__ __align__(16) BoxRun R;
     __shared__ __align__(16) RunState st;  // the box's loop state, kept on chip for the launch
-    const int box = blockIdx.x;
-    if (box >= n) return;
+    if (int(blockIdx.x) >= n) return;
+    const int box = order != nullptr ? order[blockIdx.x] : int(blockIdx.x);
     RunState *st_global = runs[box].st;
     if (st_global == nullptr) return;  // an empty serving slot
     {
@@ -90,12 +90,13 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_run(const BoxRun *runs, int n,
 // 1) + rank - 1] is the query scratch of helper rank 'rank'.
 template <int NT>
 __global__ void __launch_bounds__(NT, 512 / NT) k_run_spec(const BoxRun *runs, const SpecScratch *helpers, int n,
-                                                           long long max_steps, long long budget_ns) {
+                                                           long long max_steps, long long budget_ns,
+                                                           const int *order) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     const int K = int(cluster.num_blocks());
     const int rank = int(cluster.block_rank());
-    const int box = int(blockIdx.x) / K;
+    const int box = order != nullptr ? order[int(blockIdx.x) / K] : int(blockIdx.x) / K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RunSmemFor<NT> &sm = *reinterpret_cast<RunSmemFor<NT> *>(smem_raw);
     __shared__ __align__(16) BoxRun R;
@@ -273,14 +274,15 @@ cudaError_t prepare_all_k_run() {
     if (e == cudaSuccess) e = prepare_k_run<512>();
     return e;
 }
+// order (may be null): the box each block takes, block b box order[b].
 cudaError_t launch_k_run(int nt, int grid, cudaStream_t s, const BoxRun *runs, int n, long long steps,
-                         long long budget_ns = 0) {
+                         long long budget_ns = 0, const int *order = nullptr) {
     switch (nt) {
-        case 32: k_run<32><<<grid, 32, sizeof(RunSmemFor<32>), s>>>(runs, n, steps, budget_ns); break;
-        case 64: k_run<64><<<grid, 64, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
-        case 128: k_run<128><<<grid, 128, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
-        case 512: k_run<512><<<grid, 512, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
-        default: k_run<256><<<grid, 256, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns); break;
+        case 32: k_run<32><<<grid, 32, sizeof(RunSmemFor<32>), s>>>(runs, n, steps, budget_ns, order); break;
+        case 64: k_run<64><<<grid, 64, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns, order); break;
+        case 128: k_run<128><<<grid, 128, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns, order); break;
+        case 512: k_run<512><<<grid, 512, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns, order); break;
+        default: k_run<256><<<grid, 256, sizeof(RunSmem), s>>>(runs, n, steps, budget_ns, order); break;
     }
     return cudaGetLastError();
 }
@@ -301,7 +303,7 @@ cudaLaunchConfig_t spec_config(int k, int n, cudaStream_t s, cudaLaunchAttribute
 }
 template <int NT>
 cudaError_t launch_spec_t(int k, int n, cudaStream_t s, const BoxRun *runs, const SpecScratch *h, long long steps,
-                          long long budget_ns) {
+                          long long budget_ns, const int *order) {
     static bool prepared = false;
     if (!prepared) {
         cudaError_t e = cudaFuncSetAttribute(k_run_spec<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -311,16 +313,16 @@ cudaError_t launch_spec_t(int k, int n, cudaStream_t s, const BoxRun *runs, cons
     }
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = spec_config<NT>(k, n, s, attr);
-    return cudaLaunchKernelEx(&cfg, k_run_spec<NT>, runs, h, n, steps, budget_ns);
+    return cudaLaunchKernelEx(&cfg, k_run_spec<NT>, runs, h, n, steps, budget_ns, order);
 }
 cudaError_t launch_spec(int nt, int k, int n, cudaStream_t s, const BoxRun *runs, const SpecScratch *h,
-                        long long steps, long long budget_ns) {
+                        long long steps, long long budget_ns, const int *order) {
     switch (nt) {
-        case 32: return launch_spec_t<32>(k, n, s, runs, h, steps, budget_ns);
-        case 64: return launch_spec_t<64>(k, n, s, runs, h, steps, budget_ns);
-        case 128: return launch_spec_t<128>(k, n, s, runs, h, steps, budget_ns);
-        case 512: return launch_spec_t<512>(k, n, s, runs, h, steps, budget_ns);
-        default: return launch_spec_t<256>(k, n, s, runs, h, steps, budget_ns);
+        case 32: return launch_spec_t<32>(k, n, s, runs, h, steps, budget_ns, order);
+        case 64: return launch_spec_t<64>(k, n, s, runs, h, steps, budget_ns, order);
+        case 128: return launch_spec_t<128>(k, n, s, runs, h, steps, budget_ns, order);
+        case 512: return launch_spec_t<512>(k, n, s, runs, h, steps, budget_ns, order);
+        default: return launch_spec_t<256>(k, n, s, runs, h, steps, budget_ns, order);
     }
 }
 // Clusters of k CTAs of nt threads the device keeps resident at once.
@@ -422,6 +424,7 @@ BatchRunner::~BatchRunner() {
     for (void *p : trees_) cudaFree(p);
     if (spec_mem_) cudaFree(spec_mem_);
     if (spec_tab_) cudaFree(spec_tab_);
+    if (order_dev_) cudaFree(order_dev_);
     if (runs_dev_) cudaFree(runs_dev_);
     if (states_dev_) cudaFree(states_dev_);
     if (sc_dev_) cudaFree(sc_dev_);
@@ -552,6 +555,21 @@ int BatchRunner::init(const std::vector<mcacg_params> &params, const std::vector
         return ST_CUDA;
     k_tree_build<<<n, 256, 0, s>>>(static_cast<const BoxRun *>(runs_dev_), n);
     if (!ok_cuda(cudaGetLastError(), err, "k_tree_build")) return ST_CUDA;
+    // Launch order, largest box first: blocks are handed to the SMs in index
+    // order, one per SM before a second, so the largest boxes -- the longest
+    // chains of steps -- start on SMs of their own and share them only with
+    // smaller boxes (which finish first). Each box's result does not depend
+    // on where it runs.
+    {
+        std::vector<int> order(static_cast<size_t>(n));
+        for (int i = 0; i < n; ++i) order[size_t(i)] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int c) { return boxes_[size_t(a)]->ns() > boxes_[size_t(c)]->ns(); });
+        if (!ok_cuda(cudaMalloc(&order_dev_, sizeof(int) * size_t(n)), err, "cudaMalloc") ||
+            !ok_cuda(cudaMemcpyAsync(order_dev_, order.data(), sizeof(int) * size_t(n), cudaMemcpyHostToDevice, s),
+                     err, "upload"))
+            return ST_CUDA;
+    }
     if (!ok_cuda(prepare_all_k_run(), err, "cudaFuncSetAttribute")) return ST_CUDA;
     if (!ok_cuda(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
     return ST_OK;
@@ -634,8 +652,9 @@ cudaError_t BatchRunner::launch_run(int nt, int k, long long steps, long long bu
     const int n = int(boxes_.size());
     const BoxRun *runs = static_cast<const BoxRun *>(runs_dev_);
     if (k > 1) k = std::min(k, spec_room(nullptr));  // helper scratch set up at the first such launch
-    if (k <= 1 || !spec_tab_) return launch_k_run(nt, n, s, runs, n, steps, budget_ns);
-    return launch_spec(nt, k, n, s, runs, static_cast<const SpecScratch *>(spec_tab_), steps, budget_ns);
+    const int *order = static_cast<const int *>(order_dev_);
+    if (k <= 1 || !spec_tab_) return launch_k_run(nt, n, s, runs, n, steps, budget_ns, order);
+    return launch_spec(nt, k, n, s, runs, static_cast<const SpecScratch *>(spec_tab_), steps, budget_ns, order);
 }
 
 int BatchRunner::set_threads(int threads) {

@@ -121,6 +121,7 @@ class BatchRunner {
     int spec_max_ = 0;        // CTAs per box the helper scratch allows (0: not set up yet)
     void *spec_mem_ = nullptr;  // helper query scratch
     void *spec_tab_ = nullptr;  // SpecScratch[n * (kSpecMax - 1)]
+    void *order_dev_ = nullptr; // int[n]: the box of each block of a launch, largest first
 };
 
 // Continuous-batching request loop: 'capacity' block slots; between kernel

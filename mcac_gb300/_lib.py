@@ -306,11 +306,13 @@ class StateBuffers:
         nsph = self.n_spheres[:na].copy()
         cells = np.zeros((na, 3), dtype=np.int64)
         step = st.n_verlet_divisions / st.box_length if st.box_length > 0 else 0.0
+        agg = self.aggregates.reshape(-1)[:21 * na].reshape(21, na)  # stored packed as [21][na]
         for k, f in enumerate((7, 8, 9)):
-            cells[:, k] = np.floor(self.aggregates[f, :na] * step).astype(np.int64)
+            cells[:, k] = np.floor(agg[f] * step).astype(np.int64)
         return Snapshot(
             n_div=int(st.n_verlet_divisions), box_length=float(st.box_length), maxradius=float(st.maxradius),
             time=float(st.time), physics=np.zeros(9) if physics is None else np.asarray(physics, float),
-            volsurf_method=volsurf_method, spheres=self.spheres[:, :ns].copy(),
-            sphere_label=self.sphere_label[:ns].copy(), aggregates=self.aggregates[:, :na].copy(),
+            volsurf_method=volsurf_method, spheres=self.spheres.reshape(-1)[:9 * ns].reshape(9, ns).copy(),
+            sphere_label=self.sphere_label[:ns].copy(),
+            aggregates=self.aggregates.reshape(-1)[:21 * na].reshape(21, na).copy(),
             n_spheres=nsph, members=self.members[:int(nsph.sum())].copy(), cells=cells)

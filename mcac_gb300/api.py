@@ -480,6 +480,10 @@ class Batch:
             na = int(b.state.n_aggregates)
             if na != b.aggregates.shape[1]:  # the table is stored packed as [21][na]
                 b.aggregates = b.aggregates.reshape(-1)[:21 * na].reshape(21, na)
+            ns = int(b.state.n_spheres)
+            if ns != b.spheres.shape[1]:  # spheres removed by oxidation: packed as [9][ns]
+                b.spheres = b.spheres.reshape(-1)[:9 * ns].reshape(9, ns)
+                b.sphere_label = b.sphere_label[:ns]
         if raw:
             return bufs
         return [b.to_snapshot(volsurf_method=int(self.models[k].params.volsurf_method)) for k, b in enumerate(bufs)]

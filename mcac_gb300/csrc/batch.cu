@@ -400,7 +400,9 @@ int make_box_run(const DevBox &b, const mcacg_params &p, double time, RunState *
                            1.0 / p.fractal_dimension,
                            p.with_surface_reactions ? 1 : 0,
                            p.with_surface_reactions && p.individual_surf_reactions ? 1 : 0,
-                           int(std::max<int64_t>(1, p.full_aggregate_update_frequency))};
+                           int(std::max<int64_t>(1, p.full_aggregate_update_frequency)),
+                           p.with_surface_reactions && p.u_sg < 0.0 ? 1 : 0,
+                           p.rp_min_oxid};
     run->lim.number_of_aggregates_limit = p.number_of_aggregates_limit;
     run->lim.n_iter_without_event_limit = p.n_iter_without_event_limit;
     run->lim.mean_monomere_per_aggregate_limit = p.mean_monomere_per_aggregate_limit;
@@ -1029,9 +1031,8 @@ Server::~Server() {
 }
 
 int Server::submit(const mcacg_params &p, int64_t *id, std::string *err) {
-    if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges ||
-        (p.with_surface_reactions && p.u_sg < 0.0)) {
-        if (err) *err = "served boxes cover collisions with optional surface growth (u_sg >= 0)";
+    if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges) {
+        if (err) *err = "served boxes cover collisions with optional surface reactions";
         return ST_INPUT;
     }
     if (footprint(p) > budget_) {

@@ -1361,6 +1361,15 @@ int DeviceBox::store(mcacg_state *out, std::string *err, void *copy_stream) {
         !cuda_ok(cudaStreamSynchronize(cs), err, "store"))
         return ST_CUDA;
     const int na = sc.n_alive;
+    if (na == 0) {  // every sphere oxidised: an empty state
+        out->n_spheres = 0;
+        out->n_aggregates = 0;
+        out->n_verlet_divisions = b.n_div;
+        out->box_length = b.L;
+        out->maxradius = sc.maxradius;
+        out->time = sc.time;
+        return ST_OK;
+    }
     if (out->n_spheres < b.ns || out->n_aggregates < na || na < 1) {
         if (err) *err = "state buffers too small";
         return ST_BAD_ARGUMENT;
@@ -1430,8 +1439,10 @@ int DeviceBox::store_many(const std::vector<DeviceBox *> &boxes, const std::vect
                  "store") ||
         !cuda_ok(cudaStreamSynchronize(s), err, "sync"))
         return ST_CUDA;
-    // per box: the live count, or -1 for a box that cannot be stored
+    // per box: the live count, or -1 for a box that cannot be stored or has
+    // no aggregate left (every sphere oxidised: an empty state)
     std::vector<BoxArg> args(static_cast<size_t>(n));
+    std::vector<char> empty(static_cast<size_t>(n), 0);
     for (int i = 0; i < n; ++i) {
         const DevBox &b = host_boxes[size_t(i)];
         const mcacg_state *o = outs[size_t(i)];
@@ -1440,6 +1451,8 @@ int DeviceBox::store_many(const std::vector<DeviceBox *> &boxes, const std::vect
         if (!o || !o->spheres || !o->sphere_label || !o->aggregates || !o->n_spheres_per_aggregate || !o->members) {
             (*rcs)[size_t(i)] = ST_BAD_ARGUMENT;
             (*errs)[size_t(i)] = "incomplete state buffers";
+        } else if (na == 0) {
+            empty[size_t(i)] = 1;
         } else if (o->n_spheres < b.ns || o->n_aggregates < na || na < 1) {
             (*rcs)[size_t(i)] = ST_BAD_ARGUMENT;
             (*errs)[size_t(i)] = "state buffers too small";
@@ -1482,11 +1495,11 @@ int DeviceBox::store_many(const std::vector<DeviceBox *> &boxes, const std::vect
     }
     if (!copies.join(s) || !cuda_ok(cudaStreamSynchronize(s), err, "sync")) return ST_CUDA;
     for (int i = 0; i < n; ++i) {
-        if (args[size_t(i)].a < 0) continue;
+        if (args[size_t(i)].a < 0 && !empty[size_t(i)]) continue;
         const DevBox &b = host_boxes[size_t(i)];
         mcacg_state *o = outs[size_t(i)];
-        o->n_spheres = b.ns;
-        o->n_aggregates = args[size_t(i)].a;
+        o->n_spheres = empty[size_t(i)] ? 0 : b.ns;
+        o->n_aggregates = empty[size_t(i)] ? 0 : args[size_t(i)].a;
         o->n_verlet_divisions = b.n_div;
         o->box_length = b.L;
         o->maxradius = sc[size_t(i)].maxradius;

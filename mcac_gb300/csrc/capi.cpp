@@ -57,7 +57,10 @@ int store_host_state(const mcacg::HostState &st, mcacg_state *out, std::string *
     out->time = st.time;
     if (out->spheres) std::copy(st.sph.begin(), st.sph.end(), out->spheres);
     if (out->sphere_label)
-        for (int s = 0; s < st.ns; ++s) out->sphere_label[s] = label_of[size_t(st.sph_slot[size_t(s)])];
+        for (int s = 0; s < st.ns; ++s) {
+            const int a = st.sph_slot[size_t(s)];
+            out->sphere_label[s] = a >= 0 && a < st.nslots ? label_of[size_t(a)] : -1;
+        }
     int64_t off = 0;
     for (int a = 0; a < st.nslots; ++a) {
         int l = label_of[size_t(a)];
@@ -71,6 +74,37 @@ int store_host_state(const mcacg::HostState &st, mcacg_state *out, std::string *
         off += int64_t(m.size());
     }
     return mcacg::ST_OK;
+}
+
+// Spheres taken out by oxidation (label -1) leave a stored state, as they
+// leave the reference's sphere storage (aggregat.cpp:629-641): the others
+// keep their order, the tables are packed as [9][n_spheres], and the member
+// lists are renumbered.
+void drop_removed_spheres(mcacg_state *out) {
+    const int64_t ns = out->n_spheres;
+    if (!out->sphere_label || !out->spheres) return;
+    bool any = false;
+    for (int64_t s = 0; s < ns && !any; ++s) any = out->sphere_label[s] < 0;
+    if (!any) return;
+    std::vector<int64_t> new_index(static_cast<size_t>(ns), -1);
+    int64_t live = 0;
+    for (int64_t s = 0; s < ns; ++s)
+        if (out->sphere_label[s] >= 0) new_index[size_t(s)] = live++;
+    // destinations never pass their sources: in place, in increasing order
+    for (int64_t f = 0; f < 9; ++f)
+        for (int64_t s = 0; s < ns; ++s)
+            if (new_index[size_t(s)] >= 0) out->spheres[f * live + new_index[size_t(s)]] = out->spheres[f * ns + s];
+    for (int64_t s = 0; s < ns; ++s)
+        if (new_index[size_t(s)] >= 0) out->sphere_label[new_index[size_t(s)]] = out->sphere_label[s];
+    if (out->members && out->n_spheres_per_aggregate) {
+        int64_t total = 0;
+        for (int64_t a = 0; a < out->n_aggregates; ++a) total += out->n_spheres_per_aggregate[a];
+        for (int64_t k = 0; k < total && k < ns; ++k) {
+            const int64_t m = out->members[k];
+            out->members[k] = m >= 0 && m < ns ? new_index[size_t(m)] : -1;
+        }
+    }
+    out->n_spheres = live;
 }
 
 thread_local std::string g_last_error;
@@ -190,7 +224,9 @@ int mcacg_state_synthetic(const mcacg_params *params, int32_t n_aggregates, int3
         std::string err;
         int rc = mcacg::make_synthetic_state(*params, n_aggregates, max_size, &st, &err);
         if (rc != 0) return finish(rc, err);
-        return finish(store_host_state(st, state, &err), err);
+        const int rc2 = store_host_state(st, state, &err);
+        if (rc2 == 0) drop_removed_spheres(state);
+        return finish(rc2, err);
     });
 }
 
@@ -481,9 +517,8 @@ int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_s
         *batch = nullptr;
         std::vector<mcacg_params> ps(params, params + n_boxes);
         for (const auto &p : ps)
-            if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges ||
-                (p.with_surface_reactions && p.u_sg < 0.0))
-                return fail(mcacg::ST_INPUT, "batched boxes cover collisions with optional surface growth (u_sg >= 0)");
+            if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges)
+                return fail(mcacg::ST_INPUT, "batched boxes cover collisions with optional surface reactions");
         // placements in parallel: each box draws from its own copy of the C
         // library stream, so the result equals a sequential placement
         std::vector<mcacg::HostState> states(static_cast<size_t>(n_boxes));
@@ -510,9 +545,17 @@ int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state
         if (!params || !states || !batch || n_boxes <= 0) return fail(MCACG_ERR_BAD_ARGUMENT, "bad argument");
         *batch = nullptr;
         std::vector<mcacg_params> ps(params, params + n_boxes);
+        for (const auto &p : ps)
+            if (p.with_nucleation || p.with_potentials || p.with_flame_coupling || p.with_electric_charges)
+                return fail(mcacg::ST_INPUT, "batched boxes cover collisions with optional surface reactions");
         // the boxes load straight from the caller's arrays (by DMA when they
         // are page-locked); the device checks labels, counts and member lists
         std::vector<mcacg::StateView> views(static_cast<size_t>(n_boxes));
+        // a box that oxidises needs a slot for every sphere (splits): its
+        // aggregate table is copied into one with dead slots after the live ones
+        std::vector<std::vector<double>> pad_agg(static_cast<size_t>(n_boxes));
+        std::vector<std::vector<int64_t>> pad_count(static_cast<size_t>(n_boxes));
+        bool padded = false;
         for (int i = 0; i < n_boxes; ++i) {
             const mcacg_state &in = states[i];
             if (in.n_spheres <= 0 || in.n_aggregates <= 0 || in.n_spheres > INT32_MAX ||
@@ -536,7 +579,23 @@ int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state
             v.dead_slots = false;
             ps[size_t(i)].box_length = in.box_length;
             ps[size_t(i)].n_verlet_divisions = in.n_verlet_divisions;
+            const mcacg_params &p = ps[size_t(i)];
+            if (p.with_surface_reactions && p.u_sg < 0.0 && v.nslots < v.ns) {
+                const size_t ns = size_t(v.ns), na = size_t(v.nslots);
+                std::vector<double> &agg = pad_agg[size_t(i)];
+                agg.assign(21 * ns, 0.0);
+                for (size_t f = 0; f < 21; ++f)
+                    std::copy(in.aggregates + f * na, in.aggregates + (f + 1) * na, agg.begin() + long(f * ns));
+                pad_count[size_t(i)].assign(ns, 0);
+                std::copy(in.n_spheres_per_aggregate, in.n_spheres_per_aggregate + na, pad_count[size_t(i)].begin());
+                v.nslots = v.ns;
+                v.agg = agg.data();
+                v.agg_n = pad_count[size_t(i)].data();
+                padded = true;
+            }
         }
+        if (padded)
+            for (auto &v : views) v.dead_slots = true;
         std::string err;
         std::unique_ptr<mcacg_batch> b(new mcacg_batch());
         int rc = mcacg::BatchRunner::create(ps, views, cuda_stream, &b->impl, &err);
@@ -620,12 +679,15 @@ int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state)
             int rc = batch->impl->times(&times, &err);
             if (rc == 0) rc = batch->impl->box(box).store(state, &err);
             if (rc == 0) state->time = times[size_t(box)];
+            if (rc == 0) drop_removed_spheres(state);
             return finish(rc, err);
         }
         mcacg::HostState st;
         int rc = batch->impl->download(box, &st, &err);
         if (rc != 0) return finish(rc, err);
-        return finish(store_host_state(st, state, &err), err);
+        const int rc2 = store_host_state(st, state, &err);
+        if (rc2 == 0) drop_removed_spheres(state);
+        return finish(rc2, err);
     });
 }
 
@@ -654,6 +716,7 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
         for (size_t k = 0; k < direct.size(); ++k) {
             if (rcs[k] != 0) return fail(rcs[k], "box " + std::to_string(direct[k]) + ": " + errs[k]);
             states[direct[k]].time = times[size_t(direct[k])];
+            drop_removed_spheres(&states[direct[k]]);
         }
         // growing boxes with volsurf "none": overlap and coordination
         // refreshed on the host, one copy stream per worker thread
@@ -675,6 +738,7 @@ int mcacg_batch_store_states(mcacg_batch *batch, mcacg_state *states, int32_t n_
             mcacg::host_refresh_overlap(&st);
             st.time = times[size_t(i)];
             rcs[size_t(k)] = store_host_state(st, &states[i], &errs[size_t(k)]);
+            if (rcs[size_t(k)] == 0) drop_removed_spheres(&states[i]);
         });
         for (size_t k = 0; k < grown.size(); ++k)
             if (rcs[k] != 0) return fail(rcs[k], "box " + std::to_string(grown[k]) + ": " + errs[k]);
@@ -947,7 +1011,9 @@ int mcacg_server_final_state(mcacg_server *server, int64_t id, mcacg_state *stat
         mcacg::HostState st;
         if (server->impl->final_state(id, &st) != 0) return fail(MCACG_ERR_BAD_ARGUMENT, "no final state for id");
         std::string err;
-        return finish(store_host_state(st, state, &err), err);
+        const int rc2 = store_host_state(st, state, &err);
+        if (rc2 == 0) drop_removed_spheres(state);
+        return finish(rc2, err);
     });
 }
 

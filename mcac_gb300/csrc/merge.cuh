@@ -115,13 +115,149 @@ __device__ __forceinline__ double ordered_sum(const double *v, int n) {
     return acc;
 }
 
+// Every pair i < j of the n spheres mem[0..n) of one aggregate whose FP32
+// relative positions pass the screen |rel_i - rel_j| <= (r_i + r_j) 1.0001 +
+// margin + extra goes to test(i, j) (any thread, any order); the margin is
+// 1e-5 of the aggregate's extent, far above the FP32 rounding, so every pair
+// within (r_i + r_j)(1 + 1e-4) + extra in FP64 is handed over. All threads
+// call it; b.work holds the staging (52 n + 4 bytes at most).
+template <class SM, class F>
+__device__ inline void block_pair_scan(const DevBox &b, const int *mem, int n, SM &sm, float extra, F &&test) {
+    constexpr int kPairTile = SM::kPairTile;
+    const int tid = threadIdx.x, NT = blockDim.x;
+    // stage relative positions (FP32) and the extent for the screening margin
+    float4 *relf = reinterpret_cast<float4 *>(b.work);  // reuse: n float4 fit in work[0..n/2)
+    float ext = 0.f, rmx = 0.f;
+    for (int k = tid; k < n; k += NT) {
+        int s = mem[k];
+        float4 v = make_float4(float(S(b, SPH_RX, s)), float(S(b, SPH_RY, s)), float(S(b, SPH_RZ, s)),
+                               float(S(b, SPH_R, s)));
+        relf[k] = v;
+        ext = fmaxf(ext, fabsf(v.x) + fabsf(v.y) + fabsf(v.z) + v.w);
+        rmx = fmaxf(rmx, v.w);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
+        rmx = fmaxf(rmx, __shfl_xor_sync(0xffffffffu, rmx, o));
+    }
+    if ((tid & 31) == 0) {
+        sm.warp_f[tid >> 5] = ext;
+        sm.warp_tmp[tid >> 5] = __float_as_int(rmx);  // non-negative: int order is float order
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float m = 0.f, r = 0.f;
+        for (int k = 0; k < NT / 32; ++k) {
+            m = fmaxf(m, sm.warp_f[k]);
+            r = fmaxf(r, __int_as_float(sm.warp_tmp[k]));
+        }
+        sm.margin = 1.0e-5f * m;  // FP32 error of |rel_i - rel_j| is ~1e-7 of the extent
+        sm.ext = m;
+        sm.rmax_f = r;
+    }
+    __syncthreads();
+    const float pm_margin = sm.margin + extra;
+    // the FP32 screen of one pair i < j; the survivors go to 'test'
+    auto pair_test = [&](int i, int j, const float4 &pi_, const float4 &pj_) {
+        const float dx = pi_.x - pj_.x, dy = pi_.y - pj_.y, dz = pi_.z - pj_.z;
+        const float reach = (pi_.w + pj_.w) * 1.0001f + pm_margin;
+        if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz)) > reach * reach) return;
+        test(i, j);
+    };
+    if (n >= b.grid_pairs_min) {
+        // Large aggregates: a hashed cell grid over the relative positions
+        // (cells wider than any pair's screening reach, 2 r_max 1.0001 +
+        // margin, by one more margin -- 100 times the FP32 rounding of the
+        // cell coordinates -- and 0.1%), so that every pair
+        // that can pass the screen sits in neighbouring cells; each sphere
+        // meets the spheres of its 27 cells with a larger index. The same
+        // pairs as the all-pairs loop, found in O(n) (a merge of two
+        // 8000-sphere aggregates needs 10^8 pair tests otherwise).
+        // Scratch after the n float4 of relf: cell coordinates (int4, n),
+        // bucket counts/starts (2^k + 1 >= 2n + 1), sorted sphere indices (n).
+        // With nb < 4n that is 16n + 16n + 4(nb + 1) + 4n <= 52n + 4 bytes,
+        // inside the work area of 8 doubles (64 B) per sphere of the box
+        // (n <= ns); a larger carve needs a larger work area.
+        int4 *cellc = reinterpret_cast<int4 *>(relf + n);
+        int nb = 1;
+        while (nb < 2 * n) nb <<= 1;
+        int *bstart = reinterpret_cast<int *>(cellc + n);
+        int *sorted = bstart + nb + 1;
+        const float h = ((2.f * sm.rmax_f) * 1.0001f + 2.f * pm_margin) * 1.001f;
+        const float inv_h = 1.f / h, e0 = sm.ext;
+        auto bucket_of = [&](int cx, int cy, int cz) {
+            const unsigned hsh = (unsigned(cx) * 73856093u) ^ (unsigned(cy) * 19349663u) ^ (unsigned(cz) * 83492791u);
+            return int(hsh & unsigned(nb - 1));
+        };
+        for (int k = tid; k <= nb; k += NT) bstart[k] = 0;
+        __syncthreads();
+        for (int k = tid; k < n; k += NT) {
+            const float4 v = relf[k];
+            const int cx = int(floorf((v.x + e0) * inv_h)), cy = int(floorf((v.y + e0) * inv_h)),
+                      cz = int(floorf((v.z + e0) * inv_h));
+            const int bk = bucket_of(cx, cy, cz);
+            cellc[k] = make_int4(cx, cy, cz, bk);
+            atomicAdd(&bstart[bk], 1);
+        }
+        __syncthreads();
+        block_scan_global(bstart, nb + 1, sm.warp_tmp);  // bstart[nb] = n
+        __syncthreads();
+        // scatter (bstart[bk] advances to the bucket's end; starts are then
+        // bstart[bk - 1], or 0)
+        for (int k = tid; k < n; k += NT) sorted[atomicAdd(&bstart[cellc[k].w], 1)] = k;
+        __syncthreads();
+        for (int i = tid; i < n; i += NT) {
+            const float4 pi_ = relf[i];
+            const int4 ci = cellc[i];
+            for (int ox = -1; ox <= 1; ++ox)
+                for (int oy = -1; oy <= 1; ++oy)
+                    for (int oz = -1; oz <= 1; ++oz) {
+                        const int cx = ci.x + ox, cy = ci.y + oy, cz = ci.z + oz;
+                        const int bk = bucket_of(cx, cy, cz);
+                        const int beg = bk == 0 ? 0 : bstart[bk - 1], end = bstart[bk];
+                        for (int t = beg; t < end; ++t) {
+                            const int j = sorted[t];
+                            if (j <= i) continue;
+                            const int4 cj = cellc[j];
+                            if (cj.x != cx || cj.y != cy || cj.z != cz) continue;  // another cell in the bucket
+                            pair_test(i, j, pi_, relf[j]);
+                        }
+                    }
+        }
+        __syncthreads();
+    } else {
+    for (int j0 = 0; j0 < n; j0 += kPairTile) {
+        const int nt = min(kPairTile, n - j0);
+        for (int k = tid; k < nt; k += NT) {
+            float4 v = relf[j0 + k];
+            sm.tile_f[4 * k + 0] = v.x;
+            sm.tile_f[4 * k + 1] = v.y;
+            sm.tile_f[4 * k + 2] = v.z;
+            sm.tile_f[4 * k + 3] = v.w;
+        }
+        __syncthreads();
+        for (int i = tid; i < min(n, j0 + nt); i += NT) {
+            const float4 pi_ = relf[i];
+            int jstart = max(i + 1, j0) - j0;
+            for (int jj = jstart; jj < nt; ++jj) {
+                const float4 pj_ = make_float4(sm.tile_f[4 * jj + 0], sm.tile_f[4 * jj + 1], sm.tile_f[4 * jj + 2],
+                                               sm.tile_f[4 * jj + 3]);
+                pair_test(i, j0 + jj, pi_, pj_);
+            }
+        }
+        __syncthreads();
+    }
+    }  // all pairs
+    __syncthreads();
+}
+
 // AggregatList::merge + Aggregate::merge + Aggregate::update (geometry).
 // ms / os: moving / other sphere; mslot / oslot: their aggregates at query
 // time. The physics fields (f_agg, d_m, time_step, lpm, dg_over_dp), the
 // proper time and the charge are left to the caller.
 template <class SM>
 __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, int oslot, SM &sm, MergeOut *out) {
-    constexpr int kPairTile = SM::kPairTile;
     const int tid = threadIdx.x, NT = blockDim.x;
     DevScalars *sc = b.sc;
     if (tid == 0) {
@@ -223,47 +359,9 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
     const int *mem = pool_id + new_off;
 
     // ---- update_distances_and_overlapping: contact pairs i < j
-    // stage relative positions (FP32) and the extent for the screening margin
-    float4 *relf = reinterpret_cast<float4 *>(b.work);  // reuse: n float4 fit in work[0..n/2)
-    float ext = 0.f, rmx = 0.f;
-    for (int k = tid; k < n; k += NT) {
-        int s = mem[k];
-        float4 v = make_float4(float(S(b, SPH_RX, s)), float(S(b, SPH_RY, s)), float(S(b, SPH_RZ, s)),
-                               float(S(b, SPH_R, s)));
-        relf[k] = v;
-        ext = fmaxf(ext, fabsf(v.x) + fabsf(v.y) + fabsf(v.z) + v.w);
-        rmx = fmaxf(rmx, v.w);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
-        rmx = fmaxf(rmx, __shfl_xor_sync(0xffffffffu, rmx, o));
-    }
-    if ((tid & 31) == 0) {
-        sm.warp_f[tid >> 5] = ext;
-        sm.warp_tmp[tid >> 5] = __float_as_int(rmx);  // non-negative: int order is float order
-    }
-    if (tid < n + 1 && tid <= b.ns) b.row_cnt[tid] = 0;
     for (int k = tid; k <= n; k += NT) b.row_cnt[k] = 0;
     if (tid == 0) b.counters[0] = 0;
-    __syncthreads();
-    if (tid == 0) {
-        float m = 0.f, r = 0.f;
-        for (int k = 0; k < NT / 32; ++k) {
-            m = fmaxf(m, sm.warp_f[k]);
-            r = fmaxf(r, __int_as_float(sm.warp_tmp[k]));
-        }
-        sm.margin = 1.0e-5f * m;  // FP32 error of |rel_i - rel_j| is ~1e-7 of the extent
-        sm.ext = m;
-        sm.rmax_f = r;
-    }
-    __syncthreads();
-    const float pm_margin = sm.margin;
-    // one candidate pair i < j: the FP32 screen, then the exact FP64 test
-    auto pair_test = [&](int i, int j, const float4 &pi_, const float4 &pj_) {
-        const float dx = pi_.x - pj_.x, dy = pi_.y - pj_.y, dz = pi_.z - pj_.z;
-        const float reach = (pi_.w + pj_.w) * 1.0001f + pm_margin;
-        if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz)) > reach * reach) return;
+    block_pair_scan(b, mem, n, sm, 0.f, [&](int i, int j) {
         const int si = mem[i], sj = mem[j];
         double ex = S(b, SPH_RX, si) - S(b, SPH_RX, sj);
         double ey = S(b, SPH_RY, si) - S(b, SPH_RY, sj);
@@ -279,91 +377,7 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
                 atomicAdd(&b.row_cnt[i], 1);
             }
         }
-    };
-    if (n >= b.grid_pairs_min) {
-        // Large aggregates: a hashed cell grid over the relative positions
-        // (cells wider than any pair's screening reach, 2 r_max 1.0001 +
-        // margin, by one more margin -- 100 times the FP32 rounding of the
-        // cell coordinates -- and 0.1%), so that every pair
-        // that can pass the screen sits in neighbouring cells; each sphere
-        // meets the spheres of its 27 cells with a larger index. The same
-        // pairs as the all-pairs loop, found in O(n) (a merge of two
-        // 8000-sphere aggregates needs 10^8 pair tests otherwise).
-        // Scratch after the n float4 of relf: cell coordinates (int4, n),
-        // bucket counts/starts (2^k + 1 >= 2n + 1), sorted sphere indices (n).
-        // With nb < 4n that is 16n + 16n + 4(nb + 1) + 4n <= 52n + 4 bytes,
-        // inside the work area of 8 doubles (64 B) per sphere of the box
-        // (n <= ns); a larger carve needs a larger work area.
-        int4 *cellc = reinterpret_cast<int4 *>(relf + n);
-        int nb = 1;
-        while (nb < 2 * n) nb <<= 1;
-        int *bstart = reinterpret_cast<int *>(cellc + n);
-        int *sorted = bstart + nb + 1;
-        const float h = ((2.f * sm.rmax_f) * 1.0001f + 2.f * pm_margin) * 1.001f;
-        const float inv_h = 1.f / h, e0 = sm.ext;
-        auto bucket_of = [&](int cx, int cy, int cz) {
-            const unsigned hsh = (unsigned(cx) * 73856093u) ^ (unsigned(cy) * 19349663u) ^ (unsigned(cz) * 83492791u);
-            return int(hsh & unsigned(nb - 1));
-        };
-        for (int k = tid; k <= nb; k += NT) bstart[k] = 0;
-        __syncthreads();
-        for (int k = tid; k < n; k += NT) {
-            const float4 v = relf[k];
-            const int cx = int(floorf((v.x + e0) * inv_h)), cy = int(floorf((v.y + e0) * inv_h)),
-                      cz = int(floorf((v.z + e0) * inv_h));
-            const int bk = bucket_of(cx, cy, cz);
-            cellc[k] = make_int4(cx, cy, cz, bk);
-            atomicAdd(&bstart[bk], 1);
-        }
-        __syncthreads();
-        block_scan_global(bstart, nb + 1, sm.warp_tmp);  // bstart[nb] = n
-        __syncthreads();
-        // scatter (bstart[bk] advances to the bucket's end; starts are then
-        // bstart[bk - 1], or 0)
-        for (int k = tid; k < n; k += NT) sorted[atomicAdd(&bstart[cellc[k].w], 1)] = k;
-        __syncthreads();
-        for (int i = tid; i < n; i += NT) {
-            const float4 pi_ = relf[i];
-            const int4 ci = cellc[i];
-            for (int ox = -1; ox <= 1; ++ox)
-                for (int oy = -1; oy <= 1; ++oy)
-                    for (int oz = -1; oz <= 1; ++oz) {
-                        const int cx = ci.x + ox, cy = ci.y + oy, cz = ci.z + oz;
-                        const int bk = bucket_of(cx, cy, cz);
-                        const int beg = bk == 0 ? 0 : bstart[bk - 1], end = bstart[bk];
-                        for (int t = beg; t < end; ++t) {
-                            const int j = sorted[t];
-                            if (j <= i) continue;
-                            const int4 cj = cellc[j];
-                            if (cj.x != cx || cj.y != cy || cj.z != cz) continue;  // another cell in the bucket
-                            pair_test(i, j, pi_, relf[j]);
-                        }
-                    }
-        }
-        __syncthreads();
-    } else {
-    for (int j0 = 0; j0 < n; j0 += kPairTile) {
-        const int nt = min(kPairTile, n - j0);
-        for (int k = tid; k < nt; k += NT) {
-            float4 v = relf[j0 + k];
-            sm.tile_f[4 * k + 0] = v.x;
-            sm.tile_f[4 * k + 1] = v.y;
-            sm.tile_f[4 * k + 2] = v.z;
-            sm.tile_f[4 * k + 3] = v.w;
-        }
-        __syncthreads();
-        for (int i = tid; i < min(n, j0 + nt); i += NT) {
-            const float4 pi_ = relf[i];
-            int jstart = max(i + 1, j0) - j0;
-            for (int jj = jstart; jj < nt; ++jj) {
-                const float4 pj_ = make_float4(sm.tile_f[4 * jj + 0], sm.tile_f[4 * jj + 1], sm.tile_f[4 * jj + 2],
-                                               sm.tile_f[4 * jj + 3]);
-                pair_test(i, j0 + jj, pi_, pj_);
-            }
-        }
-        __syncthreads();
-    }
-    }  // all pairs
+    });
     const int P = b.counters[0];
     if (P > b.pair_cap) {
         if (tid == 0) {

@@ -31,6 +31,8 @@ struct PhysParams {
     int growth;         // with_surface_reactions
     int individual;     // individual_surf_reactions: only the moved aggregate grows and is updated
     int full_update_every;  // full_aggregate_update_frequency
+    int oxidation;      // growth with u_sg < 0: spheres at or below rp_min leave, aggregates split
+    double rp_min;      // rp_min_oxid (m)
 };
 
 struct RunLimits {
@@ -52,7 +54,8 @@ struct RunState {
     long long steps, events, n_iter_without_event;
     int finished;
     int status;
-    int pad[2];
+    int removed_spheres;  // spheres taken out by oxidation
+    int splits;           // aggregates split by oxidation
     // work counters of the contact queries and merges (algorithmic bytes)
     long long c_queries, c_mov, c_scanned, c_cells, c_candidates, c_cand_spheres, c_refined;
     long long c_merged_spheres, c_merge_pairs;
@@ -119,6 +122,7 @@ struct RunSmemT {
     unsigned long long deadline;  // %globaltimer time after which no step starts (0: none)
     double dt, full, move;
     int slot, contact, stop, merged, rescale;
+    int split, disappear;  // this step's oxidation events
     int keep, removed;
     int ms, os, oslot;  // contact of this step: spheres and the other slot
     unsigned long long tree_tmp;  // block reduction scratch
@@ -396,7 +400,7 @@ __device__ __forceinline__ bool run_finished(const BoxRun &R, const RunState &st
     if (L.n_iter_without_event_limit > 0 && st.n_iter_without_event >= L.n_iter_without_event_limit) return true;
     if (L.physical_time_limit > 0 && st.time >= L.physical_time_limit) return true;
     if (L.mean_monomere_per_aggregate_limit > 0 &&
-        double(R.box.ns) / double(n_alive) >= double(L.mean_monomere_per_aggregate_limit))
+        double(R.box.ns - st.removed_spheres) / double(n_alive) >= double(L.mean_monomere_per_aggregate_limit))
         return true;
     return false;
 }
@@ -408,6 +412,7 @@ __device__ __forceinline__ bool run_finished(const BoxRun &R, const RunState &st
 // r += u_sg dt, volume and surface from the new radius. Each sphere is found
 // once through the live segments of the member pool, whose FP32 copy is
 // refreshed too.
+// With oxidation, b.counters[3] is set when a sphere ends at or below rp_min.
 __device__ inline void block_grow_spheres(const BoxRun &R, double dt) {
     const DevBox &b = R.box;
     const double pi = pi_value();
@@ -419,6 +424,7 @@ __device__ inline void block_grow_spheres(const BoxRun &R, double dt) {
         const int s = pool_id[k];
         if (s < 0 || s >= b.ns) continue;
         const int a = b.sph_slot[s];
+        if (a < 0 || a >= b.nslots) continue;  // a sphere removed by oxidation
         const int rel = k - b.agg_off[a];
         if (b.agg_n[a] == 0 || rel < 0 || rel >= b.agg_n[a]) continue;  // a stale pool entry
         const double r = S(b, SPH_R, s) + R.phys.u_sg * dt;                // PhysicalModel::grow
@@ -427,6 +433,7 @@ __device__ inline void block_grow_spheres(const BoxRun &R, double dt) {
         S(b, SPH_VOLUME, s) = vf * r3;
         S(b, SPH_SURFACE, s) = sf * r2;
         pool_pos[k].w = float(r);
+        if (R.phys.oxidation && r <= R.phys.rp_min) b.counters[3] = 1;
     }
 }
 
@@ -738,6 +745,331 @@ __device__ inline void block_update_one_or_all(const BoxRun &R, RS &sm, int slot
     }
 }
 
+// ---------------------------------------------------------------- oxidation
+// With u_sg < 0 the spheres shrink (block_grow_*). Then, as in
+// Aggregate::croissance_surface (aggregat.cpp:230-243), a sphere whose radius
+// is at or below rp_min leaves its aggregate (remove_sphere,
+// aggregat.cpp:629-655: the list keeps its order, relative positions are
+// taken again from the first sphere left, the aggregate is updated); an
+// aggregate left without spheres disappears (aggregat_list.cpp:549-579);
+// and an aggregate whose spheres no longer form one network of contacts
+// splits into one aggregate per connected part (Aggregate::split,
+// aggregat.cpp:545-628; AggregatList::split, aggregat_list.cpp:409-446).
+// Slots stay where they are: the part holding the first sphere keeps the
+// slot, the others take free slots (a box that oxidises has a slot for every
+// sphere), each part's spheres in list order, with the split aggregate's
+// record (its proper time) before their own update. A removed sphere keeps
+// its index with the slot -1.
+
+// Relative positions from the first member (remove_sphere and split:
+// position minus the first sphere's position); one thread.
+__device__ inline void thread_rebase(const DevBox &b, const int *mem, int n) {
+    const int s0 = mem[0];
+    const double x0 = S(b, SPH_X, s0), y0 = S(b, SPH_Y, s0), z0 = S(b, SPH_Z, s0);
+    for (int k = 0; k < n; ++k) {
+        const int s = mem[k];
+        S(b, SPH_RX, s) = S(b, SPH_X, s) - x0;
+        S(b, SPH_RY, s) = S(b, SPH_Y, s) - y0;
+        S(b, SPH_RZ, s) = S(b, SPH_Z, s) - z0;
+    }
+}
+
+// One slot's spheres at or below rp_min leave its list, the others keep
+// their order (one thread). Returns how many left.
+__device__ inline int thread_remove_small(const BoxRun &R, int a) {
+    const DevBox &b = R.box;
+    const int off = b.agg_off[a], n = b.agg_n[a];
+    int *pid = b.pool_id[b.sc->pool_sel] + off;
+    float4 *pp = b.pool_pos[b.sc->pool_sel] + off;
+    int w = 0;
+    for (int k = 0; k < n; ++k) {
+        const int s = pid[k];
+        if (S(b, SPH_R, s) <= R.phys.rp_min) {
+            b.sph_slot[s] = -1;
+            continue;
+        }
+        if (w != k) {
+            pid[w] = s;
+            pp[w] = pp[k];
+        }
+        ++w;
+    }
+    b.agg_n[a] = w;
+    if (w > 0 && w < n) {
+        thread_rebase(b, pid, w);
+        thread_update_aggregate(R, a, true);
+    }
+    return n - w;
+}
+
+// Removal in one slot (slot >= 0) or in every slot once a sphere reached
+// rp_min; slots left empty leave the grids. Sets sm.disappear.
+template <class RS>
+__device__ inline void block_remove_small(const BoxRun &R, RS &sm, int slot) {
+    const DevBox &b = R.box;
+    DevScalars *sc = b.sc;
+    const int tid = threadIdx.x, NT = blockDim.x;
+    int *emptied = b.row_cnt;  // per slot: 1 when this step left it empty
+    if (slot >= 0) {
+        if (tid == 0) {
+            const int gone = thread_remove_small(R, slot);
+            R.st->removed_spheres += gone;
+            if (gone > 0 && b.agg_n[slot] == 0) {
+                cell_remove(b, cell_index(b, b.agg_cell[slot]), slot);
+                if (b.fine_div > 0) fine_unlink(b, slot);
+                sc->n_alive -= 1;
+                sm.disappear = 1;
+            }
+        }
+        __syncthreads();
+        return;
+    }
+    if (b.counters[3] == 0) return;  // no sphere reached rp_min (set by the growth pass)
+    __syncthreads();
+    if (tid == 0) {
+        b.counters[1] = 0;
+        b.counters[2] = 0;
+    }
+    for (int a = tid; a < b.nslots; a += NT) emptied[a] = 0;
+    __syncthreads();
+    for (int a = tid; a < b.nslots; a += NT) {
+        const int n = b.agg_n[a];
+        if (n == 0) continue;
+        const int *mem = b.pool_id[sc->pool_sel] + b.agg_off[a];
+        bool any = false;
+        for (int k = 0; k < n && !any; ++k) any = S(b, SPH_R, mem[k]) <= R.phys.rp_min;
+        if (!any) continue;
+        const int gone = thread_remove_small(R, a);
+        atomicAdd(&b.counters[2], gone);
+        if (gone == n) {
+            emptied[a] = 1;
+            atomicAdd(&b.counters[1], 1);
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const int n_empty = b.counters[1];
+        R.st->removed_spheres += b.counters[2];
+        // the grids' lists change one slot at a time, in slot order
+        for (int a = 0, left = n_empty; a < b.nslots && left > 0; ++a) {
+            if (!emptied[a]) continue;
+            cell_remove(b, cell_index(b, b.agg_cell[a]), a);
+            if (b.fine_div > 0) fine_unlink(b, a);
+            --left;
+        }
+        sc->n_alive -= n_empty;
+        if (n_empty > 0) sm.disappear = 1;
+        b.counters[3] = 0;
+    }
+    __syncthreads();
+}
+
+// Disjoint-set forest over an aggregate's spheres: each root is the
+// smallest index of its set (a larger root is hooked under a smaller one),
+// so a parent never exceeds its child and every walk ends.
+__device__ __forceinline__ int uf_find(int *parent, int x) {
+    volatile int *p = parent;
+    for (;;) {
+        const int up = p[x];
+        if (up == x) return x;
+        const int gp = p[up];
+        if (gp != up) p[x] = gp;  // path halving (still an ancestor)
+        x = up;
+    }
+}
+// Returns false when the retries ran out (they cannot: each failed hook
+// means another root was hooked, at most n - 1 times).
+__device__ __forceinline__ bool uf_unite(int *parent, int i, int j, int n) {
+    for (int it = 0; it <= n + 1; ++it) {
+        int ri = uf_find(parent, i), rj = uf_find(parent, j);
+        if (ri == rj) return true;
+        if (ri < rj) {
+            const int t = ri;
+            ri = rj;
+            rj = t;
+        }
+        if (atomicCAS(&parent[ri], ri, rj) == ri) return true;
+    }
+    return false;
+}
+
+// Aggregate::split of one slot (all threads): its contact network's
+// connected parts (sphere_distances.cpp:81-90, the 1e-28 tolerance), one
+// aggregate each. Sets sm.split when it splits.
+template <class RS>
+__device__ inline void block_split_slot(const BoxRun &R, RS &sm, int a) {
+    const DevBox &b = R.box;
+    DevScalars *sc = b.sc;
+    const int tid = threadIdx.x, NT = blockDim.x;
+    const int n = b.agg_n[a];
+    if (n < 2) return;
+    const int *mem = b.pool_id[sc->pool_sel] + b.agg_off[a];
+    if (tid == 0) {
+        b.counters[0] = 0;
+        b.counters[4] = 0;
+    }
+    // spheres in contact: |d| <= r_i + r_j + 1e-14 m, inside the scan's reach
+    block_pair_scan(b, mem, n, sm.u.m, 2e-14f, [&](int i, int j) {
+        const int si = mem[i], sj = mem[j];
+        if (!spheres_in_contact(sph_pos(b, si), S(b, SPH_R, si), sph_pos(b, sj), S(b, SPH_R, sj), b.L)) return;
+        const int p = atomicAdd(&b.counters[0], 1);
+        if (p < b.pair_cap) {
+            b.pair_tmp_i[p] = i;
+            b.pair_tmp_j[p] = j;
+        }
+    });
+    const int P = b.counters[0];
+    if (P > b.pair_cap) {
+        if (tid == 0) sc->status = ST_CAPACITY;
+        __syncthreads();
+        return;
+    }
+    int *parent = b.row_cnt;
+    for (int i = tid; i < n; i += NT) parent[i] = i;
+    __syncthreads();
+    for (int p = tid; p < P; p += NT)
+        if (!uf_unite(parent, b.pair_tmp_i[p], b.pair_tmp_j[p], n)) b.counters[4] = 1;
+    __syncthreads();
+    for (int i = tid; i < n; i += NT) parent[i] = uf_find(parent, i);
+    __syncthreads();
+    if (b.counters[4] != 0) {
+        if (tid == 0) sc->status = ST_UNKNOWN;
+        __syncthreads();
+        return;
+    }
+    // parts in the order of their first sphere
+    int *rank = reinterpret_cast<int *>(b.work);  // n + 1
+    for (int i = tid; i < n; i += NT) rank[i] = parent[i] == i ? 1 : 0;
+    __syncthreads();
+    const int K = block_scan_global(rank, n, sm.u.m.warp_tmp);
+    if (K < 2) return;
+    int *cnt = rank + n + 1;   // K + 1: part sizes, then ends
+    int *part = cnt + K + 1;   // n: part of each member
+    int *ord = part + n;       // n: members grouped by part, list order kept
+    float4 *ordf = reinterpret_cast<float4 *>(b.work + ((size_t(ord + n - rank) * sizeof(int) + 15) / 16) * 2);
+    for (int c = tid; c <= K; c += NT) cnt[c] = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += NT) {
+        const int c = rank[parent[i]];
+        part[i] = c;
+        atomicAdd(&cnt[c], 1);
+    }
+    __syncthreads();
+    block_scan_global(cnt, K + 1, sm.u.m.warp_tmp);  // starts
+    const float4 *pp0 = b.pool_pos[sc->pool_sel] + b.agg_off[a];
+    if (tid == 0) {
+        for (int i = 0; i < n; ++i) {
+            const int q = cnt[part[i]]++;  // cnt[c] ends as the end of part c
+            ord[q] = mem[i];
+            ordf[q] = pp0[i];
+        }
+    }
+    // free slots for parts 1..K-1, in slot order
+    int *freef = b.cand_prefix;
+    int *freelist = b.cand_slot;
+    for (int x = tid; x < b.nslots; x += NT) freef[x] = b.agg_n[x] == 0 ? 1 : 0;
+    __syncthreads();
+    const int nfree = block_scan_global(freef, b.nslots, sm.u.m.warp_tmp);
+    if (nfree < K - 1) {
+        if (tid == 0) sc->status = ST_CAPACITY;
+        __syncthreads();
+        return;
+    }
+    for (int x = tid; x < b.nslots; x += NT)
+        if (b.agg_n[x] == 0 && freef[x] < K - 1) freelist[freef[x]] = x;
+    const int n0 = cnt[0];
+    if (sc->pool_top + (n - n0) > b.pool_cap) block_compact_pool(b, sm.u.m.warp_tmp);
+    __syncthreads();
+    const int off0 = b.agg_off[a], base = sc->pool_top;
+    int *pid = b.pool_id[sc->pool_sel];
+    float4 *pp = b.pool_pos[sc->pool_sel];
+    for (int q = tid; q < n; q += NT) {
+        int lo = 0, hi = K - 1;  // the part of position q: the first end above q
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (cnt[mid] > q) hi = mid; else lo = mid + 1;
+        }
+        const int s = ord[q];
+        if (lo == 0) {
+            pid[off0 + q] = s;
+            pp[off0 + q] = ordf[q];
+        } else {
+            pid[base + q - n0] = s;
+            pp[base + q - n0] = ordf[q];
+            b.sph_slot[s] = freelist[lo - 1];
+        }
+    }
+    for (int t = tid; t < (K - 1) * AGG_NFIELDS; t += NT)
+        A(b, t % AGG_NFIELDS, freelist[t / AGG_NFIELDS]) = A(b, t % AGG_NFIELDS, a);
+    __syncthreads();
+    if (tid == 0) {
+        b.agg_n[a] = n0;
+        for (int c = 1; c < K; ++c) {
+            const int x = freelist[c - 1];
+            b.agg_off[x] = base + cnt[c - 1] - n0;
+            b.agg_n[x] = cnt[c] - cnt[c - 1];
+        }
+        sc->pool_top = base + (n - n0);
+        sc->n_alive += K - 1;
+    }
+    __syncthreads();
+    for (int c = tid; c < K; c += NT) {
+        const int x = c == 0 ? a : freelist[c - 1];
+        thread_rebase(b, pid + b.agg_off[x], b.agg_n[x]);
+        thread_update_aggregate(R, x, true);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        regrid(b, a, agg_pos(b, a));
+        for (int c = 1; c < K; ++c) {
+            const int x = freelist[c - 1];
+            const Vec3 p = agg_pos(b, x);
+            const int key = cell_of(b, p);
+            cell_insert(b, cell_index(b, key), x);
+            b.agg_cell[x] = key;
+            if (b.fine_div > 0) fine_link(b, x, fine_cell_of(b, p));
+        }
+        R.st->splits += 1;
+        sm.split = 1;
+    }
+    __syncthreads();
+}
+
+// The oxidation of a step (all threads), after the spheres shrank: removals
+// and disappearances, then splits -- of the moved aggregate (slot >= 0, the
+// individual mode, calcul.cpp:159-163) or of every aggregate (calcul.cpp:
+// 165-169). Sets sm.split and sm.disappear.
+template <class RS>
+__device__ inline void block_oxidize(const BoxRun &R, RS &sm, int slot) {
+    const DevBox &b = R.box;
+    const int tid = threadIdx.x, NT = blockDim.x;
+    if (tid == 0) {
+        sm.split = 0;
+        sm.disappear = 0;
+    }
+    __syncthreads();
+    block_remove_small(R, sm, slot);
+    if (slot >= 0) {
+        if (!sm.disappear) block_split_slot(R, sm, slot);
+        return;
+    }
+    // the aggregates of two or more spheres, in slot order (the parts made
+    // by a split are connected and are not visited)
+    int *flag = b.cand_order;
+    long long *list = b.cand_key;
+    for (int a = tid; a < b.nslots; a += NT) flag[a] = b.agg_n[a] >= 2 ? 1 : 0;
+    __syncthreads();
+    const int m = block_scan_global(flag, b.nslots, sm.u.m.warp_tmp);
+    for (int a = tid; a < b.nslots; a += NT)
+        if (b.agg_n[a] >= 2) list[flag[a]] = a;
+    __syncthreads();
+    for (int k = 0; k < m; ++k) {
+        block_split_slot(R, sm, int(list[k]));
+        if (b.sc->status != ST_OK) break;
+    }
+    __syncthreads();
+}
+
 // The query's answer into the step's shared state and the box's counters
 // (thread 0).
 template <class RS>
@@ -797,8 +1129,29 @@ __device__ inline bool step_commit(const BoxRun &R, RS &sm, long long &t_phase) 
             block_grow_spheres(R, sm.step_dt);
     }
     __syncthreads();
-    if (sm.contact) {
-        block_merge(b, ms, os, slot, oslot, sm.u.m, &sm.mout);
+    bool try_merge = sm.contact;
+    int mslot = slot, cslot = oslot;
+    if (R.phys.oxidation) {
+        block_oxidize(R, sm, R.phys.individual ? slot : -1);
+        if (tid == 0 && b.sc->status != ST_OK) {
+            st.status = b.sc->status;
+            sm.stop = 1;
+        }
+        __syncthreads();
+        if (sm.stop) return false;
+        // AggregatList::merge takes the two spheres where they are now, and
+        // merges nothing when one is gone or they no longer touch
+        // (aggregat_list.cpp:367-378); the individual mode merges nothing
+        // after a split or a disappearance (calcul.cpp:173-178)
+        if (try_merge) {
+            mslot = b.sph_slot[ms];
+            cslot = b.sph_slot[os];
+            if (mslot < 0 || cslot < 0 || mslot == cslot) try_merge = false;
+            if (R.phys.individual && (sm.split || sm.disappear)) try_merge = false;
+        }
+    }
+    if (try_merge) {
+        block_merge(b, ms, os, mslot, cslot, sm.u.m, &sm.mout);
         if (tid == 0) {
             if (sm.mout.status != ST_OK) {
                 st.status = sm.mout.status;
@@ -851,7 +1204,8 @@ __device__ inline bool step_commit(const BoxRun &R, RS &sm, long long &t_phase) 
         __syncthreads();
         const long long every = R.phys.full_update_every > 0 ? R.phys.full_update_every : 1;
         const bool full = st.n_iter_without_event % every == 0;
-        if (!R.phys.individual || sm.merged)
+        const bool event = sm.merged || (R.phys.oxidation && (sm.split || sm.disappear));
+        if (!R.phys.individual || event)
             block_update_one_or_all(R, sm, -1, full);
         else
             block_update_one_or_all(R, sm, slot, full);
@@ -859,7 +1213,7 @@ __device__ inline bool step_commit(const BoxRun &R, RS &sm, long long &t_phase) 
     if (tid == 0) {
         st.cyc_merge += clock64() - t_phase;
         st.steps += 1;
-        if (sm.merged) {
+        if (sm.merged || (R.phys.oxidation && (sm.split || sm.disappear))) {
             st.events += 1;
             st.n_iter_without_event = 0;
         } else {

@@ -12,6 +12,9 @@
 //                                         the listed steps
 //   calcul  <ini> <prefix>                run the reference's own mcac::calcul and
 //                                         write its final state (validates 'trace')
+//   calcul_from <ini> <snap> <prefix>     load a state, run mcac::calcul on it with
+//                                         the INI's parameters (e.g. oxidation) and
+//                                         write its final state
 //   queries <ini> <snap> <nq> <seed> <out> [update]
 //                                         load a state, answer nq seeded
 //                                         distance_to_next_contact queries
@@ -393,6 +396,24 @@ int mode_calcul(const std::string &ini, const std::string &prefix) {
     return 0;
 }
 
+int mode_calcul_from(const std::string &ini, const std::string &snap, const std::string &prefix) {
+    std::unique_ptr<PhysicalModel> pm_holder;
+    PhysicalModel &pm = fresh_model(ini, pm_holder);
+    Snapshot s = read_snapshot(snap);
+    prepare_for_snapshot(pm, s);
+    AggregatList al(&pm);
+    load_snapshot(s, pm, al, true);
+    {
+        std::ofstream devnull("/dev/null");
+        auto *old = std::cout.rdbuf(devnull.rdbuf());
+        calcul(pm, al);
+        std::cout.rdbuf(old);
+    }
+    write_snapshot(prefix + "_final.snap", pm, al);
+    std::printf("n_agg %zu n_spheres %zu time %.17g\n", al.size(), al.spheres.size(), pm.time);
+    return 0;
+}
+
 // Query record: inputs and the reference answer.
 struct QueryRecord {
     int64_t label;
@@ -504,6 +525,7 @@ int main(int argc, char **argv) {
             return rc;
         }
         if (mode == "calcul" && argc >= 4) return mode_calcul(argv[2], argv[3]);
+        if (mode == "calcul_from" && argc >= 5) return mode_calcul_from(argv[2], argv[3], argv[4]);
         if (mode == "queries" && argc >= 7) {
             std::ofstream devnull("/dev/null");
             auto *old = std::cout.rdbuf(devnull.rdbuf());

@@ -97,6 +97,60 @@ __global__ void __launch_bounds__(kQueryThreads) k_merge(DevBox b, int ms, int o
     block_merge(b, ms, os, mslot, oslot, sm, out);
 }
 
+// Surface growth of the host-driven loop (Sphere::croissance_surface,
+// sphere.cpp:113-120): every sphere of one slot (slot >= 0) or of every live
+// slot becomes r + du, its volume and surface from the new radius.
+__global__ void k_grow(DevBox b, int slot, double du) {
+    const double pi = pi_value();
+    const double vf = 4. * pi / 3., sf = 4. * pi;
+    const int *pool_id = b.pool_id[b.sc->pool_sel];
+    float4 *pool_pos = b.pool_pos[b.sc->pool_sel];
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const int k0 = slot >= 0 ? b.agg_off[slot] : 0;
+    const int k1 = slot >= 0 ? k0 + b.agg_n[slot] : b.sc->pool_top;
+    for (int k = k0 + t0; k < k1; k += stride) {
+        const int s = pool_id[k];
+        if (s < 0 || s >= b.ns) continue;
+        const int a = b.sph_slot[s];
+        if (a < 0 || a >= b.nslots) continue;
+        const int rel = k - b.agg_off[a];
+        if (b.agg_n[a] == 0 || rel < 0 || rel >= b.agg_n[a]) continue;  // a stale pool entry
+        const double r = S(b, SPH_R, s) + du;
+        const double r2 = r * r, r3 = r2 * r;
+        S(b, SPH_R, s) = r;
+        S(b, SPH_VOLUME, s) = vf * r3;
+        S(b, SPH_SURFACE, s) = sf * r2;
+        pool_pos[k].w = float(r);
+    }
+}
+
+// The geometry of every live slot (slot < 0) or of one (Aggregate::update
+// when 'full', with the overlap and coordination fields, else
+// update_partial; without the physics fields), one thread per slot; vol_pp[a] receives update_partial's mean sphere volume. Slots
+// whose Verlet or fine cell changed are listed in moved[] (count in
+// counters[5]) for k_regrid_moved.
+__global__ void k_update_geometry(DevBox b, int slot, int full, double *vol_pp, int *moved) {
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const int a0 = slot >= 0 ? slot : 0, a1 = slot >= 0 ? slot + 1 : b.nslots;
+    for (int a = a0 + t0; a < a1; a += stride) {
+        if (b.agg_n[a] == 0) continue;
+        double vp = 0.0;
+        thread_update_geometry(b, a, full != 0, &vp, true);
+        vol_pp[a] = vp;
+        const Vec3 p = agg_pos(b, a);
+        if (cell_of(b, p) != b.agg_cell[a] || (b.fine_div > 0 && fine_cell_of(b, p) != b.fine_cell[a]))
+            moved[atomicAdd(&b.counters[5], 1)] = a;
+    }
+}
+// The listed slots follow their new positions in the grids (one thread; the
+// grid lists are unordered, so the order of the moves sets no result).
+__global__ void k_regrid_moved(DevBox b, const int *moved) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const int n = b.counters[5];
+    for (int k = 0; k < n && k < b.nslots; ++k) regrid(b, moved[k], agg_pos(b, moved[k]));
+    b.counters[5] = 0;
+}
+
 struct FieldUpdate {
     double v[21];
 };
@@ -1284,6 +1338,46 @@ int DeviceBox::set_fields(int slot, const double fields[21], unsigned mask, std:
     std::memcpy(u.v, fields, sizeof(u.v));
     k_set_fields<<<1, 32, 0, s>>>(b, slot, u, mask);
     if (!cuda_ok(cudaGetLastError(), err, "k_set_fields")) return ST_CUDA;
+    return ST_OK;
+}
+
+int DeviceBox::grow(int slot, double du, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    k_grow<<<slot >= 0 ? 1 : std::max(1, std::min(1024, (b.pool_cap + 255) / 256)), 256, 0, s>>>(b, slot, du);
+    if (!cuda_ok(cudaGetLastError(), err, "k_grow")) return ST_CUDA;
+    return ST_OK;
+}
+
+int DeviceBox::update_geometry(int slot, bool full, std::vector<double> *agg, std::vector<double> *vol_pp,
+                               std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    const int slot_blocks = std::max(1, std::min(1024, (b.nslots + 255) / 256));
+    // query scratch, free between queries: the mean sphere volumes and the moved slots
+    if (!cuda_ok(cudaMemsetAsync(b.counters + 5, 0, sizeof(int), s), err, "memset")) return ST_CUDA;
+    k_update_geometry<<<slot >= 0 ? 1 : slot_blocks, 256, 0, s>>>(b, slot, full ? 1 : 0, b.cand_db, b.cand_slot);
+    k_regrid_moved<<<1, 1, 0, s>>>(b, b.cand_slot);
+    if (!cuda_ok(cudaGetLastError(), err, "k_update_geometry")) return ST_CUDA;
+    agg->resize(size_t(21) * size_t(b.nslots));
+    vol_pp->resize(size_t(b.nslots));
+    if (!cuda_ok(cudaMemcpyAsync(agg->data(), b.agg, sizeof(double) * agg->size(), cudaMemcpyDeviceToHost, s), err,
+                 "download") ||
+        !cuda_ok(cudaMemcpyAsync(vol_pp->data(), b.cand_db, sizeof(double) * vol_pp->size(), cudaMemcpyDeviceToHost,
+                                 s),
+                 err, "download") ||
+        !cuda_ok(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
+    return check_status(err);
+}
+
+int DeviceBox::set_maxradius(double r, std::string *err) {
+    DevBox &b = *static_cast<DevBox *>(devbox_);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_);
+    // the value is read before the call returns (synchronised below)
+    if (!cuda_ok(cudaMemcpyAsync(&b.sc->maxradius, &r, sizeof(double), cudaMemcpyHostToDevice, s), err, "upload") ||
+        !cuda_ok(cudaStreamSynchronize(s), err, "sync"))
+        return ST_CUDA;
     return ST_OK;
 }
 

@@ -153,6 +153,17 @@ class DeviceBox {
     int set_fields(int slot, const double fields[21], unsigned mask, std::string *err);
     // Overwrites the whole aggregate table ([21][nslots], slot order).
     int upload_aggregates(const std::vector<double> &agg, std::string *err);
+    // Surface growth for the host-driven loop: the spheres of one slot
+    // (slot >= 0) or of every live slot grow by du.
+    int grow(int slot, double du, std::string *err);
+    // The geometry of one slot (slot >= 0) or of every live slot
+    // (Aggregate::update when 'full', else update_partial, without the
+    // physics fields); the slots follow their positions in the grids. *agg
+    // receives the whole table ([21][nslots]) and *vol_pp each slot's mean
+    // sphere volume.
+    int update_geometry(int slot, bool full, std::vector<double> *agg, std::vector<double> *vol_pp,
+                        std::string *err);
+    int set_maxradius(double r, std::string *err);
     // Copies the whole state back (spheres, aggregates, members, scalars),
     // on copy_stream when given (so several boxes can come back at once),
     // else on the box's stream.

@@ -794,13 +794,48 @@ bool HostBox::finished() const {
     return false;
 }
 
+// Aggregate::update, or update_partial, of one aggregate (slot >= 0) or of
+// every one after surface growth (calcul.cpp:180-206): the geometry on the
+// device, the physics fields here with the C library's functions (as the
+// reference computes them), then back to the device with the list's
+// maxradius; the pick order is rebuilt at the next sort.
+int HostBox::update_aggregates(int slot, bool full, std::string *err) {
+    std::vector<double> agg, vol_pp;
+    int rc = dev_->update_geometry(slot, full, &agg, &vol_pp, err);
+    if (rc != ST_OK) return rc;
+    // the geometry the device recomputed (the proper times live here only)
+    const int geometry[] = {AGG_RG, AGG_RMAX, AGG_VOLUME, AGG_SURFACE, AGG_X, AGG_Y, AGG_Z, AGG_RX, AGG_RY, AGG_RZ,
+                            AGG_DP, AGG_OVERLAPPING, AGG_COORDINATION_NUMBER};
+    auto physics = [&](int a) {
+        for (int f : geometry) F(f, a) = agg[size_t(f) * size_t(nslots_) + size_t(a)];
+        const AggregatePhysics ph = aggregate_physics(p_, F(AGG_VOLUME, a), vol_pp[size_t(a)], F(AGG_DP, a), F(AGG_RG, a));
+        F(AGG_F_AGG, a) = ph.f_agg;
+        F(AGG_D_M, a) = ph.d_m;
+        F(AGG_TIME_STEP, a) = ph.time_step;
+        F(AGG_LPM, a) = ph.lpm;
+        F(AGG_DG_OVER_DP, a) = ph.dg_over_dp;
+        if (F(AGG_RMAX, a) > maxradius_) maxradius_ = F(AGG_RMAX, a);
+    };
+    if (slot >= 0) {
+        physics(slot);
+    } else {
+        for (int a : alive_) physics(a);
+    }
+    dt_order_valid_ = false;
+    rc = dev_->upload_aggregates(agg_, err);
+    if (rc != ST_OK) return rc;
+    return dev_->set_maxradius(maxradius_, err);
+}
+
 int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::string *err) {
-    if (p_.with_surface_reactions || p_.with_domain_duplication || p_.with_domain_reduction ||
-        p_.pick_method != MCACG_PICK_RANDOM) {
-        if (err) *err = "the host-driven loop covers the collision-only configuration "
-                        "(no surface reactions, no domain duplication/reduction, pick_method=random)";
+    if (p_.with_domain_duplication || p_.with_domain_reduction || p_.pick_method != MCACG_PICK_RANDOM ||
+        (p_.with_surface_reactions && p_.u_sg < 0.0)) {
+        if (err) *err = "the host-driven loop covers collisions with optional surface growth (u_sg >= 0; no "
+                        "domain duplication/reduction, pick_method=random); oxidation runs in the device loop";
         return ST_INPUT;
     }
+    const bool surface = p_.with_surface_reactions != 0;
+    const bool individual = surface && p_.individual_surf_reactions != 0;
     if (opts.advancement_path && (p_.write_events_frequency <= 0 || p_.write_between_event_frequency <= 0)) {
         if (err) *err = "write_events_frequency and write_between_event_frequency must be positive";
         return ST_INPUT;
@@ -810,11 +845,13 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
         if (opts.max_steps > 0 && steps >= opts.max_steps) break;
         if (time_to_write() && opts.advancement_path) save_advancement(opts.advancement_path);
         double max = max_time_step_;
-        if (event_) sort_time_steps(max);
+        if (event_ || surface) sort_time_steps(max);  // every step when time steps change (calcul.cpp:100-102)
         const int64_t label = pick_random();
         double deltatemps = get_time_step(max);
         const double deltatemps_pick = deltatemps;
-        const double full_distance = F(AGG_LPM, alive_[size_t(label)]);
+        const int slot = alive_[size_t(label)];
+        double deltatemps_indiv = F(AGG_TIME_STEP, slot);
+        const double full_distance = F(AGG_LPM, slot);
         double dir[3];
         random_direction(dir);
         double move_distance = full_distance;
@@ -831,11 +868,28 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
         int rc = translate(label, v, err);
         if (rc != ST_OK) return rc;
         deltatemps = deltatemps * (move_distance / full_distance + static_cast<double>(n_try - 1));
+        deltatemps_indiv = deltatemps_indiv * (move_distance / full_distance + static_cast<double>(n_try - 1));
         time_forward(label, deltatemps, err);
         time_ = time_ + deltatemps;
+        // surface growth before the merge (calcul.cpp:157-170): every
+        // sphere, or the moved aggregate's by its own time step
+        if (surface) {
+            rc = individual ? dev_->grow(slot, p_.u_sg * deltatemps_indiv, err)
+                            : dev_->grow(-1, p_.u_sg * deltatemps, err);
+            if (rc != ST_OK) return rc;
+        }
         int32_t merged = 0;
         if (contact) {
             rc = merge(c, &merged, err);
+            if (rc != ST_OK) return rc;
+        }
+        if (surface) {
+            // update() every full_aggregate_update_frequency-th step without
+            // event, else update_partial(); the moved aggregate alone in the
+            // individual mode unless there was a merge (calcul.cpp:180-206)
+            const int64_t every = std::max<int64_t>(1, p_.full_aggregate_update_frequency);
+            const bool full = n_iter_without_event_ % every == 0;
+            rc = update_aggregates(individual && !merged ? slot : -1, full, err);
             if (rc != ST_OK) return rc;
         }
         event_ = merged != 0;
@@ -844,12 +898,15 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
             ++events;
             ++total_events_;
             refresh();
-            // PhysicalModel::update after an event (calcul.cpp:274-279)
+        } else {
+            n_iter_without_event_++;
+        }
+        if (event_ || surface) {
+            // PhysicalModel::update after an event or with surface reactions
+            // (calcul.cpp:274-279)
             aggregate_concentration_ = static_cast<double>(alive_.size()) / p_.box_volume;
             monomer_concentration_ = static_cast<double>(ns_) / p_.box_volume;
             volume_fraction_ = total_volume() / p_.box_volume;
-        } else {
-            n_iter_without_event_++;
         }
         if (opts.trace && steps < opts.trace_capacity) {
             mcacg_step_record &r = opts.trace[steps];
@@ -893,6 +950,7 @@ int HostBox::store(mcacg_state *out, std::string *err) {
     HostState st;
     int rc = dev_->download(&st, err);
     if (rc != ST_OK) return rc;
+
     const int na = int(alive_.size());
     if (out->n_spheres < ns_ || out->n_aggregates < na) {
         if (err) *err = "state buffers too small";

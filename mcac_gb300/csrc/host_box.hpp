@@ -58,7 +58,8 @@ class HostBox {
     // the reference's stop criteria (physical_model.cpp:288-337, without the
     // STOPCODE file and CPU-time checks)
     bool finished() const;
-    // one run of the MC loop of src/calcul.cpp:66-281 (collision-only)
+    // one run of the MC loop of src/calcul.cpp:66-281 (collisions, with
+    // surface growth when the parameters ask for it)
     int calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::string *err);
 
     // whole state (store) in label order
@@ -68,6 +69,7 @@ class HostBox {
     int run_device(int64_t max_steps, mcacg_run_stats *stats, std::string *err);
 
   private:
+    int update_aggregates(int slot, bool full, std::string *err);
     void invalidate_device_run();
     int refresh_from_device(std::string *err);
     std::unique_ptr<BatchRunner> runner_;

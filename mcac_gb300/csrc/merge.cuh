@@ -604,4 +604,141 @@ __device__ inline void block_merge(const DevBox &b, int ms, int os, int mslot, i
     __syncthreads();
 }
 
+// The geometry of Aggregate::update / update_partial (aggregat.cpp:247-288,
+// 321-483) of one slot by one thread, sums in list order, without the
+// physics fields (friction, mobility diameter, time step, lpm, Rg/dp).
+// Returns r_max, and the mean sphere volume of update_partial in *vol_pp_out.
+// 'full' is update(): compute_volume_surface refreshes the aggregate's
+// volume and surface and each sphere's entry of the per-sphere volumes
+// (sph_volw); update_partial weighs the centre of mass and Rg with those
+// entries as last set, as the reference does. For "none" the overlap and
+// coordination fields, which need every pair of the aggregate and do not act
+// on the dynamics, are left to the merge and to the read-back unless
+// 'overlap' asks for them; "caps" and "alphas" need the pairs for the volume
+// and set them here.
+__device__ inline double thread_update_geometry(const DevBox &b, int a, bool full, double *vol_pp_out,
+                                                bool overlap = false) {
+    const int n = b.agg_n[a];
+    const int *mem = b.pool_id[b.sc->pool_sel] + b.agg_off[a];
+    double volume = A(b, AGG_VOLUME, a);
+    if (full && b.volsurf == VS_NONE && !overlap) {
+        double v = 0.0, sfc = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const double vi = S(b, SPH_VOLUME, mem[i]);
+            v = v + vi;
+            sfc = sfc + S(b, SPH_SURFACE, mem[i]);
+            b.sph_volw[mem[i]] = vi;
+        }
+        volume = v;
+        A(b, AGG_VOLUME, a) = v;
+        A(b, AGG_SURFACE, a) = sfc;
+    } else if (full) {
+        // update_distances_and_overlapping, then compute_volume_surface
+        // ("caps": sph_volw and the work area hold the per-sphere volumes and
+        // surfaces as the caps come off; "alphas": sums over the pairs, each
+        // pair twice in a row, in (i, j) order)
+        double *surf_w = b.work;  // by sphere index; free outside a merge
+        for (int i = 0; i < n; ++i) {
+            b.sph_volw[mem[i]] = S(b, SPH_VOLUME, mem[i]);
+            surf_w[mem[i]] = S(b, SPH_SURFACE, mem[i]);
+        }
+        double ov = 0.0;
+        int inter = 0;
+        AlphaSums al{0., 0., 0., 0., 0., 0.};
+        for (int i = 0; i < n; ++i) {
+            const int si = mem[i];
+            const double ri = S(b, SPH_R, si);
+            for (int j = i + 1; j < n; ++j) {
+                const int sj = mem[j];
+                const double ex = S(b, SPH_RX, si) - S(b, SPH_RX, sj);
+                const double ey = S(b, SPH_RY, si) - S(b, SPH_RY, sj);
+                const double ez = S(b, SPH_RZ, si) - S(b, SPH_RZ, sj);
+                const double dist = sqrt(ex * ex + ey * ey + ez * ez);
+                const double rj = S(b, SPH_R, sj);
+                const double rsum = ri + rj;
+                if (!(dist <= (1. + kCoordinationEpsilon) * rsum)) continue;
+                ov += 2.0 * ((rsum - dist) / rsum);
+                inter += 2;
+                if (b.volsurf == VS_CAPS) {
+                    const SphereCaps k = sphere_caps(ri, S(b, SPH_VOLUME, si), S(b, SPH_SURFACE, si), rj,
+                                                     S(b, SPH_VOLUME, sj), S(b, SPH_SURFACE, sj), dist);
+                    b.sph_volw[si] = b.sph_volw[si] - k.v1;
+                    surf_w[si] = surf_w[si] - k.s1;
+                    b.sph_volw[sj] = b.sph_volw[sj] - k.v2;
+                    surf_w[sj] = surf_w[sj] - k.s2;
+                } else if (b.volsurf == VS_ALPHAS) {
+                    alpha_add(al, ri, rj, dist);
+                    alpha_add(al, rj, ri, dist);
+                }
+            }
+            if (b.volsurf == VS_CAPS) {
+                b.sph_volw[si] = dmax(b.sph_volw[si], 0.0);
+                surf_w[si] = dmax(surf_w[si], 0.0);
+            }
+        }
+        double overlapping = 0.0, coordination = 0.0;
+        if (inter > 0) {
+            overlapping = ov / static_cast<double>(inter);
+            coordination = static_cast<double>(inter) / static_cast<double>(n);
+        }
+        double v = 0.0, sfc = 0.0;
+        for (int i = 0; i < n; ++i) {
+            v = v + b.sph_volw[mem[i]];
+            sfc = sfc + surf_w[mem[i]];
+        }
+        if (b.volsurf == VS_ALPHAS) alpha_finish(al, n, inter, &v, &sfc, &overlapping, &coordination);
+        volume = v;
+        A(b, AGG_VOLUME, a) = v;
+        A(b, AGG_SURFACE, a) = sfc;
+        A(b, AGG_OVERLAPPING, a) = overlapping;
+        A(b, AGG_COORDINATION_NUMBER, a) = coordination;
+    }
+    // compute_mass_center (aggregat.cpp:431-452)
+    double rx = 0., ry = 0., rz = 0.;
+    for (int i = 0; i < n; ++i) {
+        const int s = mem[i];
+        const double vol = b.sph_volw[s];
+        rx += S(b, SPH_RX, s) * vol;
+        ry += S(b, SPH_RY, s) * vol;
+        rz += S(b, SPH_RZ, s) * vol;
+    }
+    rx /= volume;
+    ry /= volume;
+    rz /= volume;
+    // compute_max_radius, compute_giration_radius (aggregat.cpp:453-483),
+    // and update_partial's mean radius and mean sphere volume
+    double rmax = 0.0, arg = 0., brg = 0., dp = 0., vol_pp = 0.;
+    for (int i = 0; i < n; ++i) {
+        const int s = mem[i];
+        const double dx = S(b, SPH_RX, s) - rx, dy = S(b, SPH_RY, s) - ry, dz = S(b, SPH_RZ, s) - rz;
+        const double dc = sqrt(dx * dx + dy * dy + dz * dz);
+        const double rs = S(b, SPH_R, s), volw = b.sph_volw[s];
+        rmax = dmax(rmax, rs + dc);
+        arg = arg + volw * (dc * dc);
+        brg = brg + volw * (rs * rs);
+        vol_pp += S(b, SPH_VOLUME, s);
+        dp += rs;
+    }
+    const double rg = sqrt(fabs((arg + (3. / 5.) * brg) / volume));
+    dp = 2 * dp / double(n);
+    vol_pp = vol_pp / double(n);
+    // the aggregate's position (aggregat.cpp:431-452, as in the merge)
+    const int s0 = mem[0];
+    const double x = periodic_position(S(b, SPH_X, s0) + rx, b.L);
+    const double y = periodic_position(S(b, SPH_Y, s0) + ry, b.L);
+    const double z = periodic_position(S(b, SPH_Z, s0) + rz, b.L);
+    A(b, AGG_RX, a) = rx;
+    A(b, AGG_RY, a) = ry;
+    A(b, AGG_RZ, a) = rz;
+    A(b, AGG_X, a) = x;
+    A(b, AGG_Y, a) = y;
+    A(b, AGG_Z, a) = z;
+    A(b, AGG_RMAX, a) = rmax;
+    A(b, AGG_RG, a) = rg;
+    A(b, AGG_DP, a) = dp;
+    b.agg_f4[a] = make_float4(float(x), float(y), float(z), float(rmax));
+    *vol_pp_out = vol_pp;
+    return rmax;
+}
+
 }  // namespace mcacg

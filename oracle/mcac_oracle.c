@@ -74,6 +74,7 @@ struct mo_box {
     int n_div;
     int64_t ns, na;
     double *sph[9];
+    double *volw;  /* each sphere's volume as the last Aggregate::update counted it */
     int64_t *sph_label;
     double *agg[21];  /* by label (positional list, aggregat_list.hpp:29) */
     int64_t *agg_n;
@@ -245,42 +246,52 @@ static double mobility_diameter(const mo_params *p, double V, double v, double r
 }
 
 /* Aggregate::update (aggregat.cpp:247-288, 321-483, 719-764), method
- * "none": all FP64 sums in list order. Returns 0 or the VolSurfError code. */
-static int update_aggregate(mo_box *b, int64_t a) {
+ * "none": all FP64 sums in list order; with 'partial', update_partial
+ * (aggregat.cpp:247-282): no overlap or volume pass, the centre of mass and
+ * Rg weighed with the sphere volumes the last update counted, the
+ * aggregate's volume as it was. Returns 0 or the VolSurfError code. */
+static int update_aggregate_part(mo_box *b, int64_t a, int partial);
+static int update_aggregate(mo_box *b, int64_t a) { return update_aggregate_part(b, a, 0); }
+static int update_aggregate_part(mo_box *b, int64_t a, int partial) {
     const ivec *m = &b->members[a];
     const int64_t n = m->n;
-    double overlapping = 0.0, coordination = 0.0;
-    int64_t inter = 0;
-    for (int64_t i = 0; i < n; i++)
-        for (int64_t j = i + 1; j < n; j++) {
-            int64_t si = m->v[i], sj = m->v[j];
-            double dx = SPH(b, S_RX, si) - SPH(b, S_RX, sj), dy = SPH(b, S_RY, si) - SPH(b, S_RY, sj),
-                   dz = SPH(b, S_RZ, si) - SPH(b, S_RZ, sj);
-            double dist = sqrt(dx * dx + dy * dy + dz * dz);
-            if (dist <= (1. + kCoordinationEpsilon) * (SPH(b, S_R, si) + SPH(b, S_R, sj))) {
-                double cij = (SPH(b, S_R, si) + SPH(b, S_R, sj) - dist) / (SPH(b, S_R, si) + SPH(b, S_R, sj));
-                overlapping += 2.0 * cij;
-                inter += 2;
+    double V = AGG(b, A_VOLUME, a);
+    if (!partial) {
+        double overlapping = 0.0, coordination = 0.0;
+        int64_t inter = 0;
+        for (int64_t i = 0; i < n; i++)
+            for (int64_t j = i + 1; j < n; j++) {
+                int64_t si = m->v[i], sj = m->v[j];
+                double dx = SPH(b, S_RX, si) - SPH(b, S_RX, sj), dy = SPH(b, S_RY, si) - SPH(b, S_RY, sj),
+                       dz = SPH(b, S_RZ, si) - SPH(b, S_RZ, sj);
+                double dist = sqrt(dx * dx + dy * dy + dz * dz);
+                if (dist <= (1. + kCoordinationEpsilon) * (SPH(b, S_R, si) + SPH(b, S_R, sj))) {
+                    double cij = (SPH(b, S_R, si) + SPH(b, S_R, sj) - dist) / (SPH(b, S_R, si) + SPH(b, S_R, sj));
+                    overlapping += 2.0 * cij;
+                    inter += 2;
+                }
             }
+        if (inter > 0) {
+            overlapping /= (double)inter;
+            coordination = (double)inter / (double)n;
         }
-    if (inter > 0) {
-        overlapping /= (double)inter;
-        coordination = (double)inter / (double)n;
+        double Sf = 0.0;
+        V = 0.0;
+        for (int64_t i = 0; i < n; i++) {
+            V = V + SPH(b, S_VOL, m->v[i]);
+            Sf = Sf + SPH(b, S_SURF, m->v[i]);
+            b->volw[m->v[i]] = SPH(b, S_VOL, m->v[i]);
+        }
+        AGG(b, A_VOLUME, a) = V;
+        AGG(b, A_SURFACE, a) = Sf;
+        AGG(b, A_OVERLAPPING, a) = overlapping;
+        AGG(b, A_COORDINATION, a) = coordination;
+        if (V <= 0 || Sf <= 0) return 8;
     }
-    double V = 0.0, Sf = 0.0;
-    for (int64_t i = 0; i < n; i++) {
-        V = V + SPH(b, S_VOL, m->v[i]);
-        Sf = Sf + SPH(b, S_SURF, m->v[i]);
-    }
-    AGG(b, A_VOLUME, a) = V;
-    AGG(b, A_SURFACE, a) = Sf;
-    AGG(b, A_OVERLAPPING, a) = overlapping;
-    AGG(b, A_COORDINATION, a) = coordination;
-    if (V <= 0 || Sf <= 0) return 8;
     double r[3] = {0., 0., 0.};
     for (int64_t i = 0; i < n; i++) {
         int64_t s = m->v[i];
-        double vol = SPH(b, S_VOL, s);
+        double vol = b->volw[s];
         r[0] += SPH(b, S_RX, s) * vol;
         r[1] += SPH(b, S_RY, s) * vol;
         r[2] += SPH(b, S_RZ, s) * vol;
@@ -305,7 +316,7 @@ static int update_aggregate(mo_box *b, int64_t a) {
     AGG(b, A_RMAX, a) = rmax;
     double arg = 0., brg = 0.;
     for (int64_t i = 0; i < n; i++) {
-        double vol = SPH(b, S_VOL, m->v[i]), rs = SPH(b, S_R, m->v[i]);
+        double vol = b->volw[m->v[i]], rs = SPH(b, S_R, m->v[i]);
         arg = arg + vol * (dcen[i] * dcen[i]);
         brg = brg + vol * (rs * rs);
     }
@@ -384,6 +395,7 @@ static mo_box *alloc_box(const mo_params *p, int64_t ns, int64_t na, int n_div, 
     b->ns = ns;
     b->na = na;
     for (int f = 0; f < 9; ++f) b->sph[f] = (double *)calloc((size_t)ns, sizeof(double));
+    b->volw = (double *)calloc((size_t)ns, sizeof(double));
     b->sph_label = (int64_t *)calloc((size_t)ns, sizeof(int64_t));
     for (int f = 0; f < 21; ++f) b->agg[f] = (double *)calloc((size_t)na, sizeof(double));
     b->agg_n = (int64_t *)calloc((size_t)na, sizeof(int64_t));
@@ -400,6 +412,7 @@ static mo_box *alloc_box(const mo_params *p, int64_t ns, int64_t na, int n_div, 
 void mo_box_free(mo_box *b) {
     if (!b) return;
     for (int f = 0; f < 9; ++f) free(b->sph[f]);
+    free(b->volw);
     free(b->sph_label);
     for (int f = 0; f < 21; ++f) free(b->agg[f]);
     free(b->agg_n);
@@ -444,6 +457,7 @@ void mo_params_derive(mo_params *p, double pressure) {
     const double T = p->temperature, Tref = 293.15, Sc = 110, Pref = 101300;
     p->viscosity = 18.203E-6 * (Sc + Tref) / (Sc + T) * pow(T / Tref, 1.5);
     p->gaz_mean_free_path = 66.5E-9 * (Pref / pressure) * (T / Tref) * (1. + Sc / Tref) / (1. + Sc / T);
+    p->u_sg = p->flux_surfgrowth / p->density; /* physical_model.cpp:264 */
 }
 
 /* AggregatList::refresh (aggregat_list.cpp:100-108) */
@@ -540,6 +554,7 @@ int mo_box_new_random(const mo_params *p, mo_box **out) {
             SPH(b, S_R, s) = SPH(b, S_R, s) * corr;
             SPH(b, S_VOL, s) = vf * pow(SPH(b, S_R, s), 3);
             SPH(b, S_SURF, s) = sf * pow(SPH(b, S_R, s), 2);
+            b->volw[s] = SPH(b, S_VOL, s); /* compute_volume_surface's per-sphere volumes */
         }
         for (int64_t a = 0; a < N; ++a) {
             double V = 0.0, S = 0.0;
@@ -562,6 +577,7 @@ int mo_box_new_state(const mo_params *p, int64_t ns, int64_t na, int64_t n_div, 
     b->time = time;
     b->maxradius = maxradius;
     for (int f = 0; f < 9; ++f) memcpy(b->sph[f], spheres + (size_t)f * ns, (size_t)ns * sizeof(double));
+    memcpy(b->volw, b->sph[S_VOL], (size_t)ns * sizeof(double));
     memcpy(b->sph_label, sphere_label, (size_t)ns * sizeof(int64_t));
     for (int f = 0; f < 21; ++f) memcpy(b->agg[f], aggregates + (size_t)f * na, (size_t)na * sizeof(double));
     int64_t off = 0;
@@ -927,16 +943,35 @@ static int finished(const mo_box *b) {
     return 0;
 }
 
-/* calcul (src/calcul.cpp:66-281), collision-only */
+/* Sphere::croissance_surface (sphere.cpp:113-120) of one aggregate's
+ * spheres: r + u_sg dt, volume and surface from the new radius. */
+static void grow_aggregate(mo_box *b, int64_t a, double dt) {
+    const ivec *m = &b->members[a];
+    for (int64_t i = 0; i < m->n; i++) {
+        const int64_t s = m->v[i];
+        const double r = SPH(b, S_R, s) + b->p.u_sg * dt;
+        const double r2 = r * r, r3 = r2 * r;
+        SPH(b, S_R, s) = r;
+        SPH(b, S_VOL, s) = 4 * PI / 3 * r3;
+        SPH(b, S_SURF, s) = 4 * PI * r2;
+    }
+}
+
+/* calcul (src/calcul.cpp:66-281): collisions, with surface growth
+ * (u_sg >= 0) when the parameters ask for it */
 int mo_calcul(mo_box *b, int64_t max_steps, mo_step_record *trace, int64_t cap, mo_stats *stats) {
     int64_t steps = 0, events = 0;
+    const int surface = b->p.with_surface_reactions != 0;
+    const int individual = surface && b->p.individual_surf_reactions != 0;
+    if (surface && b->p.u_sg < 0.0) return 4; /* oxidation is not restated here */
     while (!finished(b)) {
         if (max_steps > 0 && steps >= max_steps) break;
         double max = b->max_time_step;
-        if (b->event) mo_sort_time_steps(b, max);
+        if (b->event || surface) mo_sort_time_steps(b, max);
         int64_t label = mo_pick_random(b);
         double deltatemps = mo_get_time_step(b, max);
         const double deltatemps_pick = deltatemps;
+        double deltatemps_indiv = AGG(b, A_TIME_STEP, label);
         double full = AGG(b, A_LPM, label);
         double dir[3];
         random_direction(dir);
@@ -952,12 +987,35 @@ int mo_calcul(mo_box *b, int64_t max_steps, mo_step_record *trace, int64_t cap, 
         double v[3] = {dir[0] * move, dir[1] * move, dir[2] * move};
         mo_translate(b, label, v);
         deltatemps = deltatemps * (move / full + (double)(n_try - 1));
+        deltatemps_indiv = deltatemps_indiv * (move / full + (double)(n_try - 1));
         AGG(b, A_TIME, label) += deltatemps;
         b->time = b->time + deltatemps;
+        /* surface growth before the merge (calcul.cpp:157-170) */
+        if (individual) {
+            grow_aggregate(b, label, deltatemps_indiv);
+        } else if (surface) {
+            for (int64_t a = 0; a < b->na; ++a) grow_aggregate(b, a, deltatemps);
+        }
         int32_t merged = 0;
         if (contact_flag) {
             int rc = mo_merge(b, &c, &merged);
             if (rc) return rc;
+        }
+        if (surface) {
+            /* update() every full_aggregate_update_frequency-th step without
+             * event, else update_partial(); the moved aggregate alone in the
+             * individual mode unless there was a merge (calcul.cpp:180-206) */
+            const int64_t every = b->p.full_aggregate_update_frequency > 0 ? b->p.full_aggregate_update_frequency : 1;
+            const int partial = b->n_iter_without_event % every != 0;
+            if (individual && !merged) {
+                int rc = update_aggregate_part(b, label, partial);
+                if (rc) return rc;
+            } else {
+                for (int64_t a = 0; a < b->na; ++a) {
+                    int rc = update_aggregate_part(b, a, partial);
+                    if (rc) return rc;
+                }
+            }
         }
         b->event = merged;
         if (merged) {

@@ -32,6 +32,10 @@ typedef struct mo_params {
     int32_t enforce_volume_fraction, with_collisions;
     int64_t number_of_aggregates_limit, n_iter_without_event_limit, mean_monomere_per_aggregate_limit;
     double physical_time_limit;
+    /* [surface_growth]: growth only (flux >= 0); u_sg is derived */
+    int32_t with_surface_reactions, individual_surf_reactions;
+    double flux_surfgrowth, u_sg;
+    int64_t full_aggregate_update_frequency;
 } mo_params;
 
 typedef struct mo_contact {
@@ -53,7 +57,7 @@ typedef struct mo_stats {
 
 typedef struct mo_box mo_box;
 
-/* Fills box_length, viscosity and gaz_mean_free_path from the raw fields. */
+/* Fills box_length, viscosity, gaz_mean_free_path and u_sg from the raw fields. */
 void mo_params_derive(mo_params *p, double pressure);
 
 /* AggregatList::AggregatList: seeds rand() and places n_monomeres monomers. */

@@ -28,7 +28,9 @@ class MoParams(C.Structure):
                 ("gaz_mean_free_path", f64), ("box_length", f64), ("n_verlet_divisions", i64),
                 ("enforce_volume_fraction", i32), ("with_collisions", i32),
                 ("number_of_aggregates_limit", i64), ("n_iter_without_event_limit", i64),
-                ("mean_monomere_per_aggregate_limit", i64), ("physical_time_limit", f64)]
+                ("mean_monomere_per_aggregate_limit", i64), ("physical_time_limit", f64),
+                ("with_surface_reactions", i32), ("individual_surf_reactions", i32), ("flux_surfgrowth", f64),
+                ("u_sg", f64), ("full_aggregate_update_frequency", i64)]
 
 
 class MoContact(C.Structure):
@@ -143,6 +145,10 @@ def params_from_ini(text: str) -> MoParams:
     p.enforce_volume_fraction = get("numerics", "enforce_volume_fraction", bool, True)
     p.n_verlet_divisions = get("numerics", "n_verlet_divisions", int, 10)
     p.random_seed = get("numerics", "random_seed", int, -1)
+    p.with_surface_reactions = get("surface_growth", "with_surface_reactions", bool, False)
+    p.flux_surfgrowth = get("surface_growth", "flux_surfgrowth", float, 0.0)
+    p.full_aggregate_update_frequency = get("surface_growth", "full_aggregate_update_frequency", int, 1)
+    p.individual_surf_reactions = get("numerics", "individual_surf_reactions", bool, False)
     lib().mo_params_derive(C.byref(p), pressure)
     return p
 

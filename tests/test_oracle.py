@@ -40,6 +40,19 @@ def test_oracle_initial_state_and_full_run():
     assert digest(box.store()) == str(g["final_digest"])
 
 
+@pytest.mark.parametrize("case", ["collective", "individual", "partial"])
+def test_oracle_surface_growth_runs(case):
+    """Surface growth (every aggregate, the moved one only, update_partial
+    between full updates): the reference's own runs' final states, byte for
+    byte (tests/golden/make_growth_exact_golden.py)."""
+    g = load_golden("growth_exact.npz")
+    box = O.OracleBox(str(g[f"{case}_ini"]))
+    st, _ = box.calcul()
+    assert st.n_aggregates == int(g[f"{case}_na"])
+    assert st.time == float(g[f"{case}_time"])
+    assert digest(box.store()) == str(g[f"{case}_digest"])
+
+
 def test_oracle_lognormal_run_final_state():
     g = load_golden("ln_late.npz")
     box = O.OracleBox(str(g["ini"]))

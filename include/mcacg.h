@@ -13,8 +13,8 @@
  *
  * Labels are the reference's aggregate labels: the position of the aggregate
  * in AggregatList, renumbered after every merge (keep = min label). Sphere
- * indices are storage indices (Sphere::index_in_storage), stable in the
- * collision-only path.
+ * indices are storage indices (Sphere::index_in_storage), stable unless
+ * oxidation removes spheres (see mcacg_batch_store_state).
  */
 #ifndef MCACG_H
 #define MCACG_H
@@ -297,10 +297,14 @@ int mcacg_get_total_surface(const mcacg_box *box, double *surface);
 int mcacg_get_aggregate(const mcacg_box *box, int64_t label, double fields[21], int64_t *n_spheres);
 
 /* ---- whole runs ---- */
-/* The MC loop of mcac::calcul (src/calcul.cpp:66-281) for the
- * collision-only configuration, driven from the host one step at a time
- * through the entry points above: results are bit-identical with the
- * reference binary built with FP contraction off. */
+/* The MC loop of mcac::calcul (src/calcul.cpp:66-281) for collisions, with
+ * surface growth when the parameters ask for it (with_surface_reactions,
+ * u_sg >= 0: every sphere or the moved aggregate's grows, then the
+ * aggregates are updated, calcul.cpp:157-206), driven from the host one step
+ * at a time through the entry points above: results are bit-identical with
+ * the reference binary built with FP contraction off. Oxidation (u_sg < 0)
+ * runs in the device-resident forms below; here it gives
+ * MCACG_ERR_INPUT_ERROR. */
 int mcacg_calcul(mcacg_box *box, const mcacg_run_opts *opts, mcacg_run_stats *stats);
 
 /* ---- device-resident runs (batched and served forms) ----
@@ -318,13 +322,20 @@ typedef struct mcacg_batch mcacg_batch;
  * criterion of its parameters). */
 int mcacg_run_device(mcacg_box *box, int64_t max_steps, mcacg_run_stats *stats);
 /* n_boxes independent boxes, box i placed as mcacg_box_create would place it
- * with params[i] (size, seed, physics and stop criteria per box). */
+ * with params[i] (size, seed, physics and stop criteria per box).
+ * Surface reactions run here in both directions: growth (u_sg >= 0), and
+ * oxidation (u_sg < 0: spheres shrink; a sphere at or below rp_min_oxid
+ * leaves its aggregate, an aggregate left empty disappears and one whose
+ * spheres no longer form one network of contacts splits into one aggregate
+ * per connected part; aggregat.cpp:230-243, 545-655). Nucleation,
+ * potentials, flame coupling and electric charges give MCACG_ERR_INPUT_ERROR. */
 int mcacg_batch_create(const mcacg_params *params, int32_t n_boxes, void *cuda_stream, mcacg_batch **batch);
 /* n_boxes boxes from host states (states[i] as for mcacg_box_create_from_state);
  * params[i] gives box i's physics, stop criteria and device stream seed. The
  * arrays are read in place (by DMA when they are page-locked, e.g. from
  * mcacg_host_alloc) and checked on the device: an inconsistent state gives
- * MCACG_ERR_BAD_ARGUMENT. */
+ * MCACG_ERR_BAD_ARGUMENT. A box that oxidises gets a slot for every sphere
+ * (its aggregate table is copied into a larger one), room for any split. */
 int mcacg_batch_create_from_states(const mcacg_params *params, const mcacg_state *states, int32_t n_boxes,
                                    void *cuda_stream, mcacg_batch **batch);
 /* Page-locked host memory (freed by mcacg_host_free), for state arrays that
@@ -404,6 +415,11 @@ int mcacg_draw_directions(int64_t n, uint32_t seed, double *out);
 int mcacg_batch_stats(mcacg_batch *batch, mcacg_run_stats *stats);
 int mcacg_batch_size(const mcacg_batch *batch, int32_t *n_boxes);
 int mcacg_batch_box_sizes(mcacg_batch *batch, int32_t box, int64_t *n_spheres, int64_t *n_aggregates);
+/* The state of one box in label order. Spheres removed by oxidation leave
+ * the stored state as they leave the reference's storage: the others keep
+ * their order and n_spheres shrinks (the tables are packed as
+ * [9][n_spheres] and [21][n_aggregates]); a box whose spheres all went
+ * stores an empty state (no spheres, no aggregates). */
 int mcacg_batch_store_state(mcacg_batch *batch, int32_t box, mcacg_state *state);
 /* mcacg_batch_store_state for every box at once (states[i] for box i, all
  * n_boxes of them), the conversions spread over the host's cores. */

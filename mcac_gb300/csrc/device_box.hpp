@@ -140,6 +140,7 @@ class DeviceBox {
     // (MCACG_VOLSURF_NONE, _CAPS or _ALPHAS); set before the box runs.
     int set_volsurf(int method);
     void *stream() const { return stream_; }
+    bool owns_stream() const { return own_stream_; }
     int query(int src_slot, const double dir[3], double dist, QueryResult *out, std::string *err);
     // n independent queries on the current state (nothing is moved): slots[k],
     // dirs[3k..3k+2], dists[k] -> out[k]. The queries run concurrently, one

@@ -2,6 +2,7 @@
 #include "host_box.hpp"
 
 #include <algorithm>
+#include <array>
 #include <fstream>
 #include <cmath>
 #include <cstring>
@@ -381,6 +382,9 @@ int HostBox::upload(const HostState &st, void *stream, std::string *err) {
     alive_.clear();
     for (int a = 0; a < nslots_; ++a)
         if (agg_n_[size_t(a)] > 0) alive_.push_back(a);
+    uid_.resize(alive_.size());
+    std::iota(uid_.begin(), uid_.end(), int64_t(0));
+    next_uid_ = int64_t(alive_.size());
     maxradius_ = st.maxradius;
     time_ = st.time;
     DeviceBox *d = nullptr;
@@ -624,15 +628,20 @@ int HostBox::time_forward(int64_t label, double dt, std::string *err) {
 
 int HostBox::merge(const mcacg_contact &c, int32_t *merged, std::string *err) {
     *merged = 0;
-    if (c.moving_sphere < 0 || c.other_sphere < 0 || c.moving_aggregate < 0 || c.other_aggregate < 0) return ST_OK;
+    // a sphere of the contact that is gone (oxidation): nothing to merge
+    // (aggregat_list.cpp:369-374)
+    if (c.moving_sphere < 0 || c.other_sphere < 0) return ST_OK;
     if (c.moving_aggregate >= int64_t(alive_.size()) || c.other_aggregate >= int64_t(alive_.size()) ||
         c.moving_sphere >= ns_ || c.other_sphere >= ns_) {
         if (err) *err = "contact refers to an unknown aggregate or sphere";
         return ST_BAD_ARGUMENT;
     }
     invalidate_device_run();
-    const int mslot = alive_[size_t(c.moving_aggregate)];
-    const int oslot = alive_[size_t(c.other_aggregate)];
+    // an aggregate of the contact that is gone (-1, oxidation split it):
+    // the device merge refuses with MergeError if the spheres still touch,
+    // as the reference does (aggregat.cpp:488-504)
+    const int mslot = c.moving_aggregate >= 0 ? alive_[size_t(c.moving_aggregate)] : -1;
+    const int oslot = c.other_aggregate >= 0 ? alive_[size_t(c.other_aggregate)] : -1;
     MergeResult m;
     int rc = dev_->merge(int(c.moving_sphere), int(c.other_sphere), mslot, oslot, &m, err);
     if (rc != ST_OK) return rc;
@@ -657,7 +666,10 @@ int HostBox::merge(const mcacg_contact &c, int32_t *merged, std::string *err) {
     agg_n_[size_t(removed)] = 0;
     maxradius_ = m.maxradius;
     auto it = std::lower_bound(alive_.begin(), alive_.end(), removed);
-    if (it != alive_.end() && *it == removed) alive_.erase(it);
+    if (it != alive_.end() && *it == removed) {
+        uid_.erase(uid_.begin() + (it - alive_.begin()));
+        alive_.erase(it);
+    }
     double upd[21];
     for (int f = 0; f < 21; ++f) upd[f] = F(f, keep);
     unsigned mask = (1u << AGG_F_AGG) | (1u << AGG_D_M) | (1u << AGG_TIME_STEP) | (1u << AGG_LPM) |
@@ -761,6 +773,7 @@ int64_t HostBox::pick_random() {
 }
 
 void HostBox::refresh() {
+    if (alive_.empty()) return;  // every sphere oxidised
     max_time_step_ = F(AGG_TIME_STEP, alive_[0]);
     for (int slot : alive_) max_time_step_ = std::max(F(AGG_TIME_STEP, slot), max_time_step_);
     avg_npp_ = static_cast<double>(ns_) / static_cast<double>(alive_.size());
@@ -827,15 +840,286 @@ int HostBox::update_aggregates(int slot, bool full, std::string *err) {
     return dev_->set_maxradius(maxradius_, err);
 }
 
-int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::string *err) {
-    if (p_.with_domain_duplication || p_.with_domain_reduction || p_.pick_method != MCACG_PICK_RANDOM ||
-        (p_.with_surface_reactions && p_.u_sg < 0.0)) {
-        if (err) *err = "the host-driven loop covers collisions with optional surface growth (u_sg >= 0; no "
-                        "domain duplication/reduction, pick_method=random); oxidation runs in the device loop";
-        return ST_INPUT;
+namespace {
+// A box in the reference's own order, for oxidation: aggregates by label,
+// spheres by storage index, both renumbered as the reference renumbers them.
+struct LabelBox {
+    HostState st;                           // spheres ([9][ns]); st.ns
+    std::vector<std::array<double, 21>> f;  // fields by label
+    std::vector<std::vector<int>> mem;      // members by label, list order
+    std::vector<int64_t> uid;
+};
+
+// spheres.remove(id) (list_storage_methods.hpp:78-87): later spheres move
+// down one index; member lists and the contact's sphere references follow
+// (a reference to the removed sphere becomes -1, an expired weak pointer).
+void remove_storage(LabelBox &w, int id, int64_t *refs[], int nrefs) {
+    const int ns = w.st.ns;
+    std::vector<double> sph(size_t(9) * size_t(ns - 1));
+    for (int f = 0; f < 9; ++f) {
+        const double *src = w.st.sph.data() + size_t(f) * size_t(ns);
+        double *dst = sph.data() + size_t(f) * size_t(ns - 1);
+        std::copy(src, src + id, dst);
+        std::copy(src + id + 1, src + ns, dst + id);
     }
+    w.st.sph.swap(sph);
+    w.st.ns = ns - 1;
+    for (auto &m : w.mem)
+        for (int &x : m)
+            if (x > id) --x;
+    for (int r = 0; r < nrefs; ++r) {
+        if (*refs[r] == id) *refs[r] = -1;
+        else if (*refs[r] > id) --(*refs[r]);
+    }
+}
+}  // namespace
+
+// Relative positions from the first sphere, Aggregate::update, then each
+// sphere placed back from the aggregate's position (remove_sphere and split,
+// aggregat.cpp:596-609, 641-654); all on the host, as the reference.
+static int rebase_update_place(const mcacg_params &p, LabelBox &w, int a, double *maxradius) {
+    HostState &st = w.st;
+    const std::vector<int> &m = w.mem[size_t(a)];
+    auto SFr = [&](int f, int s) -> double & { return st.sph[size_t(f) * size_t(st.ns) + size_t(s)]; };
+    const int s0 = m[0];
+    const double r0[3] = {SFr(SPH_X, s0), SFr(SPH_Y, s0), SFr(SPH_Z, s0)};
+    for (int s : m) {
+        SFr(SPH_RX, s) = SFr(SPH_X, s) - r0[0];
+        SFr(SPH_RY, s) = SFr(SPH_Y, s) - r0[1];
+        SFr(SPH_RZ, s) = SFr(SPH_Z, s) - r0[2];
+    }
+    int rc = host_update_aggregate(p, st, MemberLists::View{m.data(), int(m.size())}, w.f[size_t(a)].data(), maxradius);
+    if (rc != ST_OK) return rc;
+    const double *F = w.f[size_t(a)].data();
+    const double ref[3] = {F[AGG_X] - F[AGG_RX], F[AGG_Y] - F[AGG_RY], F[AGG_Z] - F[AGG_RZ]};
+    for (int s : m) {
+        SFr(SPH_X, s) = ref[0] + SFr(SPH_RX, s);
+        SFr(SPH_Y, s) = ref[1] + SFr(SPH_RY, s);
+        SFr(SPH_Z, s) = ref[2] + SFr(SPH_RZ, s);
+    }
+    return ST_OK;
+}
+
+int64_t HostBox::label_of_uid(int64_t uid) const {
+    for (size_t l = 0; l < uid_.size(); ++l)
+        if (uid_[l] == uid) return int64_t(l);
+    return -1;
+}
+
+// The box's state replaced by one in label order (slot = label), for the
+// spheres and aggregates oxidation renumbered: a new device box, the host
+// mirrors from it. Nothing else changes (the pick factor and mean size stay
+// as the last event left them).
+int HostBox::replace_state(const HostState &st, std::string *err) {
+    invalidate_device_run();
+    DeviceBox *d = nullptr;
+    void *stream = dev_->owns_stream() ? nullptr : dev_->stream();
+    int rc = DeviceBox::create(st, stream, &d, err);
+    if (rc != ST_OK) return rc;
+    dev_.reset(d);
+    rc = dev_->set_volsurf(p_.volsurf_method);
+    if (rc != ST_OK) {
+        if (err) *err = "volsurf_method not available";
+        return rc;
+    }
+    ns_ = st.ns;
+    nslots_ = st.nslots;
+    agg_ = st.agg;
+    agg_n_ = st.agg_n;
+    alive_.resize(size_t(st.nslots));
+    std::iota(alive_.begin(), alive_.end(), 0);
+    maxradius_ = st.maxradius;
+    dt_order_valid_ = false;
+    return ST_OK;
+}
+
+// Oxidation after the spheres shrank on the device (calcul.cpp:157-170):
+// Aggregate::croissance_surface with remove_sphere (aggregat.cpp:230-243,
+// 629-655) and AggregatList::croissance_surface (aggregat_list.cpp:549-579),
+// then Aggregate::split (aggregat.cpp:545-628, aggregat_list.cpp:409-446) of
+// every aggregate, or of the moved one (label >= 0, the individual mode).
+// Worked on the host in the reference's own order, every step being
+// sequential and exact; when anything changed the device box is rebuilt in
+// that order. The contact's sphere references are renumbered.
+int HostBox::oxidize(int64_t label, mcacg_contact *c, bool *split, bool *disappear, std::string *err) {
+    *split = *disappear = false;
+    HostState cur;
+    int rc = dev_->download(&cur, err);
+    if (rc != ST_OK) return rc;
+    LabelBox w;
+    w.st.n_div = cur.n_div;
+    w.st.box_length = cur.box_length;
+    w.st.ns = cur.ns;
+    w.st.sph.swap(cur.sph);
+    const size_t na = alive_.size();
+    w.f.resize(na);
+    w.mem.resize(na);
+    w.uid = uid_;
+    for (size_t l = 0; l < na; ++l) {
+        const int slot = alive_[l];
+        for (int f = 0; f < 21; ++f) w.f[l][size_t(f)] = F(f, slot);
+        const auto v = cur.members[size_t(slot)];
+        w.mem[l].assign(v.begin(), v.end());
+    }
+    const double L = w.st.box_length, rp_min = p_.rp_min_oxid;
+    double maxr = maxradius_;
+    bool changed = false;
+    int64_t *refs[2] = {&c->moving_sphere, &c->other_sphere};
+    auto R = [&](int s) { return w.st.sph[size_t(SPH_R) * size_t(w.st.ns) + size_t(s)]; };
+    auto P = [&](int s) {
+        const size_t ns = size_t(w.st.ns);
+        return Vec3{w.st.sph[size_t(SPH_X) * ns + size_t(s)], w.st.sph[size_t(SPH_Y) * ns + size_t(s)],
+                    w.st.sph[size_t(SPH_Z) * ns + size_t(s)]};
+    };
+    // removal in one aggregate; true when it is left empty
+    auto remove_small = [&](int a, int *status) {
+        std::vector<int> &m = w.mem[size_t(a)];
+        for (size_t k = 0; k < m.size();) {
+            const int id = m[k];
+            if (!(R(id) <= rp_min)) {
+                ++k;
+                continue;
+            }
+            m.erase(m.begin() + long(k));
+            remove_storage(w, id, refs, 2);
+            changed = true;
+            if (!m.empty()) {
+                const int r2 = rebase_update_place(p_, w, a, &maxr);
+                if (r2 != ST_OK) {
+                    *status = r2;
+                    return false;
+                }
+            }
+        }
+        return m.empty();
+    };
+    auto erase_label = [&](int a) {
+        w.f.erase(w.f.begin() + a);
+        w.mem.erase(w.mem.begin() + a);
+        w.uid.erase(w.uid.begin() + a);
+        changed = true;
+        *disappear = true;
+    };
+    // Aggregate::split of label a: parts as the reference walks them, each
+    // appended as a copy of a's record with its spheres in discovery order
+    // and updated, then a removed. Returns true when it split.
+    auto split_one = [&](int a, int *status) {
+        const std::vector<int> m = w.mem[size_t(a)];
+        const int n = int(m.size());
+        if (n < 2) return false;
+        std::vector<int> unvisited(static_cast<size_t>(n));
+        std::iota(unvisited.begin(), unvisited.end(), 0);
+        std::vector<std::vector<int>> parts;
+        while (!unvisited.empty()) {
+            std::vector<int> part{unvisited.front()};
+            unvisited.erase(unvisited.begin());
+            std::vector<int> discovered = part;
+            while (!discovered.empty()) {
+                const int i1 = discovered.back();
+                discovered.pop_back();
+                for (size_t idx = 0; idx < unvisited.size();) {
+                    const int i2 = unvisited[idx];
+                    if (spheres_in_contact(P(m[size_t(i1)]), R(m[size_t(i1)]), P(m[size_t(i2)]), R(m[size_t(i2)]), L)) {
+                        part.push_back(i2);
+                        discovered.push_back(i2);
+                        unvisited.erase(unvisited.begin() + long(idx));
+                    } else {
+                        ++idx;
+                    }
+                }
+            }
+            parts.push_back(std::move(part));
+        }
+        if (parts.size() < 2) return false;
+        const std::array<double, 21> fa = w.f[size_t(a)];
+        for (const auto &part : parts) {
+            w.f.push_back(fa);
+            w.uid.push_back(next_uid_++);
+            std::vector<int> pm;
+            for (int i : part) pm.push_back(m[size_t(i)]);
+            w.mem.push_back(std::move(pm));
+            const int r2 = rebase_update_place(p_, w, int(w.mem.size()) - 1, &maxr);
+            if (r2 != ST_OK) {
+                *status = r2;
+                return true;
+            }
+        }
+        erase_label(a);
+        *disappear = false;  // a split, not a disappearance
+        changed = true;
+        return true;
+    };
+    int status = ST_OK;
+    bool any_disappear = false;
+    if (label >= 0) {
+        if (remove_small(int(label), &status)) {
+            erase_label(int(label));
+            any_disappear = true;
+        } else if (status == ST_OK) {
+            *split = split_one(int(label), &status);
+        }
+    } else {
+        for (int a = 0; a < int(w.mem.size()) && status == ST_OK;) {
+            if (remove_small(a, &status)) {
+                erase_label(a);
+                any_disappear = true;
+            } else {
+                ++a;
+            }
+        }
+        for (int a = 0; a < int(w.mem.size()) && status == ST_OK;) {
+            if (split_one(a, &status)) *split = true;
+            else ++a;
+        }
+    }
+    *disappear = any_disappear;
+    if (status != ST_OK) {
+        if (err) *err = "volume/surface error in an oxidised aggregate";
+        return status;
+    }
+    if (!changed) return ST_OK;
+    // the state in label order (slot = label)
+    HostState st;
+    st.n_div = w.st.n_div;
+    st.box_length = w.st.box_length;
+    st.maxradius = maxr;
+    st.time = time_;
+    st.ns = w.st.ns;
+    st.nslots = int(w.mem.size());
+    st.sph.swap(w.st.sph);
+    st.sph_slot.assign(size_t(st.ns), -1);
+    st.agg.assign(size_t(21) * size_t(st.nslots), 0.0);
+    st.agg_n.assign(size_t(st.nslots), 0);
+    st.members.clear();
+    for (int l = 0; l < st.nslots; ++l) {
+        for (int f = 0; f < 21; ++f) st.agg[size_t(f) * size_t(st.nslots) + size_t(l)] = w.f[size_t(l)][size_t(f)];
+        st.agg_n[size_t(l)] = int(w.mem[size_t(l)].size());
+        st.members.push_list(w.mem[size_t(l)].data(), int(w.mem[size_t(l)].size()));
+        for (int s : w.mem[size_t(l)]) st.sph_slot[size_t(s)] = l;
+    }
+    if (st.nslots == 0) {  // every sphere gone: an empty box
+        alive_.clear();
+        uid_.clear();
+        ns_ = st.ns;
+        maxradius_ = maxr;
+        return ST_OK;
+    }
+    rc = replace_state(st, err);
+    if (rc != ST_OK) return rc;
+    uid_ = w.uid;
+    return ST_OK;
+}
+
+int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::string *err) {
     const bool surface = p_.with_surface_reactions != 0;
     const bool individual = surface && p_.individual_surf_reactions != 0;
+    const bool oxidation = surface && p_.u_sg < 0.0;
+    if (p_.with_domain_duplication || p_.with_domain_reduction || p_.pick_method != MCACG_PICK_RANDOM ||
+        (oxidation && p_.full_aggregate_update_frequency > 1)) {
+        if (err) *err = "the host-driven loop covers collisions with optional surface reactions (no domain "
+                        "duplication/reduction, pick_method=random; oxidation with a full update every step)";
+        return ST_INPUT;
+    }
     if (opts.advancement_path && (p_.write_events_frequency <= 0 || p_.write_between_event_frequency <= 0)) {
         if (err) *err = "write_events_frequency and write_between_event_frequency must be positive";
         return ST_INPUT;
@@ -871,28 +1155,42 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
         deltatemps_indiv = deltatemps_indiv * (move_distance / full_distance + static_cast<double>(n_try - 1));
         time_forward(label, deltatemps, err);
         time_ = time_ + deltatemps;
-        // surface growth before the merge (calcul.cpp:157-170): every
-        // sphere, or the moved aggregate's by its own time step
+        // surface reactions before the merge (calcul.cpp:157-170): every
+        // sphere, or the moved aggregate's by its own time step, grows or
+        // shrinks; with oxidation spheres leave, aggregates disappear or split
+        const int64_t moving_uid = oxidation ? uid_[size_t(label)] : -1;
+        const int64_t other_uid = oxidation && contact && c.other_aggregate >= 0 ? uid_[size_t(c.other_aggregate)] : -1;
+        bool split = false, disappear = false;
         if (surface) {
             rc = individual ? dev_->grow(slot, p_.u_sg * deltatemps_indiv, err)
                             : dev_->grow(-1, p_.u_sg * deltatemps, err);
             if (rc != ST_OK) return rc;
         }
+        if (oxidation) {
+            rc = oxidize(individual ? label : -1, &c, &split, &disappear, err);
+            if (rc != ST_OK) return rc;
+        }
         int32_t merged = 0;
-        if (contact) {
+        if (contact && (!individual || !(split || disappear))) {
+            if (oxidation) {
+                // the contact's aggregates where they are now (-1: split or gone)
+                c.moving_aggregate = label_of_uid(moving_uid);
+                c.other_aggregate = label_of_uid(other_uid);
+            }
             rc = merge(c, &merged, err);
             if (rc != ST_OK) return rc;
         }
-        if (surface) {
+        if (surface && !alive_.empty()) {
             // update() every full_aggregate_update_frequency-th step without
             // event, else update_partial(); the moved aggregate alone in the
-            // individual mode unless there was a merge (calcul.cpp:180-206)
+            // individual mode unless there was an event (calcul.cpp:180-206)
             const int64_t every = std::max<int64_t>(1, p_.full_aggregate_update_frequency);
             const bool full = n_iter_without_event_ % every == 0;
-            rc = update_aggregates(individual && !merged ? slot : -1, full, err);
+            const bool alone = individual && !merged && !split && !disappear;
+            rc = update_aggregates(alone ? alive_[size_t(label)] : -1, full, err);
             if (rc != ST_OK) return rc;
         }
-        event_ = merged != 0;
+        event_ = merged != 0 || split || disappear;
         if (event_) {
             n_iter_without_event_ = 0;
             ++events;

@@ -70,6 +70,9 @@ class HostBox {
 
   private:
     int update_aggregates(int slot, bool full, std::string *err);
+    int oxidize(int64_t label, mcacg_contact *c, bool *split, bool *disappear, std::string *err);
+    int replace_state(const HostState &st, std::string *err);
+    int64_t label_of_uid(int64_t uid) const;
     void invalidate_device_run();
     int refresh_from_device(std::string *err);
     std::unique_ptr<BatchRunner> runner_;
@@ -91,6 +94,8 @@ class HostBox {
     std::vector<double> agg_;   // [21][nslots] mirror
     std::vector<int> agg_n_;    // members per slot (0: dead)
     std::vector<int> alive_;    // slot of each label
+    std::vector<int64_t> uid_;  // identity of each label's aggregate (the reference's weak pointers)
+    int64_t next_uid_ = 0;
     double maxradius_ = 0;
     double max_time_step_ = 0, avg_npp_ = 1;
     std::vector<size_t> index_sorted_;

@@ -78,6 +78,8 @@ struct mo_box {
     int64_t *sph_label;
     double *agg[21];  /* by label (positional list, aggregat_list.hpp:29) */
     int64_t *agg_n;
+    int64_t *agg_uid; /* identity of each aggregate (the reference's weak pointers) */
+    int64_t next_uid;
     ivec *members;
     int64_t (*vidx)[3];
     ivec *cells;
@@ -397,14 +399,19 @@ static mo_box *alloc_box(const mo_params *p, int64_t ns, int64_t na, int n_div, 
     for (int f = 0; f < 9; ++f) b->sph[f] = (double *)calloc((size_t)ns, sizeof(double));
     b->volw = (double *)calloc((size_t)ns, sizeof(double));
     b->sph_label = (int64_t *)calloc((size_t)ns, sizeof(int64_t));
-    for (int f = 0; f < 21; ++f) b->agg[f] = (double *)calloc((size_t)na, sizeof(double));
-    b->agg_n = (int64_t *)calloc((size_t)na, sizeof(int64_t));
-    b->members = (ivec *)calloc((size_t)na, sizeof(ivec));
-    b->vidx = (int64_t(*)[3])calloc((size_t)na, sizeof(int64_t[3]));
+    /* room for an aggregate per sphere: oxidation splits append aggregates */
+    const int64_t cap = na > ns ? na : ns;
+    for (int f = 0; f < 21; ++f) b->agg[f] = (double *)calloc((size_t)cap, sizeof(double));
+    b->agg_n = (int64_t *)calloc((size_t)cap, sizeof(int64_t));
+    b->agg_uid = (int64_t *)calloc((size_t)cap, sizeof(int64_t));
+    for (int64_t a = 0; a < na; ++a) b->agg_uid[a] = a;
+    b->next_uid = na;
+    b->members = (ivec *)calloc((size_t)cap, sizeof(ivec));
+    b->vidx = (int64_t(*)[3])calloc((size_t)cap, sizeof(int64_t[3]));
     b->cells = (ivec *)calloc((size_t)n_div * n_div * n_div, sizeof(ivec));
-    b->index_sorted = (int64_t *)calloc((size_t)na, sizeof(int64_t));
-    b->cumulative = (double *)calloc((size_t)na, sizeof(double));
-    b->tp = (double *)calloc((size_t)na, sizeof(double));
+    b->index_sorted = (int64_t *)calloc((size_t)cap, sizeof(int64_t));
+    b->cumulative = (double *)calloc((size_t)cap, sizeof(double));
+    b->tp = (double *)calloc((size_t)cap, sizeof(double));
     b->event = 1;
     return b;
 }
@@ -416,6 +423,7 @@ void mo_box_free(mo_box *b) {
     free(b->sph_label);
     for (int f = 0; f < 21; ++f) free(b->agg[f]);
     free(b->agg_n);
+    free(b->agg_uid);
     for (int64_t a = 0; a < b->na; ++a) free(b->members[a].v);
     free(b->members);
     free(b->vidx);
@@ -462,6 +470,7 @@ void mo_params_derive(mo_params *p, double pressure) {
 
 /* AggregatList::refresh (aggregat_list.cpp:100-108) */
 void mo_refresh(mo_box *b) {
+    if (b->na < 1) return;
     b->max_time_step = AGG(b, A_TIME_STEP, 0);
     for (int64_t a = 0; a < b->na; ++a) b->max_time_step = dmax(AGG(b, A_TIME_STEP, a), b->max_time_step);
     b->avg_npp = (double)b->ns / (double)b->na;
@@ -723,6 +732,7 @@ static void remove_aggregate(mo_box *b, int64_t a) {
     int64_t tail = b->na - a - 1;
     for (int f = 0; f < 21; ++f) memmove(b->agg[f] + a, b->agg[f] + a + 1, (size_t)tail * sizeof(double));
     memmove(b->agg_n + a, b->agg_n + a + 1, (size_t)tail * sizeof(int64_t));
+    memmove(b->agg_uid + a, b->agg_uid + a + 1, (size_t)tail * sizeof(int64_t));
     memmove(b->members + a, b->members + a + 1, (size_t)tail * sizeof(ivec));
     memmove(b->vidx + a, b->vidx + a + 1, (size_t)tail * sizeof(int64_t[3]));
     b->na--;
@@ -744,6 +754,9 @@ int mo_merge(mo_box *b, const mo_contact *c, int32_t *merged) {
     double pm[3] = {SPH(b, S_X, ms), SPH(b, S_Y, ms), SPH(b, S_Z, ms)};
     double po[3] = {SPH(b, S_X, os), SPH(b, S_Y, os), SPH(b, S_Z, os)};
     if (!contact(pm, SPH(b, S_R, ms), po, SPH(b, S_R, os), b->L)) return 0;
+    /* an aggregate of the contact that split or disappeared since the query
+     * (aggregat.cpp:488-493): the reference's merge refuses */
+    if (c->moving_aggregate < 0 || c->other_aggregate < 0) return 9; /* MergeError */
     int64_t la = b->sph_label[ms], lb = b->sph_label[os];
     int64_t keep = la < lb ? la : lb, removed = la < lb ? lb : la;
     double newtime = AGG(b, A_TIME, keep) + AGG(b, A_TIME, removed) - b->time;
@@ -957,13 +970,155 @@ static void grow_aggregate(mo_box *b, int64_t a, double dt) {
     }
 }
 
-/* calcul (src/calcul.cpp:66-281): collisions, with surface growth
- * (u_sg >= 0) when the parameters ask for it */
+/* ---------------------------------------------------------- oxidation */
+/* spheres.remove(id) (list_storage_methods.hpp:78-87): the later spheres move
+ * down one index; member lists and the tracked sphere references follow
+ * (a reference to the removed sphere becomes -1, as an expired weak pointer). */
+static void remove_sphere_storage(mo_box *b, int64_t id, int64_t **refs, int nrefs) {
+    const int64_t tail = b->ns - id - 1;
+    for (int f = 0; f < 9; ++f) memmove(b->sph[f] + id, b->sph[f] + id + 1, (size_t)tail * sizeof(double));
+    memmove(b->volw + id, b->volw + id + 1, (size_t)tail * sizeof(double));
+    memmove(b->sph_label + id, b->sph_label + id + 1, (size_t)tail * sizeof(int64_t));
+    b->ns--;
+    for (int64_t a = 0; a < b->na; ++a)
+        for (int64_t k = 0; k < b->members[a].n; ++k)
+            if (b->members[a].v[k] > id) b->members[a].v[k]--;
+    for (int r = 0; r < nrefs; ++r) {
+        if (*refs[r] == id) *refs[r] = -1;
+        else if (*refs[r] > id) (*refs[r])--;
+    }
+}
+
+/* Relative positions from the first sphere, Aggregate::update, then every
+ * sphere placed back from the aggregate's position (remove_sphere and
+ * split, aggregat.cpp:596-609, 641-654). */
+static int rebase_update_place(mo_box *b, int64_t a) {
+    const ivec *m = &b->members[a];
+    const int64_t s0 = m->v[0];
+    const double ref0[3] = {SPH(b, S_X, s0), SPH(b, S_Y, s0), SPH(b, S_Z, s0)};
+    for (int64_t k = 0; k < m->n; ++k) {
+        const int64_t s = m->v[k];
+        SPH(b, S_RX, s) = SPH(b, S_X, s) - ref0[0];
+        SPH(b, S_RY, s) = SPH(b, S_Y, s) - ref0[1];
+        SPH(b, S_RZ, s) = SPH(b, S_Z, s) - ref0[2];
+    }
+    int rc = update_aggregate(b, a);
+    if (rc) return rc;
+    const double ref[3] = {AGG(b, A_X, a) - AGG(b, A_RX, a), AGG(b, A_Y, a) - AGG(b, A_RY, a),
+                           AGG(b, A_Z, a) - AGG(b, A_RZ, a)};
+    for (int64_t k = 0; k < m->n; ++k) {
+        const int64_t s = m->v[k];
+        SPH(b, S_X, s) = ref[0] + SPH(b, S_RX, s);
+        SPH(b, S_Y, s) = ref[1] + SPH(b, S_RY, s);
+        SPH(b, S_Z, s) = ref[2] + SPH(b, S_RZ, s);
+    }
+    return 0;
+}
+
+/* Aggregate::croissance_surface (aggregat.cpp:230-243) with remove_sphere
+ * (aggregat.cpp:629-655): the spheres shrink, each one at or below rp_min
+ * leaves (the list keeps its order) and the aggregate is updated after each
+ * removal. *empty is set when no sphere is left. */
+static int oxidize_aggregate(mo_box *b, int64_t a, double dt, double rp_min, int64_t **refs, int nrefs, int *empty) {
+    grow_aggregate(b, a, dt);
+    ivec *m = &b->members[a];
+    for (int64_t k = 0; k < m->n;) {
+        const int64_t id = m->v[k];
+        if (!(SPH(b, S_R, id) <= rp_min)) {
+            ++k;
+            continue;
+        }
+        memmove(m->v + k, m->v + k + 1, (size_t)(m->n - k - 1) * sizeof(int64_t));
+        m->n--;
+        remove_sphere_storage(b, id, refs, nrefs);
+        b->agg_n[a] = m->n;
+        if (m->n > 0) {
+            int rc = rebase_update_place(b, a);
+            if (rc) return rc;
+        }
+    }
+    *empty = m->n == 0;
+    return 0;
+}
+
+/* Aggregate::split (aggregat.cpp:545-628): the connected parts of the
+ * aggregate's contact network, found as the reference walks it (the first
+ * unvisited sphere starts a part; the last discovered sphere is explored
+ * next against the unvisited ones in order), each appended as a copy of the
+ * aggregate's record with its own spheres in discovery order, updated;
+ * then AggregatList::remove of the aggregate. *did is set when it split. */
+static int split_aggregate(mo_box *b, int64_t a, int *did) {
+    *did = 0;
+    const ivec *m = &b->members[a];
+    const int64_t n = m->n;
+    if (n < 2) return 0;
+    int64_t *unvisited = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    int64_t *order = (int64_t *)malloc((size_t)n * sizeof(int64_t));  /* parts back to back */
+    int64_t *part_end = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+    int64_t *stack = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    int64_t nu = n, no = 0, np = 0;
+    for (int64_t i = 0; i < n; ++i) unvisited[i] = i;
+    while (nu > 0) {
+        int64_t first = unvisited[0];
+        memmove(unvisited, unvisited + 1, (size_t)(nu - 1) * sizeof(int64_t));
+        nu--;
+        order[no++] = first;
+        int64_t ns_ = 0;
+        stack[ns_++] = first;
+        while (ns_ > 0) {
+            const int64_t s1 = m->v[stack[--ns_]];
+            const double p1[3] = {SPH(b, S_X, s1), SPH(b, S_Y, s1), SPH(b, S_Z, s1)};
+            for (int64_t idx = 0; idx < nu;) {
+                const int64_t s2 = m->v[unvisited[idx]];
+                const double p2[3] = {SPH(b, S_X, s2), SPH(b, S_Y, s2), SPH(b, S_Z, s2)};
+                if (contact(p1, SPH(b, S_R, s1), p2, SPH(b, S_R, s2), b->L)) {
+                    order[no++] = unvisited[idx];
+                    stack[ns_++] = unvisited[idx];
+                    memmove(unvisited + idx, unvisited + idx + 1, (size_t)(nu - idx - 1) * sizeof(int64_t));
+                    nu--;
+                } else {
+                    ++idx;
+                }
+            }
+        }
+        part_end[np++] = no;
+    }
+    int rc = 0;
+    if (np > 1) {
+        *did = 1;
+        for (int64_t c = 0; c < np && !rc; ++c) {
+            const int64_t beg = c == 0 ? 0 : part_end[c - 1];
+            const int64_t L = b->na;
+            for (int f = 0; f < 21; ++f) AGG(b, f, L) = AGG(b, f, a);
+            b->agg_uid[L] = b->next_uid++;
+            memset(&b->members[L], 0, sizeof(ivec));
+            for (int64_t k = beg; k < part_end[c]; ++k) {
+                const int64_t s = b->members[a].v[order[k]];
+                iv_push(&b->members[L], s);
+                b->sph_label[s] = L;
+            }
+            b->agg_n[L] = b->members[L].n;
+            b->na++;
+            verlet_index(b, L, b->vidx[L]);
+            set_insert(cell(b, b->vidx[L]), L);
+            rc = rebase_update_place(b, L);
+        }
+        if (!rc) remove_aggregate(b, a);
+    }
+    free(unvisited);
+    free(order);
+    free(part_end);
+    free(stack);
+    return rc;
+}
+
+/* calcul (src/calcul.cpp:66-281): collisions, with surface growth or
+ * oxidation when the parameters ask for it */
 int mo_calcul(mo_box *b, int64_t max_steps, mo_step_record *trace, int64_t cap, mo_stats *stats) {
     int64_t steps = 0, events = 0;
     const int surface = b->p.with_surface_reactions != 0;
     const int individual = surface && b->p.individual_surf_reactions != 0;
-    if (surface && b->p.u_sg < 0.0) return 4; /* oxidation is not restated here */
+    const int oxidation = surface && b->p.u_sg < 0.0;
     while (!finished(b)) {
         if (max_steps > 0 && steps >= max_steps) break;
         double max = b->max_time_step;
@@ -990,14 +1145,60 @@ int mo_calcul(mo_box *b, int64_t max_steps, mo_step_record *trace, int64_t cap, 
         deltatemps_indiv = deltatemps_indiv * (move / full + (double)(n_try - 1));
         AGG(b, A_TIME, label) += deltatemps;
         b->time = b->time + deltatemps;
-        /* surface growth before the merge (calcul.cpp:157-170) */
-        if (individual) {
+        /* surface reactions before the merge (calcul.cpp:157-170) */
+        int split = 0, disappear = 0;
+        const int64_t moving_uid = b->agg_uid[label];
+        const int64_t other_uid = contact_flag && c.other_aggregate >= 0 ? b->agg_uid[c.other_aggregate] : -1;
+        if (oxidation) {
+            int64_t *refs[2] = {&c.moving_sphere, &c.other_sphere};
+            const double rp_min = b->p.rp_min_oxid;
+            if (individual) {
+                int empty = 0;
+                int rc = oxidize_aggregate(b, label, deltatemps_indiv, rp_min, refs, 2, &empty);
+                if (rc) return rc;
+                if (empty) {
+                    remove_aggregate(b, label);
+                    disappear = 1;
+                } else {
+                    rc = split_aggregate(b, label, &split);
+                    if (rc) return rc;
+                }
+            } else {
+                for (int64_t a = 0; a < b->na;) {
+                    int empty = 0;
+                    int rc = oxidize_aggregate(b, a, deltatemps, rp_min, refs, 2, &empty);
+                    if (rc) return rc;
+                    if (empty) {
+                        remove_aggregate(b, a);
+                        disappear = 1;
+                    } else {
+                        ++a;
+                    }
+                }
+                for (int64_t a = 0; a < b->na;) {
+                    int did = 0;
+                    int rc = split_aggregate(b, a, &did);
+                    if (rc) return rc;
+                    if (did) split = 1;
+                    else ++a;
+                }
+            }
+        } else if (individual) {
             grow_aggregate(b, label, deltatemps_indiv);
         } else if (surface) {
             for (int64_t a = 0; a < b->na; ++a) grow_aggregate(b, a, deltatemps);
         }
         int32_t merged = 0;
-        if (contact_flag) {
+        if (contact_flag && (!individual || !(split || disappear))) {
+            if (oxidation) {
+                /* the aggregates of the contact where they are now (-1 when
+                 * split or gone: the reference's expired weak pointers) */
+                c.moving_aggregate = c.other_aggregate = -1;
+                for (int64_t a = 0; a < b->na; ++a) {
+                    if (b->agg_uid[a] == moving_uid) c.moving_aggregate = a;
+                    if (b->agg_uid[a] == other_uid) c.other_aggregate = a;
+                }
+            }
             int rc = mo_merge(b, &c, &merged);
             if (rc) return rc;
         }
@@ -1007,7 +1208,7 @@ int mo_calcul(mo_box *b, int64_t max_steps, mo_step_record *trace, int64_t cap, 
              * individual mode unless there was a merge (calcul.cpp:180-206) */
             const int64_t every = b->p.full_aggregate_update_frequency > 0 ? b->p.full_aggregate_update_frequency : 1;
             const int partial = b->n_iter_without_event % every != 0;
-            if (individual && !merged) {
+            if (individual && !merged && !split && !disappear) {
                 int rc = update_aggregate_part(b, label, partial);
                 if (rc) return rc;
             } else {
@@ -1017,8 +1218,8 @@ int mo_calcul(mo_box *b, int64_t max_steps, mo_step_record *trace, int64_t cap, 
                 }
             }
         }
-        b->event = merged;
-        if (merged) {
+        b->event = merged || split || disappear;
+        if (b->event) {
             b->n_iter_without_event = 0;
             ++events;
             mo_refresh(b);

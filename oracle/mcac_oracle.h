@@ -32,10 +32,11 @@ typedef struct mo_params {
     int32_t enforce_volume_fraction, with_collisions;
     int64_t number_of_aggregates_limit, n_iter_without_event_limit, mean_monomere_per_aggregate_limit;
     double physical_time_limit;
-    /* [surface_growth]: growth only (flux >= 0); u_sg is derived */
+    /* [surface_growth] (flux < 0: oxidation) and [oxidation]; u_sg is derived */
     int32_t with_surface_reactions, individual_surf_reactions;
     double flux_surfgrowth, u_sg;
     int64_t full_aggregate_update_frequency;
+    double rp_min_oxid;
 } mo_params;
 
 typedef struct mo_contact {

@@ -30,7 +30,7 @@ class MoParams(C.Structure):
                 ("number_of_aggregates_limit", i64), ("n_iter_without_event_limit", i64),
                 ("mean_monomere_per_aggregate_limit", i64), ("physical_time_limit", f64),
                 ("with_surface_reactions", i32), ("individual_surf_reactions", i32), ("flux_surfgrowth", f64),
-                ("u_sg", f64), ("full_aggregate_update_frequency", i64)]
+                ("u_sg", f64), ("full_aggregate_update_frequency", i64), ("rp_min_oxid", f64)]
 
 
 class MoContact(C.Structure):
@@ -149,6 +149,7 @@ def params_from_ini(text: str) -> MoParams:
     p.flux_surfgrowth = get("surface_growth", "flux_surfgrowth", float, 0.0)
     p.full_aggregate_update_frequency = get("surface_growth", "full_aggregate_update_frequency", int, 1)
     p.individual_surf_reactions = get("numerics", "individual_surf_reactions", bool, False)
+    p.rp_min_oxid = get("oxidation", "rp_min", float, 0.166e-09)
     lib().mo_params_derive(C.byref(p), pressure)
     return p
 

@@ -19,7 +19,12 @@ oracle/ref.mk (oracle/_ref/mcac_ref_harness):
    the aggregates they form are stored (coll_<case>_<k>_*);
 3. the same 6 us / 13 nm case with the shrink of the moved aggregate only
    (individual_surf_reactions), 8 seeds from each start: the numbers of
-   aggregates and spheres left are stored (ind_*).
+   aggregates and spheres left are stored (ind_*);
+4. for the step-exact check of the oracle, from each start the 6 us / 13 nm
+   case both ways with the seed 900 + k: the final state's digest, the
+   numbers of aggregates and spheres and the physical time (exact_*). The
+   harness places one monomer before it loads the state, which draws four
+   values from the seeded stream first.
 
 The device loop is compared with these runs in tests/test_oxidation_gpu.py.
 
@@ -71,6 +76,15 @@ def oxidation_ini(seed: int, time_limit: float, rp_min: float, individual: bool)
             + ("individual_surf_reactions = true\n" if individual else "") + "[output]\noutput_dir = out\n")
 
 
+def digest(snap) -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for arr in (snap.spheres, snap.sphere_label, snap.aggregates, snap.n_spheres, snap.members):
+        h.update(np.ascontiguousarray(arr).tobytes())
+    h.update(np.array([snap.maxradius, snap.box_length], dtype=np.float64).tobytes())
+    return h.hexdigest()
+
+
 def run(args: list[str], cwd: Path) -> None:
     subprocess.run([str(HARNESS)] + args, cwd=cwd, check=True, stdout=subprocess.DEVNULL,
                    stderr=subprocess.DEVNULL)
@@ -99,6 +113,15 @@ def main() -> int:
                 out[f"coll_{name}_{k}_sizes"] = np.sort(end.n_spheres)[::-1].copy()
                 out[f"coll_{name}_{k}_ns"] = np.array(end.ns)
                 out[f"coll_{name}_{k}_time"] = np.array(end.time)
+            for mode, individual in (("coll", False), ("ind", True)):
+                (work / "x.ini").write_text(oxidation_ini(900 + k, start.time + INDIVIDUAL[0], INDIVIDUAL[1],
+                                                          individual))
+                run(["calcul_from", "x.ini", "g_final.snap", "x"], work)
+                end = Snapshot.load(work / "x_final.snap")
+                out[f"exact_{mode}_{k}_digest"] = np.array(digest(end))
+                out[f"exact_{mode}_{k}_na"] = np.array(end.na)
+                out[f"exact_{mode}_{k}_ns"] = np.array(end.ns)
+                out[f"exact_{mode}_{k}_time"] = np.array(end.time)
             for j in range(IND_SEEDS):
                 (work / "i.ini").write_text(oxidation_ini(seed + 200 + j, start.time + INDIVIDUAL[0], INDIVIDUAL[1],
                                                           True))

@@ -53,6 +53,34 @@ def test_oracle_surface_growth_runs(case):
     assert digest(box.store()) == str(g[f"{case}_digest"])
 
 
+@pytest.mark.parametrize("mode", ["coll", "ind"])
+@pytest.mark.parametrize("k", [0, 1, 2, 3])
+def test_oracle_oxidation_runs(mode, k):
+    """Oxidation from states the reference grew (spheres shrink, those at or
+    below rp_min leave, empty aggregates disappear, disconnected ones split;
+    every aggregate at every step, or the moved one): the reference's own
+    runs' final states, byte for byte (tests/golden/make_oxidation_golden.py).
+    The reference's harness placed one monomer before loading the state, four
+    draws of the seeded stream."""
+    import ctypes
+
+    from test_oxidation_gpu import oxidation_ini
+    g = load_golden("oxidation.npz")
+    start = Snapshot.from_npz(g, f"start_{k}_")
+    text = oxidation_ini(900 + k, start.time + float(g["ind_dt"]), float(g["ind_rp_min"]), mode == "ind",
+                         float(g["flux"]))
+    libc = ctypes.CDLL(None)
+    libc.srand(900 + k)
+    for _ in range(4):
+        libc.rand()
+    box = O.OracleBox(text, start)
+    st, _ = box.calcul()
+    out = box.store()
+    assert (out.na, out.ns) == (int(g[f"exact_{mode}_{k}_na"]), int(g[f"exact_{mode}_{k}_ns"]))
+    assert st.time == float(g[f"exact_{mode}_{k}_time"])
+    assert digest(out) == str(g[f"exact_{mode}_{k}_digest"])
+
+
 def test_oracle_lognormal_run_final_state():
     g = load_golden("ln_late.npz")
     box = O.OracleBox(str(g["ini"]))

@@ -17,6 +17,10 @@ alone, not on the moves: the device loop must give the reference's numbers
 of spheres and aggregate sizes (up to contacts that break within the last
 step, whose end time differs). With the shrink of the moved aggregate only
 the outcome is random: 32 runs a side are compared by their means.
+
+The host-driven loop runs oxidation step-exactly: from two of those states,
+both ways, it must match the oracle (itself pinned byte for byte to the
+reference's runs, tests/test_oracle.py) step by step and byte for byte.
 """
 import numpy as np
 import pytest
@@ -181,3 +185,38 @@ def test_every_sphere_oxidised_leaves_an_empty_box():
     # the radius reached rp_min after (15 nm - 10 nm) / |u_sg|
     u = 0.5 / 1800.0
     assert st["time"][0] >= (15e-9 - 1e-8) / u * (1 - 1e-9)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["coll", "ind"])
+def test_host_loop_oxidation_matches_oracle_step_by_step(mode):
+    """The host-driven loop with oxidation, from two of the reference-grown
+    states: every step picks, moves, removes, splits and merges as the oracle
+    (pinned byte for byte to the reference's own runs, tests/test_oracle.py),
+    and the final state is identical byte for byte."""
+    import ctypes
+
+    from mcac_gb300 import AggregatList
+    from oracle import oracle_py as O
+    from test_calcul_gpu import DFIELDS, FIELDS, digest
+    g = load_golden("oxidation.npz")
+    libc = ctypes.CDLL(None)
+    for k in (0, 1):
+        start = starts(g)[k]
+        text = oxidation_ini(900 + k, start.time + float(g["ind_dt"]), float(g["ind_rp_min"]), mode == "ind",
+                             float(g["flux"]))
+        libc.srand(900 + k)
+        ob = O.OracleBox(text, start)
+        ost, otr = ob.calcul(trace=True, trace_capacity=200000)
+        libc.srand(900 + k)
+        with AggregatList(PhysicalModel(text=text), start) as box:
+            st, tr = box.calcul(trace=True, trace_capacity=200000)
+            assert (st.steps, st.events, st.n_aggregates) == (ost.steps, ost.events, ost.n_aggregates)
+            for f in FIELDS:
+                np.testing.assert_array_equal(tr[f], otr[f], err_msg=f)
+            for f in DFIELDS:
+                np.testing.assert_array_equal(tr[f].view(np.int64), otr[f].view(np.int64), err_msg=f)
+            assert st.time == ost.time
+            out = box.store()
+            assert digest(out) == digest(ob.store())
+        assert out.ns < start.ns and out.na > start.na  # spheres removed, aggregates split

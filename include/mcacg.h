@@ -298,13 +298,15 @@ int mcacg_get_aggregate(const mcacg_box *box, int64_t label, double fields[21], 
 
 /* ---- whole runs ---- */
 /* The MC loop of mcac::calcul (src/calcul.cpp:66-281) for collisions, with
- * surface growth when the parameters ask for it (with_surface_reactions,
- * u_sg >= 0: every sphere or the moved aggregate's grows, then the
- * aggregates are updated, calcul.cpp:157-206), driven from the host one step
- * at a time through the entry points above: results are bit-identical with
- * the reference binary built with FP contraction off. Oxidation (u_sg < 0)
- * runs in the device-resident forms below; here it gives
- * MCACG_ERR_INPUT_ERROR. */
+ * surface reactions when the parameters ask for them (with_surface_reactions:
+ * every sphere or the moved aggregate's grows or, u_sg < 0, shrinks; with
+ * oxidation spheres at or below rp_min_oxid leave, empty aggregates
+ * disappear and disconnected ones split; then the aggregates are updated,
+ * calcul.cpp:157-206), driven from the host one step at a time through the
+ * entry points above: results are bit-identical with the reference binary
+ * built with FP contraction off. Oxidation renumbers spheres and labels as
+ * the reference does; it needs a full update every step
+ * (full_aggregate_update_frequency 1, else MCACG_ERR_INPUT_ERROR). */
 int mcacg_calcul(mcacg_box *box, const mcacg_run_opts *opts, mcacg_run_stats *stats);
 
 /* ---- device-resident runs (batched and served forms) ----

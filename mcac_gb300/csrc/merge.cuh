@@ -248,8 +248,7 @@ __device__ inline void block_pair_scan(const DevBox &b, const int *mem, int n, S
         }
         __syncthreads();
     }
-    }  // all pairs
-    __syncthreads();
+    }  // all pairs: both branches end on a barrier
 }
 
 // AggregatList::merge + Aggregate::merge + Aggregate::update (geometry).

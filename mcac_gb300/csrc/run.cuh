@@ -122,7 +122,6 @@ struct RunSmemT {
     unsigned long long deadline;  // %globaltimer time after which no step starts (0: none)
     double dt, full, move;
     int slot, contact, stop, merged, rescale;
-    int split, disappear;  // this step's oxidation events
     int keep, removed;
     int ms, os, oslot;  // contact of this step: spheres and the other slot
     unsigned long long tree_tmp;  // block reduction scratch
@@ -132,6 +131,7 @@ struct RunSmemT {
     int moved[kMovedCap];
     TC tree;                      // top levels of the pick tree
     LL live;                      // the live slots when few are left (box.cuh)
+    int split, disappear;         // this step's oxidation events
 };
 using RunSmem = RunSmemT<QuerySmem, MergeSmem, TreeCacheLarge, LiveList>;
 using RunSmemSmall = RunSmemT<QuerySmemSmall, MergeSmemSmall, TreeCache, LiveListNone>;
@@ -915,9 +915,10 @@ __device__ inline void block_split_slot(const BoxRun &R, RS &sm, int a) {
 // The oxidation of a step (all threads), after the spheres shrank: removals
 // and disappearances, then splits -- of the moved aggregate (slot >= 0, the
 // individual mode, calcul.cpp:159-163) or of every aggregate (calcul.cpp:
-// 165-169). Sets sm.split and sm.disappear.
+// 165-169). Sets sm.split and sm.disappear. Out of line: the loop's steps
+// without oxidation keep their code compact.
 template <class RS>
-__device__ inline void block_oxidize(const BoxRun &R, RS &sm, int slot) {
+__device__ __noinline__ void block_oxidize(const BoxRun &R, RS &sm, int slot) {
     const DevBox &b = R.box;
     const int tid = threadIdx.x, NT = blockDim.x;
     if (tid == 0) {

@@ -566,7 +566,8 @@ def run_device(aggregates: AggregatList, max_steps: int = 0) -> RunStats:
 
 
 def calcul(model: PhysicalModel, aggregates: AggregatList, max_steps: int = 0, advancement=None):
-    """mcac::calcul (src/calcul.cpp:55-290) for the collision-only configuration."""
+    """mcac::calcul (src/calcul.cpp:55-290): collisions, with surface growth or
+    oxidation when the model asks for them."""
     return aggregates.calcul(max_steps=max_steps, advancement=advancement)
 
 

@@ -1,7 +1,7 @@
 // Device-resident MC loop: one thread block advances one box for many steps
 // without returning to the host (the batched / served form).
 //
-// Per step (src/calcul.cpp:94-281, collision-only):
+// Per step (src/calcul.cpp:94-281):
 //   pick   a slot with probability 1/time_step / sum(1/time_step), by a
 //          descent of a 32-ary FP64 sum tree (warp-wide scans), and advance
 //          time by 1 / sum(1/time_step) -- the reference's
@@ -9,7 +9,10 @@
 //   move   random direction from the box's own C-library rand() stream,
 //          contact search (block_query), translation (block_translate);
 //   merge  block_merge, then the aggregate physics of update_partial
-//          (erf/exp/pow from CUDA's libm) and two tree updates.
+//          (erf/exp/pow from CUDA's libm) and two tree updates;
+//   with surface reactions, the spheres grow or shrink before the merge
+//   (oxidation: removals, disappearances, splits) and the aggregates are
+//   updated after it.
 // The contact search and merge geometry are the exact kernels of the
 // single-box path; pick order and libm differ from the reference, so runs
 // agree with it statistically, not step by step (the host-driven loop is the

@@ -1,5 +1,6 @@
 /*
- * mcac_oracle.c -- CPU restatement of the MCAC collision-only MC loop.
+ * mcac_oracle.c -- CPU restatement of the MCAC MC loop (collisions, surface
+ * growth and oxidation).
  *
  * TEST INFRASTRUCTURE: the oracle of the test suite and the CPU baseline of
  * bench.py. Never linked by the product. Each function names the reference

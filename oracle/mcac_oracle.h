@@ -3,9 +3,9 @@
  *
  * This is the oracle of the test suite and the CPU baseline of bench.py: a
  * plain-C restatement of the reference algorithm (giraldeau/MCAC) for the
- * collision-only MC loop -- initial placement, the Verlet grid of aggregate
- * labels, the contact search, translation, merge with label renumbering, and
- * the pick CDF. It keeps the reference's data structures where they set the
+ * MC loop -- initial placement, the Verlet grid of aggregate labels, the
+ * contact search, translation, merge with label renumbering, the pick CDF,
+ * surface growth, and oxidation with sphere removal and splits. It keeps the reference's data structures where they set the
  * result or the cost (sorted label sets per cell, a positional aggregate list
  * renumbered on every removal, an introsort with libstdc++'s element order).
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU arms use it; the
@@ -87,8 +87,9 @@ void mo_set_time(mo_box *b, double t);
  * stages: down to some aggregate count, then on). */
 void mo_set_aggregate_limit(mo_box *b, int64_t limit);
 
-/* The MC loop of src/calcul.cpp:66-281 (collision-only). Stops at the
- * parameters' criteria or after max_steps (> 0). */
+/* The MC loop of src/calcul.cpp:66-281 (collisions, with surface growth or
+ * oxidation when the parameters ask for them). Stops at the parameters'
+ * criteria or after max_steps (> 0). */
 int mo_calcul(mo_box *b, int64_t max_steps, mo_step_record *trace, int64_t trace_capacity, mo_stats *stats);
 
 /* libstdc++ std::sort order of indices 0..n-1 by 'keys' (ascending); the

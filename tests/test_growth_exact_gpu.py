@@ -1,6 +1,6 @@
 """Surface growth in the host-driven loop, step by step against the oracle.
 
-With ``with_surface_reactions`` (u_sg >= 0) every sphere grows at every step
+With ``with_surface_reactions`` and a positive flux every sphere grows at every step
 (or those of the moved aggregate, individual_surf_reactions) and the
 aggregates are updated, fully or with update_partial (src/calcul.cpp:157-206).
 The host-driven loop grows the spheres and recomputes the geometry on the

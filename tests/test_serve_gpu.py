@@ -95,3 +95,38 @@ def test_time_capped_epochs_give_the_same_runs(threads):
             b.run(max_steps=0, steps_per_launch=5000)
             assert int(b.stats()["steps"][0]) == int(done[rid]["steps"])
             assert same_state(b.store(0), finals[rid])
+
+
+@pytest.mark.gpu
+def test_oxidising_requests_served_match_alone():
+    """Requests that oxidise (spheres shrink and leave; one box loses every
+    sphere) beside collision-only ones: each served run ends as it does alone."""
+    ox = ("[monomers]\nnumber = {n}\nmean_diameter = 30\ndispersion_diameter = {disp}\n"
+          "initialisation_mode = lognormal\n[environment]\nvolume_fraction = 3e-3\ntemperature = 1700\n"
+          "[surface_growth]\nwith_surface_reactions = true\nflux_surfgrowth = -0.5\n"
+          "[oxidation]\nrp_min = {rp}\n[limits]\nnumber_of_aggregates = 0\nphysical_time = {tl}\n"
+          "[numerics]\nrandom_seed = {seed}\nwith_domain_duplication = false\n")
+    models = [PhysicalModel(text=ox.format(n=250, disp=1.0, rp=1e-8, tl=1.0, seed=71)),
+              PhysicalModel(text=ox.format(n=400, disp=1.25, rp=1.2e-8, tl=1e-5, seed=72)),
+              PhysicalModel(text=req_ini(300, 73)), PhysicalModel(text=req_ini(350, 74))]
+    done = {}
+    with Server(capacity=2, keep_final_states=True) as srv:
+        ids = [srv.submit(m) for m in models]
+        for _ in range(10_000):
+            active, pending = srv.step(2000)
+            for c in srv.poll():
+                done[int(c["id"])] = c
+            if len(done) == len(models) and active == 0 and pending == 0:
+                break
+        assert len(done) == len(models)
+        finals = [srv.final_state(rid) for rid in ids]
+    for rid in ids:
+        assert done[rid]["status"] == 0 and done[rid]["finished"] == 1
+    assert finals[0].ns == 0 and finals[0].na == 0  # every sphere of the monodisperse box went
+    assert 0 < finals[1].ns < 400
+    for k, m in enumerate(models):
+        with Batch([m]) as b:
+            b.run(max_steps=0, steps_per_launch=5000)
+            alone = b.store(0)
+        assert alone.ns == finals[k].ns and alone.na == finals[k].na
+        assert same_state(alone, finals[k]), k

@@ -517,6 +517,29 @@ ENS_WINDOWS = (f"every box from its reference initial placement through window a
                f"is met), then window b (the next {ENS_B_STEPS} MC steps under the box's own stop criteria)")
 
 
+def init_ranks(backend: str) -> None:
+    """Joins the ranks (RANK, WORLD_SIZE, MASTER_ADDR/PORT from the
+    environment). A rank that dies or never arrives ends the others' next
+    collective with an error after MCACG_PG_TIMEOUT_S seconds (default 600)
+    instead of holding their GPUs: the ranks exchange only timing scalars,
+    between steps, with no kernel in flight."""
+    import datetime
+
+    import torch.distributed as dist
+    timeout = datetime.timedelta(seconds=float(os.environ.get("MCACG_PG_TIMEOUT_S", "600")))
+    dist.init_process_group(backend, timeout=timeout)
+
+
+def reduce_max_sum(t):
+    """The benchmarks' only exchange: the max (wall and kernel times) and the
+    sum (steps) of each rank's timing scalars."""
+    import torch.distributed as dist
+    tmax, tsum = t.clone(), t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+    return tmax, tsum
+
+
 def ensemble_inis(n_boxes: int = 512, first_seed: int = 1000) -> list[str]:
     """Parameter files of the ensemble (seeded with numpy's PCG64 per box)."""
     import numpy as np
@@ -700,10 +723,7 @@ def run_ensemble_windows(args, rank: int, world: int) -> dict | None:
     last_stats = st
     times = torch.tensor([tot_ms / 1000.0, float(tot_steps), tot_wall], device="cuda", dtype=torch.float64)
     if world > 1:
-        import torch.distributed as dist
-        tmax, tsum = times.clone(), times.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        tmax, tsum = reduce_max_sum(times)
         kern_s, steps_all, wall_s = float(tmax[0]), float(tsum[1]), float(tmax[2])
     else:
         kern_s, steps_all, wall_s = float(times[0]), float(times[1]), float(times[2])
@@ -1053,9 +1073,8 @@ def main() -> int:
         return 0
     if world > 1:
         import torch
-        import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        dist.init_process_group("nccl")
+        init_ranks("nccl")
     runner = {"c2": run_ours, "contact-search": run_contact_search, "ensemble": run_ensemble_windows,
               "serve": run_serve}[args.workload]
     out = runner(args, rank, world)

@@ -8,7 +8,9 @@ data path: each rank takes its own replicas of the 100k-monomer box
 the shards are disjoint, cover the work and hold near-equal monomers; each
 rank runs the two benchmark windows on its own boxes (with the oracle, the
 CPU stand-in for a rank's GPU) and the reduced totals equal those of one
-process running every box.
+process running every box. A rank that dies between steps is learned of by
+the others at their next exchange, as an error of the collective within the
+process group's timeout, not as a hang.
 """
 import os
 import socket
@@ -98,3 +100,42 @@ def test_two_ranks_split_boxes_without_overlap(tmp_path):
         assert merged[b] == (r["steps_a"], r["steps_b"], r["n_aggregates_b"])
     assert res["wall"] == 2.0
     assert res["steps"] == float(sum(r["steps_a"] + r["steps_b"] for r in alone.values()))
+
+
+def _dying_worker(rank: int, world: int, port: int, out_dir: str):
+    """Rank 1 leaves between steps (nothing in flight); rank 0 must learn of it
+    at its next exchange, as an error, not hang."""
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      MCACG_PG_TIMEOUT_S="5")
+    import bench
+    bench.init_ranks("gloo")
+    if rank == 1:
+        os._exit(3)  # a worker that dies
+    try:
+        bench.reduce_max_sum(torch.tensor([1.0, 2.0], dtype=torch.float64))
+        outcome = "no error"
+    except Exception as e:  # the dead peer surfaces as an error of the collective
+        outcome = "detected: " + type(e).__name__
+    Path(out_dir, "rank0.txt").write_text(outcome)
+    os._exit(0)
+
+
+def test_a_rank_that_dies_is_detected_by_the_others(tmp_path):
+    import time
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    procs = [ctx.Process(target=_dying_worker, args=(r, 2, port, str(tmp_path))) for r in range(2)]
+    t0 = time.monotonic()
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+    alive = [p for p in procs if p.is_alive()]
+    for p in alive:
+        p.kill()
+    assert not alive, "a rank hung"
+    assert procs[1].exitcode == 3
+    assert procs[0].exitcode == 0
+    assert (tmp_path / "rank0.txt").read_text().startswith("detected")
+    assert time.monotonic() - t0 < 120

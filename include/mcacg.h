@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define MCACG_ABI_VERSION 1
+#define MCACG_ABI_VERSION 2
 
 /* status codes beyond the reference's ErrorCodes */
 #define MCACG_ERR_CUDA 100         /* a CUDA call failed */
@@ -72,7 +72,7 @@ typedef struct mcacg_params {
     /* [limits] */
     int64_t number_of_aggregates_limit;
     int64_t n_iter_without_event_limit; /* <= 0: none */
-    double cpu_limit;                   /* <= 0: none */
+    double cpu_limit;                   /* <= 0: none; CPU seconds (mcacg_calcul only) */
     double physical_time_limit;         /* <= 0: none */
     int64_t mean_monomere_per_aggregate_limit; /* <= 0: none */
     /* [numerics] */
@@ -101,6 +101,9 @@ typedef struct mcacg_params {
     int64_t write_events_frequency;        /* default 1 */
     int64_t write_between_event_frequency; /* default 100 */
     double write_delta_t;                  /* seconds; <= 0: none (default -1) */
+    /* [limits] cpu_event (physical_model.cpp:153): CPU seconds since the last
+     * event; with cpu_limit, a stop criterion of mcacg_calcul only */
+    double cpu_event_limit;                /* <= 0: none (default -1) */
 } mcacg_params;
 
 /* Result of a contact search: AggregateContactInfo

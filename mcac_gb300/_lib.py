@@ -35,6 +35,7 @@ class Params(C.Structure):
         ("box_length", f64), ("box_volume", f64), ("viscosity", f64), ("gaz_mean_free_path", f64),
         ("mean_massic_radius", f64), ("friction_exponnant", f64), ("u_sg", f64),
         ("write_events_frequency", i64), ("write_between_event_frequency", i64), ("write_delta_t", f64),
+        ("cpu_event_limit", f64),
     ]
 
 

@@ -73,6 +73,7 @@ class PhysicalModel:
             "[oxidation]", f"rp_min = {p.rp_min_oxid!r}",
             "[limits]", f"number_of_aggregates = {p.number_of_aggregates_limit}",
             f"n_iter_without_event = {p.n_iter_without_event_limit}", f"cpu = {p.cpu_limit!r}",
+            f"cpu_event = {p.cpu_event_limit!r}",
             f"physical_time = {p.physical_time_limit!r}",
             f"mean_monomere_per_aggregate = {p.mean_monomere_per_aggregate_limit}",
             "[numerics]", f"with_domain_duplication = {b(p.with_domain_duplication)}",

@@ -385,6 +385,7 @@ int HostBox::upload(const HostState &st, void *stream, std::string *err) {
     uid_.resize(alive_.size());
     std::iota(uid_.begin(), uid_.end(), int64_t(0));
     next_uid_ = int64_t(alive_.size());
+    cpu_last_event_ = cpu_start_ = std::clock();  // physical_model.cpp:286
     maxradius_ = st.maxradius;
     time_ = st.time;
     DeviceBox *d = nullptr;
@@ -801,6 +802,11 @@ bool HostBox::finished() const {
     if (n < 1) return true;
     if (n <= static_cast<uint64_t>(p_.number_of_aggregates_limit)) return true;
     if (p_.n_iter_without_event_limit > 0 && n_iter_without_event_ >= p_.n_iter_without_event_limit) return true;
+    // processor time since the box was made, and since the last event
+    // (physical_model.cpp:311-326)
+    if (p_.cpu_limit > 0 && double(std::clock() - cpu_start_) / CLOCKS_PER_SEC >= p_.cpu_limit) return true;
+    if (p_.cpu_event_limit > 0 && double(std::clock() - cpu_last_event_) / CLOCKS_PER_SEC >= p_.cpu_event_limit)
+        return true;
     if (p_.physical_time_limit > 0 && time_ >= p_.physical_time_limit) return true;
     if (p_.mean_monomere_per_aggregate_limit > 0 && avg_npp_ >= double(p_.mean_monomere_per_aggregate_limit))
         return true;
@@ -1196,6 +1202,7 @@ int HostBox::calcul(const mcacg_run_opts &opts, mcacg_run_stats *stats, std::str
             ++events;
             ++total_events_;
             refresh();
+            cpu_last_event_ = std::clock();  // calcul.cpp:238
         } else {
             n_iter_without_event_++;
         }

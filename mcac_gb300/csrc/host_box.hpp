@@ -5,6 +5,7 @@
 // order; the spheres, member lists and Verlet grid live on the GPU. Every
 // per-step operation of src/calcul.cpp maps to one method here.
 #pragma once
+#include <ctime>
 #include <cstdint>
 #include <memory>
 #include <string>
@@ -56,7 +57,7 @@ class HostBox {
     int64_t label_of(int slot) const;
 
     // the reference's stop criteria (physical_model.cpp:288-337, without the
-    // STOPCODE file and CPU-time checks)
+    // STOPCODE file: this library writes no output directory)
     bool finished() const;
     // one run of the MC loop of src/calcul.cpp:66-281 (collisions, with
     // surface growth when the parameters ask for it)
@@ -95,6 +96,9 @@ class HostBox {
     std::vector<int> agg_n_;    // members per slot (0: dead)
     std::vector<int> alive_;    // slot of each label
     std::vector<int64_t> uid_;  // identity of each label's aggregate (the reference's weak pointers)
+    // processor time at the box's creation and at the last event, for the
+    // cpu and cpu_event limits (PhysicalModel::cpu_start, cpu_last_event)
+    std::clock_t cpu_start_ = 0, cpu_last_event_ = 0;
     int64_t next_uid_ = 0;
     double maxradius_ = 0;
     double max_time_step_ = 0, avg_npp_ = 1;

@@ -90,6 +90,7 @@ void params_defaults(mcacg_params *p) {
     p->number_of_aggregates_limit = 1;
     p->n_iter_without_event_limit = -1;
     p->cpu_limit = -1;
+    p->cpu_event_limit = -1;
     p->physical_time_limit = -1;
     p->mean_monomere_per_aggregate_limit = -1;
     p->with_domain_duplication = 1;
@@ -150,6 +151,7 @@ int params_from_ini(const IniData &ini, mcacg_params *p, std::string *error) {
     extract(value_of(ini, "limits", "number_of_aggregates"), p->number_of_aggregates_limit);
     extract(value_of(ini, "limits", "n_iter_without_event"), p->n_iter_without_event_limit);
     extract(value_of(ini, "limits", "cpu"), p->cpu_limit);
+    extract(value_of(ini, "limits", "cpu_event"), p->cpu_event_limit);
     extract(value_of(ini, "limits", "physical_time"), p->physical_time_limit);
     extract(value_of(ini, "limits", "mean_monomere_per_aggregate"), p->mean_monomere_per_aggregate_limit);
     extract_bool(value_of(ini, "numerics", "with_domain_duplication"), p->with_domain_duplication);

@@ -29,7 +29,7 @@ def test_python_binding_covers_header():
 def test_abi_version_and_errors():
     from mcac_gb300 import _lib
     lib = _lib.lib()
-    assert lib.mcacg_abi_version() == 1
+    assert lib.mcacg_abi_version() == 2
     # a null argument is rejected with a status, not a crash
     assert lib.mcacg_params_default(None) == 103
     assert b"null" in lib.mcacg_last_error()

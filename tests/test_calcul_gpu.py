@@ -145,3 +145,26 @@ def test_dense_box_run_matches_oracle_step_by_step():
            "[limits]\nnumber_of_aggregates = 100\n[numerics]\nrandom_seed = 1\nwith_domain_duplication = false\n")
     st = compare_runs(ini, max_steps=4000)
     assert st.events > 100
+
+
+@pytest.mark.gpu
+def test_cpu_time_limits_stop_the_run():
+    """[limits] cpu and cpu_event (physical_model.cpp:311-326): processor
+    seconds since the box was made, and since the last event, stop calcul."""
+    import time
+
+    base = ("[monomers]\nnumber = 3000\nmean_diameter = 30\ndispersion_diameter = 1.25\n"
+            "initialisation_mode = lognormal\n[environment]\nvolume_fraction = {fv}\ntemperature = 1700\n"
+            "[limits]\nnumber_of_aggregates = 1\n{limit}\n"
+            "[numerics]\nrandom_seed = 31\nwith_domain_duplication = false\n")
+    # (events are rare in the dilute box: 0.05 s pass between two of them)
+    for limit, fv in (("cpu = 0.3", "1e-3"), ("cpu_event = 0.05", "1e-6")):
+        pm = PhysicalModel(text=base.format(limit=limit, fv=fv))
+        with AggregatList(pm) as box:
+            c0 = time.process_time()
+            st, _ = box.calcul(max_steps=2_000_000)
+            used = time.process_time() - c0
+        assert st.finished == 1 and st.n_aggregates > 1, limit
+        assert st.steps < 2_000_000
+        if limit.startswith("cpu ="):
+            assert used >= 0.3 * 0.9
